@@ -1,0 +1,180 @@
+/* tesseract_cuda.h — the C ABI of the GB300 engine for Tesseract's bit-sliced NAND/STO machine.
+
+   This is `--engine cuda`: it sits beside the reference's ref, lanes and jit engines and takes the
+   same program format, the same lane numbering and the same result structures.  Everything below
+   is plain C: pointers, sizes and the reference's own structs.  No C++ or CUDA type crosses the
+   boundary.  Every entry point returns 1 on success, or 0 with a message in `err` (the reference's
+   convention, src/enum.c:248-260, src/jit.c:672-674).
+
+   The data types are byte-for-byte the reference's, so a Program, Enum, EnumResult or
+   CheckResult built by the reference's own code can be passed straight in:
+     Instr, CellInfo, Program   src/isa.h:14-46
+     Enum, EnumResult           src/enum.h:15-36
+     CheckResult                src/check.h:8-20
+     Spec (opaque here)         layout of src/spec.c:20-29
+   When the reference's headers are included first, their definitions are used and the ones here
+   are skipped (same include guards). */
+#ifndef TESSERACT_CUDA_H
+#define TESSERACT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- the program model (src/isa.h:8-46) -------------------------------------------------- */
+#ifndef ALPHA_ISA_H
+#define ALPHA_ISA_H
+enum { OP_NAND = 0, OP_STO = 1 };
+enum { CELL_ZERO = 0, CELL_ONE = 1, CELL_FIRST_FREE = 2 };
+typedef struct {
+    uint8_t  op;    /* OP_NAND or OP_STO */
+    uint32_t addr;  /* cell address */
+} Instr;
+enum { CUBE_DIMS = 9, CUBE_SIZE = 1 << CUBE_DIMS, CUBE_MAX_DIMS = 16,
+       CUBE_MAX_GROUPS = 1 << (CUBE_MAX_DIMS - CUBE_DIMS) };
+enum { CK_PLAIN, CK_ID, CK_LINK };
+typedef struct {
+    uint8_t  kind;  /* CK_PLAIN, CK_ID (bit `dim` of the machine number), CK_LINK */
+    uint8_t  dim;
+    uint32_t src;   /* CK_LINK: the cell read in machine k XOR 2^dim */
+} CellInfo;
+typedef struct {
+    Instr    *code;
+    size_t    len;
+    uint32_t  ncells;      /* cells used, including ZERO and ONE */
+    char    **cell_names;
+    uint32_t *inputs;      /* .in cells, in declaration order */
+    size_t    ninputs;
+    uint32_t *outputs;     /* .out cells, in declaration order */
+    size_t    noutputs;
+    CellInfo *special;     /* NULL when the program has no id or link cells */
+} Program;
+#endif
+
+/* ---- specifications (src/spec.h) ---------------------------------------------------------- */
+#ifndef ALPHA_SPEC_H
+#define ALPHA_SPEC_H
+typedef struct Spec Spec;
+#endif
+
+/* ---- exhaustive enumeration (src/enum.h:10-36) ------------------------------------------- */
+#ifndef ALPHA_ENUM_H
+#define ALPHA_ENUM_H
+enum { EN_VERIFY, EN_EQUIV, EN_SEARCH };
+#define EN_SHOW    16  /* hits kept: the smallest assignments */
+#define EN_MAX_IN  46  /* inputs */
+typedef struct {
+    int                  mode;
+    const Program       *a, *b;   /* b: equiv only; inputs and outputs matched by name */
+    const Spec          *spec;    /* verify: outputs = expression; search: outputs = constant */
+    unsigned             ticks;   /* passes per assignment */
+    int                  threads; /* CPU engines only; ignored on the GPU */
+    int                  idle;    /* CPU engines only; ignored on the GPU */
+    const unsigned char *excluded;
+    int                  part, part_end, parts;  /* shares part..part_end of `parts` */
+} Enum;
+typedef struct {
+    uint64_t space;  /* assignments in total: 2^inputs */
+    uint64_t tried;  /* assignments run (this share) */
+    uint64_t hits;   /* verify, equiv: mismatches; search: matches */
+    uint64_t hit[EN_SHOW];
+    int      nhit;
+    double   seconds;
+    uint64_t ops;    /* 1-bit operations: ticks x length x 512 per pass, as the reference counts */
+    int      threads;
+} EnumResult;
+#endif
+
+/* ---- engine-vs-reference check (src/check.h:8-20) ---------------------------------------- */
+#ifndef ALPHA_CHECK_H
+#define ALPHA_CHECK_H
+typedef struct {
+    int      ok;
+    uint64_t compared;  /* lane states compared */
+    uint64_t tick;      /* 1-based tick of the first difference */
+    long     pc;        /* -1: end of the tick */
+    unsigned lane;      /* machine number */
+    long     cell;      /* cell address, or -1 = RR */
+    unsigned want;      /* reference machine */
+    unsigned got;       /* this engine */
+} CheckResult;
+#endif
+
+/* ========================================================================================== */
+/* Entry points.  Each names the reference interface it replaces.                             */
+/* ========================================================================================== */
+
+/* Library and device.  cuda_device_info writes "NVIDIA GB300, 152 SMs, sm_103" style text. */
+int  cuda_engine_init(int device, char *err, size_t errlen);
+int  cuda_device_info(char *buf, size_t len);
+
+/* Measurement.  cuda_last_launch reports the last kernel launch of this process: device time
+   (CUDA events on the engine's stream), registers per thread, local-memory bytes per thread
+   (spills), grid and block, and the NVRTC compile time of its module (cached = 1 when the module
+   came from the cache).  cuda_lop3_peak measures the device's 3-input logic issue rate with a
+   microbenchmark: 32-bit LOP3 operations per second (each is 32 one-bit lane operations).
+   Neither has a counterpart in the reference, whose engines run on the CPU. */
+typedef struct {
+    double   kernel_ms;
+    int      regs, local_bytes;
+    unsigned grid, block;
+    double   compile_seconds;
+    int      cached;
+} CudaLaunchStats;
+int  cuda_last_launch(CudaLaunchStats *s);
+int  cuda_lop3_peak(double *ops_per_second, double *seconds, char *err, size_t errlen);
+
+/* Specifications.  Replaces spec_parse / spec_free / spec_width / spec_out_cell / spec_value
+   (src/spec.h:22-29) with the same grammar, errors and results; the Spec it returns has the
+   layout of src/spec.c:20-29, so a Spec from the reference's spec_parse is accepted as well. */
+Spec    *cuda_spec_parse(const char *text, const Program *p, int inputs_allowed, char *err,
+                         size_t errlen);
+void     cuda_spec_free(Spec *s);
+int      cuda_spec_width(const Spec *s);
+uint32_t cuda_spec_out_cell(const Spec *s, int bit);
+uint64_t cuda_spec_value(const Spec *s, uint64_t x);
+
+/* Compiled code.  Replaces jit_compile / jit_free (src/jit.h:45-48): the program becomes one
+   CUDA kernel per pass, generated as CUDA C and compiled by NVRTC for sm_103a; compiled modules
+   are cached by content hash for the life of the process. */
+typedef struct CudaCode CudaCode;
+int  cuda_compile(const Program *p, CudaCode **out, char *err, size_t errlen);
+void cuda_free(CudaCode *c);
+
+/* verify / equiv / search over every assignment.  Replaces enum_run (src/enum.h:37,
+   src/enum.c:244-332): same refusals, same --part shares, same hits, same 16 smallest hits,
+   same ops accounting.  r->threads reports the GPU threads used; r->seconds the wall time of
+   the device work. */
+int  cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen);
+void cuda_enum_add_hit(EnumResult *r, uint64_t x);   /* enum_add_hit, src/enum.c:31-46 */
+
+/* Random-state parity against the reference semantics.  Replaces
+   check_lanes(p, jit, seed, ticks, 0, r) (src/check.h:25, src/check.c:52-113): every machine of
+   the program's cube gets the same random state from splitmix64(seed) as there, runs `ticks`
+   passes on the GPU, and the full state (RR and every cell) is compared after each tick with the
+   reference machine, run on the host. */
+int  cuda_check(const Program *p, uint64_t seed, unsigned ticks, CheckResult *r, char *err,
+                size_t errlen);
+
+/* The cube (programs with id and link cells, up to 2^16 machines).  Replaces LaneCube +
+   jit_cube_run (src/lanes.h:66-80, src/jit.h:58-61).  The state lives on the device.  Lines use
+   the reference's layout: per group of 512 machines, `ncells` lines of 8 uint64 each, machine k
+   of the group at bit k%64 of word k/64 (src/lanes.h:13-15), and one line for RR. */
+typedef struct CudaCube CudaCube;
+int  cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen);
+void cuda_cube_free(CudaCube *c);
+unsigned cuda_cube_groups(const CudaCube *c);
+unsigned cuda_cube_segments(const CudaCube *c);
+int  cuda_cube_load(CudaCube *c, unsigned group, const uint64_t *mem_lines, const uint64_t *rr_line,
+                    char *err, size_t errlen);
+int  cuda_cube_store(const CudaCube *c, unsigned group, uint64_t *mem_lines, uint64_t *rr_line,
+                     char *err, size_t errlen);
+int  cuda_cube_run(CudaCube *c, uint64_t passes, char *err, size_t errlen);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

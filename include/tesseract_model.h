@@ -1,0 +1,57 @@
+/* tesseract_model.h — the host-side program model that ships with the GB300 engine: programs,
+   the assembler, the gate builder and the workload generators, in plain C.
+
+   These are the engine's own implementations of the reference's host helpers, with a tc_ prefix
+   so that they link next to the reference's.  Each gives the same Program, cell for cell and
+   instruction for instruction, as the reference function it names.  Programs returned here are
+   freed with tc_program_free. */
+#ifndef TESSERACT_MODEL_H
+#define TESSERACT_MODEL_H
+
+#include "tesseract_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* src/asm.c:767-801 and src/isa.h:48-62 */
+void     tc_program_free(Program *p);
+int      tc_program_find_cell(const Program *p, const char *name, uint32_t *addr);
+int      tc_program_readonly(const Program *p, uint32_t cell);
+uint32_t tc_program_resolve(const Program *p, uint32_t cell, unsigned *mask);
+unsigned tc_program_dims(const Program *p);
+int      tc_program_id_name(const char *name);
+/* Writes the program as assembly text (src/build.c:432-444); returns bytes written, or the
+   length needed when buf is too small (buf may be NULL with len 0). */
+size_t   tc_program_print(const Program *p, char *buf, size_t len);
+/* Deep copy (names included). */
+int      tc_program_copy(const Program *src, Program *dst);
+
+/* The assembler (src/asm.h:7-17): same language, same cell numbering, same @local names. */
+int tc_asm_string(const char *src, const char *name, const char *base_dir, Program *out,
+                  char *err, size_t errlen);
+int tc_asm_file(const char *path, Program *out, char *err, size_t errlen);
+
+/* Generators (src/gen.h, src/tester.h:18): the same instruction sequences as the reference's
+   gen_mul, gen_hash, gen_life, gen_life_cube, random_program. */
+void     tc_gen_mul(Program *p, int bits);
+int      tc_gen_hash(Program *p, int bits, int rounds);
+uint64_t tc_toyhash(uint64_t x, int bits, int rounds);
+void     tc_gen_life(Program *p, int w, int h, uint32_t *board);
+void     tc_gen_life_cube(Program *p, int w, int h, int rbits, int cbits, uint32_t *board);
+unsigned tc_grid_machine(unsigned row, unsigned col, int cbits);
+void     tc_random_program(Program *p, uint32_t cells, size_t len, uint64_t seed);
+/* Random program with `width` input cells (.in w0.., never written) beside `cells` working cells
+   (.out c0..): the input-width extension the batched equivalence workload needs; same
+   splitmix64 stream as random_program. */
+void     tc_random_program_in(Program *p, uint32_t cells, uint32_t width, size_t len,
+                              uint64_t seed);
+/* A copy of p rewritten by local NAND identities (double negation, commuted NAND pairs,
+   De Morgan through a scratch cell) chosen by splitmix64(seed): the same function, a different
+   program.  mutate != 0 also flips one instruction's operand, which normally changes it. */
+void     tc_rewrite_program(const Program *p, Program *out, uint64_t seed, int mutate);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,160 @@
+"""ORACLE -- test infrastructure, not product code.
+
+ctypes bindings of oracle/liboracle.so, the CPU restatement of the reference's semantics
+(oracle/oracle.c), and of the reference itself where it was built from its sources
+(oracle/_ref/libalpha.so, x86 hosts with the sources mounted).  Imported only by tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import tesseract_gb300 as T
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libalpha.so")
+REF_BIN = os.path.join(HERE, "_ref", "alpha")
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_LIB):
+            raise RuntimeError(f"{ORACLE_LIB} is missing: build first")
+        L = C.CDLL(ORACLE_LIB)
+        P = C.POINTER(T.ProgramStruct)
+        L.orc_enum_run.restype = C.c_int
+        L.orc_enum_run.argtypes = [C.POINTER(T.EnumStruct), C.POINTER(T.EnumResult), C.c_int,
+                                   C.c_uint64, C.c_char_p, C.c_size_t]
+        L.orc_enum_ref.restype = C.c_int
+        L.orc_enum_ref.argtypes = [C.POINTER(T.EnumStruct), C.POINTER(T.EnumResult), C.c_char_p,
+                                   C.c_size_t]
+        L.orc_spec_value.restype = C.c_uint64
+        L.orc_spec_value.argtypes = [C.c_void_p, C.c_uint64]
+        L.orc_cube_new.restype = C.c_void_p
+        L.orc_cube_new.argtypes = [P, C.c_uint]
+        L.orc_cube_free.argtypes = [C.c_void_p]
+        L.orc_cube_get.restype = C.c_uint8
+        L.orc_cube_get.argtypes = [C.c_void_p, C.c_uint, C.c_uint32]
+        L.orc_cube_set.argtypes = [C.c_void_p, C.c_uint, C.c_uint32, C.c_uint8]
+        L.orc_cube_rr.restype = C.c_uint8
+        L.orc_cube_rr.argtypes = [C.c_void_p, C.c_uint]
+        L.orc_cube_set_rr.argtypes = [C.c_void_p, C.c_uint, C.c_uint8]
+        L.orc_cube_step.argtypes = [C.c_void_p]
+        L.orc_cube_tick.argtypes = [C.c_void_p]
+        L.orc_check_state.argtypes = [C.c_void_p, C.c_uint64]
+        L.orc_dims.restype = C.c_uint
+        L.orc_dims.argtypes = [P]
+        L.orc_life_scalar.argtypes = [C.POINTER(C.c_uint8), C.c_int, C.c_int]
+        L.orc_toyhash.restype = C.c_uint64
+        L.orc_toyhash.argtypes = [C.c_uint64, C.c_int, C.c_int]
+        _lib = L
+    return _lib
+
+
+def enum_run(mode, a, b=None, spec=None, ticks=1, part=0, part_end=None, parts=1, threads=None,
+             limit_chunks=0) -> dict:
+    """The enumeration on the CPU oracle's bit-sliced engine (orc_enum_run)."""
+    e = T.make_enum(mode, a, b, spec, ticks, part, part_end, parts)
+    r, err = T.EnumResult(), C.create_string_buffer(1024)
+    if not lib().orc_enum_run(C.byref(e), C.byref(r), threads or os.cpu_count() or 1,
+                              limit_chunks, err, len(err)):
+        raise T.EngineError(err.value.decode())
+    return r.as_dict()
+
+
+def enum_ref(mode, a, b=None, spec=None, ticks=1, part=0, part_end=None, parts=1) -> dict:
+    """The enumeration on the reference machine, one assignment at a time (small inputs)."""
+    e = T.make_enum(mode, a, b, spec, ticks, part, part_end, parts)
+    r, err = T.EnumResult(), C.create_string_buffer(1024)
+    if not lib().orc_enum_ref(C.byref(e), C.byref(r), err, len(err)):
+        raise T.EngineError(err.value.decode())
+    return r.as_dict()
+
+
+def spec_value(spec, x: int) -> int:
+    return lib().orc_spec_value(spec.p, x)
+
+
+def life_scalar(board: bytearray, w: int, h: int) -> None:
+    buf = (C.c_uint8 * (w * h)).from_buffer(board)
+    lib().orc_life_scalar(buf, w, h)
+
+
+def toyhash(x: int, bits: int, rounds: int) -> int:
+    return lib().orc_toyhash(x, bits, rounds)
+
+
+class RefCube:
+    """The reference machine: a lockstep cube of `machines` one-byte-per-cell machines."""
+
+    def __init__(self, program, machines: int):
+        self.program = program
+        self.machines = machines
+        self.h = lib().orc_cube_new(program.ptr, machines)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_cube_free(self.h)
+            self.h = None
+
+    def get(self, k, a):
+        return lib().orc_cube_get(self.h, k, a)
+
+    def set(self, k, a, v):
+        lib().orc_cube_set(self.h, k, a, v)
+
+    def rr(self, k):
+        return lib().orc_cube_rr(self.h, k)
+
+    def set_rr(self, k, v):
+        lib().orc_cube_set_rr(self.h, k, v)
+
+    def step(self):
+        lib().orc_cube_step(self.h)
+
+    def tick(self):
+        lib().orc_cube_tick(self.h)
+
+    def check_state(self, seed):
+        lib().orc_check_state(self.h, seed)
+
+
+# ---- the reference itself (only where built from its sources) ----------------------------
+
+def have_reference() -> bool:
+    return os.path.exists(REF_LIB) and os.path.exists(REF_BIN)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        L = C.CDLL(REF_LIB)
+        P = C.POINTER(T.ProgramStruct)
+        L.asm_string.restype = C.c_int
+        L.asm_string.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, P, C.c_char_p, C.c_size_t]
+        L.asm_file.restype = C.c_int
+        L.asm_file.argtypes = [C.c_char_p, P, C.c_char_p, C.c_size_t]
+        L.program_free.argtypes = [P]
+        L.gen_mul.argtypes = [P, C.c_int]
+        L.gen_hash.restype = C.c_int
+        L.gen_hash.argtypes = [P, C.c_int, C.c_int]
+        L.gen_life_cube.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.POINTER(C.c_uint32)]
+        L.gen_life.argtypes = [P, C.c_int, C.c_int, C.POINTER(C.c_uint32)]
+        L.random_program.argtypes = [P, C.c_uint32, C.c_size_t, C.c_uint64]
+        L.spec_parse.restype = C.c_void_p
+        L.spec_parse.argtypes = [C.c_char_p, P, C.c_int, C.c_char_p, C.c_size_t]
+        L.spec_value.restype = C.c_uint64
+        L.spec_value.argtypes = [C.c_void_p, C.c_uint64]
+        L.spec_free.argtypes = [C.c_void_p]
+        L.enum_run.restype = C.c_int
+        L.enum_run.argtypes = [C.POINTER(T.EnumStruct), C.POINTER(T.EnumResult), C.c_char_p,
+                               C.c_size_t]
+        _ref = L
+    return _ref

@@ -1,0 +1,349 @@
+"""Python bindings of the GB300 engine for Tesseract's bit-sliced NAND/STO machine.
+
+The engine itself is C and CUDA behind a C ABI (include/tesseract_cuda.h,
+include/tesseract_model.h) in ``libtesseract_gb300.so``; this module binds it with ctypes and
+mirrors the reference's host interface for the hot path:
+
+    Program            src/isa.h Program, built by the assembler or the generators
+    Spec               spec_parse / spec_value (src/spec.h)
+    enum_run           enum_run (src/enum.h:37): verify / equiv / search
+    check              check_lanes (src/check.h:25) with the CUDA engine
+    Cube               LaneCube + jit_cube_run (src/lanes.h, src/jit.h)
+
+There is no CPU fallback: when the shared library is missing every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtesseract_gb300.so")
+
+EN_VERIFY, EN_EQUIV, EN_SEARCH = 0, 1, 2
+EN_SHOW = 16
+OP_NAND, OP_STO = 0, 1
+CK_PLAIN, CK_ID, CK_LINK = 0, 1, 2
+
+
+class Instr(C.Structure):
+    _fields_ = [("op", C.c_uint8), ("addr", C.c_uint32)]
+
+
+class CellInfo(C.Structure):
+    _fields_ = [("kind", C.c_uint8), ("dim", C.c_uint8), ("src", C.c_uint32)]
+
+
+class ProgramStruct(C.Structure):
+    _fields_ = [("code", C.POINTER(Instr)), ("len", C.c_size_t), ("ncells", C.c_uint32),
+                ("cell_names", C.POINTER(C.c_char_p)), ("inputs", C.POINTER(C.c_uint32)),
+                ("ninputs", C.c_size_t), ("outputs", C.POINTER(C.c_uint32)),
+                ("noutputs", C.c_size_t), ("special", C.POINTER(CellInfo))]
+
+
+class EnumStruct(C.Structure):
+    _fields_ = [("mode", C.c_int), ("a", C.POINTER(ProgramStruct)),
+                ("b", C.POINTER(ProgramStruct)), ("spec", C.c_void_p), ("ticks", C.c_uint),
+                ("threads", C.c_int), ("idle", C.c_int), ("excluded", C.c_void_p),
+                ("part", C.c_int), ("part_end", C.c_int), ("parts", C.c_int)]
+
+
+class EnumResult(C.Structure):
+    _fields_ = [("space", C.c_uint64), ("tried", C.c_uint64), ("hits", C.c_uint64),
+                ("hit", C.c_uint64 * EN_SHOW), ("nhit", C.c_int), ("seconds", C.c_double),
+                ("ops", C.c_uint64), ("threads", C.c_int)]
+
+    def as_dict(self):
+        return {"space": self.space, "tried": self.tried, "hits": self.hits,
+                "hit": list(self.hit[: self.nhit]), "ops": self.ops,
+                "seconds": self.seconds, "threads": self.threads}
+
+
+class CheckResult(C.Structure):
+    _fields_ = [("ok", C.c_int), ("compared", C.c_uint64), ("tick", C.c_uint64),
+                ("pc", C.c_long), ("lane", C.c_uint), ("cell", C.c_long), ("want", C.c_uint),
+                ("got", C.c_uint)]
+
+
+class LaunchStats(C.Structure):
+    _fields_ = [("kernel_ms", C.c_double), ("regs", C.c_int), ("local_bytes", C.c_int),
+                ("grid", C.c_uint), ("block", C.c_uint), ("compile_seconds", C.c_double),
+                ("cached", C.c_int)]
+
+
+_lib = None
+
+
+class EngineError(RuntimeError):
+    pass
+
+
+def lib():
+    """The shared library, loaded once.  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise EngineError(f"{LIB_PATH} is missing: run tesseract_gb300.build.build() first")
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER(ProgramStruct)
+        sig = {
+            "tc_program_free": (None, [P]),
+            "tc_program_print": (C.c_size_t, [P, C.c_char_p, C.c_size_t]),
+            "tc_program_copy": (C.c_int, [P, P]),
+            "tc_program_dims": (C.c_uint, [P]),
+            "tc_asm_string": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, P, C.c_char_p,
+                                        C.c_size_t]),
+            "tc_asm_file": (C.c_int, [C.c_char_p, P, C.c_char_p, C.c_size_t]),
+            "tc_gen_mul": (None, [P, C.c_int]),
+            "tc_gen_hash": (C.c_int, [P, C.c_int, C.c_int]),
+            "tc_toyhash": (C.c_uint64, [C.c_uint64, C.c_int, C.c_int]),
+            "tc_gen_life": (None, [P, C.c_int, C.c_int, C.POINTER(C.c_uint32)]),
+            "tc_gen_life_cube": (None, [P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.POINTER(C.c_uint32)]),
+            "tc_grid_machine": (C.c_uint, [C.c_uint, C.c_uint, C.c_int]),
+            "tc_random_program": (None, [P, C.c_uint32, C.c_size_t, C.c_uint64]),
+            "tc_random_program_in": (None, [P, C.c_uint32, C.c_uint32, C.c_size_t, C.c_uint64]),
+            "tc_rewrite_program": (None, [P, P, C.c_uint64, C.c_int]),
+            "cuda_spec_parse": (C.c_void_p, [P, C.c_int, C.c_char_p, C.c_size_t]),
+            "cuda_spec_free": (None, [C.c_void_p]),
+            "cuda_spec_width": (C.c_int, [C.c_void_p]),
+            "cuda_spec_out_cell": (C.c_uint32, [C.c_void_p, C.c_int]),
+            "cuda_spec_value": (C.c_uint64, [C.c_void_p, C.c_uint64]),
+            "cuda_engine_init": (C.c_int, [C.c_int, C.c_char_p, C.c_size_t]),
+            "cuda_device_info": (C.c_int, [C.c_char_p, C.c_size_t]),
+            "cuda_enum_run": (C.c_int, [C.POINTER(EnumStruct), C.POINTER(EnumResult), C.c_char_p,
+                                        C.c_size_t]),
+            "tc_codegen_enum": (C.c_void_p, [C.c_void_p, C.POINTER(C.c_size_t)]),
+            "cuda_last_launch": (C.c_int, [C.POINTER(LaunchStats)]),
+            "cuda_lop3_peak": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                         C.c_char_p, C.c_size_t]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        # cuda_spec_parse takes the text first
+        L.cuda_spec_parse.argtypes = [C.c_char_p, P, C.c_int, C.c_char_p, C.c_size_t]
+        _lib = L
+    return _lib
+
+
+def _err():
+    return C.create_string_buffer(1024)
+
+
+class Program:
+    """A NAND/STO program owned by the engine's library (src/isa.h Program)."""
+
+    def __init__(self):
+        self.s = ProgramStruct()
+        self._owned = False
+
+    def __del__(self):
+        if getattr(self, "_owned", False) and _lib is not None:
+            _lib.tc_program_free(C.byref(self.s))
+            self._owned = False
+
+    @property
+    def ptr(self):
+        return C.pointer(self.s)
+
+    # ---- construction -------------------------------------------------------------------
+    @classmethod
+    def _made(cls, fn, *args):
+        p = cls()
+        fn(C.byref(p.s), *args)
+        p._owned = True
+        return p
+
+    @classmethod
+    def from_asm(cls, text: str, name: str = "<string>", base_dir: str = "."):
+        p, e = cls(), _err()
+        if not lib().tc_asm_string(text.encode(), name.encode(), base_dir.encode(),
+                                   C.byref(p.s), e, len(e)):
+            raise EngineError(e.value.decode())
+        p._owned = True
+        return p
+
+    @classmethod
+    def from_file(cls, path: str):
+        p, e = cls(), _err()
+        if not lib().tc_asm_file(path.encode(), C.byref(p.s), e, len(e)):
+            raise EngineError(e.value.decode())
+        p._owned = True
+        return p
+
+    @classmethod
+    def gen_mul(cls, bits: int):
+        return cls._made(lib().tc_gen_mul, bits)
+
+    @classmethod
+    def gen_hash(cls, bits: int, rounds: int):
+        p = cls()
+        if not lib().tc_gen_hash(C.byref(p.s), bits, rounds):
+            raise EngineError(f"no toy hash for {bits} bits")
+        p._owned = True
+        return p
+
+    @classmethod
+    def gen_life(cls, w: int, h: int):
+        board = (C.c_uint32 * (w * h))()
+        p = cls._made(lib().tc_gen_life, w, h, board)
+        p.board = list(board)
+        return p
+
+    @classmethod
+    def gen_life_cube(cls, w: int, h: int, rbits: int, cbits: int):
+        board = (C.c_uint32 * (w * h))()
+        p = cls._made(lib().tc_gen_life_cube, w, h, rbits, cbits, board)
+        p.board = list(board)
+        return p
+
+    @classmethod
+    def random(cls, cells: int, length: int, seed: int):
+        return cls._made(lib().tc_random_program, cells, length, seed)
+
+    @classmethod
+    def random_in(cls, cells: int, width: int, length: int, seed: int):
+        return cls._made(lib().tc_random_program_in, cells, width, length, seed)
+
+    def rewrite(self, seed: int, mutate: bool = False):
+        p = Program()
+        lib().tc_rewrite_program(self.ptr, C.byref(p.s), seed, int(mutate))
+        p._owned = True
+        return p
+
+    # ---- views --------------------------------------------------------------------------
+    def text(self) -> str:
+        n = lib().tc_program_print(self.ptr, None, 0)
+        buf = C.create_string_buffer(n + 1)
+        lib().tc_program_print(self.ptr, buf, n + 1)
+        return buf.value.decode()
+
+    def __len__(self):
+        return self.s.len
+
+    @property
+    def ncells(self):
+        return self.s.ncells
+
+    @property
+    def names(self):
+        return [self.s.cell_names[i].decode() for i in range(self.s.ncells)]
+
+    @property
+    def inputs(self):
+        return [self.s.inputs[i] for i in range(self.s.ninputs)]
+
+    @property
+    def outputs(self):
+        return [self.s.outputs[i] for i in range(self.s.noutputs)]
+
+    @property
+    def code(self):
+        return [(self.s.code[i].op, self.s.code[i].addr) for i in range(self.s.len)]
+
+    @property
+    def special(self):
+        if not self.s.special:
+            return None
+        return [(self.s.special[i].kind, self.s.special[i].dim, self.s.special[i].src)
+                for i in range(self.s.ncells)]
+
+    def dims(self):
+        return lib().tc_program_dims(self.ptr)
+
+
+class Spec:
+    """A specification parsed against a program (spec_parse, src/spec.c:272-327)."""
+
+    def __init__(self, program: Program, text: str, inputs_allowed: bool = True):
+        e = _err()
+        self.program = program
+        self.text = text
+        self.p = lib().cuda_spec_parse(text.encode(), program.ptr, int(inputs_allowed), e,
+                                       len(e))
+        if not self.p:
+            raise EngineError(e.value.decode())
+
+    def __del__(self):
+        if getattr(self, "p", None) and _lib is not None:
+            _lib.cuda_spec_free(self.p)
+            self.p = None
+
+    @property
+    def width(self):
+        return lib().cuda_spec_width(self.p)
+
+    def out_cell(self, bit: int):
+        return lib().cuda_spec_out_cell(self.p, bit)
+
+    def value(self, x: int):
+        return lib().cuda_spec_value(self.p, x)
+
+
+def make_enum(mode, a: Program, b: Program | None = None, spec: Spec | None = None, ticks=1,
+              part=0, part_end=None, parts=1) -> EnumStruct:
+    e = EnumStruct()
+    e.mode = mode
+    e.a = a.ptr
+    e.b = b.ptr if b is not None else C.POINTER(ProgramStruct)()
+    e.spec = spec.p if spec is not None else None
+    e.ticks = ticks
+    e.part = part
+    e.part_end = part if part_end is None else part_end
+    e.parts = parts
+    return e
+
+
+def enum_run(mode, a: Program, b: Program | None = None, spec: Spec | None = None, ticks=1,
+             part=0, part_end=None, parts=1) -> dict:
+    """verify / equiv / search on the GPU (cuda_enum_run)."""
+    e = make_enum(mode, a, b, spec, ticks, part, part_end, parts)
+    r, err = EnumResult(), _err()
+    if not lib().cuda_enum_run(C.byref(e), C.byref(r), err, len(err)):
+        raise EngineError(err.value.decode())
+    return r.as_dict()
+
+
+def last_launch() -> dict:
+    s = LaunchStats()
+    lib().cuda_last_launch(C.byref(s))
+    return {f: getattr(s, f) for f, _ in LaunchStats._fields_}
+
+
+def lop3_peak() -> float:
+    """Measured 32-bit LOP3 operations per second of the device (the roofline denominator)."""
+    ops, sec, err = C.c_double(), C.c_double(), _err()
+    if not lib().cuda_lop3_peak(C.byref(ops), C.byref(sec), err, len(err)):
+        raise EngineError(err.value.decode())
+    return ops.value
+
+
+def device_info() -> str:
+    buf = C.create_string_buffer(512)
+    if not lib().cuda_device_info(buf, len(buf)):
+        raise EngineError(buf.value.decode())
+    return buf.value.decode()
+
+
+def codegen_enum_source(mode, a: Program, b: Program | None = None, spec: Spec | None = None,
+                        ticks=1) -> str:
+    """The CUDA C the engine generates for an enumeration (for inspection and host tests)."""
+    return _codegen(mode, a, b, spec, ticks)
+
+
+def _codegen(mode, a, b, spec, ticks):
+    L = lib()
+    fn = L.tc_codegen_enum_for
+    fn.restype = C.c_void_p
+    fn.argtypes = [C.POINTER(EnumStruct), C.POINTER(C.c_size_t), C.c_char_p, C.c_size_t]
+    e = make_enum(mode, a, b, spec, ticks)
+    n, err = C.c_size_t(), _err()
+    p = fn(C.byref(e), C.byref(n), err, len(err))
+    if not p:
+        raise EngineError(err.value.decode())
+    s = C.string_at(p, n.value).decode()
+    L.tc_free.argtypes = [C.c_void_p]
+    L.tc_free(p)
+    return s

@@ -1,0 +1,34 @@
+/* The code generator's interface (codegen.c): programs to CUDA C for NVRTC. */
+#ifndef TC_CODEGEN_H
+#define TC_CODEGEN_H
+
+#include "tc_host.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int             mode;       /* EN_VERIFY, EN_EQUIV, EN_SEARCH */
+    const Program  *a, *b;      /* b: equiv */
+    const uint32_t *b_inputs;   /* equiv: b's input cell for each of a's inputs, by name */
+    const int      *out_map;    /* equiv: b's output index for each of a's outputs */
+    const TcSpec   *spec;       /* verify, search */
+    uint64_t        target;     /* search: the constant right side */
+    unsigned        ticks;
+    int             block;      /* threads per block */
+} TcGenEnum;
+
+/* CUDA C for the enumeration kernel `tc_enum` (malloc'd; *len gets its length).  The per-word
+   function tc_word(word) -> hit mask is plain C when TC_HOST_EMULATION is defined, so the tests
+   can compile the same text for the host. */
+char *tc_codegen_enum(const TcGenEnum *g, size_t *len);
+
+/* CUDA C for the cube kernels of a program with id/link cells (cube.c). */
+char *tc_codegen_cube(const Program *p, const size_t *seg_first, unsigned nseg, int block,
+                      size_t *len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

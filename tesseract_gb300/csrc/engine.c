@@ -1,0 +1,501 @@
+/* The engine's runtime: device set-up, NVRTC compilation with a content-addressed module cache,
+   and cuda_enum_run (verify / equiv / search over every assignment).
+
+   One process, one GPU, the primary context; all work goes to one engine stream.  Generated
+   modules are compiled for the device's own architecture (sm_103a on GB300) and kept for the
+   life of the process, keyed by the full text of the generated source. */
+#include <cuda_runtime_api.h>
+#include <nvrtc.h>
+#include <pthread.h>
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "codegen.h"
+#include "engine.h"
+
+TcEngine tc_engine;
+static pthread_mutex_t engine_lock = PTHREAD_MUTEX_INITIALIZER;
+
+double tc_now(void)
+{
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+int tc_fail(char *err, size_t errlen, const char *fmt, ...)
+{
+    if (err && errlen) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(err, errlen, fmt, ap);
+        va_end(ap);
+    }
+    return 0;
+}
+
+int tc_cu_check(cudaError_t rc, const char *what, char *err, size_t errlen)
+{
+    if (rc == cudaSuccess)
+        return 1;
+    return tc_fail(err, errlen, "CUDA error in %s: %s (%s)", what, cudaGetErrorName(rc),
+                   cudaGetErrorString(rc));
+}
+
+#define CU(call, what)                                               \
+    do {                                                             \
+        if (!tc_cu_check((call), (what), err, errlen))               \
+            goto fail;                                               \
+    } while (0)
+
+int cuda_engine_init(int device, char *err, size_t errlen)
+{
+    pthread_mutex_lock(&engine_lock);
+    if (tc_engine.ready) {
+        int ok = cudaSetDevice(tc_engine.dev) == cudaSuccess;
+        pthread_mutex_unlock(&engine_lock);
+        return ok ? 1 : tc_fail(err, errlen, "cannot make the engine's device current");
+    }
+    struct cudaDeviceProp prop;
+    int count = 0;
+    CU(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
+    if (device < 0 || device >= count) {
+        tc_fail(err, errlen, "no CUDA device %d (%d present)", device, count);
+        goto fail;
+    }
+    CU(cudaSetDevice(device), "cudaSetDevice");
+    CU(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+    tc_engine.dev = device;
+    tc_engine.sms = prop.multiProcessorCount;
+    tc_engine.cc_major = prop.major;
+    tc_engine.cc_minor = prop.minor;
+    tc_engine.smem_optin = (int)prop.sharedMemPerBlockOptin;
+    snprintf(tc_engine.name, sizeof tc_engine.name, "%s", prop.name);
+    CU(cudaStreamCreateWithFlags(&tc_engine.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    CU(cudaEventCreate(&tc_engine.ev0), "cudaEventCreate");
+    CU(cudaEventCreate(&tc_engine.ev1), "cudaEventCreate");
+    tc_engine.ready = 1;
+    pthread_mutex_unlock(&engine_lock);
+    return 1;
+fail:
+    pthread_mutex_unlock(&engine_lock);
+    return 0;
+}
+
+int cuda_device_info(char *buf, size_t len)
+{
+    char err[256];
+    if (!cuda_engine_init(0, err, sizeof err)) {
+        snprintf(buf, len, "%s", err);
+        return 0;
+    }
+    snprintf(buf, len, "%s, %d SMs, sm_%d%d", tc_engine.name, tc_engine.sms, tc_engine.cc_major,
+             tc_engine.cc_minor);
+    return 1;
+}
+
+int cuda_last_launch(CudaLaunchStats *s)
+{
+    memset(s, 0, sizeof *s);
+    s->kernel_ms = tc_engine.last_kernel_ms;
+    s->regs = tc_engine.last.regs;
+    s->local_bytes = tc_engine.last.local_bytes;
+    s->grid = tc_engine.last_grid;
+    s->block = tc_engine.last_block;
+    s->compile_seconds = tc_engine.last.cached ? 0 : tc_engine.last.compile_seconds;
+    s->cached = tc_engine.last.cached;
+    return tc_engine.ready;
+}
+
+/* ---- workspace ------------------------------------------------------------------------------- */
+
+int tc_scratch(TcBuf *b, size_t bytes, char *err, size_t errlen)
+{
+    if (b->bytes >= bytes)
+        return 1;
+    if (b->ptr)
+        cudaFree(b->ptr);
+    b->ptr = NULL;
+    b->bytes = 0;
+    if (!tc_cu_check(cudaMalloc(&b->ptr, bytes ? bytes : 16), "cudaMalloc", err, errlen))
+        return 0;
+    b->bytes = bytes;
+    return 1;
+}
+
+/* ---- NVRTC and the module cache -------------------------------------------------------------- */
+
+typedef struct {
+    char     *src;
+    size_t    len;
+    cudaLibrary_t lib;
+    TcModInfo     info;
+} CacheEntry;
+
+static CacheEntry *cache;
+static size_t ncache, capcache;
+
+static uint64_t text_hash(const char *s, size_t n)
+{
+    uint64_t h = 0xcbf29ce484222325ull;
+    for (size_t i = 0; i < n; i++)
+        h = (h ^ (unsigned char)s[i]) * 0x100000001b3ull;
+    return h;
+}
+
+int tc_module(const char *src, size_t len, const char *const *kernels, int nkernels,
+              const char *extra_opt, TcModule *out, char *err, size_t errlen)
+{
+    uint64_t h = text_hash(src, len);
+    pthread_mutex_lock(&engine_lock);
+    for (size_t i = 0; i < ncache; i++)
+        if (cache[i].info.hash == h && cache[i].len == len && !memcmp(cache[i].src, src, len)) {
+            out->lib = cache[i].lib;
+            out->info = cache[i].info;
+            out->info.cached = 1;
+            pthread_mutex_unlock(&engine_lock);
+            goto functions;
+        }
+    pthread_mutex_unlock(&engine_lock);
+
+    {
+        double t0 = tc_now();
+        nvrtcProgram prog;
+        nvrtcResult nr = nvrtcCreateProgram(&prog, src, "tesseract_gen.cu", 0, NULL, NULL);
+        if (nr != NVRTC_SUCCESS)
+            return tc_fail(err, errlen, "NVRTC: %s", nvrtcGetErrorString(nr));
+        char arch[64];
+        snprintf(arch, sizeof arch, "--gpu-architecture=sm_%d%da", tc_engine.cc_major,
+                 tc_engine.cc_minor);
+        const char *opts[8];
+        int nopt = 0;
+        opts[nopt++] = arch;
+        opts[nopt++] = "--std=c++17";
+        opts[nopt++] = "-lineinfo";
+        opts[nopt++] = "--ptxas-options=-v";
+        if (extra_opt && *extra_opt)
+            opts[nopt++] = extra_opt;
+        nr = nvrtcCompileProgram(prog, nopt, opts);
+        size_t loglen = 0;
+        nvrtcGetProgramLogSize(prog, &loglen);
+        char *log = tc_xmalloc(loglen + 1);
+        log[0] = '\0';
+        if (loglen)
+            nvrtcGetProgramLog(prog, log);
+        if (nr != NVRTC_SUCCESS) {
+            tc_fail(err, errlen, "NVRTC compile failed: %s: %.400s", nvrtcGetErrorString(nr), log);
+            free(log);
+            nvrtcDestroyProgram(&prog);
+            return 0;
+        }
+        size_t cubin_len = 0;
+        nvrtcGetCUBINSize(prog, &cubin_len);
+        char *cubin = tc_xmalloc(cubin_len + 1);
+        nvrtcGetCUBIN(prog, cubin);
+        nvrtcDestroyProgram(&prog);
+        cudaLibrary_t lib;
+        cudaError_t rc = cudaLibraryLoadData(&lib, cubin, NULL, NULL, 0, NULL, NULL, 0);
+        free(cubin);
+        if (!tc_cu_check(rc, "cudaLibraryLoadData", err, errlen)) {
+            free(log);
+            return 0;
+        }
+        TcModInfo info;
+        memset(&info, 0, sizeof info);
+        info.hash = h;
+        info.compile_seconds = tc_now() - t0;
+        info.cubin_bytes = cubin_len;
+        snprintf(info.log, sizeof info.log, "%s", log);
+        free(log);
+        pthread_mutex_lock(&engine_lock);
+        if (ncache == capcache) {
+            capcache = capcache ? 2 * capcache : 16;
+            cache = tc_xrealloc(cache, capcache * sizeof *cache);
+        }
+        cache[ncache].src = tc_xmalloc(len + 1);
+        memcpy(cache[ncache].src, src, len);
+        cache[ncache].src[len] = '\0';
+        cache[ncache].len = len;
+        cache[ncache].lib = lib;
+        cache[ncache].info = info;
+        ncache++;
+        pthread_mutex_unlock(&engine_lock);
+        out->lib = lib;
+        out->info = info;
+    }
+functions:
+    for (int k = 0; k < nkernels && k < TC_MAX_KERNELS; k++) {
+        if (!tc_cu_check(cudaLibraryGetKernel(&out->fn[k], out->lib, kernels[k]),
+                         "cudaLibraryGetKernel", err, errlen))
+            return 0;
+        struct cudaFuncAttributes fa;
+        if (k == 0 && cudaFuncGetAttributes(&fa, (const void *)out->fn[k]) == cudaSuccess) {
+            out->info.regs = fa.numRegs;
+            out->info.local_bytes = (int)fa.localSizeBytes;
+        }
+    }
+    return 1;
+}
+
+/* ---- verify / equiv / search ---------------------------------------------------------------- */
+
+void cuda_enum_add_hit(EnumResult *r, uint64_t x)
+{
+    int i;
+    if (r->nhit < EN_SHOW) {
+        i = r->nhit++;
+    } else {
+        if (x >= r->hit[EN_SHOW - 1])
+            return;
+        i = EN_SHOW - 1;
+    }
+    while (i > 0 && r->hit[i - 1] > x) {
+        r->hit[i] = r->hit[i - 1];
+        i--;
+    }
+    r->hit[i] = x;
+}
+
+static int match_names(const Program *a, const uint32_t *la, size_t na, const Program *b,
+                       const uint32_t *lb, size_t nb, int *map, const char *what, char *err,
+                       size_t errlen)
+{
+    if (na != nb)
+        return tc_fail(err, errlen, "the programs have %zu and %zu %s", na, nb, what);
+    for (size_t i = 0; i < na; i++) {
+        map[i] = -1;
+        for (size_t j = 0; j < nb; j++)
+            if (tc_same_name(a->cell_names[la[i]], b->cell_names[lb[j]]))
+                map[i] = (int)j;
+        if (map[i] < 0)
+            return tc_fail(err, errlen, "the second program has no %s called %s",
+                           what[0] == 'i' ? "input" : "output", a->cell_names[la[i]]);
+    }
+    return 1;
+}
+
+/* The refusals of enum_run (src/enum.c:247-260) and the name matching of enum_match
+   (src/enum.c:48-78).  in_map/out_map get n and noutputs entries. */
+int tc_enum_prepare(const Enum *e, int *in_map, int *out_map, char *err, size_t errlen)
+{
+    if (e->a->special || (e->mode == EN_EQUIV && e->b->special))
+        return tc_fail(err, errlen, "id and link cells connect the lanes, but every input needs "
+                                    "a lane of its own here");
+    if (e->a->ninputs > EN_MAX_IN)
+        return tc_fail(err, errlen, "%zu inputs is too many to try them all (at most %d)",
+                       e->a->ninputs, EN_MAX_IN);
+    if (e->parts < 1 || e->part < 0 || e->part > e->part_end || e->part_end >= e->parts ||
+        e->ticks < 1)
+        return tc_fail(err, errlen, "bad --part or --ticks");
+    if (e->mode != EN_EQUIV && !e->spec)
+        return tc_fail(err, errlen, "%s needs a specification",
+                       e->mode == EN_VERIFY ? "verify" : "search");
+    if (e->mode == EN_EQUIV)
+        return match_names(e->a, e->a->inputs, e->a->ninputs, e->b, e->b->inputs, e->b->ninputs,
+                           in_map, "inputs", err, errlen) &&
+               match_names(e->a, e->a->outputs, e->a->noutputs, e->b, e->b->outputs,
+                           e->b->noutputs, out_map, "outputs", err, errlen);
+    return 1;
+}
+
+/* What a share selection covers: chunks of 64 passes of 512 assignments (src/enum.c:11,
+   215-242).  Fills selected chunks, assignments tried and passes run. */
+void tc_enum_shares(const Enum *e, uint64_t space, uint64_t *sel_chunks, uint64_t *tried,
+                    uint64_t *passes_run)
+{
+    uint64_t passes = (space + 511) / 512, nchunks = (passes + 63) / 64;
+    uint64_t parts = (uint64_t)e->parts, sel = 0, lanes = 0, pruns = 0;
+    uint64_t last = nchunks - 1;
+    uint64_t last_lanes = space - last * 32768, last_passes = passes - last * 64;
+    for (uint64_t r = (uint64_t)e->part; r <= (uint64_t)e->part_end; r++) {
+        if (r >= nchunks)
+            continue;
+        uint64_t count = (nchunks - r + parts - 1) / parts;  /* c = r, r + parts, ... < nchunks */
+        sel += count;
+        int has_last = (last % parts) == r;
+        lanes += (count - (uint64_t)has_last) * 32768 + (has_last ? last_lanes : 0);
+        pruns += (count - (uint64_t)has_last) * 64 + (has_last ? last_passes : 0);
+    }
+    *sel_chunks = sel;
+    *tried = lanes;
+    *passes_run = pruns;
+}
+
+typedef struct {
+    uint64_t words, space, per_warp;
+    uint32_t parts, part, nsel, pad;
+    void    *hits, *list, *count;
+} EnumArgs;
+
+typedef struct {
+    int       *in_map, *out_map;
+    uint32_t  *b_in;
+    TcGenEnum  g;
+} EnumPlan;
+
+static void plan_free(EnumPlan *pl)
+{
+    free(pl->in_map);
+    free(pl->out_map);
+    free(pl->b_in);
+    memset(pl, 0, sizeof *pl);
+}
+
+/* Refusals, name matching and the code generator's input for one enumeration. */
+static int plan_enum(const Enum *e, EnumPlan *pl, char *err, size_t errlen)
+{
+    memset(pl, 0, sizeof *pl);
+    if (!e || !e->a)
+        return tc_fail(err, errlen, "no program");
+    size_t n = e->a->ninputs;
+    pl->in_map = tc_xcalloc(n + 1, sizeof *pl->in_map);
+    pl->out_map = tc_xcalloc(e->a->noutputs + 1, sizeof *pl->out_map);
+    if (!tc_enum_prepare(e, pl->in_map, pl->out_map, err, errlen)) {
+        plan_free(pl);
+        return 0;
+    }
+    TcGenEnum *g = &pl->g;
+    g->mode = e->mode;
+    g->a = e->a;
+    g->spec = (const TcSpec *)e->spec;
+    g->ticks = e->ticks;
+    g->block = TC_ENUM_BLOCK;
+    if (e->mode == EN_EQUIV) {
+        pl->b_in = tc_xcalloc(n + 1, sizeof *pl->b_in);
+        for (size_t k = 0; k < n; k++)
+            pl->b_in[k] = e->b->inputs[pl->in_map[k]];
+        g->b = e->b;
+        g->b_inputs = pl->b_in;
+        g->out_map = pl->out_map;
+    }
+    if (e->mode == EN_SEARCH)
+        g->target = cuda_spec_value(e->spec, 0);
+    return 1;
+}
+
+char *tc_codegen_enum_for(const Enum *e, size_t *len, char *err, size_t errlen)
+{
+    EnumPlan pl;
+    if (!plan_enum(e, &pl, err, errlen))
+        return NULL;
+    char *src = tc_codegen_enum(&pl.g, len);
+    plan_free(&pl);
+    return src;
+}
+
+void tc_free(void *p)
+{
+    free(p);
+}
+
+int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
+{
+    memset(r, 0, sizeof *r);
+    EnumPlan pl;
+    char *src = NULL;
+    int ok = 0;
+    if (!plan_enum(e, &pl, err, errlen))
+        return 0;
+    size_t n = e->a->ninputs;
+    if (!cuda_engine_init(0, err, errlen))
+        goto done;
+    size_t len;
+    src = tc_codegen_enum(&pl.g, &len);
+    static const char *const names[] = {"tc_enum"};
+    TcModule m;
+    if (!tc_module(src, len, names, 1, NULL, &m, err, errlen))
+        goto done;
+
+    uint64_t space = 1ull << n, sel, tried, pruns;
+    tc_enum_shares(e, space, &sel, &tried, &pruns);
+    r->space = space;
+    r->tried = tried;
+    r->ops = pruns * 512 * e->ticks * (e->a->len + (e->mode == EN_EQUIV ? e->b->len : 0));
+
+    int per_sm = 0;
+    if (!tc_cu_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)m.fn[0],
+                                                                     TC_ENUM_BLOCK, 0),
+                     "occupancy", err, errlen))
+        goto done;
+    if (per_sm < 1)
+        per_sm = 1;
+    uint64_t words = sel * 1024;
+    uint64_t blocks = (uint64_t)tc_engine.sms * (uint64_t)per_sm;
+    uint64_t warps_needed = (words + 31) / 32;
+    uint64_t max_blocks = (warps_needed + TC_ENUM_BLOCK / 32 - 1) / (TC_ENUM_BLOCK / 32);
+    if (blocks > max_blocks)
+        blocks = max_blocks ? max_blocks : 1;
+    uint64_t warps = blocks * (TC_ENUM_BLOCK / 32);
+    uint64_t per_warp = (words + warps - 1) / warps;
+    per_warp = (per_warp + 31) / 32 * 32;
+    if (!per_warp)
+        per_warp = 32;
+    if (!tc_scratch(&tc_engine.ws_hits, 8, err, errlen) ||
+        !tc_scratch(&tc_engine.ws_list, warps * 16 * 8, err, errlen) ||
+        !tc_scratch(&tc_engine.ws_count, warps * 4, err, errlen))
+        goto done;
+    CU(cudaMemsetAsync(tc_engine.ws_hits.ptr, 0, 8, tc_engine.stream), "memset");
+    EnumArgs args;
+    memset(&args, 0, sizeof args);
+    args.words = words;
+    args.space = space;
+    args.per_warp = per_warp;
+    args.parts = (uint32_t)e->parts;
+    args.part = (uint32_t)e->part;
+    args.nsel = (uint32_t)(e->part_end - e->part + 1);
+    args.hits = tc_engine.ws_hits.ptr;
+    args.list = tc_engine.ws_list.ptr;
+    args.count = tc_engine.ws_count.ptr;
+    void *params[] = {&args};
+    CU(cudaEventRecord(tc_engine.ev0, tc_engine.stream), "event");
+    CU(cudaLaunchKernel((const void *)m.fn[0], dim3u((unsigned)blocks), dim3u(TC_ENUM_BLOCK),
+                        params, 0, tc_engine.stream),
+       "launch tc_enum");
+    CU(cudaEventRecord(tc_engine.ev1, tc_engine.stream), "event");
+    uint64_t hits = 0;
+    uint32_t *count = tc_xmalloc(warps * 4);
+    uint64_t *list = tc_xmalloc(warps * 16 * 8);
+    cudaError_t rc = cudaMemcpyAsync(&hits, tc_engine.ws_hits.ptr, 8, cudaMemcpyDeviceToHost,
+                                     tc_engine.stream);
+    if (rc == cudaSuccess)
+        rc = cudaMemcpyAsync(count, tc_engine.ws_count.ptr, warps * 4, cudaMemcpyDeviceToHost,
+                             tc_engine.stream);
+    if (rc == cudaSuccess)
+        rc = cudaStreamSynchronize(tc_engine.stream);
+    if (rc != cudaSuccess) {
+        free(count);
+        free(list);
+        tc_cu_check(rc, "tc_enum", err, errlen);
+        goto done;
+    }
+    /* only the warps that recorded something; lists are short */
+    for (uint64_t w = 0; w < warps && r->nhit < EN_SHOW + 0; w++) {
+        if (!count[w])
+            continue;
+        uint64_t got[16];
+        CU(cudaMemcpy(got, (char *)tc_engine.ws_list.ptr + w * 16 * 8, (size_t)count[w] * 8,
+                      cudaMemcpyDeviceToHost),
+           "hits");
+        for (uint32_t i = 0; i < count[w]; i++)
+            cuda_enum_add_hit(r, got[i]);
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
+    r->seconds = ms / 1e3;
+    r->hits = hits;
+    r->threads = (int)(blocks * TC_ENUM_BLOCK);
+    tc_engine.last = m.info;
+    tc_engine.last_kernel_ms = ms;
+    tc_engine.last_grid = (unsigned)blocks;
+    tc_engine.last_block = TC_ENUM_BLOCK;
+    free(count);
+    free(list);
+    ok = 1;
+done:
+fail:
+    free(src);
+    plan_free(&pl);
+    return ok;
+}

@@ -1,0 +1,74 @@
+/* The engine's runtime state and helpers shared by the host files (engine.c, cube.c, batch.c,
+   serve.c, super.c). */
+#ifndef TC_ENGINE_H
+#define TC_ENGINE_H
+
+#include <cuda_runtime_api.h>
+
+#include "tc_host.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TC_ENUM_BLOCK 256
+#define TC_MAX_KERNELS 8
+
+typedef struct {
+    void  *ptr;
+    size_t bytes;
+} TcBuf;
+
+typedef struct {
+    uint64_t hash;
+    double   compile_seconds;
+    size_t   cubin_bytes;
+    int      regs, local_bytes, cached;
+    char     log[2048];
+} TcModInfo;
+
+typedef struct {
+    cudaLibrary_t lib;
+    cudaKernel_t  fn[TC_MAX_KERNELS];
+    TcModInfo     info;
+} TcModule;
+
+typedef struct {
+    int          ready;
+    int          dev;
+    cudaStream_t stream;
+    cudaEvent_t  ev0, ev1;
+    int       sms, cc_major, cc_minor, smem_optin;
+    char      name[256];
+    TcBuf     ws_hits, ws_list, ws_count;
+    /* the last launch, for reports */
+    TcModInfo last;
+    float     last_kernel_ms;
+    unsigned  last_grid, last_block;
+} TcEngine;
+
+extern TcEngine tc_engine;
+
+static inline dim3 dim3u(unsigned x)
+{
+    dim3 d;
+    d.x = x;
+    d.y = 1;
+    d.z = 1;
+    return d;
+}
+
+double tc_now(void);
+int    tc_fail(char *err, size_t errlen, const char *fmt, ...);
+int    tc_cu_check(cudaError_t rc, const char *what, char *err, size_t errlen);
+int    tc_scratch(TcBuf *b, size_t bytes, char *err, size_t errlen);
+int    tc_module(const char *src, size_t len, const char *const *kernels, int nkernels,
+                 const char *extra_opt, TcModule *out, char *err, size_t errlen);
+int    tc_enum_prepare(const Enum *e, int *in_map, int *out_map, char *err, size_t errlen);
+void   tc_enum_shares(const Enum *e, uint64_t space, uint64_t *sel_chunks, uint64_t *tried,
+                      uint64_t *passes_run);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,767 @@
+/* The gate builder and the workload generators, on the host.
+
+   Gates become short NAND/STO runs that leave their result in a cell; a few scratch cells
+   (__t0..__t5, made on first use) are shared by all gates; registers take their new value at the
+   end of the pass.  The runs are the reference's shortest forms (src/build.c:150-333: LD, LDC,
+   the 7-instruction XOR, the 8-instruction mux, the 11-instruction half adder and the
+   19-instruction full adder), and the generators place the same gates in the same order as
+   src/gen.c and src/tester.c, so every program here is instruction-for-instruction the
+   reference's.  That identity is what makes the GPU engine's workloads the reference's
+   workloads; the tests pin it against the reference's own output. */
+#include <stdlib.h>
+#include <string.h>
+
+#include "tc_host.h"
+
+enum { G_BUF, G_NOT, G_AND, G_NAND, G_OR, G_NOR, G_XOR, G_XNOR };
+
+typedef struct {
+    Instr    *code;
+    size_t    len, cap;
+    char    **names;
+    CellInfo *info;
+    uint32_t  ncells, capcells;
+    uint32_t *slots;
+    size_t    nslots;
+    uint32_t *in, *out, *rq, *rd;
+    size_t    nin, capin, nout, capout, nreg, capreg;
+    uint32_t  scratch[6];
+    int       special;
+} Bld;
+
+static uint64_t fnv(const char *s)
+{
+    uint64_t h = 0xcbf29ce484222325ull;
+    for (; *s; s++) {
+        unsigned c = (unsigned char)*s;
+        if (c >= 'A' && c <= 'Z')
+            c += 32;
+        h = (h ^ c) * 0x100000001b3ull;
+    }
+    return h;
+}
+
+static size_t bslot(const Bld *b, const char *name)
+{
+    size_t i = (size_t)fnv(name) & (b->nslots - 1);
+    while (b->slots[i] && !tc_same_name(b->names[b->slots[i] - 1], name))
+        i = (i + 1) & (b->nslots - 1);
+    return i;
+}
+
+static void brehash(Bld *b)
+{
+    free(b->slots);
+    b->nslots = b->nslots ? 2 * b->nslots : 1024;
+    b->slots = tc_xcalloc(b->nslots, sizeof *b->slots);
+    for (uint32_t c = 0; c < b->ncells; c++)
+        b->slots[bslot(b, b->names[c])] = c + 1;
+}
+
+static uint32_t bcell(Bld *b, const char *name)
+{
+    size_t i = bslot(b, name);
+    if (b->slots[i])
+        return b->slots[i] - 1;
+    if (b->ncells == b->capcells) {
+        b->capcells = b->capcells ? 2 * b->capcells : 64;
+        b->names = tc_xrealloc(b->names, b->capcells * sizeof *b->names);
+        b->info = tc_xrealloc(b->info, b->capcells * sizeof *b->info);
+    }
+    uint32_t c = b->ncells++;
+    b->names[c] = tc_xstrdup(name);
+    memset(&b->info[c], 0, sizeof b->info[c]);
+    int d = tc_program_id_name(name);
+    if (d >= 0) {
+        b->info[c].kind = CK_ID;
+        b->info[c].dim = (uint8_t)d;
+        b->special = 1;
+    }
+    b->slots[i] = c + 1;
+    if (2 * (size_t)b->ncells > b->nslots)
+        brehash(b);
+    return c;
+}
+
+static uint32_t bcellf(Bld *b, const char *fmt, int i, int j)
+{
+    char name[64];
+    snprintf(name, sizeof name, fmt, i, j);
+    return bcell(b, name);
+}
+
+static int bhas(const Bld *b, const char *name)
+{
+    return b->slots[bslot(b, name)] != 0;
+}
+
+static uint32_t blink(Bld *b, const char *name, uint32_t src, int dim)
+{
+    uint32_t c = bcell(b, name);
+    b->info[c].kind = CK_LINK;
+    b->info[c].dim = (uint8_t)dim;
+    b->info[c].src = src;
+    b->special = 1;
+    return c;
+}
+
+static Bld *bnew(void)
+{
+    Bld *b = tc_xcalloc(1, sizeof *b);
+    brehash(b);
+    bcell(b, "ZERO");
+    bcell(b, "ONE");
+    return b;
+}
+
+static uint32_t scratch(Bld *b, int i)
+{
+    if (!b->scratch[i]) {
+        char name[8];
+        snprintf(name, sizeof name, "__t%d", i);
+        b->scratch[i] = bcell(b, name);
+    }
+    return b->scratch[i];
+}
+
+static void push_list(uint32_t **list, size_t *n, size_t *cap, uint32_t v)
+{
+    if (*n == *cap) {
+        *cap = *cap ? 2 * *cap : 64;
+        *list = tc_xrealloc(*list, *cap * sizeof **list);
+    }
+    (*list)[(*n)++] = v;
+}
+
+static void binput(Bld *b, uint32_t c) { push_list(&b->in, &b->nin, &b->capin, c); }
+static void boutput(Bld *b, uint32_t c) { push_list(&b->out, &b->nout, &b->capout, c); }
+
+static void breg(Bld *b, uint32_t q, uint32_t d)
+{
+    if (b->nreg == b->capreg) {
+        b->capreg = b->capreg ? 2 * b->capreg : 64;
+        b->rq = tc_xrealloc(b->rq, b->capreg * sizeof *b->rq);
+        b->rd = tc_xrealloc(b->rd, b->capreg * sizeof *b->rd);
+    }
+    b->rq[b->nreg] = q;
+    b->rd[b->nreg++] = d;
+}
+
+static void op(Bld *b, int o, uint32_t c)
+{
+    if (b->len == b->cap) {
+        b->cap = b->cap ? 2 * b->cap : 1024;
+        b->code = tc_xrealloc(b->code, b->cap * sizeof *b->code);
+    }
+    b->code[b->len].op = (uint8_t)o;
+    b->code[b->len].addr = c;
+    b->len++;
+}
+
+static void N(Bld *b, uint32_t c) { op(b, OP_NAND, c); }
+static void S(Bld *b, uint32_t c) { op(b, OP_STO, c); }
+static void load(Bld *b, uint32_t c) { N(b, CELL_ZERO); N(b, c); N(b, CELL_ONE); }   /* RR = c */
+static void loadc(Bld *b, uint32_t c) { N(b, CELL_ZERO); N(b, c); }                /* RR = !c */
+
+/* RR = x ^ y (7 instructions, scratch 0) */
+static void rr_xor(Bld *b, uint32_t x, uint32_t y)
+{
+    uint32_t t = scratch(b, 0);
+    N(b, CELL_ZERO);
+    N(b, x);
+    N(b, y);
+    S(b, t);
+    N(b, y);
+    N(b, x);
+    N(b, t);
+}
+
+static void gate(Bld *b, int type, uint32_t out, const uint32_t *in, int n)
+{
+    switch (type) {
+    case G_BUF:
+        load(b, in[0]);
+        break;
+    case G_NOT:
+        loadc(b, in[0]);
+        break;
+    case G_AND:
+    case G_NAND:
+        load(b, in[0]);
+        for (int i = 1; i < n; i++) {
+            N(b, in[i]);
+            if (i < n - 1)
+                N(b, CELL_ONE);
+        }
+        if ((n == 1) == (type == G_NAND))
+            N(b, CELL_ONE);
+        break;
+    case G_OR:
+    case G_NOR: {
+        uint32_t t = scratch(b, 0);
+        loadc(b, in[0]);
+        for (int i = 1; i < n; i++) {
+            if (i > 1)
+                N(b, CELL_ONE);
+            S(b, t);
+            N(b, in[i]);
+            N(b, t);
+        }
+        if ((n == 1) == (type == G_OR))
+            N(b, CELL_ONE);
+        break;
+    }
+    default: /* G_XOR, G_XNOR */
+        if (n == 1) {
+            load(b, in[0]);
+        } else {
+            uint32_t acc = scratch(b, 2);  /* made before scratch 0, as the reference does */
+            rr_xor(b, in[0], in[1]);
+            for (int i = 2; i < n; i++) {
+                S(b, acc);
+                rr_xor(b, acc, in[i]);
+            }
+        }
+        if (type == G_XNOR)
+            N(b, CELL_ONE);
+        break;
+    }
+    S(b, out);
+}
+
+static void gate2(Bld *b, int type, uint32_t out, uint32_t x, uint32_t y)
+{
+    uint32_t in[2] = {x, y};
+    gate(b, type, out, in, 2);
+}
+
+static void gate1(Bld *b, int type, uint32_t out, uint32_t x)
+{
+    gate(b, type, out, &x, 1);
+}
+
+/* s = x ^ y, k = x & y (11 instructions) */
+static void half_add(Bld *b, uint32_t s, uint32_t k, uint32_t x, uint32_t y)
+{
+    uint32_t t = scratch(b, 0);
+    N(b, CELL_ZERO);
+    N(b, x);
+    N(b, y);
+    S(b, t);
+    N(b, y);
+    N(b, CELL_ONE);
+    S(b, k);
+    N(b, CELL_ONE);
+    N(b, x);
+    N(b, t);
+    S(b, s);
+}
+
+/* s = x ^ y ^ c, k = carry (19 instructions); s may be x or y, k may be c */
+static void full_add(Bld *b, uint32_t s, uint32_t k, uint32_t x, uint32_t y, uint32_t c)
+{
+    uint32_t nx = scratch(b, 0);
+    uint32_t n = scratch(b, 1);
+    uint32_t o = scratch(b, 2);
+    uint32_t q = scratch(b, 3);
+    N(b, CELL_ZERO);
+    N(b, x);
+    S(b, nx);
+    N(b, CELL_ONE);
+    N(b, y);
+    S(b, n);
+    N(b, y);
+    N(b, nx);
+    S(b, o);
+    N(b, n);
+    N(b, c);
+    S(b, q);
+    N(b, c);
+    N(b, n);
+    S(b, k);
+    N(b, CELL_ONE);
+    N(b, o);
+    N(b, q);
+    S(b, s);
+}
+
+/* Registers take their new values at the end of the pass; one whose input is another register's
+   output goes through a staging cell __r<i> first (src/build.c:349-371). */
+static void bfinish(Bld *b, Program *p)
+{
+    unsigned char *is_q = tc_xcalloc(b->ncells + 1, 1);
+    for (size_t r = 0; r < b->nreg; r++)
+        is_q[b->rq[r]] = 1;
+    uint32_t *stage = tc_xcalloc(b->nreg + 1, sizeof *stage);
+    for (size_t r = 0; r < b->nreg; r++)
+        if (is_q[b->rd[r]]) {
+            char name[32];
+            snprintf(name, sizeof name, "__r%zu", r);
+            stage[r] = bcell(b, name);
+            load(b, b->rd[r]);
+            S(b, stage[r]);
+        }
+    for (size_t r = 0; r < b->nreg; r++)
+        if (!stage[r]) {
+            load(b, b->rd[r]);
+            S(b, b->rq[r]);
+        }
+    for (size_t r = 0; r < b->nreg; r++)
+        if (stage[r]) {
+            load(b, stage[r]);
+            S(b, b->rq[r]);
+        }
+    free(stage);
+    free(is_q);
+    memset(p, 0, sizeof *p);
+    p->code = b->code;
+    p->len = b->len;
+    p->ncells = b->ncells;
+    p->cell_names = b->names;
+    p->inputs = b->in;
+    p->ninputs = b->nin;
+    p->outputs = b->out;
+    p->noutputs = b->nout;
+    if (b->special)
+        p->special = b->info;
+    else
+        free(b->info);
+    free(b->rq);
+    free(b->rd);
+    free(b->slots);
+    free(b);
+}
+
+/* ---- the array multiplier (src/gen.c:39-75) ------------------------------------------------ */
+
+/* pc[0 .. 2n-1] = a * bv over n bits: row 0 is a & b0 with the upper half 0; row j adds
+   a & bj into pc[j ..] with a half adder at its low end and full adders above, the carry of the
+   row going into pc[j + n]. */
+static void multiply(Bld *b, const uint32_t *pc, const uint32_t *a, const uint32_t *bv, int n)
+{
+    uint32_t pp = bcell(b, "pp");
+    uint32_t carry = bcell(b, "carry");
+    for (int i = 0; i < n; i++)
+        gate2(b, G_AND, pc[i], a[i], bv[0]);
+    for (int k = n; k < 2 * n; k++)
+        gate1(b, G_BUF, pc[k], CELL_ZERO);
+    for (int j = 1; j < n; j++)
+        for (int i = 0; i < n; i++) {
+            gate2(b, G_AND, pp, a[i], bv[j]);
+            if (i == 0)
+                half_add(b, pc[j], carry, pc[j], pp);
+            else
+                full_add(b, pc[i + j], i == n - 1 ? pc[j + n] : carry, pc[i + j], pp, carry);
+        }
+}
+
+void tc_gen_mul(Program *p, int n)
+{
+    Bld *b = bnew();
+    uint32_t *a = tc_xmalloc((size_t)n * sizeof *a), *bv = tc_xmalloc((size_t)n * sizeof *bv);
+    uint32_t *pc = tc_xmalloc(2 * (size_t)n * sizeof *pc);
+    for (int i = 0; i < n; i++)
+        binput(b, a[i] = bcellf(b, "a%d", i, 0));
+    for (int i = 0; i < n; i++)
+        binput(b, bv[i] = bcellf(b, "b%d", i, 0));
+    for (int k = 0; k < 2 * n; k++)
+        pc[k] = bcellf(b, "p%d", k, 0);
+    multiply(b, pc, a, bv, n);
+    for (int k = 0; k < 2 * n; k++)
+        boutput(b, pc[k]);
+    bfinish(b, p);
+    free(a);
+    free(bv);
+    free(pc);
+}
+
+/* ---- the toy hash (src/gen.c:77-160) -------------------------------------------------------- */
+
+static int coprime_step(int n)
+{
+    static const int m[] = {5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61};
+    for (size_t i = 0; i < sizeof m / sizeof m[0]; i++) {
+        int x = m[i], y = n;
+        while (y) {
+            int t = x % y;
+            x = y;
+            y = t;
+        }
+        if (x == 1)
+            return m[i];
+    }
+    return 0;
+}
+
+static uint64_t round_key(int r, int bits)
+{
+    uint64_t s = (uint64_t)r * 0x9E3779B97F4A7C15ull;  /* splitmix64 of state r: output r + 1 */
+    uint64_t z = tc_splitmix64(&s);
+    return bits == 64 ? z : z & ((1ull << bits) - 1);
+}
+
+uint64_t tc_toyhash(uint64_t x, int n, int rounds)
+{
+    int m = coprime_step(n);
+    for (int r = 0; r < rounds; r++) {
+        uint64_t y = 0, z = 0;
+        for (int i = 0; i < n; i++) {
+            uint64_t xi = (x >> i) & 1, x1 = (x >> ((i + 1) % n)) & 1, x2 = (x >> ((i + 2) % n)) & 1;
+            y |= (xi ^ (~x1 & x2 & 1)) << i;
+        }
+        for (int i = 0; i < n; i++)
+            z |= ((y >> ((m * i + 3) % n)) & 1) << i;
+        x = z ^ round_key(r, n);
+    }
+    return x;
+}
+
+int tc_gen_hash(Program *p, int n, int rounds)
+{
+    int m = coprime_step(n);
+    if (!m)
+        return 0;
+    Bld *b = bnew();
+    uint32_t *cur = tc_xmalloc((size_t)n * sizeof *cur), *nxt = tc_xmalloc((size_t)n * sizeof *nxt);
+    for (int i = 0; i < n; i++)
+        binput(b, cur[i] = bcellf(b, "x%d", i, 0));
+    uint32_t nt = bcell(b, "nt");
+    uint32_t tt = bcell(b, "tt");
+    for (int r = 0; r < rounds; r++) {
+        int bank = r % 2;
+        uint64_t rc = round_key(r, n);
+        for (int i = 0; i < n; i++) {
+            uint32_t y = bcellf(b, "y%d_%d", bank, i);
+            gate1(b, G_NOT, nt, cur[(i + 1) % n]);
+            gate2(b, G_AND, tt, nt, cur[(i + 2) % n]);
+            gate2(b, G_XOR, y, cur[i], tt);
+        }
+        for (int i = 0; i < n; i++) {
+            uint32_t src = bcellf(b, "y%d_%d", bank, (m * i + 3) % n);
+            if ((rc >> i) & 1) {
+                nxt[i] = bcellf(b, "k%d_%d", bank, i);
+                gate1(b, G_NOT, nxt[i], src);
+            } else {
+                nxt[i] = src;
+            }
+        }
+        memcpy(cur, nxt, (size_t)n * sizeof *cur);
+    }
+    for (int i = 0; i < n; i++) {
+        uint32_t h = bcellf(b, "h%d", i, 0);
+        gate1(b, G_BUF, h, cur[i]);
+        boutput(b, h);
+    }
+    bfinish(b, p);
+    free(cur);
+    free(nxt);
+    return 1;
+}
+
+/* ---- Game of Life (src/gen.c:163-319) ------------------------------------------------------- */
+
+/* One generation on the w x h board (registers); halo[(r + 1) * (w + 2) + c + 1] is the cell at
+   row r, column c for r = -1 .. h, c = -1 .. w.  Neighbour count by full and half adders, then
+   alive = c1 & (c0 | self) & !(u | v). */
+static void life_generation(Bld *b, const uint32_t *board, const uint32_t *halo, int w, int h)
+{
+    static const char *const nm[14] = {"s0", "k0", "s1", "k1", "s2", "k2", "c0",
+                                       "k3", "t",  "u",  "c1", "v",  "r1", "r2"};
+    uint32_t x[14];
+    for (int i = 0; i < 14; i++)
+        x[i] = bcell(b, nm[i]);
+    uint32_t s0 = x[0], k0 = x[1], s1 = x[2], k1 = x[3], s2 = x[4], k2 = x[5], c0 = x[6], k3 = x[7],
+             t = x[8], u = x[9], c1 = x[10], v = x[11], r1 = x[12], r2 = x[13];
+    for (int r = 0; r < h; r++)
+        for (int c = 0; c < w; c++) {
+            uint32_t nb[8];
+            int k = 0;
+            for (int dr = -1; dr <= 1; dr++)
+                for (int dc = -1; dc <= 1; dc++)
+                    if (dr || dc)
+                        nb[k++] = halo[(r + 1 + dr) * (w + 2) + c + 1 + dc];
+            full_add(b, s0, k0, nb[0], nb[1], nb[2]);
+            full_add(b, s1, k1, nb[3], nb[4], nb[5]);
+            half_add(b, s2, k2, nb[6], nb[7]);
+            full_add(b, c0, k3, s0, s1, s2);
+            full_add(b, t, u, k0, k1, k2);
+            half_add(b, c1, v, t, k3);
+            uint32_t self = board[r * w + c];
+            uint32_t next = bcellf(b, "n%d_%d", r, c);
+            uint32_t all[3] = {c1, r1, r2};
+            gate2(b, G_OR, r1, c0, self);
+            gate2(b, G_NOR, r2, u, v);
+            gate(b, G_AND, next, all, 3);
+            breg(b, self, next);
+        }
+}
+
+static uint32_t *board_and_halo(Bld *b, int w, int h, uint32_t *board)
+{
+    for (int r = 0; r < h; r++)
+        for (int c = 0; c < w; c++)
+            board[r * w + c] = bcellf(b, "x%d_%d", r, c);
+    return tc_xmalloc((size_t)(w + 2) * (size_t)(h + 2) * sizeof(uint32_t));
+}
+
+void tc_gen_life(Program *p, int w, int h, uint32_t *board)
+{
+    Bld *b = bnew();
+    uint32_t *halo = board_and_halo(b, w, h, board);
+    for (int r = -1; r <= h; r++)
+        for (int c = -1; c <= w; c++)
+            halo[(r + 1) * (w + 2) + c + 1] = board[((r + h) % h) * w + (c + w) % w];
+    life_generation(b, board, halo, w, h);
+    free(halo);
+    bfinish(b, p);
+}
+
+unsigned tc_grid_machine(unsigned row, unsigned col, int cbits)
+{
+    return (row ^ row >> 1) << cbits | (col ^ col >> 1);
+}
+
+/* Masks for a Gray-coded axis over dimensions lo .. lo+k-1: next[j] (prev[j]) is 1 in machines
+   whose next (previous) position is across dimension lo + j (src/gen.c:214-253). */
+static void axis_masks(Bld *b, int lo, int k, uint32_t *next, uint32_t *prev, const char *tag)
+{
+    char name[32];
+    uint32_t id[CUBE_DIMS], v[4];
+    for (int j = 0; j < k; j++) {
+        id[j] = bcellf(b, "ID%d", lo + j, 0);
+        snprintf(name, sizeof name, "%s_n%d", tag, j);
+        next[j] = bcell(b, name);
+        snprintf(name, sizeof name, "%s_v%d", tag, j);
+        prev[j] = bcell(b, name);
+    }
+    for (int i = 0; i < 4; i++) {
+        snprintf(name, sizeof name, "%s_%c", tag, "pqol"[i]);
+        v[i] = bcell(b, name);
+    }
+    uint32_t odd = v[0], even = v[1], below = v[2], low = v[3];
+    gate(b, G_XOR, odd, id, k);
+    gate1(b, G_NOT, even, odd);
+    gate1(b, G_BUF, next[0], even);
+    gate1(b, G_BUF, prev[0], odd);
+    gate1(b, G_BUF, below, CELL_ZERO);
+    for (int j = 0; j < k; j++) {
+        gate1(b, G_NOT, low, below);
+        gate2(b, G_AND, low, low, id[j]);
+        if (j + 1 < k) {
+            gate2(b, G_AND, next[j + 1], low, odd);
+            gate2(b, G_AND, prev[j + 1], low, even);
+        } else {
+            gate2(b, G_AND, low, low, odd);
+            gate2(b, G_OR, next[j], next[j], low);
+        }
+        gate2(b, G_OR, below, below, id[j]);
+    }
+    gate1(b, G_NOT, low, below);
+    gate2(b, G_OR, prev[k - 1], prev[k - 1], low);
+}
+
+/* New cell `name` = src of the machine mask[0..k-1] points to across lo .. lo+k-1. */
+static uint32_t axis_gather(Bld *b, const char *name, uint32_t src, int lo, int k,
+                            const uint32_t *mask)
+{
+    uint32_t t[CUBE_DIMS];
+    uint32_t out = bcell(b, name);
+    char lname[48];
+    for (int j = 0; j < k; j++) {
+        snprintf(lname, sizeof lname, "lk%u_%d", (unsigned)src, lo + j);
+        uint32_t l = bhas(b, lname) ? bcell(b, lname) : blink(b, lname, src, lo + j);
+        t[j] = bcellf(b, "gt%d", j, 0);
+        gate2(b, G_NAND, t[j], mask[j], l);
+    }
+    gate(b, G_NAND, out, t, k);
+    return out;
+}
+
+void tc_gen_life_cube(Program *p, int w, int h, int rbits, int cbits, uint32_t *board)
+{
+    Bld *b = bnew();
+    int W = w + 2;
+    uint32_t *halo = board_and_halo(b, w, h, board);
+    uint32_t right[CUBE_DIMS], left[CUBE_DIMS], down[CUBE_DIMS], up[CUBE_DIMS];
+    char name[32];
+    if (cbits)
+        axis_masks(b, 0, cbits, right, left, "gc");
+    if (rbits)
+        axis_masks(b, cbits, rbits, down, up, "gr");
+    for (int r = 0; r < h; r++)
+        for (int c = 0; c < w; c++)
+            halo[(r + 1) * W + c + 1] = board[r * w + c];
+    for (int r = 0; r < h; r++) {
+        uint32_t last = board[r * w + w - 1], first = board[r * w];
+        snprintf(name, sizeof name, "hw%d", r);
+        halo[(r + 1) * W] = cbits ? axis_gather(b, name, last, 0, cbits, left) : last;
+        snprintf(name, sizeof name, "he%d", r);
+        halo[(r + 1) * W + w + 1] = cbits ? axis_gather(b, name, first, 0, cbits, right) : first;
+    }
+    for (int c = 0; c < W; c++) {
+        uint32_t last = halo[h * W + c], first = halo[W + c];
+        snprintf(name, sizeof name, "hn%d", c);
+        halo[c] = rbits ? axis_gather(b, name, last, cbits, rbits, up) : last;
+        snprintf(name, sizeof name, "hs%d", c);
+        halo[(h + 1) * W + c] = rbits ? axis_gather(b, name, first, cbits, rbits, down) : first;
+    }
+    life_generation(b, board, halo, w, h);
+    free(halo);
+    bfinish(b, p);
+}
+
+/* ---- random programs (src/tester.c:57-81) ---------------------------------------------------- */
+
+static void random_fill(Program *p, uint32_t writable, size_t len, uint64_t seed)
+{
+    p->len = len;
+    p->code = tc_xmalloc((len ? len : 1) * sizeof *p->code);
+    uint64_t s = seed;
+    for (size_t i = 0; i < len; i++) {
+        uint64_t r = tc_splitmix64(&s);
+        p->code[i].op = (uint8_t)(r & 1);
+        p->code[i].addr = p->code[i].op == OP_NAND ? (uint32_t)((r >> 1) % p->ncells)
+                                                   : CELL_FIRST_FREE + (uint32_t)((r >> 1) % writable);
+    }
+}
+
+/* The program `alpha random --cells N --len L --seed S` prints: cells c0.. all declared .out. */
+void tc_random_program(Program *p, uint32_t cells, size_t len, uint64_t seed)
+{
+    memset(p, 0, sizeof *p);
+    p->ncells = cells + CELL_FIRST_FREE;
+    p->cell_names = tc_xmalloc(p->ncells * sizeof *p->cell_names);
+    p->outputs = tc_xmalloc(cells * sizeof *p->outputs);
+    p->noutputs = cells;
+    for (uint32_t a = 0; a < p->ncells; a++) {
+        char name[16];
+        if (a == CELL_ZERO)
+            snprintf(name, sizeof name, "ZERO");
+        else if (a == CELL_ONE)
+            snprintf(name, sizeof name, "ONE");
+        else
+            snprintf(name, sizeof name, "c%u", a - CELL_FIRST_FREE);
+        p->cell_names[a] = tc_xstrdup(name);
+        if (a >= CELL_FIRST_FREE)
+            p->outputs[a - CELL_FIRST_FREE] = a;
+    }
+    random_fill(p, cells, len, seed);
+}
+
+void tc_random_program_in(Program *p, uint32_t cells, uint32_t width, size_t len, uint64_t seed)
+{
+    memset(p, 0, sizeof *p);
+    p->ncells = cells + width + CELL_FIRST_FREE;
+    p->cell_names = tc_xmalloc(p->ncells * sizeof *p->cell_names);
+    p->outputs = tc_xmalloc((cells + 1) * sizeof *p->outputs);
+    p->inputs = tc_xmalloc((width + 1) * sizeof *p->inputs);
+    p->noutputs = cells;
+    p->ninputs = width;
+    for (uint32_t a = 0; a < p->ncells; a++) {
+        char name[16];
+        if (a == CELL_ZERO)
+            snprintf(name, sizeof name, "ZERO");
+        else if (a == CELL_ONE)
+            snprintf(name, sizeof name, "ONE");
+        else if (a < CELL_FIRST_FREE + cells)
+            snprintf(name, sizeof name, "c%u", a - CELL_FIRST_FREE);
+        else
+            snprintf(name, sizeof name, "w%u", a - CELL_FIRST_FREE - cells);
+        p->cell_names[a] = tc_xstrdup(name);
+        if (a >= CELL_FIRST_FREE && a < CELL_FIRST_FREE + cells)
+            p->outputs[a - CELL_FIRST_FREE] = a;
+        else if (a >= CELL_FIRST_FREE + cells)
+            p->inputs[a - CELL_FIRST_FREE - cells] = a;
+    }
+    random_fill(p, cells, len, seed);
+}
+
+/* ---- rewriting by local NAND identities ---------------------------------------------------- */
+
+typedef struct {
+    Instr *code;
+    size_t len, cap;
+} Code;
+
+static void put(Code *c, int o, uint32_t a)
+{
+    if (c->len == c->cap) {
+        c->cap = c->cap ? 2 * c->cap : 256;
+        c->code = tc_xrealloc(c->code, c->cap * sizeof *c->code);
+    }
+    c->code[c->len].op = (uint8_t)o;
+    c->code[c->len].addr = a;
+    c->len++;
+}
+
+/* Each NAND a, with RR = r before it, may become (chosen per instruction by splitmix64(seed)):
+     double negation   NAND ONE; NAND ONE; NAND a
+     commuted operands STO t; NAND ZERO; NAND a; NAND ONE; NAND t          = !(a & r)
+     De Morgan         STO t; NAND ZERO; NAND a; STO u; NAND ZERO; NAND t;
+                       NAND ONE; STO v; NAND u; NAND v                      = !(!r | a) | ... = !(r & a)
+   t, u, v are three new cells (__e0..__e2) that each rewrite writes before it reads, so RR and
+   every original cell hold the same values as in p after every original instruction. */
+void tc_rewrite_program(const Program *p, Program *out, uint64_t seed, int mutate)
+{
+    tc_program_copy(p, out);
+    uint32_t base = p->ncells;
+    out->ncells = p->ncells + 3;
+    out->cell_names = tc_xrealloc(out->cell_names, out->ncells * sizeof *out->cell_names);
+    for (int i = 0; i < 3; i++) {
+        char name[16];
+        snprintf(name, sizeof name, "__e%d", i);
+        out->cell_names[base + (uint32_t)i] = tc_xstrdup(name);
+    }
+    if (out->special) {
+        out->special = tc_xrealloc(out->special, out->ncells * sizeof *out->special);
+        memset(out->special + base, 0, 3 * sizeof *out->special);
+    }
+    uint32_t t = base, u = base + 1, v = base + 2;
+    Code c = {0};
+    uint64_t s = seed ^ 0xA5A5F00DCAFEull;
+    size_t flip = p->len;  /* the negative control changes the last STO: its cell keeps the
+                              value it had, which differs for some input unless that STO was
+                              redundant */
+    for (size_t i = p->len; i-- > 0;)
+        if (p->code[i].op == OP_STO) {
+            flip = i;
+            break;
+        }
+    for (size_t i = 0; i < p->len; i++) {
+        Instr in = p->code[i];
+        if (mutate && i == flip)
+            in.op = OP_NAND;
+        if (in.op != OP_NAND) {
+            put(&c, in.op, in.addr);
+            continue;
+        }
+        uint64_t r = tc_splitmix64(&s) % 8;
+        if (r == 0) {
+            put(&c, OP_NAND, CELL_ONE);
+            put(&c, OP_NAND, CELL_ONE);
+            put(&c, OP_NAND, in.addr);
+        } else if (r == 1) {
+            put(&c, OP_STO, t);
+            put(&c, OP_NAND, CELL_ZERO);
+            put(&c, OP_NAND, in.addr);
+            put(&c, OP_NAND, CELL_ONE);
+            put(&c, OP_NAND, t);
+        } else if (r == 2) {
+            put(&c, OP_STO, t);
+            put(&c, OP_NAND, CELL_ZERO);
+            put(&c, OP_NAND, in.addr);
+            put(&c, OP_STO, u);
+            put(&c, OP_NAND, CELL_ZERO);
+            put(&c, OP_NAND, t);
+            put(&c, OP_NAND, CELL_ONE);
+            put(&c, OP_STO, v);
+            put(&c, OP_NAND, u);
+            put(&c, OP_NAND, v);
+        } else {
+            put(&c, OP_NAND, in.addr);
+        }
+    }
+    free(out->code);
+    out->code = c.code;
+    out->len = c.len;
+}

@@ -1,0 +1,65 @@
+"""Shared helpers: golden cases and programs built by the engine's own generators."""
+from __future__ import annotations
+
+import json
+import os
+
+import tesseract_gb300 as T
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+MODES = {"verify": T.EN_VERIFY, "equiv": T.EN_EQUIV, "search": T.EN_SEARCH}
+
+
+def load(name):
+    with open(os.path.join(GOLDEN, name)) as f:
+        return json.load(f)
+
+
+def program(desc):
+    kind, p = desc["kind"], desc["params"]
+    if kind == "mul":
+        return T.Program.gen_mul(p["bits"])
+    if kind == "hash":
+        return T.Program.gen_hash(p["bits"], p["rounds"])
+    if kind == "life":
+        return T.Program.gen_life(p["size"], p["size"])
+    if kind == "random":
+        return T.Program.random(p["cells"], p["len"], p["seed"])
+    if kind == "random_in":
+        return T.Program.random_in(p["cells"], p["width"], p["len"], p["seed"])
+    if kind == "rewrite":
+        base = T.Program.random_in(p["cells"], p["width"], p["len"], p["seed"])
+        return base.rewrite(p["rseed"], p.get("mutate", False))
+    raise ValueError(kind)
+
+
+def setup(case):
+    """Programs, spec and enum arguments of one golden case."""
+    a = program(case["a"])
+    b = program(case["b"]) if case["mode"] == "equiv" else None
+    spec = None
+    if case["mode"] != "equiv":
+        spec = T.Spec(a, case["spec"], case["mode"] == "verify")
+    part = case.get("part", [0, 0, 1])
+    kw = dict(ticks=case.get("ticks", 1), part=part[0], part_end=part[1], parts=part[2])
+    return MODES[case["mode"]], a, b, spec, kw
+
+
+def same_result(got, want):
+    return (got["space"] == want["space"] and got["tried"] == want["tried"] and
+            got["hits"] == want["hits"] and got["hit"] == want["hit"] and
+            got["ops"] == want["ops"])
+
+
+def case_id(c):
+    s = c["mode"] + "-" + c["a"]["kind"] + "-" + "-".join(str(v) for v in c["a"]["params"].values())
+    if "spec" in c:
+        s += "-" + c["spec"].replace(" ", "")
+    if "b" in c and c["b"]["params"].get("mutate"):
+        s += "-mutated"
+    if "part" in c:
+        s += "-part" + "_".join(map(str, c["part"]))
+    if "ticks" in c:
+        s += "-ticks%d" % c["ticks"]
+    return s

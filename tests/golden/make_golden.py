@@ -1,0 +1,184 @@
+"""Regenerates the golden fixtures in this directory from the reference itself.
+
+    python tests/golden/make_golden.py [path/to/alpha]
+
+Needs the reference's `alpha` binary built from its sources (oracle/Makefile builds it into
+oracle/_ref/alpha on an x86 host that has the sources).  Programs come from the reference's own
+generators (`alpha gen mul|hash`, `alpha random`) wherever it has one; the batched-equivalence
+programs with inputs, which the reference cannot generate, come from this engine's generator and
+are written out as assembly for the reference to read.  Every result is the reference's `--raw`
+output (src/work.c:435-443): "EN mode space tried hits seconds threads ops" and "ENHIT x".
+
+Outputs:
+    programs.json   sha256 of the reference's generator output for each (kind, parameters)
+    enum.json       enumeration cases and the reference's results
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+ALPHA = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "oracle", "_ref", "alpha")
+
+
+def run(args, stdin=None):
+    r = subprocess.run([ALPHA] + args, capture_output=True, text=True)
+    return r.returncode, r.stdout, r.stderr
+
+
+def strip_comments(text):
+    return "".join(l + "\n" for l in text.splitlines() if not l.startswith(";"))
+
+
+def gen_text(kind, params):
+    if kind == "mul":
+        return strip_comments(run(["gen", "mul", "--bits", str(params["bits"])])[1])
+    if kind == "hash":
+        return strip_comments(run(["gen", "hash", "--bits", str(params["bits"]), "--rounds",
+                                   str(params["rounds"])])[1])
+    if kind == "life":
+        return strip_comments(run(["gen", "life", "--size", str(params["size"])])[1])
+    if kind == "random":
+        return strip_comments(run(["random", "--cells", str(params["cells"]), "--len",
+                                   str(params["len"]), "--seed", str(params["seed"])])[1])
+    raise ValueError(kind)
+
+
+def engine_text(kind, params):
+    """Programs the reference cannot generate: this engine's generator, as assembly."""
+    import tesseract_gb300 as T
+    if kind == "random_in":
+        p = T.Program.random_in(params["cells"], params["width"], params["len"], params["seed"])
+    elif kind == "rewrite":
+        base = T.Program.random_in(params["cells"], params["width"], params["len"],
+                                   params["seed"])
+        p = base.rewrite(params["rseed"], params.get("mutate", False))
+    else:
+        raise ValueError(kind)
+    return p.text()
+
+
+def parse_raw(out):
+    res = {"hit": []}
+    for line in out.splitlines():
+        f = line.split()
+        if f and f[0] == "EN":
+            res.update(mode=int(f[1]), space=int(f[2]), tried=int(f[3]), hits=int(f[4]),
+                       ops=int(f[7]))
+        elif f and f[0] == "ENHIT":
+            res["hit"].append(int(f[1], 16))
+    return res
+
+
+def program_file(tmp, prog):
+    kind, params = prog["kind"], prog["params"]
+    text = engine_text(kind, params) if kind in ("random_in", "rewrite") else gen_text(kind, params)
+    path = os.path.join(tmp, hashlib.sha1(json.dumps(prog, sort_keys=True).encode()).hexdigest()
+                        + ".asm")
+    with open(path, "w") as f:
+        f.write(text)
+    return path
+
+
+def cases():
+    mul = lambda b: {"kind": "mul", "params": {"bits": b}}
+    out = []
+    for b in range(1, 9):
+        out.append({"mode": "verify", "a": mul(b), "spec": "p = a * b"})
+    for spec in ["p = a * b + 1", "p = a + b", "p = (a * b) >> 1", "p = a * b - (a << 2)",
+                 "p = ~a & b | 3", "p = -a ^ b", "p = a * b >> 64", "p = a * b << 65",
+                 "p = (a * b) ^ (b << 3)", "p = a * 3 + b * 5 - 7", "p = a & b ^ a | b",
+                 "p = a << b", "p = (a * b) >> (b & 7)"]:
+        out.append({"mode": "verify", "a": mul(6), "spec": spec})
+    # a left side wider than 32 bits: 20 x 20 -> 40-bit product, one share of 65536
+    out.append({"mode": "verify", "a": mul(20), "spec": "p = a * b", "part": [0, 0, 65536]})
+    out.append({"mode": "verify", "a": mul(20), "spec": "p = a * b + 0x100000000",
+                "part": [3, 3, 65536]})
+    out.append({"mode": "verify", "a": mul(18), "spec": "p = a * b ^ (a << 30)",
+                "part": [7, 9, 16384]})
+    # shares, as on the cluster (tests/test_work.c:269-290)
+    for part in ([0, 0, 3], [1, 1, 3], [2, 2, 3], [0, 1, 3], [5, 6, 7]):
+        out.append({"mode": "verify", "a": mul(10), "spec": "p = a * b ^ 1", "part": part})
+    # ticks > 1 on a combinational program: the same answer
+    out.append({"mode": "verify", "a": mul(5), "spec": "p = a * b", "ticks": 3})
+    # search: toy hash preimages (tests/test_work.c:322-376)
+    for bits, rounds, x in ((3, 5, 5), (16, 5, 12345), (20, 8, 777), (24, 8, 0xabcdef)):
+        out.append({"mode": "search", "a": {"kind": "hash", "params": {"bits": bits,
+                                                                         "rounds": rounds}},
+                    "want_x": x, "bits": bits, "rounds": rounds})
+    # equiv: random programs with inputs against rewritten copies, and mutated controls
+    for seed, (cells, width, length) in enumerate([(8, 5, 40), (16, 12, 300), (24, 16, 900),
+                                                   (9, 20, 200), (40, 18, 2000), (64, 22, 4096),
+                                                   (12, 3, 50), (30, 14, 1500)]):
+        base = {"cells": cells, "width": width, "len": length, "seed": 1000 + seed}
+        a = {"kind": "random_in", "params": base}
+        for mutate in (False, True):
+            b = {"kind": "rewrite", "params": dict(base, rseed=77 + seed, mutate=mutate)}
+            out.append({"mode": "equiv", "a": a, "b": b})
+    out.append({"mode": "equiv", "a": {"kind": "random_in", "params": {"cells": 10, "width": 9,
+                                                                       "len": 120, "seed": 5}},
+                "b": {"kind": "rewrite", "params": {"cells": 10, "width": 9, "len": 120,
+                                                    "seed": 5, "rseed": 6, "mutate": True}},
+                "ticks": 4})
+    return out
+
+
+def main():
+    import tesseract_gb300 as T
+    from tesseract_gb300 import build
+    build.build(reference=False)
+    progs = {}
+    for kind, plist in (("mul", [{"bits": b} for b in (1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 16, 18,
+                                                       20)]),
+                        ("hash", [{"bits": b, "rounds": r} for b, r in ((3, 5), (16, 5), (20, 8),
+                                                                        (24, 8), (32, 8),
+                                                                        (40, 8))]),
+                        ("life", [{"size": s} for s in (3, 8, 10, 32)]),
+                        ("random", [{"cells": c, "len": l, "seed": s}
+                                    for c, l, s in ((8, 20, 3), (64, 4096, 1), (100, 1000, 42))])):
+        for params in plist:
+            key = kind + ":" + json.dumps(params, sort_keys=True)
+            progs[key] = hashlib.sha256(gen_text(kind, params).encode()).hexdigest()
+    with open(os.path.join(HERE, "programs.json"), "w") as f:
+        json.dump(progs, f, indent=1, sort_keys=True)
+
+    results = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for c in cases():
+            pa = program_file(tmp, c["a"])
+            args = [c["mode"], pa]
+            if c["mode"] == "equiv":
+                args.append(program_file(tmp, c["b"]))
+            if c["mode"] == "verify":
+                args += ["--spec", c["spec"]]
+            if c["mode"] == "search":
+                target = T.lib().tc_toyhash(c["want_x"] % (1 << c["bits"]), c["bits"],
+                                            c["rounds"])
+                c["spec"] = "h = %d" % target
+                args += ["--want", c["spec"]]
+            if "ticks" in c:
+                args += ["--ticks", str(c["ticks"])]
+            if "part" in c:
+                i, j, k = c["part"]
+                args += ["--part", "%d-%d/%d" % (i, j, k)]
+            args += ["--raw"]
+            rc, out, errtext = run(args)
+            if rc != 0:
+                raise RuntimeError(" ".join(args) + ": " + errtext)
+            c["result"] = parse_raw(out)
+            results.append(c)
+            print(c["mode"], c["a"]["kind"], c.get("spec", ""), c["result"]["hits"], flush=True)
+    with open(os.path.join(HERE, "enum.json"), "w") as f:
+        json.dump(results, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

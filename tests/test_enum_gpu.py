@@ -1,0 +1,94 @@
+"""verify / equiv / search on the GPU through the C ABI (cuda_enum_run), against the reference.
+
+Small and medium cases are compared bit for bit (hit count, the 16 smallest hits, assignments
+tried, ops) with the reference's golden outputs and with the oracle; the full-size workload
+(gen mul --bits 16 over all 2^32 assignments) is checked through size-independent properties:
+zero mismatches against the true spec, every assignment a mismatch against a spec off by one
+(so the 16 smallest hits are 0..15), and a share split that adds up to the whole."""
+import pytest
+
+import oracle as O
+import tesseract_gb300 as T
+from cases import case_id, load, same_result, setup
+
+pytestmark = pytest.mark.gpu
+CASES = load("enum.json")
+
+
+@pytest.mark.parametrize("case", CASES, ids=[case_id(c) for c in CASES])
+def test_gpu_matches_reference_golden(case):
+    mode, a, b, spec, kw = setup(case)
+    got = T.enum_run(mode, a, b, spec, **kw)
+    assert same_result(got, case["result"]), (got, case["result"])
+
+
+def test_gpu_equals_oracle_on_random_equivalences():
+    """Twenty random program pairs with inputs, 14..22 bits, identity-rewritten and mutated."""
+    for seed in range(20):
+        cells, width, length = 8 + (seed * 7) % 57, 14 + seed % 9, 16 + (seed * 331) % 3000
+        a = T.Program.random_in(cells, width, length, seed)
+        for mutate in (False, True):
+            b = a.rewrite(seed + 100, mutate)
+            got = T.enum_run(T.EN_EQUIV, a, b)
+            want = O.enum_run(T.EN_EQUIV, a, b)
+            assert same_result(got, want), (seed, mutate, got, want)
+            if not mutate:
+                assert got["hits"] == 0
+
+
+def test_mul16_verify_full_space():
+    p = T.Program.gen_mul(16)
+    r = T.enum_run(T.EN_VERIFY, p, spec=T.Spec(p, "p = a * b"))
+    assert r["space"] == 1 << 32 and r["tried"] == 1 << 32
+    assert r["hits"] == 0 and r["hit"] == []
+    assert r["ops"] == 6040 * (1 << 32)
+
+
+def test_mul16_verify_every_input_wrong():
+    p = T.Program.gen_mul(16)
+    r = T.enum_run(T.EN_VERIFY, p, spec=T.Spec(p, "p = a * b + 1"))
+    assert r["hits"] == 1 << 32 and r["hit"] == list(range(16))
+
+
+def test_mul16_shares_add_up():
+    p = T.Program.gen_mul(16)
+    s = T.Spec(p, "p = a * b ^ (b & 1)")
+    whole = T.enum_run(T.EN_VERIFY, p, spec=s)
+    parts = [T.enum_run(T.EN_VERIFY, p, spec=s, part=i, part_end=j, parts=5)
+             for i, j in ((0, 1), (2, 2), (3, 4))]
+    assert sum(r["tried"] for r in parts) == 1 << 32
+    assert sum(r["hits"] for r in parts) == whole["hits"] == 1 << 31
+    merged = sorted(h for r in parts for h in r["hit"])[:16]
+    assert merged == whole["hit"]
+
+
+def test_toyhash32_search():
+    """alpha search on gen hash --bits 32 --rounds 8: every preimage of toyhash(0xc0ffee42)."""
+    p = T.Program.gen_hash(32, 8)
+    x = 0xC0FFEE42
+    target = O.toyhash(x, 32, 8)
+    r = T.enum_run(T.EN_SEARCH, p, spec=T.Spec(p, "h = %d" % target, False))
+    rev = int(format(x, "032b")[::-1], 2)  # x0 is input 0, the highest bit of the assignment
+    assert rev in r["hit"]
+    for h in r["hit"]:
+        assert O.toyhash(int(format(h, "032b")[::-1], 2), 32, 8) == target
+
+
+def test_refusals_on_gpu():
+    p = T.Program.from_asm(".in a\n.out o\nNAND ID3\nSTO o\n")
+    with pytest.raises(T.EngineError, match="id and link cells"):
+        T.enum_run(T.EN_SEARCH, p, spec=T.Spec(p, "o = 1", False))
+    q = T.Program.gen_mul(4)
+    with pytest.raises(T.EngineError, match="bad --part"):
+        T.enum_run(T.EN_VERIFY, q, spec=T.Spec(q, "p = a * b"), ticks=0)
+
+
+def test_edge_widths():
+    """0, 1 and 5 inputs (less than one 32-lane word), and a program of length 0."""
+    for text, spec in ((".out o\nNAND ZERO\nSTO o\n", "o = 1"),
+                       (".in a\n.out o\nNAND a\nSTO o\n", "o = ~a"),
+                       (".in a b c d e\n.out o\nNAND a\nNAND b\nSTO o\n", "o = 0"),
+                       (".in a\n.out a\n", "a = a")):
+        p = T.Program.from_asm(text)
+        s = T.Spec(p, spec)
+        assert same_result(T.enum_run(T.EN_VERIFY, p, spec=s), O.enum_ref(T.EN_VERIFY, p, spec=s))
