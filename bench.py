@@ -163,10 +163,12 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--share", type=int, default=1,
+                    help="verify only share 0 of this many (a small case for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -191,8 +193,9 @@ def main():
     lop3 = T.lop3_peak()  # 32-bit LOP3 ops/s
     peak_lane_ops = lop3 * 32
 
+    share = dict(part=0, part_end=0, parts=args.share)
     for _ in range(max(3, args.warmup)):
-        r = T.enum_run(T.EN_VERIFY, p, spec=s)
+        r = T.enum_run(T.EN_VERIFY, p, spec=s, **share)
         assert r["hits"] == 0
     stats = T.last_launch()
 
@@ -202,7 +205,7 @@ def main():
     with Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            r = T.enum_run(T.EN_VERIFY, p, spec=s)
+            r = T.enum_run(T.EN_VERIFY, p, spec=s, **share)
             kernel_s += r["seconds"]
             ops += r["ops"]
             results.append(r["hits"])
@@ -223,12 +226,14 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * kernel_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "assignments_per_step": 1 << 32,
+        "config": {"workload": WORKLOAD + ("" if args.share == 1 else
+                                           f" (share 0 of {args.share})"),
+                   "assignments_per_step": r["tried"],
                    "lane_ops_per_step": ops // args.steps,
                    "l2": "no DRAM inputs: cell state lives in registers and every input word is "
                          "derived from the lane index, so there is nothing to flush",
                    "device": info, "parallelism": f"replicas x{world}"},
-        "result": {"mismatches": 0, "tried_per_step": 1 << 32},
+        "result": {"mismatches": 0, "tried_per_step": r["tried"]},
         "roofline": {"bound": "alu-lop3", "achieved": per_launch, "peak": peak_lane_ops,
                      "unit": "lane-op/s", "frac": per_launch / peak_lane_ops,
                      "peak_source": "measured: cuda_lop3_peak microbenchmark on this GPU "

@@ -173,6 +173,14 @@ int  cuda_cube_load(CudaCube *c, unsigned group, const uint64_t *mem_lines, cons
 int  cuda_cube_store(const CudaCube *c, unsigned group, uint64_t *mem_lines, uint64_t *rr_line,
                      char *err, size_t errlen);
 int  cuda_cube_run(CudaCube *c, uint64_t passes, char *err, size_t errlen);
+/* The whole cube at once, cell-major: cell c of machine m is bit m % 32 of word c * W + m / 32,
+   W = machines / 32 (ncells x W words), and RR as W words; ZERO and ONE keep their values.
+   cuda_cube_kernels: kernel launches per pass (segments, long ones split). */
+int  cuda_cube_read_words(const CudaCube *c, uint32_t *mem, uint32_t *rr, char *err,
+                          size_t errlen);
+int  cuda_cube_write_words(CudaCube *c, const uint32_t *mem, const uint32_t *rr, char *err,
+                           size_t errlen);
+unsigned cuda_cube_kernels(const CudaCube *c);
 
 #ifdef __cplusplus
 }

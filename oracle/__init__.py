@@ -51,6 +51,7 @@ def lib():
         L.orc_dims.restype = C.c_uint
         L.orc_dims.argtypes = [P]
         L.orc_life_scalar.argtypes = [C.POINTER(C.c_uint8), C.c_int, C.c_int]
+        L.orc_life_words.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc_toyhash.restype = C.c_uint64
         L.orc_toyhash.argtypes = [C.c_uint64, C.c_int, C.c_int]
         _lib = L
@@ -84,6 +85,13 @@ def spec_value(spec, x: int) -> int:
 def life_scalar(board: bytearray, w: int, h: int) -> None:
     buf = (C.c_uint8 * (w * h)).from_buffer(board)
     lib().orc_life_scalar(buf, w, h)
+
+
+def life_words(board, gens: int, threads=None):
+    """Game of Life on a torus of packed rows (numpy uint64 array, rows x words, bit j of word k
+    = column 64 k + j), in place, on host threads."""
+    h, w64 = board.shape
+    lib().orc_life_words(board.ctypes.data, w64, h, gens, threads or os.cpu_count() or 1)
 
 
 def toyhash(x: int, bits: int, rounds: int) -> int:

@@ -648,3 +648,85 @@ uint64_t orc_toyhash(uint64_t x, int n, int rounds)
     }
     return x;
 }
+
+/* ---- plain C Game of Life, 64 cells per word ------------------------------------------------- */
+
+/* The same rule as life_scalar (src/gen.c:686-700): a cell is alive next if it has 3 live
+   neighbours, or 2 and is alive now, on a torus.  Rows of w64 words (64 w64 columns, bit j of word
+   k = column 64 k + j), `gens` generations, rows split over `threads` host threads.  The eight
+   neighbour bitmaps are added with bit-sliced full adders (counts 0..8 in four bit planes). */
+typedef struct {
+    const uint64_t *cur;
+    uint64_t       *next;
+    int             w64, h, r0, r1;
+} LifeRows;
+
+static inline uint64_t west(const uint64_t *row, int k, int w64)  /* column c-1 */
+{
+    uint64_t x = row[k], prev = row[(k + w64 - 1) % w64];
+    return (x << 1) | (prev >> 63);
+}
+
+static inline uint64_t east(const uint64_t *row, int k, int w64)  /* column c+1 */
+{
+    uint64_t x = row[k], nxt = row[(k + 1) % w64];
+    return (x >> 1) | (nxt << 63);
+}
+
+static void *life_rows(void *arg)
+{
+    LifeRows *L = arg;
+    int w64 = L->w64, h = L->h;
+    for (int r = L->r0; r < L->r1; r++) {
+        const uint64_t *up = L->cur + (size_t)((r + h - 1) % h) * w64;
+        const uint64_t *me = L->cur + (size_t)r * w64;
+        const uint64_t *dn = L->cur + (size_t)((r + 1) % h) * w64;
+        uint64_t *out = L->next + (size_t)r * w64;
+        for (int k = 0; k < w64; k++) {
+            uint64_t n[8] = {west(up, k, w64), up[k], east(up, k, w64), west(me, k, w64),
+                             east(me, k, w64), west(dn, k, w64), dn[k], east(dn, k, w64)};
+            uint64_t b0 = 0, b1 = 0, b2 = 0, b3 = 0;  /* count bits */
+            for (int i = 0; i < 8; i++) {
+                uint64_t c0 = b0 & n[i];
+                b0 ^= n[i];
+                uint64_t c1 = b1 & c0;
+                b1 ^= c0;
+                uint64_t c2 = b2 & c1;
+                b2 ^= c1;
+                b3 |= c2;
+            }
+            uint64_t three = b0 & b1 & ~b2 & ~b3, two = ~b0 & b1 & ~b2 & ~b3;
+            out[k] = three | (two & me[k]);
+        }
+    }
+    return NULL;
+}
+
+void orc_life_words(uint64_t *board, int w64, int h, int gens, int threads)
+{
+    if (threads < 1)
+        threads = 1;
+    if (threads > h)
+        threads = h;
+    uint64_t *tmp = malloc((size_t)w64 * (size_t)h * sizeof *tmp);
+    pthread_t *tid = calloc((size_t)threads, sizeof *tid);
+    LifeRows *rows = calloc((size_t)threads, sizeof *rows);
+    uint64_t *cur = board, *next = tmp;
+    for (int g = 0; g < gens; g++) {
+        for (int t = 0; t < threads; t++) {
+            rows[t] = (LifeRows){cur, next, w64, h, (int)((long)h * t / threads),
+                                 (int)((long)h * (t + 1) / threads)};
+            pthread_create(&tid[t], NULL, life_rows, &rows[t]);
+        }
+        for (int t = 0; t < threads; t++)
+            pthread_join(tid[t], NULL);
+        uint64_t *s = cur;
+        cur = next;
+        next = s;
+    }
+    if (cur != board)
+        memcpy(board, cur, (size_t)w64 * (size_t)h * sizeof *board);
+    free(tmp);
+    free(tid);
+    free(rows);
+}

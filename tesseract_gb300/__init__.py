@@ -115,6 +115,22 @@ def lib():
                                         C.c_size_t]),
             "tc_codegen_enum": (C.c_void_p, [C.c_void_p, C.POINTER(C.c_size_t)]),
             "cuda_last_launch": (C.c_int, [C.POINTER(LaunchStats)]),
+            "cuda_check": (C.c_int, [P, C.c_uint64, C.c_uint, C.POINTER(CheckResult),
+                                     C.c_char_p, C.c_size_t]),
+            "cuda_cube_new": (C.c_int, [P, C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]),
+            "cuda_cube_free": (None, [C.c_void_p]),
+            "cuda_cube_groups": (C.c_uint, [C.c_void_p]),
+            "cuda_cube_segments": (C.c_uint, [C.c_void_p]),
+            "cuda_cube_kernels": (C.c_uint, [C.c_void_p]),
+            "cuda_cube_load": (C.c_int, [C.c_void_p, C.c_uint, C.c_void_p, C.c_void_p,
+                                         C.c_char_p, C.c_size_t]),
+            "cuda_cube_store": (C.c_int, [C.c_void_p, C.c_uint, C.c_void_p, C.c_void_p,
+                                          C.c_char_p, C.c_size_t]),
+            "cuda_cube_read_words": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p,
+                                               C.c_size_t]),
+            "cuda_cube_write_words": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p,
+                                                C.c_size_t]),
+            "cuda_cube_run": (C.c_int, [C.c_void_p, C.c_uint64, C.c_char_p, C.c_size_t]),
             "cuda_lop3_peak": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double),
                                          C.c_char_p, C.c_size_t]),
         }
@@ -318,6 +334,84 @@ def lop3_peak() -> float:
     if not lib().cuda_lop3_peak(C.byref(ops), C.byref(sec), err, len(err)):
         raise EngineError(err.value.decode())
     return ops.value
+
+
+def check(program: Program, seed: int = 1, ticks: int = 8) -> dict:
+    """`alpha check --engine cuda` (check_lanes, src/check.c:52-113): random state, `ticks`
+    passes on the GPU, every machine compared with the reference machine after every tick."""
+    r, err = CheckResult(), _err()
+    if not lib().cuda_check(program.ptr, seed, ticks, C.byref(r), err, len(err)):
+        raise EngineError(err.value.decode())
+    return {f: getattr(r, f) for f, _ in CheckResult._fields_}
+
+
+class Cube:
+    """A program's cube of machines on the device (LaneCube + jit_cube_run).
+
+    words are cell-major: cell c of machine m is bit m % 32 of word c * W + m // 32, W = machines
+    // 32; RR is W more words.  load/store move one group of 512 machines in the reference's
+    Line layout: ncells lines of 8 uint64."""
+
+    def __init__(self, program: Program):
+        import numpy as np
+        self.np = np
+        self.program = program
+        self.h = C.c_void_p()
+        e = _err()
+        if not lib().cuda_cube_new(program.ptr, C.byref(self.h), e, len(e)):
+            raise EngineError(e.value.decode())
+        self.groups = lib().cuda_cube_groups(self.h)
+        self.machines = self.groups * 512
+        self.W = self.machines // 32
+        self.segments = lib().cuda_cube_segments(self.h)
+        self.kernels = lib().cuda_cube_kernels(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.cuda_cube_free(self.h)
+            self.h = None
+
+    def run(self, passes: int = 1) -> float:
+        e = _err()
+        if not lib().cuda_cube_run(self.h, passes, e, len(e)):
+            raise EngineError(e.value.decode())
+        return last_launch()["kernel_ms"]
+
+    def read(self):
+        np = self.np
+        mem = np.zeros(self.program.ncells * self.W, dtype=np.uint32)
+        rr = np.zeros(self.W, dtype=np.uint32)
+        e = _err()
+        if not lib().cuda_cube_read_words(self.h, mem.ctypes.data, rr.ctypes.data, e, len(e)):
+            raise EngineError(e.value.decode())
+        return mem.reshape(self.program.ncells, self.W), rr
+
+    def write(self, mem, rr=None):
+        np = self.np
+        mem = np.ascontiguousarray(mem, dtype=np.uint32)
+        rr = None if rr is None else np.ascontiguousarray(rr, dtype=np.uint32)
+        e = _err()
+        if not lib().cuda_cube_write_words(self.h, mem.ctypes.data,
+                                           None if rr is None else rr.ctypes.data, e, len(e)):
+            raise EngineError(e.value.decode())
+
+    def load_group(self, g, lines, rr_line=None):
+        np = self.np
+        lines = np.ascontiguousarray(lines, dtype=np.uint64)
+        rr_line = None if rr_line is None else np.ascontiguousarray(rr_line, dtype=np.uint64)
+        e = _err()
+        if not lib().cuda_cube_load(self.h, g, lines.ctypes.data,
+                                    None if rr_line is None else rr_line.ctypes.data, e, len(e)):
+            raise EngineError(e.value.decode())
+
+    def store_group(self, g):
+        np = self.np
+        lines = np.zeros((self.program.ncells, 8), dtype=np.uint64)
+        rr = np.zeros(8, dtype=np.uint64)
+        e = _err()
+        if not lib().cuda_cube_store(self.h, g, lines.ctypes.data, rr.ctypes.data, e, len(e)):
+            raise EngineError(e.value.decode())
+        return lines, rr
 
 
 def device_info() -> str:

@@ -1,0 +1,649 @@
+/* The cube on the GPU: programs with id and link cells over 2^dims machines (dims 9..16), the
+   replacement of LaneCube + jit_cube_run (src/lanes.c:341-415, src/jit.c:526-560, 775-793), and
+   cuda_check, the replacement of check_lanes (src/check.c:52-113).
+
+   Layout.  Machine m is bit m % 32 of word m / 32; the device holds cell c of every machine as
+   W = 2^dims / 32 consecutive words (mem[c * W + w]) and RR as W more.  Per group of 512 machines
+   this is exactly the reference's Line layout (lane k at bit k % 64 of u64 word k / 64), so a
+   group's lines copy in and out with one strided copy.
+
+   One thread runs one word (32 machines) through straight-line generated code; cells are loaded
+   into registers at their first use in a kernel and written back at its end.  A read across a
+   link from machine m reaches machine m ^ M:
+     M bits 0..4   move lanes inside the word (bit swaps, byte permutes, a 16-bit rotate)
+     M bits 5..9   another lane of the same warp: __shfl_xor_sync on the register
+     M bits 10..15 another warp: a load of that word from the cell's memory
+   Warps do not run in lockstep, so the pass is cut into segments as src/jit.c:526-560 cuts it
+   for groups: wherever a segment would both write a cell and read it across a dimension of 10 or
+   more.  Each segment is its own kernel launch; inside a segment every far read sees the value the
+   cell had when the segment started, which is what lockstep shows it.  Long segments are split
+   into kernels of at most TC_CUBE_CHUNK instructions that hand their cells over through memory,
+   so no single kernel is too large for the compiler.  When the whole pass is one kernel and no
+   read crosses warps (at most 1024 machines), the passes loop inside the kernel. */
+#include <pthread.h>
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "codegen.h"
+#include "engine.h"
+#include "ref_host.h"
+
+#define TC_CUBE_BLOCK 32
+#define TC_CUBE_CHUNK 12000
+#define FAR_DIM 10
+
+struct CudaCube {
+    Program     p;
+    unsigned    dims, groups, W, machines;
+    uint32_t   *mem, *rr;   /* device */
+    size_t     *first;      /* kernel k runs instructions first[k] .. first[k + 1] - 1 */
+    unsigned    nk, nseg;
+    int         loop;       /* one kernel, passes loop inside it */
+    cudaKernel_t *fn;
+    cudaGraphExec_t graph;
+    unsigned    graph_passes;
+};
+
+struct CudaCode {
+    CudaCube *cube;
+};
+
+/* ---- the plan --------------------------------------------------------------------------------- */
+
+/* Segment starts: a cut wherever a segment would both write a cell and read it across a far
+   dimension (either order), as late as possible.  Returns the number of segments; first[n] = len. */
+static unsigned find_cuts(const Program *p, size_t *first)
+{
+    uint32_t *stored = tc_xcalloc(p->ncells + 1, sizeof *stored);
+    uint32_t *read = tc_xcalloc(p->ncells + 1, sizeof *read);
+    uint32_t seg = 1;
+    unsigned n = 0;
+    first[n++] = 0;
+    for (size_t i = 0; i < p->len; i++) {
+        Instr in = p->code[i];
+        if (in.op == OP_NAND) {
+            unsigned mask;
+            uint32_t a = tc_program_resolve(p, in.addr, &mask);
+            if ((mask >> FAR_DIM) && !tc_program_readonly(p, a)) {
+                if (stored[a] == seg) {
+                    seg++;
+                    first[n++] = i;
+                }
+                read[a] = seg;
+            }
+        } else if (!tc_program_readonly(p, in.addr)) {
+            if (read[in.addr] == seg) {
+                seg++;
+                first[n++] = i;
+            }
+            stored[in.addr] = seg;
+        }
+    }
+    first[n] = p->len;
+    free(stored);
+    free(read);
+    return n;
+}
+
+/* ---- code generation ------------------------------------------------------------------------ */
+
+typedef struct {
+    char  *s;
+    size_t len, cap;
+} Src;
+
+static void emit(Src *o, const char *fmt, ...)
+{
+    for (;;) {
+        va_list ap;
+        va_start(ap, fmt);
+        size_t room = o->cap - o->len;
+        int k = vsnprintf(o->s ? o->s + o->len : NULL, room, fmt, ap);
+        va_end(ap);
+        if (k >= 0 && (size_t)k < room) {
+            o->len += (size_t)k;
+            return;
+        }
+        o->cap = o->cap ? 2 * o->cap + (size_t)k : 65536 + (size_t)k;
+        o->s = tc_xrealloc(o->s, o->cap);
+    }
+}
+
+static const char *CUBE_PRELUDE =
+    "typedef unsigned int u32;\n"
+    "#define TC_ONES 0xffffffffu\n"
+    "#define TC_FULL 0xffffffffu\n"
+    /* lane k of the word reads lane k ^ mask (mask < 32): swap blocks of 1, 2, 4, 8, 16 lanes */
+    "__device__ __forceinline__ u32 tc_perm(u32 v, const u32 mask)\n{\n"
+    "    if (mask & 1u) v = ((v & 0x55555555u) << 1) | ((v >> 1) & 0x55555555u);\n"
+    "    if (mask & 2u) v = ((v & 0x33333333u) << 2) | ((v >> 2) & 0x33333333u);\n"
+    "    if (mask & 4u) v = ((v & 0x0f0f0f0fu) << 4) | ((v >> 4) & 0x0f0f0f0fu);\n"
+    "    if (mask & 8u) v = __byte_perm(v, 0u, 0x2301);\n"
+    "    if (mask & 16u) v = __funnelshift_l(v, v, 16);\n"
+    "    return v;\n}\n";
+
+/* The word of id cell bit d for machines 32 w .. 32 w + 31 */
+static void id_word(Src *o, unsigned d, unsigned flip)
+{
+    static const char *pat[5] = {"0xaaaaaaaau", "0xccccccccu", "0xf0f0f0f0u", "0xff00ff00u",
+                                 "0xffff0000u"};
+    if (d < 5)
+        emit(o, "%s%s", flip ? "~" : "", pat[d]);
+    else
+        emit(o, "(%s(0u - ((w >> %uu) & 1u)))", flip ? "~" : "", d - 5);
+}
+
+typedef struct {
+    const Program *p;
+    unsigned       W;
+    unsigned char *loaded, *written;
+} Chunk;
+
+static void use_cell(Src *o, Chunk *k, uint32_t c)
+{
+    if (!k->loaded[c]) {
+        emit(o, "    u32 c%u = m[%uu * W];\n", (unsigned)c, (unsigned)c);
+        k->loaded[c] = 1;
+    }
+}
+
+/* Emits the NAND operand expression for cell a (declaring loads first). */
+static void operand(Src *o, Chunk *k, uint32_t a, char *expr, size_t len)
+{
+    const Program *p = k->p;
+    unsigned mask;
+    uint32_t c = tc_program_resolve(p, a, &mask);
+    if (c == CELL_ZERO || c == CELL_ONE) {
+        snprintf(expr, len, "%s", c == CELL_ONE ? "TC_ONES" : "0u");
+        return;
+    }
+    if (p->special && p->special[c].kind == CK_ID) {
+        Src t = {0};
+        unsigned d = p->special[c].dim;
+        id_word(&t, d, (mask >> d) & 1);
+        snprintf(expr, len, "%s", t.s);
+        free(t.s);
+        return;
+    }
+    unsigned hi = mask >> 5, lo = mask & 31;
+    char v[96];
+    if (hi == 0) {
+        use_cell(o, k, c);
+        snprintf(v, sizeof v, "c%u", (unsigned)c);
+    } else if (hi < 32) {
+        use_cell(o, k, c);
+        snprintf(v, sizeof v, "__shfl_xor_sync(TC_FULL, c%u, %uu)", (unsigned)c, hi);
+    } else {
+        snprintf(v, sizeof v, "mem[%uu * W + (w ^ %uu)]", (unsigned)c, hi);
+    }
+    if (lo)
+        snprintf(expr, len, "tc_perm(%s, %uu)", v, lo);
+    else
+        snprintf(expr, len, "%s", v);
+}
+
+static void chunk_body(Src *o, Chunk *k, size_t from, size_t to)
+{
+    const Program *p = k->p;
+    char expr[160];
+    for (size_t i = from; i < to; i++) {
+        Instr in = p->code[i];
+        if (in.op == OP_NAND) {
+            operand(o, k, in.addr, expr, sizeof expr);
+            emit(o, "    r = ~(r & %s);\n", expr);
+        } else if (!tc_program_readonly(p, in.addr)) {
+            if (!k->loaded[in.addr]) {
+                emit(o, "    u32 c%u;\n", (unsigned)in.addr);
+                k->loaded[in.addr] = 1;
+            }
+            emit(o, "    c%u = r;\n", (unsigned)in.addr);
+            k->written[in.addr] = 1;
+        }
+    }
+}
+
+/* One kernel for instructions from .. to-1; with loop != 0 the whole pass, `passes` times. */
+static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size_t from, size_t to,
+                        int loop)
+{
+    Chunk k = {p, W, tc_xcalloc(p->ncells + 1, 1), tc_xcalloc(p->ncells + 1, 1)};
+    emit(o, "extern \"C\" __global__ void __launch_bounds__(%d) tc_cube_%u(u32 *__restrict__ mem, "
+            "u32 *__restrict__ rr, const u32 passes)\n{\n", TC_CUBE_BLOCK, idx);
+    emit(o, "    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;\n");
+    emit(o, "    const u32 w = t & (W - 1u);\n");
+    emit(o, "    u32 *const m = mem + w;\n");
+    emit(o, "    u32 r = rr[w];\n");
+    if (loop) {
+        /* every cell the pass touches is loop-carried: load before the loop */
+        for (size_t i = from; i < to; i++) {
+            unsigned mask;
+            uint32_t a = p->code[i].op == OP_NAND ? tc_program_resolve(p, p->code[i].addr, &mask)
+                                                  : p->code[i].addr;
+            if (a >= CELL_FIRST_FREE && !tc_program_readonly(p, a))
+                use_cell(o, &k, a);
+        }
+        emit(o, "#pragma unroll 1\n    for (u32 pass = 0; pass < passes; pass++) {\n");
+    }
+    chunk_body(o, &k, from, to);
+    if (loop)
+        emit(o, "    }\n");
+    emit(o, "    if (t < W) {\n");
+    for (uint32_t c = CELL_FIRST_FREE; c < p->ncells; c++)
+        if (k.written[c])
+            emit(o, "        m[%uu * W] = c%u;\n", (unsigned)c, (unsigned)c);
+    emit(o, "        rr[w] = r;\n    }\n}\n");
+    free(k.loaded);
+    free(k.written);
+}
+
+char *tc_codegen_cube(const Program *p, const size_t *first, unsigned nk, int block, size_t *len)
+{
+    (void)block;
+    unsigned dims = tc_program_dims(p);
+    unsigned W = (1u << dims) / 32;
+    int loop = nk == 1 && dims <= FAR_DIM;
+    Src o = {0};
+    emit(&o, "// generated by the tesseract GB300 engine: cube of 2^%u machines, %u kernel(s)\n",
+         dims, nk);
+    emit(&o, "#define W %uu\n", W);
+    emit(&o, "%s", CUBE_PRELUDE);
+    for (unsigned k = 0; k < nk; k++)
+        emit_kernel(&o, p, W, k, first[k], first[k + 1], loop);
+    if (len)
+        *len = o.len;
+    return o.s;
+}
+
+/* ---- compilation: kernels in parallel NVRTC programs ---------------------------------------- */
+
+typedef struct {
+    CudaCube *c;
+    unsigned  k0, k1;  /* kernels of this module */
+    int       ok;
+    char      err[512];
+} CompileJob;
+
+static void *compile_job(void *arg)
+{
+    CompileJob *j = arg;
+    CudaCube *c = j->c;
+    size_t len;
+    /* a module with kernels k0..k1-1: generate with shifted indices */
+    unsigned nk = j->k1 - j->k0;
+    size_t *first = tc_xmalloc((nk + 1) * sizeof *first);
+    for (unsigned k = 0; k <= nk; k++)
+        first[k] = c->first[j->k0 + k];
+    int loop = c->nk == 1 && c->dims <= FAR_DIM;
+    Src o = {0};
+    emit(&o, "// generated by the tesseract GB300 engine: cube of 2^%u machines, kernels %u..%u\n",
+         c->dims, j->k0, j->k1 - 1);
+    emit(&o, "#define W %uu\n", c->W);
+    emit(&o, "%s", CUBE_PRELUDE);
+    for (unsigned k = 0; k < nk; k++)
+        emit_kernel(&o, &c->p, c->W, j->k0 + k, first[k], first[k + 1], loop);
+    len = o.len;
+    char **names = tc_xmalloc(nk * sizeof *names);
+    for (unsigned k = 0; k < nk; k++) {
+        names[k] = tc_xmalloc(32);
+        snprintf(names[k], 32, "tc_cube_%u", j->k0 + k);
+    }
+    TcModule m;
+    j->ok = 1;
+    for (unsigned k0 = 0; k0 < nk && j->ok; k0 += TC_MAX_KERNELS) {
+        unsigned n = nk - k0 < TC_MAX_KERNELS ? nk - k0 : TC_MAX_KERNELS;
+        j->ok = tc_module(o.s, len, (const char *const *)names + k0, (int)n, NULL, &m, j->err,
+                          sizeof j->err);
+        for (unsigned k = 0; j->ok && k < n; k++)
+            c->fn[j->k0 + k0 + k] = m.fn[k];
+    }
+    for (unsigned k = 0; k < nk; k++)
+        free(names[k]);
+    free(names);
+    free(first);
+    free(o.s);
+    return NULL;
+}
+
+/* ---- the cube -------------------------------------------------------------------------------- */
+
+unsigned cuda_cube_groups(const CudaCube *c) { return c->groups; }
+unsigned cuda_cube_segments(const CudaCube *c) { return c->nseg; }
+unsigned cuda_cube_kernels(const CudaCube *c) { return c->nk; }
+
+void cuda_cube_free(CudaCube *c)
+{
+    if (!c)
+        return;
+    if (c->graph)
+        cudaGraphExecDestroy(c->graph);
+    cudaFree(c->mem);
+    cudaFree(c->rr);
+    free(c->first);
+    free(c->fn);
+    tc_program_free(&c->p);
+    free(c);
+}
+
+int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
+{
+    *out = NULL;
+    if (!cuda_engine_init(0, err, errlen))
+        return 0;
+    CudaCube *c = tc_xcalloc(1, sizeof *c);
+    tc_program_copy(p, &c->p);
+    c->dims = tc_program_dims(p);
+    c->machines = 1u << c->dims;
+    c->groups = c->machines / 512;
+    c->W = c->machines / 32;
+    size_t *cuts = tc_xmalloc((p->len + 2) * sizeof *cuts);
+    c->nseg = find_cuts(p, cuts);
+    /* split long segments into kernels of at most TC_CUBE_CHUNK instructions */
+    c->first = tc_xmalloc((p->len / TC_CUBE_CHUNK + c->nseg + 2) * sizeof *c->first);
+    c->nk = 0;
+    for (unsigned s = 0; s < c->nseg; s++)
+        for (size_t i = cuts[s]; i < cuts[s + 1] || (i == cuts[s] && cuts[s] == cuts[s + 1]);
+             i += TC_CUBE_CHUNK) {
+            c->first[c->nk++] = i;
+            if (cuts[s] == cuts[s + 1])
+                break;
+        }
+    c->first[c->nk] = p->len;
+    free(cuts);
+    c->loop = c->nk == 1 && c->dims <= FAR_DIM;
+    c->fn = tc_xcalloc(c->nk, sizeof *c->fn);
+    size_t words = (size_t)c->W * (p->ncells + 1);
+    if (!tc_cu_check(cudaMalloc((void **)&c->mem, words * 4), "cudaMalloc", err, errlen) ||
+        !tc_cu_check(cudaMalloc((void **)&c->rr, (size_t)c->W * 4), "cudaMalloc", err, errlen))
+        goto fail;
+    /* power-on state (src/lanes.c:176-192): all 0, ONE all 1, RR 0; id cells are computed */
+    if (!tc_cu_check(cudaMemset(c->mem, 0, words * 4), "cudaMemset", err, errlen) ||
+        !tc_cu_check(cudaMemset(c->mem + (size_t)CELL_ONE * c->W, 0xff, (size_t)c->W * 4),
+                     "cudaMemset", err, errlen) ||
+        !tc_cu_check(cudaMemset(c->rr, 0, (size_t)c->W * 4), "cudaMemset", err, errlen))
+        goto fail;
+    /* compile: modules of up to 2 kernels each, in parallel */
+    unsigned per = 2, nj = (c->nk + per - 1) / per;
+    CompileJob *jobs = tc_xcalloc(nj, sizeof *jobs);
+    pthread_t *tid = tc_xcalloc(nj, sizeof *tid);
+    for (unsigned j = 0; j < nj; j++) {
+        jobs[j].c = c;
+        jobs[j].k0 = j * per;
+        jobs[j].k1 = (j + 1) * per < c->nk ? (j + 1) * per : c->nk;
+        pthread_create(&tid[j], NULL, compile_job, &jobs[j]);
+    }
+    int ok = 1;
+    for (unsigned j = 0; j < nj; j++) {
+        pthread_join(tid[j], NULL);
+        if (!jobs[j].ok && ok) {
+            ok = 0;
+            tc_fail(err, errlen, "%s", jobs[j].err);
+        }
+    }
+    free(jobs);
+    free(tid);
+    if (!ok)
+        goto fail;
+    *out = c;
+    return 1;
+fail:
+    cuda_cube_free(c);
+    return 0;
+}
+
+int cuda_cube_load(CudaCube *c, unsigned g, const uint64_t *lines, const uint64_t *rr, char *err,
+                   size_t errlen)
+{
+    if (g >= c->groups)
+        return tc_fail(err, errlen, "group %u of %u", g, c->groups);
+    uint32_t *dst = c->mem + (size_t)g * 16;
+    if (lines && !tc_cu_check(cudaMemcpy2D(dst, (size_t)c->W * 4, lines, 64, 64, c->p.ncells,
+                                           cudaMemcpyHostToDevice), "load", err, errlen))
+        return 0;
+    /* ZERO and ONE keep their values whatever the host line holds */
+    if (lines && (!tc_cu_check(cudaMemset(c->mem + (size_t)g * 16, 0, 64), "load", err, errlen) ||
+                  !tc_cu_check(cudaMemset(c->mem + (size_t)CELL_ONE * c->W + (size_t)g * 16, 0xff,
+                                          64), "load", err, errlen)))
+        return 0;
+    if (rr && !tc_cu_check(cudaMemcpy(c->rr + (size_t)g * 16, rr, 64, cudaMemcpyHostToDevice),
+                           "load", err, errlen))
+        return 0;
+    return 1;
+}
+
+int cuda_cube_store(const CudaCube *c, unsigned g, uint64_t *lines, uint64_t *rr, char *err,
+                    size_t errlen)
+{
+    if (g >= c->groups)
+        return tc_fail(err, errlen, "group %u of %u", g, c->groups);
+    if (lines && !tc_cu_check(cudaMemcpy2D(lines, 64, c->mem + (size_t)g * 16, (size_t)c->W * 4,
+                                           64, c->p.ncells, cudaMemcpyDeviceToHost),
+                              "store", err, errlen))
+        return 0;
+    if (rr && !tc_cu_check(cudaMemcpy(rr, c->rr + (size_t)g * 16, 64, cudaMemcpyDeviceToHost),
+                           "store", err, errlen))
+        return 0;
+    return 1;
+}
+
+/* Whole-cube copies: cell-major words, W per cell (ncells x W u32), and W words of RR. */
+int cuda_cube_read_words(const CudaCube *c, uint32_t *mem, uint32_t *rr, char *err, size_t errlen)
+{
+    if (mem && !tc_cu_check(cudaMemcpy(mem, c->mem, (size_t)c->W * c->p.ncells * 4,
+                                       cudaMemcpyDeviceToHost), "read", err, errlen))
+        return 0;
+    if (rr && !tc_cu_check(cudaMemcpy(rr, c->rr, (size_t)c->W * 4, cudaMemcpyDeviceToHost), "read",
+                           err, errlen))
+        return 0;
+    return 1;
+}
+
+int cuda_cube_write_words(CudaCube *c, const uint32_t *mem, const uint32_t *rr, char *err,
+                          size_t errlen)
+{
+    if (mem && !tc_cu_check(cudaMemcpy(c->mem, mem, (size_t)c->W * c->p.ncells * 4,
+                                       cudaMemcpyHostToDevice), "write", err, errlen))
+        return 0;
+    if (mem && (!tc_cu_check(cudaMemset(c->mem, 0, (size_t)c->W * 4), "write", err, errlen) ||
+                !tc_cu_check(cudaMemset(c->mem + (size_t)CELL_ONE * c->W, 0xff, (size_t)c->W * 4),
+                             "write", err, errlen)))
+        return 0;
+    if (rr && !tc_cu_check(cudaMemcpy(c->rr, rr, (size_t)c->W * 4, cudaMemcpyHostToDevice), "write",
+                           err, errlen))
+        return 0;
+    return 1;
+}
+
+static int launch_pass(CudaCube *c, cudaStream_t s, unsigned passes)
+{
+    unsigned threads = c->W < 32 ? 32 : c->W;
+    unsigned block = threads < TC_CUBE_BLOCK ? threads : TC_CUBE_BLOCK;
+    unsigned grid = (threads + block - 1) / block;
+    for (unsigned k = 0; k < c->nk; k++) {
+        uint32_t *mem = c->mem, *rr = c->rr;
+        void *args[] = {&mem, &rr, &passes};
+        if (cudaLaunchKernel((const void *)c->fn[k], dim3u(grid), dim3u(block), args, 0, s) !=
+            cudaSuccess)
+            return 0;
+    }
+    return 1;
+}
+
+int cuda_cube_run(CudaCube *c, uint64_t passes, char *err, size_t errlen)
+{
+    cudaStream_t s = tc_engine.stream;
+    if (!tc_cu_check(cudaEventRecord(tc_engine.ev0, s), "event", err, errlen))
+        return 0;
+    if (c->loop) {
+        while (passes) {
+            unsigned n = passes > (1u << 30) ? 1u << 30 : (unsigned)passes;
+            if (!launch_pass(c, s, n))
+                return tc_cu_check(cudaGetLastError(), "cube launch", err, errlen);
+            passes -= n;
+        }
+    } else {
+        /* many passes of several kernels: replay a captured graph of up to 16 passes */
+        const unsigned G = 16;
+        if (passes >= G && !c->graph) {
+            cudaGraph_t g;
+            cudaStream_t cs;
+            if (!tc_cu_check(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream", err,
+                             errlen))
+                return 0;
+            int ok = tc_cu_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal),
+                                 "capture", err, errlen);
+            for (unsigned i = 0; ok && i < G; i++)
+                ok = launch_pass(c, cs, 1);
+            cudaError_t e = cudaStreamEndCapture(cs, &g);
+            if (ok)
+                ok = tc_cu_check(e, "capture", err, errlen);
+            if (ok)
+                ok = tc_cu_check(cudaGraphInstantiate(&c->graph, g, 0), "graph", err, errlen);
+            if (ok)
+                cudaGraphDestroy(g);
+            cudaStreamDestroy(cs);
+            if (!ok)
+                return 0;
+            c->graph_passes = G;
+        }
+        while (c->graph && passes >= c->graph_passes) {
+            if (!tc_cu_check(cudaGraphLaunch(c->graph, s), "graph launch", err, errlen))
+                return 0;
+            passes -= c->graph_passes;
+        }
+        for (; passes; passes--)
+            if (!launch_pass(c, s, 1))
+                return tc_cu_check(cudaGetLastError(), "cube launch", err, errlen);
+    }
+    if (!tc_cu_check(cudaEventRecord(tc_engine.ev1, s), "event", err, errlen) ||
+        !tc_cu_check(cudaEventSynchronize(tc_engine.ev1), "cube run", err, errlen))
+        return 0;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
+    tc_engine.last_kernel_ms = ms;
+    return 1;
+}
+
+/* ---- compiled code handles (jit_compile / jit_free) ----------------------------------------- */
+
+int cuda_compile(const Program *p, CudaCode **out, char *err, size_t errlen)
+{
+    *out = NULL;
+    CudaCube *c;
+    if (!cuda_cube_new(p, &c, err, errlen))
+        return 0;
+    *out = tc_xcalloc(1, sizeof **out);
+    (*out)->cube = c;
+    return 1;
+}
+
+void cuda_free(CudaCode *code)
+{
+    if (!code)
+        return;
+    cuda_cube_free(code->cube);
+    free(code);
+}
+
+/* ---- check_lanes on the GPU ------------------------------------------------------------------- */
+
+static int differ(CheckResult *r, unsigned lane, long cell, unsigned want, unsigned got)
+{
+    r->ok = 0;
+    r->lane = lane;
+    r->cell = cell;
+    r->want = want;
+    r->got = got;
+    return 0;
+}
+
+/* Compares RR and every cell, constants, ids and links included, of every machine, in the
+   order of src/check.c:35-50. */
+static int same_state(const CudaCube *c, const TcRef *ref, const uint32_t *mem, const uint32_t *rr,
+                      CheckResult *r)
+{
+    const Program *p = &c->p;
+    for (unsigned k = 0; k < c->machines; k++) {
+        unsigned got = (rr[k >> 5] >> (k & 31)) & 1;
+        if (got != ref->rr[k])
+            return differ(r, k, -1, ref->rr[k], got);
+        for (uint32_t a = 0; a < p->ncells; a++) {
+            unsigned mask;
+            uint32_t cell = tc_program_resolve(p, a, &mask);
+            unsigned mk = k ^ mask, g;
+            if (p->special && p->special[cell].kind == CK_ID)
+                g = (mk >> p->special[cell].dim) & 1;
+            else
+                g = (mem[(size_t)cell * c->W + (mk >> 5)] >> (mk & 31)) & 1;
+            unsigned want = tc_ref_get(ref, k, a);
+            if (g != want)
+                return differ(r, k, (long)a, want, g);
+        }
+        r->compared++;
+    }
+    return 1;
+}
+
+int cuda_check(const Program *p, uint64_t seed, unsigned ticks, CheckResult *r, char *err,
+               size_t errlen)
+{
+    memset(r, 0, sizeof *r);
+    r->ok = 1;
+    CudaCube *c;
+    if (!cuda_cube_new(p, &c, err, errlen))
+        return 0;
+    TcRef ref;
+    size_t nwords = (size_t)c->W * p->ncells;
+    uint32_t *mem = tc_xcalloc(nwords + 1, 4), *rr = tc_xcalloc(c->W + 1, 4);
+    int ok = 0;
+    if (!tc_ref_init(&ref, p, c->machines)) {
+        tc_fail(err, errlen, "out of memory");
+        goto done;
+    }
+    /* the starting state of src/check.c:60-72: splitmix64(seed), per group every cell from 2 up
+       (kept only where writable), then RR */
+    uint64_t s = seed;
+    for (unsigned g = 0; g < c->groups; g++) {
+        for (uint32_t a = CELL_FIRST_FREE; a < p->ncells; a++)
+            for (int w = 0; w < 8; w++) {
+                uint64_t v = tc_splitmix64(&s);
+                if (tc_program_readonly(p, a))
+                    continue;
+                size_t at = (size_t)a * c->W + (size_t)g * 16 + 2 * (size_t)w;
+                mem[at] = (uint32_t)v;
+                mem[at + 1] = (uint32_t)(v >> 32);
+            }
+        for (int w = 0; w < 8; w++) {
+            uint64_t v = tc_splitmix64(&s);
+            rr[g * 16 + 2 * w] = (uint32_t)v;
+            rr[g * 16 + 2 * w + 1] = (uint32_t)(v >> 32);
+        }
+    }
+    for (uint32_t w = 0; w < c->W; w++)
+        mem[(size_t)CELL_ONE * c->W + w] = 0xffffffffu;
+    for (unsigned k = 0; k < c->machines; k++) {
+        for (uint32_t a = CELL_FIRST_FREE; a < p->ncells; a++)
+            if (!tc_program_readonly(p, a))
+                ref.mem[(size_t)k * p->ncells + a] =
+                    (uint8_t)((mem[(size_t)a * c->W + (k >> 5)] >> (k & 31)) & 1);
+        ref.rr[k] = (uint8_t)((rr[k >> 5] >> (k & 31)) & 1);
+    }
+    if (!cuda_cube_write_words(c, mem, rr, err, errlen))
+        goto done;
+    same_state(c, &ref, mem, rr, r);
+    for (unsigned t = 1; r->ok && t <= ticks; t++) {
+        r->tick = t;
+        r->pc = -1;
+        if (!cuda_cube_run(c, 1, err, errlen) || !cuda_cube_read_words(c, mem, rr, err, errlen))
+            goto done;
+        tc_ref_tick(&ref);
+        same_state(c, &ref, mem, rr, r);
+    }
+    ok = 1;
+done:
+    tc_ref_free(&ref);
+    free(mem);
+    free(rr);
+    cuda_cube_free(c);
+    return ok;
+}
