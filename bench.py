@@ -160,6 +160,96 @@ def run_reference(args):
     return 0
 
 
+def bench_life(args):
+    """Config 2: one 8192 x 8192 B3/S23 board on 65,536 machines (gen_life_cube 32 x 32 tiles,
+    2^8 x 2^8 machines), board from splitmix64(42), `gens` generations on the GPU cube engine,
+    checked bit for bit against plain C Life (the oracle's word-parallel life_scalar)."""
+    import numpy as np
+    import oracle as O
+    import tesseract_gb300 as T
+    from tesseract_gb300 import build
+    from tesseract_gb300.life import LifeCube, pack_rows, unpack_rows
+    build.build(reference=False)
+    t0 = time.perf_counter()
+    L = LifeCube(16)
+    setup_s = time.perf_counter() - t0
+    L.seed(42)
+    start = L.board()
+    L.run(16)                       # warm-up: graph capture, first launches
+    L.seed(42)
+    with Clocks(0) as clk:
+        t0 = time.perf_counter()
+        ms = L.run(args.gens)
+        wall = time.perf_counter() - t0
+    final = L.board()
+    packed = pack_rows(start)
+    tc = time.perf_counter()
+    O.life_words(packed, args.gens)
+    cpu_s = time.perf_counter() - tc
+    ok = bool((unpack_rows(packed) == final).all())
+    n = L.program
+    cells = 8192 * 8192
+    line = {"config": "life", "metric": "generations/s (cube Life, 65,536 machines)",
+            "value": args.gens / (ms / 1e3), "unit": "gen/s", "gens": args.gens,
+            "bit_exact_vs_plain_c": ok, "kernel_ms": ms, "wall_s": wall,
+            "cell_updates_per_s": args.gens * cells / (ms / 1e3),
+            "lane_ops_per_s": args.gens * len(n) * 65536 / (ms / 1e3),
+            "program": {"instructions": len(n), "cells": n.ncells,
+                        "segments": L.cube.segments, "kernels_per_pass": L.cube.kernels},
+            "setup_s_incl_nvrtc": setup_s,
+            "cpu_word_parallel_life_s": cpu_s, "cpu_threads": os.cpu_count()}
+    c = clk.summary()
+    if c:
+        line["clocks"] = c
+    print(json.dumps(line), flush=True)
+    return 0 if ok else 3
+
+
+def bench_batch(args):
+    """Config 3: 4,096 random equivalence jobs (workloads.batch_equiv_jobs) in one persistent
+    launch, against the plain engine (one NVRTC-compiled kernel per job) on a sample."""
+    import tesseract_gb300 as T
+    from tesseract_gb300 import build
+    from tesseract_gb300.workloads import batch_equiv_jobs
+    build.build(reference=False)
+    jobs = batch_equiv_jobs(args.jobs)
+    T.batch_run(jobs[:64])          # warm-up
+    with Clocks(0) as clk:
+        t0 = time.perf_counter()
+        res = T.batch_run(jobs)
+        wall = time.perf_counter() - t0
+    ms = T.last_launch()["kernel_ms"]
+    ops = sum(r["ops"] for r in res)
+    bad_equal = [j["seed"] for j, r in zip(jobs, res) if not j["mutated"] and r["hits"]]
+    controls = [r["hits"] for j, r in zip(jobs, res) if j["mutated"]]
+    # the plain engine, one generated kernel per job, on a sample: compile + run, then cached
+    sample = jobs[:: max(1, len(jobs) // 32)][:32]
+    t0 = time.perf_counter()
+    plain = [T.enum_run(j["mode"], j["a"], j["b"]) for j in sample]
+    plain_cold = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    plain2 = [T.enum_run(j["mode"], j["a"], j["b"]) for j in sample]
+    plain_warm = time.perf_counter() - t0
+    idx = {j["seed"]: i for i, j in enumerate(jobs)}
+    same = all(p["hits"] == q["hits"] == res[idx[j["seed"]]]["hits"] and
+               p["hit"] == res[idx[j["seed"]]]["hit"] for p, q, j in zip(plain, plain2, sample))
+    line = {"config": "batch", "metric": "batched equivalence jobs/s", "jobs": len(jobs),
+            "value": len(jobs) / wall, "unit": "jobs/s", "kernel_ms": ms, "wall_s": wall,
+            "lane_ops_per_s_kernel": ops / (ms / 1e3), "lane_ops": ops,
+            "equal_pairs_with_hits": bad_equal[:10], "negative_controls": len(controls),
+            "negative_controls_detected": sum(1 for h in controls if h),
+            "plain_sample_jobs": len(sample),
+            "plain_jobs_per_s_with_compile": len(sample) / plain_cold,
+            "plain_jobs_per_s_cached": len(sample) / plain_warm,
+            "speedup_vs_plain_cached": (len(jobs) / wall) / (len(sample) / plain_warm),
+            "sample_identical_to_plain": same}
+    c = clk.summary()
+    if c:
+        line["clocks"] = c
+    print(json.dumps(line), flush=True)
+    return 0 if (same and not bad_equal) else 3
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -169,9 +259,18 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--share", type=int, default=1,
                     help="verify only share 0 of this many (a small case for profiling)")
+    ap.add_argument("--config", default="verify", choices=["verify", "life", "batch"],
+                    help="verify: the headline; life: cube Life 2^16 machines, 1000 "
+                         "generations; batch: 4,096 equivalence jobs in one launch")
+    ap.add_argument("--jobs", type=int, default=4096, help="batch: number of jobs")
+    ap.add_argument("--gens", type=int, default=1000, help="life: generations")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "life":
+        return bench_life(args)
+    if args.config == "batch":
+        return bench_batch(args)
 
     world, rank, local = dist_env()
     dist = None

@@ -151,6 +151,15 @@ void cuda_free(CudaCode *c);
 int  cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen);
 void cuda_enum_add_hit(EnumResult *r, uint64_t x);   /* enum_add_hit, src/enum.c:31-46 */
 
+/* Batches.  Runs every job of an array of enumerations (verify, equiv, search; whole spaces, no
+   --part) in one persistent launch of a precompiled interpreter kernel fed from a device work
+   queue, and writes one EnumResult per job with the same fields as cuda_enum_run.  No per-program
+   compilation, so thousands of different programs cost one launch; jobs are refused when their
+   cells exceed the interpreter's 255 shared-memory slots.  No counterpart in the reference, which
+   runs one enumeration per command. */
+int  cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char *err,
+                    size_t errlen);
+
 /* Random-state parity against the reference semantics.  Replaces
    check_lanes(p, jit, seed, ticks, 0, r) (src/check.h:25, src/check.c:52-113): every machine of
    the program's cube gets the same random state from splitmix64(seed) as there, runs `ticks`

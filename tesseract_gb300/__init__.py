@@ -336,6 +336,24 @@ def lop3_peak() -> float:
     return ops.value
 
 
+def batch_run(jobs) -> list:
+    """Many enumerations in one persistent launch (cuda_batch_run).  jobs: iterable of dicts
+    with keys mode, a, b, spec, ticks.  Returns one result dict per job."""
+    jobs = list(jobs)
+    n = len(jobs)
+    structs = [make_enum(j["mode"], j["a"], j.get("b"), j.get("spec"), j.get("ticks", 1))
+               for j in jobs]
+    arr = (C.POINTER(EnumStruct) * max(n, 1))(*[C.pointer(s) for s in structs])
+    res = (EnumResult * max(n, 1))()
+    err = _err()
+    L = lib()
+    L.cuda_batch_run.restype = C.c_int
+    L.cuda_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_char_p, C.c_size_t]
+    if not L.cuda_batch_run(C.cast(arr, C.c_void_p), n, C.cast(res, C.c_void_p), err, len(err)):
+        raise EngineError(err.value.decode())
+    return [res[i].as_dict() for i in range(n)]
+
+
 def check(program: Program, seed: int = 1, ticks: int = 8) -> dict:
     """`alpha check --engine cuda` (check_lanes, src/check.c:52-113): random state, `ticks`
     passes on the GPU, every machine compared with the reference machine after every tick."""

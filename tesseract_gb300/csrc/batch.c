@@ -1,0 +1,341 @@
+/* The batched engine's host side: packs many enumeration jobs (verify, equiv, search) into one
+   set of device arrays, cuts them into work units, runs the persistent interpreter kernel
+   (batch_kernels.cu) and turns its counters back into one EnumResult per job, with the same
+   fields, hits, 16 smallest hits and ops accounting as enum_run (src/enum.c:244-332).
+
+   Nothing here is compiled per program, so a batch of thousands of different programs costs one
+   launch.  Jobs whose cells do not fit the interpreter's slot space (255 slots per job) or that
+   ask for --part shares are refused with an error; cuda_enum_run handles those. */
+#include <stdlib.h>
+#include <string.h>
+
+#include "batch.h"
+#include "engine.h"
+
+
+int tc_batch_launch(const struct TcBatchDev *d, int slots, cudaStream_t stream, int *grid_out,
+                    char *err, size_t errlen);
+
+typedef struct {
+    void  *p;
+    size_t n, cap, elem;
+} Vec;
+
+static size_t vpush(Vec *v, const void *x, size_t count)
+{
+    if (v->n + count > v->cap) {
+        v->cap = v->cap ? 2 * v->cap : 1024;
+        while (v->cap < v->n + count)
+            v->cap *= 2;
+        v->p = tc_xrealloc(v->p, v->cap * v->elem);
+    }
+    memcpy((char *)v->p + v->n * v->elem, x, count * v->elem);
+    size_t at = v->n;
+    v->n += count;
+    return at;
+}
+
+/* Packs program p (its cell c in slot base + c) into bundles: each run of NANDs then STOs,
+   up to 4 and 3 per bundle. */
+static uint32_t pack_code(Vec *code, const Program *p, unsigned base, uint32_t *count)
+{
+    uint32_t first = (uint32_t)code->n, nb = 0;
+    size_t i = 0;
+    while (i < p->len) {
+        uint32_t nN = 0, nS = 0;
+        uint8_t a[4] = {0, 0, 0, 0}, s[3] = {0, 0, 0};
+        while (i < p->len && p->code[i].op == OP_NAND && nN < 4)
+            a[nN++] = (uint8_t)(base + p->code[i++].addr);
+        while (i < p->len && p->code[i].op == OP_STO && nS < 3) {
+            if (!tc_program_readonly(p, p->code[i].addr))
+                s[nS++] = (uint8_t)(base + p->code[i].addr);
+            i++;
+            if (i < p->len && p->code[i].op == OP_NAND)
+                break;
+        }
+        uint64_t b = (uint64_t)(nN | nS << 4) | (uint64_t)a[0] << 8 | (uint64_t)a[1] << 16 |
+                     (uint64_t)a[2] << 24 | (uint64_t)a[3] << 32 | (uint64_t)s[0] << 40 |
+                     (uint64_t)s[1] << 48 | (uint64_t)s[2] << 56;
+        vpush(code, &b, 1);
+        nb++;
+    }
+    *count = nb;
+    return first;
+}
+
+/* Cells that must be 0 before each assignment: read before written, or compared and never
+   written (src/enum.c:90-111 resets the first kind; the second keep their power-on 0). */
+static void clear_list(Vec *lists, const Program *p, unsigned base, const unsigned char *is_input,
+                       uint16_t *n)
+{
+    unsigned char *seen = tc_xcalloc(p->ncells + 1, 1);
+    for (size_t i = 0; i < p->len; i++) {
+        uint32_t c = p->code[i].addr;
+        if (c < CELL_FIRST_FREE || seen[c] || is_input[c])
+            continue;
+        seen[c] = p->code[i].op == OP_NAND ? 2 : 1;
+    }
+    for (uint32_t c = CELL_FIRST_FREE; c < p->ncells; c++)
+        if (!is_input[c] && seen[c] != 1) {  /* read first, or never touched */
+            uint16_t s = (uint16_t)(base + c);
+            vpush(lists, &s, 1);
+            (*n)++;
+        }
+    free(seen);
+}
+
+typedef struct {
+    Vec jobs, code, lists, rpn, vars;
+    uint32_t units;
+    int      slots;
+} Pack;
+
+static int pack_job(Pack *pk, const Enum *e, char *err, size_t errlen)
+{
+    const Program *a = e->a, *b = e->b;
+    size_t n = a->ninputs;
+    int *in_map = tc_xcalloc(n + 1, sizeof *in_map);
+    int *out_map = tc_xcalloc(a->noutputs + 1, sizeof *out_map);
+    int ok = 0;
+    if (!tc_enum_prepare(e, in_map, out_map, err, errlen))
+        goto done;
+    if (e->parts != 1) {
+        tc_fail(err, errlen, "the batched engine runs whole jobs, not --part shares");
+        goto done;
+    }
+    if (e->ticks > 255) {
+        tc_fail(err, errlen, "the batched engine runs at most 255 ticks");
+        goto done;
+    }
+    unsigned slots = a->ncells + (e->mode == EN_EQUIV ? b->ncells : 0);
+    if (slots > TC_BATCH_MAX_SLOTS) {
+        tc_fail(err, errlen, "%u cells: more than the batched engine's %d slots", slots,
+                TC_BATCH_MAX_SLOTS);
+        goto done;
+    }
+    const TcSpec *sp = (const TcSpec *)e->spec;
+    if (e->mode == EN_VERIFY && sp->max_depth > 24) {
+        tc_fail(err, errlen, "the batched engine evaluates specs nested at most 24 deep");
+        goto done;
+    }
+    TcBatchJob J;
+    memset(&J, 0, sizeof J);
+    J.space = 1ull << n;
+    J.words = (J.space + 31) / 32;
+    J.mode = (uint8_t)e->mode;
+    J.ticks = (uint8_t)e->ticks;
+    J.slots = (uint16_t)slots;
+    J.one_a = CELL_ONE;
+    unsigned bb = a->ncells;
+    J.one_b = (uint16_t)(bb + CELL_ONE);
+    J.code_a = pack_code(&pk->code, a, 0, &J.nb_a);
+    if (e->mode == EN_EQUIV)
+        J.code_b = pack_code(&pk->code, b, bb, &J.nb_b);
+    J.lists = (uint32_t)pk->lists.n;
+    J.n_in = (uint16_t)n;
+    unsigned char *in_a = tc_xcalloc(a->ncells + 1, 1);
+    unsigned char *in_b = tc_xcalloc((b ? b->ncells : 0) + 1, 1);
+    for (size_t k = 0; k < n; k++) {
+        uint16_t s[2] = {(uint16_t)a->inputs[k], 0};
+        in_a[a->inputs[k]] = 1;
+        if (e->mode == EN_EQUIV) {
+            uint32_t cb = b->inputs[in_map[k]];
+            s[1] = (uint16_t)(bb + cb);
+            in_b[cb] = 1;
+        }
+        vpush(&pk->lists, s, 2);
+    }
+    clear_list(&pk->lists, a, 0, in_a, &J.n_zero);
+    if (e->mode == EN_EQUIV)
+        clear_list(&pk->lists, b, bb, in_b, &J.n_zero);
+    free(in_a);
+    free(in_b);
+    if (e->mode == EN_EQUIV) {
+        for (size_t o = 0; o < a->noutputs; o++) {
+            uint16_t s[2] = {(uint16_t)a->outputs[o], (uint16_t)(bb + b->outputs[out_map[o]])};
+            vpush(&pk->lists, s, 2);
+        }
+        J.n_cmp = (uint16_t)a->noutputs;
+    } else if (e->mode == EN_SEARCH) {
+        uint64_t target = cuda_spec_value(e->spec, 0);
+        for (int i = 0; i < sp->width; i++) {
+            uint16_t s[2] = {(uint16_t)sp->out[i], (uint16_t)((target >> i) & 1)};
+            vpush(&pk->lists, s, 2);
+        }
+        J.n_cmp = (uint16_t)sp->width;
+    } else {
+        for (int i = 0; i < sp->width; i++) {
+            uint16_t s = (uint16_t)sp->out[i];
+            vpush(&pk->lists, &s, 1);
+        }
+        J.n_cmp = (uint16_t)sp->width;
+        J.rpn = (uint32_t)pk->rpn.n;
+        J.nrpn = (uint16_t)sp->nrpn;
+        for (int i = 0; i < sp->nrpn; i++) {
+            TcBatchRpn it = {(uint32_t)sp->rpn[i].op, 0, sp->rpn[i].v};
+            vpush(&pk->rpn, &it, 1);
+        }
+        J.vars = (uint32_t)pk->vars.n;
+        J.nvars = (uint16_t)sp->nvars;
+        for (int k = 0; k < sp->nvars; k++) {
+            uint8_t d[65];
+            memset(d, 0, sizeof d);
+            d[0] = (uint8_t)sp->var_bits[k];
+            for (int bit = 0; bit < sp->var_bits[k]; bit++)
+                d[1 + bit] = (uint8_t)sp->var_pos[k][bit];
+            vpush(&pk->vars, d, 65);
+        }
+    }
+    J.first_unit = pk->units;
+    J.units = (uint32_t)((J.words + TC_BATCH_UNIT_WORDS - 1) / TC_BATCH_UNIT_WORDS);
+    pk->units += J.units;
+    if ((int)slots > pk->slots)
+        pk->slots = (int)slots;
+    vpush(&pk->jobs, &J, 1);
+    ok = 1;
+done:
+    free(in_map);
+    free(out_map);
+    return ok;
+}
+
+static void *upload(const Vec *v, int *ok, char *err, size_t errlen)
+{
+    void *d = NULL;
+    size_t bytes = (v->n ? v->n : 1) * v->elem;
+    if (!*ok)
+        return NULL;
+    if (!tc_cu_check(cudaMalloc(&d, bytes), "cudaMalloc", err, errlen) ||
+        (v->n && !tc_cu_check(cudaMemcpy(d, v->p, bytes, cudaMemcpyHostToDevice), "upload", err,
+                              errlen))) {
+        *ok = 0;
+        cudaFree(d);
+        return NULL;
+    }
+    return d;
+}
+
+/* Runs every job in one persistent launch.  results[i] is job i's EnumResult; seconds is the
+   device time of the whole batch. */
+int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char *err,
+                   size_t errlen)
+{
+    if (njobs <= 0)
+        return 1;
+    if (!cuda_engine_init(0, err, errlen))
+        return 0;
+    Pack pk;
+    memset(&pk, 0, sizeof pk);
+    pk.jobs.elem = sizeof(TcBatchJob);
+    pk.code.elem = 8;
+    pk.lists.elem = 2;
+    pk.rpn.elem = sizeof(TcBatchRpn);
+    pk.vars.elem = 1;
+    int ok = 1;
+    for (int i = 0; i < njobs && ok; i++) {
+        memset(&results[i], 0, sizeof results[i]);
+        char e2[400];
+        if (!pack_job(&pk, jobs[i], e2, sizeof e2)) {
+            tc_fail(err, errlen, "job %d: %s", i, e2);
+            ok = 0;
+        }
+    }
+    uint32_t *unit_job = NULL;
+    void *d_jobs = NULL, *d_code = NULL, *d_lists = NULL, *d_rpn = NULL, *d_vars = NULL;
+    void *d_unit_job = NULL, *d_next = NULL, *d_hits = NULL, *d_uhits = NULL, *d_ucount = NULL;
+    unsigned long long *hits = NULL, *uhits = NULL;
+    uint32_t *ucount = NULL;
+    if (ok) {
+        unit_job = tc_xmalloc(pk.units * sizeof *unit_job);
+        const TcBatchJob *J = pk.jobs.p;
+        for (int i = 0; i < njobs; i++)
+            for (uint32_t u = 0; u < J[i].units; u++)
+                unit_job[J[i].first_unit + u] = (uint32_t)i;
+        Vec uj = {unit_job, pk.units, pk.units, 4};
+        d_jobs = upload(&pk.jobs, &ok, err, errlen);
+        d_code = upload(&pk.code, &ok, err, errlen);
+        d_lists = upload(&pk.lists, &ok, err, errlen);
+        d_rpn = upload(&pk.rpn, &ok, err, errlen);
+        d_vars = upload(&pk.vars, &ok, err, errlen);
+        d_unit_job = upload(&uj, &ok, err, errlen);
+    }
+    if (ok)
+        ok = tc_cu_check(cudaMalloc(&d_next, 4), "cudaMalloc", err, errlen) &&
+             tc_cu_check(cudaMalloc(&d_hits, (size_t)njobs * 8), "cudaMalloc", err, errlen) &&
+             tc_cu_check(cudaMalloc(&d_uhits, (size_t)pk.units * TC_BATCH_SHOW * 8), "cudaMalloc",
+                         err, errlen) &&
+             tc_cu_check(cudaMalloc(&d_ucount, (size_t)pk.units * 4), "cudaMalloc", err, errlen) &&
+             tc_cu_check(cudaMemsetAsync(d_next, 0, 4, tc_engine.stream), "memset", err, errlen) &&
+             tc_cu_check(cudaMemsetAsync(d_hits, 0, (size_t)njobs * 8, tc_engine.stream),
+                         "memset", err, errlen);
+    float ms = 0;
+    int grid = 0;
+    if (ok) {
+        struct TcBatchDev d = {d_jobs, d_code, d_lists, d_rpn, d_vars, d_unit_job, pk.units,
+                               d_next, d_hits, d_uhits, d_ucount};
+        ok = tc_cu_check(cudaEventRecord(tc_engine.ev0, tc_engine.stream), "event", err, errlen) &&
+             tc_batch_launch(&d, pk.slots, tc_engine.stream, &grid, err, errlen) &&
+             tc_cu_check(cudaEventRecord(tc_engine.ev1, tc_engine.stream), "event", err, errlen) &&
+             tc_cu_check(cudaEventSynchronize(tc_engine.ev1), "batch", err, errlen);
+        if (ok)
+            cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
+    }
+    if (ok) {
+        hits = tc_xmalloc((size_t)njobs * 8);
+        ucount = tc_xmalloc((size_t)pk.units * 4);
+        ok = tc_cu_check(cudaMemcpy(hits, d_hits, (size_t)njobs * 8, cudaMemcpyDeviceToHost),
+                         "download", err, errlen) &&
+             tc_cu_check(cudaMemcpy(ucount, d_ucount, (size_t)pk.units * 4,
+                                    cudaMemcpyDeviceToHost), "download", err, errlen);
+    }
+    if (ok) {
+        const TcBatchJob *J = pk.jobs.p;
+        for (int i = 0; i < njobs && ok; i++) {
+            const Enum *e = jobs[i];
+            EnumResult *r = &results[i];
+            r->space = J[i].space;
+            r->tried = J[i].space;
+            uint64_t passes = (J[i].space + 511) / 512;
+            r->ops = passes * 512 * e->ticks *
+                     (e->a->len + (e->mode == EN_EQUIV ? e->b->len : 0));
+            r->hits = hits[i];
+            r->seconds = ms / 1e3;
+            r->threads = grid * TC_BATCH_BLOCK;
+            for (uint32_t u = 0; u < J[i].units && r->nhit < EN_SHOW && r->hits; u++) {
+                uint32_t c = ucount[J[i].first_unit + u];
+                if (!c)
+                    continue;
+                unsigned long long got[TC_BATCH_SHOW];
+                ok = tc_cu_check(cudaMemcpy(got, (char *)d_uhits + (size_t)(J[i].first_unit + u) *
+                                                                       TC_BATCH_SHOW * 8,
+                                            (size_t)c * 8, cudaMemcpyDeviceToHost),
+                                 "download", err, errlen);
+                for (uint32_t h = 0; ok && h < c; h++)
+                    cuda_enum_add_hit(r, got[h]);
+            }
+        }
+        tc_engine.last_kernel_ms = ms;
+        tc_engine.last_grid = (unsigned)grid;
+        tc_engine.last_block = TC_BATCH_BLOCK;
+    }
+    cudaFree(d_jobs);
+    cudaFree(d_code);
+    cudaFree(d_lists);
+    cudaFree(d_rpn);
+    cudaFree(d_vars);
+    cudaFree(d_unit_job);
+    cudaFree(d_next);
+    cudaFree(d_hits);
+    cudaFree(d_uhits);
+    cudaFree(d_ucount);
+    free(hits);
+    free(uhits);
+    free(ucount);
+    free(unit_job);
+    free(pk.jobs.p);
+    free(pk.code.p);
+    free(pk.lists.p);
+    free(pk.rpn.p);
+    free(pk.vars.p);
+    return ok;
+}

@@ -1,0 +1,47 @@
+"""The benchmark workloads beyond the headline verify, built from the engine's own generators.
+
+batch_equiv_jobs   4,096 random programs with inputs (seeds 0..4095; cells uniform 8..64;
+                   length log-uniform 16..4,096; input width uniform 16..28), each paired with a
+                   copy rewritten by local NAND identities; every `mutate_every`-th pair is a
+                   negative control whose last STO became a NAND.  The parameters of job s come
+                   from splitmix64(s).
+"""
+from __future__ import annotations
+
+import tesseract_gb300 as T
+
+M64 = (1 << 64) - 1
+
+
+def splitmix64(state: int):
+    state = (state + 0x9E3779B97F4A7C15) & M64
+    z = state
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+    return state, z ^ (z >> 31)
+
+
+def job_shape(seed: int):
+    """(cells, width, length) of batch job `seed`."""
+    s = seed * 0x2545F4914F6CDD1D & M64
+    s, r1 = splitmix64(s)
+    s, r2 = splitmix64(s)
+    s, r3 = splitmix64(s)
+    cells = 8 + r1 % 57
+    width = 16 + r2 % 13
+    u = (r3 >> 11) / float(1 << 53)
+    length = int(round(16 * 256 ** u))
+    return cells, width, max(16, min(4096, length))
+
+
+def batch_equiv_jobs(n: int = 4096, mutate_every: int = 8, width_cap: int | None = None):
+    jobs = []
+    for seed in range(n):
+        cells, width, length = job_shape(seed)
+        if width_cap:
+            width = min(width, width_cap)
+        a = T.Program.random_in(cells, width, length, seed)
+        b = a.rewrite(seed, mutate=(seed % mutate_every) == mutate_every - 1)
+        jobs.append(dict(mode=T.EN_EQUIV, a=a, b=b, ticks=1, seed=seed,
+                         mutated=(seed % mutate_every) == mutate_every - 1))
+    return jobs

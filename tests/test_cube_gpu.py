@@ -1,0 +1,100 @@
+"""The cube engine on the GPU: `check --engine cuda` (every machine's full state against the
+reference machine after every tick, src/check.c:52-113) on random programs with and without id and
+link cells over 512 to 4096 machines, and Game of Life on the cube against plain C Life
+(src/work.c:601-622) up to the full 65,536-machine, 8192 x 8192 board."""
+import random
+
+import numpy as np
+import pytest
+
+import oracle as O
+import tesseract_gb300 as T
+from tesseract_gb300.life import LifeCube, pack_rows, unpack_rows
+
+pytestmark = pytest.mark.gpu
+
+
+def random_link_program(seed: int, dims: int, cells: int, links: int, length: int) -> str:
+    """A random program over plain, id and link cells reaching dimensions below `dims`
+    (the shape of tests/test_cube.c:198-241, from Python's own generator)."""
+    rnd = random.Random(seed)
+    names = ["c%d" % i for i in range(cells)]
+    lines = [".out " + " ".join(names[: min(cells, 16)])]
+    readable = list(names) + ["ZERO", "ONE"] + ["ID%d" % d for d in range(dims)]
+    for i in range(links):
+        src = rnd.choice(readable)
+        d = rnd.randrange(dims)
+        if i == 0:
+            d = dims - 1  # the cube spans exactly `dims` dimensions
+        lines.append(".link l%d = %s @ %d" % (i, src, d))
+        readable.append("l%d" % i)
+    for _ in range(length):
+        if rnd.random() < 0.6:
+            lines.append("NAND " + rnd.choice(readable))
+        else:
+            lines.append("STO " + rnd.choice(names))
+    return "\n".join(lines) + "\n"
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_check_random_plain_programs(seed):
+    """Random programs without links (tests/test_jit.c:173-200 style), 512 machines."""
+    rnd = random.Random(seed)
+    p = T.Program.random(rnd.randrange(1, 400), rnd.randrange(1, 3000), seed)
+    r = T.check(p, seed=seed + 1, ticks=3)
+    assert r["ok"], r
+    assert r["compared"] == 512 * 4
+
+
+@pytest.mark.parametrize("seed,dims", [(s, d) for s in range(6) for d in (9, 10, 11, 12)])
+def test_check_random_link_programs(seed, dims):
+    text = random_link_program(seed * 31 + dims, dims, cells=6 + seed * 5, links=4 + seed * 3,
+                               length=40 + seed * 60)
+    p = T.Program.from_asm(text)
+    assert p.dims() == dims
+    r = T.check(p, seed=seed + 7, ticks=4)
+    assert r["ok"], (r, text)
+    assert r["compared"] == (1 << dims) * 5
+
+
+@pytest.mark.parametrize("w,h,rb,cb", [(4, 4, 5, 5), (3, 5, 6, 6), (2, 2, 4, 5)])
+def test_check_life_cube_programs(w, h, rb, cb):
+    p = T.Program.gen_life_cube(w, h, rb, cb)
+    r = T.check(p, seed=3, ticks=3)
+    assert r["ok"], r
+
+
+def life_reference(board: np.ndarray, gens: int) -> np.ndarray:
+    packed = pack_rows(board)
+    O.life_words(packed, gens)
+    return unpack_rows(packed)
+
+
+def test_life_oracle_matches_life_scalar():
+    """The word-parallel plain C Life the checks use equals life_scalar (src/gen.c:686-700)."""
+    rng = np.random.default_rng(5)
+    b = rng.integers(0, 2, size=(64, 128), dtype=np.uint8)
+    want = bytearray(b.tobytes())
+    for _ in range(7):
+        O.life_scalar(want, 128, 64)
+    got = life_reference(b, 7)
+    assert (got == np.frombuffer(bytes(want), dtype=np.uint8).reshape(64, 128)).all()
+
+
+@pytest.mark.parametrize("dims,rbits,gens", [(9, 4, 30), (10, 5, 25), (12, 6, 20), (14, 7, 12)])
+def test_life_cube_small(dims, rbits, gens):
+    L = LifeCube(dims, rbits, w=8, h=8)
+    L.seed(42)
+    start = L.board()
+    L.run(gens)
+    assert (L.board() == life_reference(start, gens)).all()
+
+
+def test_life_dims16_full_board():
+    """The benchmark board: 65,536 machines, 32 x 32 tiles, 8192 x 8192, seed 42."""
+    L = LifeCube(16)
+    assert L.board().shape == (8192, 8192)
+    L.seed(42)
+    start = L.board()
+    L.run(10)
+    assert (L.board() == life_reference(start, 10)).all()
