@@ -103,6 +103,48 @@ typedef struct {
 } CheckResult;
 #endif
 
+/* ---- the superoptimizer (src/super.h:19-72) ---------------------------------------------- */
+#ifndef ALPHA_SUPER_H
+#define ALPHA_SUPER_H
+enum { SUPER_VARS = 6, SUPER_CELLS = 16, SUPER_LEN = 64, SUPER_NAME = 24 };
+typedef struct {
+    int      nvars;      /* input variables; truth tables have 2^nvars rows */
+    uint64_t mask;       /* the 2^nvars rows */
+    int      rr_in;      /* RR's first value is variable 0 */
+    int      rr_out;     /* RR must end as rr_target */
+    uint64_t rr_target;
+    int      ncells;
+    struct {
+        char     name[SUPER_NAME];
+        int      in, out;   /* holds init at the start / must hold target at the end */
+        uint64_t init, target;
+        uint32_t alias;     /* bit i: this output may share input cell i's cell */
+        int      sym_prev;  /* interchangeable inputs: read only after cell sym_prev; -1 none */
+    } cell[SUPER_CELLS];
+} SuperSpec;
+typedef struct {
+    int len;
+    struct {
+        uint8_t op;  /* OP_NAND or OP_STO */
+        char    cell[SUPER_NAME];
+    } code[SUPER_LEN];
+} SuperProg;
+typedef struct {
+    int threads;      /* CPU search only; ignored on the GPU */
+    int part, parts;  /* CPU cluster shares; the GPU search runs the whole tree */
+    int max_cost;
+    int quiet;
+} SuperOpts;
+typedef struct {
+    int       found, cost;    /* the shortest program, and its length */
+    int       below;          /* every program shorter than this was tried: none exists */
+    int       contradiction;  /* found one shorter than `below`: the search is wrong */
+    SuperProg prog;
+    uint64_t  nodes;
+    double    seconds;
+} SuperResult;
+#endif
+
 /* ========================================================================================== */
 /* Entry points.  Each names the reference interface it replaces.                             */
 /* ========================================================================================== */
@@ -159,6 +201,17 @@ void cuda_enum_add_hit(EnumResult *r, uint64_t x);   /* enum_add_hit, src/enum.c
    runs one enumeration per command. */
 int  cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char *err,
                     size_t errlen);
+
+/* The superoptimizer.  cuda_super_parse replaces super_parse (src/super.c:225-371): same
+   language, same SuperSpec.  cuda_super_search replaces super_search (src/super.c:821-896):
+   iterative deepening over the budget from the same lower bound, the same chain-program model
+   and pruning rules, every budget below the answer searched in full on the GPU, so `cost` and
+   `below` mean what they mean there (node counts differ: there is no transposition table).
+   cuda_super_check replaces super_check (src/super.c:908-1001). */
+int  cuda_super_parse(const char *text, SuperSpec *sp, char *err, size_t errlen);
+int  cuda_super_search(const SuperSpec *sp, const SuperOpts *o, SuperResult *r, char *err,
+                       size_t errlen);
+int  cuda_super_check(const SuperSpec *sp, const SuperProg *p, char *err, size_t errlen);
 
 /* Random-state parity against the reference semantics.  Replaces
    check_lanes(p, jit, seed, ticks, 0, r) (src/check.h:25, src/check.c:52-113): every machine of

@@ -65,6 +65,40 @@ class CheckResult(C.Structure):
                 ("got", C.c_uint)]
 
 
+SUPER_CELLS, SUPER_LEN, SUPER_NAME = 16, 64, 24
+
+
+class SuperCell(C.Structure):
+    _fields_ = [("name", C.c_char * SUPER_NAME), ("in_", C.c_int), ("out", C.c_int),
+                ("init", C.c_uint64), ("target", C.c_uint64), ("alias", C.c_uint32),
+                ("sym_prev", C.c_int)]
+
+
+class SuperSpec(C.Structure):
+    _fields_ = [("nvars", C.c_int), ("mask", C.c_uint64), ("rr_in", C.c_int), ("rr_out", C.c_int),
+                ("rr_target", C.c_uint64), ("ncells", C.c_int),
+                ("cell", SuperCell * SUPER_CELLS)]
+
+
+class SuperInstr(C.Structure):
+    _fields_ = [("op", C.c_uint8), ("cell", C.c_char * SUPER_NAME)]
+
+
+class SuperProg(C.Structure):
+    _fields_ = [("len", C.c_int), ("code", SuperInstr * SUPER_LEN)]
+
+
+class SuperOpts(C.Structure):
+    _fields_ = [("threads", C.c_int), ("part", C.c_int), ("parts", C.c_int), ("max_cost", C.c_int),
+                ("quiet", C.c_int)]
+
+
+class SuperResult(C.Structure):
+    _fields_ = [("found", C.c_int), ("cost", C.c_int), ("below", C.c_int),
+                ("contradiction", C.c_int), ("prog", SuperProg), ("nodes", C.c_uint64),
+                ("seconds", C.c_double)]
+
+
 class LaunchStats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("regs", C.c_int), ("local_bytes", C.c_int),
                 ("grid", C.c_uint), ("block", C.c_uint), ("compile_seconds", C.c_double),
@@ -352,6 +386,45 @@ def batch_run(jobs) -> list:
     if not L.cuda_batch_run(C.cast(arr, C.c_void_p), n, C.cast(res, C.c_void_p), err, len(err)):
         raise EngineError(err.value.decode())
     return [res[i].as_dict() for i in range(n)]
+
+
+def super_parse(text: str) -> SuperSpec:
+    sp, err = SuperSpec(), _err()
+    L = lib()
+    L.cuda_super_parse.restype = C.c_int
+    L.cuda_super_parse.argtypes = [C.c_char_p, C.POINTER(SuperSpec), C.c_char_p, C.c_size_t]
+    if not L.cuda_super_parse(text.encode(), C.byref(sp), err, len(err)):
+        raise EngineError(err.value.decode())
+    return sp
+
+
+def super_search(text: str, max_cost: int = 30, quiet: bool = True) -> dict:
+    """`alpha super SPEC` on the GPU: the shortest NAND/STO program, proven (cuda_super_search)."""
+    sp = super_parse(text)
+    o = SuperOpts(0, 0, 1, max_cost, int(quiet))
+    r, err = SuperResult(), _err()
+    L = lib()
+    L.cuda_super_search.restype = C.c_int
+    L.cuda_super_search.argtypes = [C.POINTER(SuperSpec), C.POINTER(SuperOpts),
+                                    C.POINTER(SuperResult), C.c_char_p, C.c_size_t]
+    if not L.cuda_super_search(C.byref(sp), C.byref(o), C.byref(r), err, len(err)):
+        raise EngineError(err.value.decode())
+    prog = [("NAND" if r.prog.code[i].op == OP_NAND else "STO", r.prog.code[i].cell.decode())
+            for i in range(r.prog.len)] if r.found else []
+    ok, why = super_check(sp, r.prog) if r.found else (False, "")
+    return {"found": bool(r.found), "cost": r.cost, "below": r.below,
+            "contradiction": bool(r.contradiction), "nodes": r.nodes, "seconds": r.seconds,
+            "program": prog, "checked": ok, "check_error": why}
+
+
+def super_check(sp: SuperSpec, prog: SuperProg):
+    err = _err()
+    L = lib()
+    L.cuda_super_check.restype = C.c_int
+    L.cuda_super_check.argtypes = [C.POINTER(SuperSpec), C.POINTER(SuperProg), C.c_char_p,
+                                   C.c_size_t]
+    ok = L.cuda_super_check(C.byref(sp), C.byref(prog), err, len(err))
+    return bool(ok), err.value.decode()
 
 
 def check(program: Program, seed: int = 1, ticks: int = 8) -> dict:

@@ -30,7 +30,7 @@ NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 REFERENCE = os.environ.get("TESSERACT_REFERENCE", "/root/reference")
 
-HOST_C = ["program", "asm", "spec", "gen", "codegen", "engine", "cube", "ref_host", "batch",
+HOST_C = ["program", "asm", "spec", "gen", "lutmap", "codegen", "engine", "cube", "ref_host", "batch",
           "serve", "super_host", "cli_support"]
 CUDA_SRC = ["peak_kernels", "batch_kernels", "super_kernels"]
 CFLAGS = ["-std=c11", "-O2", "-g", "-Wall", "-Wextra", "-fPIC", "-D_GNU_SOURCE",

@@ -26,6 +26,7 @@
 #include <string.h>
 
 #include "codegen.h"
+#include "lutmap.h"
 
 typedef struct {
     char  *s;
@@ -57,8 +58,17 @@ static const char *PRELUDE =
     "#define TC_ONES 0xffffffffu\n"
     "#ifndef TC_HOST_EMULATION\n"
     "#define TC_DEV __device__ __forceinline__\n"
+    "#define TC_LOP3(d, a, b, c, tt) asm(\"lop3.b32 %0, %1, %2, %3, \" #tt \";\" "
+    ": \"=r\"(d) : \"r\"(a), \"r\"(b), \"r\"(c))\n"
     "#else\n"
     "#define TC_DEV static inline\n"
+    "#define TC_LOP3(d, a, b, c, tt) ((d) = tc_lop3_host((a), (b), (c), (tt)))\n"
+    "static inline u32 tc_lop3_host(u32 a, u32 b, u32 c, u32 tt)\n{\n"
+    "    u32 r = 0;\n"
+    "    for (int k = 0; k < 8; k++)\n"
+    "        if ((tt >> k) & 1)\n"
+    "            r |= ((k & 4) ? a : ~a) & ((k & 2) ? b : ~b) & ((k & 1) ? c : ~c);\n"
+    "    return r;\n}\n"
     "#endif\n"
     /* lane patterns: bit l of TC_PAT[j] is bit j of l */
     "#define TC_PAT0 0xaaaaaaaau\n#define TC_PAT1 0xccccccccu\n#define TC_PAT2 0xf0f0f0f0u\n"
@@ -114,6 +124,67 @@ static void body(Src *o, const Program *p, const char *pf, const uint32_t *in_ce
     }
     if (ticks > 1)
         emit(o, "    }\n");
+}
+
+/* ---- the program body mapped onto LOP3 ----------------------------------------------------- */
+
+typedef struct {
+    TcNet *net;
+    int   *order;
+    int    norder;
+} Mapped;
+
+/* One pass of p from power-on with input k in leaf k: the network of every cell's final value.
+   cur[c] gets the node holding cell c at the end of the pass. */
+static void build_pass(TcNet *net, const Program *p, const uint32_t *in_cells, size_t n,
+                       const int *leaf_of_input, int *cur)
+{
+    for (uint32_t c = 0; c < p->ncells; c++)
+        cur[c] = 0;
+    cur[CELL_ONE] = 1;
+    for (size_t k = 0; k < n; k++)
+        cur[in_cells[k]] = leaf_of_input[k];
+    int rr = 0;
+    for (size_t i = 0; i < p->len; i++) {
+        Instr in = p->code[i];
+        if (in.op == OP_NAND)
+            rr = tc_net_nand(net, rr, cur[in.addr]);
+        else if (in.addr >= CELL_FIRST_FREE)
+            cur[in.addr] = rr;
+    }
+}
+
+static void node_name(char *buf, size_t len, const TcNet *net, int node)
+{
+    const TcNode *x = tc_net_node(net, node);
+    if (node == 0)
+        snprintf(buf, len, "0u");
+    else if (node == 1)
+        snprintf(buf, len, "TC_ONES");
+    else if (x->kind == TN_LEAF)
+        snprintf(buf, len, "in%d", x->id);
+    else
+        snprintf(buf, len, "n%d", node);
+}
+
+/* Emits the chosen LUTs as lop3.b32 instructions; returns the count. */
+static int emit_luts(Src *o, TcNet *net, const int *want, int nwant)
+{
+    int *order = tc_xmalloc(((size_t)tc_net_size(net) + 1) * sizeof *order), norder = 0;
+    int luts = tc_net_map(net, want, nwant, order, &norder);
+    for (int i = 0; i < norder; i++) {
+        int leaves[3], nl;
+        uint8_t tt;
+        tc_net_lut(net, order[i], leaves, &nl, &tt);
+        char a[32], b[32], c[32];
+        node_name(a, sizeof a, net, leaves[0]);
+        node_name(b, sizeof b, net, nl > 1 ? leaves[1] : 0);
+        node_name(c, sizeof c, net, nl > 2 ? leaves[2] : 0);
+        emit(o, "    u32 n%d; TC_LOP3(n%d, %s, %s, %s, 0x%02x);\n", order[i], order[i], a, b, c,
+             (unsigned)tt);
+    }
+    free(order);
+    return luts;
 }
 
 /* ---- the specification --------------------------------------------------------------------- */
@@ -235,27 +306,61 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         else
             emit(o, "    const u32 in%zu = 0u - (u32)((word >> %d) & 1ull);\n", k, j - 5);
     }
-    body(o, a, "a", a->inputs, n, g->ticks);
-    if (g->mode == EN_EQUIV)
-        body(o, g->b, "b", g->b_inputs, n, g->ticks);
     const TcSpec *s = g->spec;
+    /* the cells compared, as (program, cell) pairs: a first */
+    char (*val_a)[24] = tc_xcalloc(a->ncells + 1, sizeof *val_a);
+    char (*val_b)[24] = tc_xcalloc((g->b ? g->b->ncells : 0) + 1, sizeof *val_b);
+    if (g->ticks == 1 && !g->no_map) {
+        TcNet *net = tc_net_new();
+        int *leaf = tc_xmalloc((n + 1) * sizeof *leaf);
+        for (size_t k = 0; k < n; k++)
+            leaf[k] = tc_net_leaf(net, (int)k);
+        int *cur_a = tc_xmalloc((a->ncells + 1) * sizeof *cur_a);
+        int *cur_b = g->b ? tc_xmalloc((g->b->ncells + 1) * sizeof *cur_b) : NULL;
+        build_pass(net, a, a->inputs, n, leaf, cur_a);
+        if (g->mode == EN_EQUIV)
+            build_pass(net, g->b, g->b_inputs, n, leaf, cur_b);
+        int *want = tc_xmalloc(((size_t)a->noutputs * 2 + 65) * sizeof *want), nwant = 0;
+        if (g->mode == EN_EQUIV)
+            for (size_t k = 0; k < a->noutputs; k++) {
+                want[nwant++] = cur_a[a->outputs[k]];
+                want[nwant++] = cur_b[g->b->outputs[g->out_map[k]]];
+            }
+        else
+            for (int bit = 0; bit < s->width; bit++)
+                want[nwant++] = cur_a[s->out[bit]];
+        int luts = emit_luts(o, net, want, nwant);
+        emit(o, "    // %d LOP3 for %zu + %zu NAND/STO instructions\n", luts, a->len,
+             g->b ? g->b->len : (size_t)0);
+        for (uint32_t c = 0; c < a->ncells; c++)
+            node_name(val_a[c], sizeof val_a[c], net, cur_a[c]);
+        for (uint32_t c = 0; g->mode == EN_EQUIV && c < g->b->ncells; c++)
+            node_name(val_b[c], sizeof val_b[c], net, cur_b[c]);
+        free(want);
+        free(cur_a);
+        free(cur_b);
+        free(leaf);
+        tc_net_free(net);
+    } else {
+        body(o, a, "a", a->inputs, n, g->ticks);
+        if (g->mode == EN_EQUIV)
+            body(o, g->b, "b", g->b_inputs, n, g->ticks);
+        for (uint32_t c = 0; c < a->ncells; c++)
+            snprintf(val_a[c], sizeof val_a[c], c == 0 ? "0u" : c == 1 ? "TC_ONES" : "a%u", c);
+        for (uint32_t c = 0; g->mode == EN_EQUIV && c < g->b->ncells; c++)
+            snprintf(val_b[c], sizeof val_b[c], c == 0 ? "0u" : c == 1 ? "TC_ONES" : "b%u", c);
+    }
     if (g->mode == EN_SEARCH) {
         emit(o, "    u32 m = TC_ONES;\n");
         for (int b = 0; b < s->width; b++) {
             int bit = (int)((g->target >> b) & 1);
-            emit(o, "    m &= %s", bit ? "" : "~");
-            operand(o, "a", s->out[b]);
-            emit(o, ";\n");
+            emit(o, "    m &= %s%s;\n", bit ? "" : "~", val_a[s->out[b]]);
         }
     } else if (g->mode == EN_EQUIV) {
         emit(o, "    u32 m = 0u;\n");
-        for (size_t k = 0; k < a->noutputs; k++) {
-            emit(o, "    m |= ");
-            operand(o, "a", a->outputs[k]);
-            emit(o, " ^ ");
-            operand(o, "b", g->b->outputs[g->out_map[k]]);
-            emit(o, ";\n");
-        }
+        for (size_t k = 0; k < a->noutputs; k++)
+            emit(o, "    m |= %s ^ %s;\n", val_a[a->outputs[k]],
+                 val_b[g->b->outputs[g->out_map[k]]]);
     } else {
         int narrow = spec_fits_32(s);
         emit(o, "    const u64 xw = word << 5;\n");
@@ -271,12 +376,11 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         if (!narrow)
             emit(o, "    tc_transpose32(eh);\n");
         emit(o, "    u32 m = 0u;\n");
-        for (int b = 0; b < s->width; b++) {
-            emit(o, "    m |= ");
-            operand(o, "a", s->out[b]);
-            emit(o, " ^ %s[%d];\n", b < 32 ? "e" : "eh", b & 31);
-        }
+        for (int b = 0; b < s->width; b++)
+            emit(o, "    m |= %s ^ %s[%d];\n", val_a[s->out[b]], b < 32 ? "e" : "eh", b & 31);
     }
+    free(val_a);
+    free(val_b);
     emit(o, "    return m;\n}\n");
 }
 

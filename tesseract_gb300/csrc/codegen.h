@@ -17,6 +17,7 @@ typedef struct {
     uint64_t        target;     /* search: the constant right side */
     unsigned        ticks;
     int             block;      /* threads per block */
+    int             no_map;     /* 1: keep the NAND/STO body as written (no LOP3 mapping) */
 } TcGenEnum;
 
 /* CUDA C for the enumeration kernel `tc_enum` (malloc'd; *len gets its length).  The per-word

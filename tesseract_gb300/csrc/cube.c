@@ -27,11 +27,15 @@
 
 #include "codegen.h"
 #include "engine.h"
+#include "lutmap.h"
 #include "ref_host.h"
 
 #define TC_CUBE_BLOCK 32
 #define TC_CUBE_CHUNK 12000
 #define FAR_DIM 10
+
+/* 1: cube kernels are LOP3-mapped networks (lutmap.c); 0: the instructions as written */
+int tc_cube_map = 1;
 
 struct CudaCube {
     Program     p;
@@ -114,6 +118,8 @@ static const char *CUBE_PRELUDE =
     "typedef unsigned int u32;\n"
     "#define TC_ONES 0xffffffffu\n"
     "#define TC_FULL 0xffffffffu\n"
+    "#define TC_LOP3(d, a, b, c, tt) asm(\"lop3.b32 %0, %1, %2, %3, \" #tt \";\" "
+    ": \"=r\"(d) : \"r\"(a), \"r\"(b), \"r\"(c))\n"
     /* lane k of the word reads lane k ^ mask (mask < 32): swap blocks of 1, 2, 4, 8, 16 lanes */
     "__device__ __forceinline__ u32 tc_perm(u32 v, const u32 mask)\n{\n"
     "    if (mask & 1u) v = ((v & 0x55555555u) << 1) | ((v >> 1) & 0x55555555u);\n"
@@ -203,6 +209,157 @@ static void chunk_body(Src *o, Chunk *k, size_t from, size_t to)
     }
 }
 
+/* The chunk's instructions as a NAND network mapped onto LOP3.  Leaves: every cell's value at
+   the start of the chunk (variable c<cell>), RR (variable r), id patterns, and link reads: a
+   read across dimensions 0..9 is an opaque leaf computed from the source cell's value at that
+   instruction (which is then kept in the cover), a read across 10 and up a load of the
+   segment-start value.  At the end every written cell and RR get their new values. */
+typedef struct {
+    char  **expr;   /* per node: the expression of a leaf, or NULL */
+    size_t  n, cap;
+} Leaves;
+
+static int leaf(TcNet *net, Leaves *L, const char *expr)
+{
+    int id = (int)L->n;
+    int node = tc_net_leaf(net, id);
+    if ((size_t)node >= L->cap) {
+        size_t cap = L->cap ? 2 * L->cap : 256;
+        while (cap <= (size_t)node)
+            cap *= 2;
+        L->expr = tc_xrealloc(L->expr, cap * sizeof *L->expr);
+        memset(L->expr + L->cap, 0, (cap - L->cap) * sizeof *L->expr);
+        L->cap = cap;
+    }
+    L->expr[node] = tc_xstrdup(expr);
+    L->n++;
+    return node;
+}
+
+static void name_of(char *buf, size_t len, const TcNet *net, int node)
+{
+    if (node == 0)
+        snprintf(buf, len, "0u");
+    else if (node == 1)
+        snprintf(buf, len, "TC_ONES");
+    else
+        snprintf(buf, len, "n%d", node);
+    (void)net;
+}
+
+static void mapped_body(Src *o, Chunk *k, size_t from, size_t to)
+{
+    const Program *p = k->p;
+    TcNet *net = tc_net_new();
+    Leaves L = {0};
+    int *cur = tc_xmalloc((p->ncells + 1) * sizeof *cur);
+    int *start = tc_xmalloc((p->ncells + 1) * sizeof *start);
+    int *need = tc_xmalloc(((to - from) + p->ncells + 4) * sizeof *need), nneed = 0;
+    char buf[160];
+    for (uint32_t c = 0; c < p->ncells; c++)
+        cur[c] = start[c] = -1;
+    cur[CELL_ZERO] = 0;
+    cur[CELL_ONE] = 1;
+    int rr = leaf(net, &L, "r");
+    for (size_t i = from; i < to; i++) {
+        Instr in = p->code[i];
+        if (in.op != OP_NAND) {
+            if (!tc_program_readonly(p, in.addr)) {
+                cur[in.addr] = rr;
+                k->written[in.addr] = 1;
+            }
+            continue;
+        }
+        unsigned mask;
+        uint32_t c = tc_program_resolve(p, in.addr, &mask);
+        int v;
+        if (c == CELL_ZERO || c == CELL_ONE) {
+            v = (int)c;
+        } else if (p->special && p->special[c].kind == CK_ID) {
+            Src t = {0};
+            unsigned d = p->special[c].dim;
+            id_word(&t, d, (mask >> d) & 1);
+            v = leaf(net, &L, t.s);
+            free(t.s);
+        } else {
+            unsigned hi = mask >> 5, lo = mask & 31;
+            if (hi < 32 && cur[c] < 0) {  /* first use: the value loaded at the chunk start */
+                use_cell(o, k, c);
+                snprintf(buf, sizeof buf, "c%u", (unsigned)c);
+                cur[c] = start[c] = leaf(net, &L, buf);
+            }
+            if (hi == 0 && lo == 0) {
+                v = cur[c];
+            } else {
+                char src[96];
+                if (hi >= 32) {
+                    snprintf(src, sizeof src, "mem[%uu * W + (w ^ %uu)]", (unsigned)c, hi);
+                } else {
+                    need[nneed++] = cur[c];  /* the source value must exist as a register */
+                    char nm[32];
+                    name_of(nm, sizeof nm, net, cur[c]);
+                    if (hi)
+                        snprintf(src, sizeof src, "__shfl_xor_sync(TC_FULL, %s, %uu)", nm, hi);
+                    else
+                        snprintf(src, sizeof src, "%s", nm);
+                }
+                if (lo)
+                    snprintf(buf, sizeof buf, "tc_perm(%s, %uu)", src, lo);
+                else
+                    snprintf(buf, sizeof buf, "%s", src);
+                v = leaf(net, &L, buf);
+            }
+        }
+        rr = tc_net_nand(net, rr, v);
+    }
+    for (uint32_t c = CELL_FIRST_FREE; c < p->ncells; c++)
+        if (k->written[c])
+            need[nneed++] = cur[c];
+    need[nneed++] = rr;
+    int *order = tc_xmalloc(((size_t)tc_net_size(net) + 1) * sizeof *order), norder = 0;
+    int luts = tc_net_map(net, need, nneed, order, &norder);
+    emit(o, "    // %d LOP3 for %zu NAND/STO instructions\n", luts, to - from);
+    /* leaves and LUTs interleaved in node order: a link leaf comes after its source */
+    int oi = 0;
+    for (int node = 2; node < tc_net_size(net); node++) {
+        if ((size_t)node < L.cap && L.expr[node]) {
+            emit(o, "    const u32 n%d = %s;\n", node, L.expr[node]);
+            continue;
+        }
+        if (oi < norder && order[oi] == node) {
+            int lv[3], nl;
+            uint8_t tt;
+            tc_net_lut(net, node, lv, &nl, &tt);
+            char a[32], b[32], c[32];
+            name_of(a, sizeof a, net, lv[0]);
+            name_of(b, sizeof b, net, nl > 1 ? lv[1] : 0);
+            name_of(c, sizeof c, net, nl > 2 ? lv[2] : 0);
+            emit(o, "    u32 n%d; TC_LOP3(n%d, %s, %s, %s, 0x%02x);\n", node, node, a, b, c,
+                 (unsigned)tt);
+            oi++;
+        }
+    }
+    for (uint32_t c = CELL_FIRST_FREE; c < p->ncells; c++)
+        if (k->written[c]) {
+            if (!k->loaded[c]) {
+                emit(o, "    u32 c%u;\n", (unsigned)c);
+                k->loaded[c] = 1;
+            }
+            name_of(buf, sizeof buf, net, cur[c]);
+            emit(o, "    c%u = %s;\n", (unsigned)c, buf);
+        }
+    name_of(buf, sizeof buf, net, rr);
+    emit(o, "    r = %s;\n", buf);
+    for (size_t i = 0; i < L.cap; i++)
+        free(L.expr[i]);
+    free(L.expr);
+    free(order);
+    free(need);
+    free(cur);
+    free(start);
+    tc_net_free(net);
+}
+
 /* One kernel for instructions from .. to-1; with loop != 0 the whole pass, `passes` times. */
 static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size_t from, size_t to,
                         int loop)
@@ -225,7 +382,10 @@ static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size
         }
         emit(o, "#pragma unroll 1\n    for (u32 pass = 0; pass < passes; pass++) {\n");
     }
-    chunk_body(o, &k, from, to);
+    if (tc_cube_map)
+        mapped_body(o, &k, from, to);
+    else
+        chunk_body(o, &k, from, to);
     if (loop)
         emit(o, "    }\n");
     emit(o, "    if (t < W) {\n");

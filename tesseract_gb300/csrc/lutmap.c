@@ -1,0 +1,359 @@
+/* Technology mapping of a NAND network onto 3-input lookup tables: the LOP3 instruction.
+
+   One pass of a NAND/STO program is a network of 2-input NANDs once STOs are read as renames.
+   GB300's integer ALU evaluates any function of three 32-bit words per instruction (lop3.b32
+   with an 8-bit truth table), so the fewest instructions for the pass are the fewest 3-input
+   LUTs that cover the network.  This file builds the network with constant folding and
+   structural hashing, enumerates the 3-feasible cuts of every node bottom up (keeping the best
+   few by area flow, the usual priority-cuts method of FPGA mapping), selects a cover from the
+   required outputs down, and lists the chosen LUTs in topological order with their truth tables.
+   A full adder's sum and carry, for example, become one LUT each over (x, y, c), where the
+   19-instruction NAND/STO form needs eight or more 2-input operations. */
+#include <stdlib.h>
+#include <string.h>
+
+#include "lutmap.h"
+
+#define PRIO 8  /* cuts kept per node */
+
+typedef struct {
+    int     leaf[3];
+    int     n;
+    uint8_t tt;     /* over leaf patterns 0xf0, 0xcc, 0xaa */
+    float   flow;   /* area flow */
+} Cut;
+
+struct TcNet {
+    TcNode  *node;
+    int      n, cap;
+    int     *slot;   /* hash table of gates: node + 1 */
+    size_t   nslot;
+    Cut     *cuts;   /* PRIO per node */
+    int     *ncut;
+    int     *refs;   /* fanout in the network */
+    float   *flow;   /* best area flow */
+    int     *best;   /* chosen cut index */
+    char    *need;   /* in the cover */
+};
+
+TcNet *tc_net_new(void)
+{
+    TcNet *t = tc_xcalloc(1, sizeof *t);
+    t->nslot = 1 << 12;
+    t->slot = tc_xcalloc(t->nslot, sizeof *t->slot);
+    tc_net_const(t, 0);  /* node 0 = 0, node 1 = ~0 */
+    tc_net_const(t, 1);
+    return t;
+}
+
+void tc_net_free(TcNet *t)
+{
+    if (!t)
+        return;
+    free(t->node);
+    free(t->slot);
+    free(t->cuts);
+    free(t->ncut);
+    free(t->refs);
+    free(t->flow);
+    free(t->best);
+    free(t->need);
+    free(t);
+}
+
+static int add(TcNet *t, int kind, int a, int b, int id)
+{
+    if (t->n == t->cap) {
+        t->cap = t->cap ? 2 * t->cap : 1024;
+        t->node = tc_xrealloc(t->node, (size_t)t->cap * sizeof *t->node);
+    }
+    TcNode *x = &t->node[t->n];
+    x->kind = kind;
+    x->a = a;
+    x->b = b;
+    x->id = id;
+    return t->n++;
+}
+
+int tc_net_const(TcNet *t, int v)
+{
+    if (t->n >= 2)
+        return v ? 1 : 0;
+    return add(t, TN_CONST, v, 0, 0);
+}
+
+int tc_net_leaf(TcNet *t, int id)
+{
+    return add(t, TN_LEAF, 0, 0, id);
+}
+
+static uint64_t hkey(int a, int b)
+{
+    return ((uint64_t)(uint32_t)a * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)(uint32_t)b * 0xC2B2AE3D27D4EB4Full);
+}
+
+static void rehash(TcNet *t)
+{
+    free(t->slot);
+    t->nslot *= 2;
+    t->slot = tc_xcalloc(t->nslot, sizeof *t->slot);
+    for (int i = 0; i < t->n; i++)
+        if (t->node[i].kind == TN_NAND) {
+            size_t h = hkey(t->node[i].a, t->node[i].b) & (t->nslot - 1);
+            while (t->slot[h])
+                h = (h + 1) & (t->nslot - 1);
+            t->slot[h] = i + 1;
+        }
+}
+
+/* ~(a & b), folded: with a constant, or an input twice, or a double negation. */
+int tc_net_nand(TcNet *t, int a, int b)
+{
+    if (a > b) {
+        int s = a;
+        a = b;
+        b = s;
+    }
+    if (a == 0)
+        return 1;                    /* ~(0 & x) = ~0 */
+    if (a == 1)
+        return tc_net_not(t, b);     /* ~(~0 & x) = ~x */
+    if (a == b)
+        return tc_net_not(t, a);
+    size_t h = hkey(a, b) & (t->nslot - 1);
+    while (t->slot[h]) {
+        const TcNode *x = &t->node[t->slot[h] - 1];
+        if (x->kind == TN_NAND && x->a == a && x->b == b)
+            return t->slot[h] - 1;
+        h = (h + 1) & (t->nslot - 1);
+    }
+    int n = add(t, TN_NAND, a, b, 0);
+    t->slot[h] = n + 1;
+    if (2 * (size_t)t->n > t->nslot)
+        rehash(t);
+    return n;
+}
+
+/* ~a, represented as a one-input NAND; ~~x folds to x and ~const to the other constant. */
+int tc_net_not(TcNet *t, int a)
+{
+    if (a == 0)
+        return 1;
+    if (a == 1)
+        return 0;
+    if (t->node[a].kind == TN_NOT)
+        return t->node[a].a;
+    size_t h = hkey(a, -1) & (t->nslot - 1);
+    while (t->slot[h]) {
+        const TcNode *x = &t->node[t->slot[h] - 1];
+        if (x->kind == TN_NOT && x->a == a)
+            return t->slot[h] - 1;
+        h = (h + 1) & (t->nslot - 1);
+    }
+    int n = add(t, TN_NOT, a, -1, 0);
+    t->slot[h] = n + 1;
+    if (2 * (size_t)t->n > t->nslot)
+        rehash(t);
+    return n;
+}
+
+const TcNode *tc_net_node(const TcNet *t, int i) { return &t->node[i]; }
+int tc_net_size(const TcNet *t) { return t->n; }
+
+/* ---- cuts --------------------------------------------------------------------------------------- */
+
+static const uint8_t PAT[3] = {0xf0, 0xcc, 0xaa};
+
+/* tt over leaves `from` (nf of them) re-expressed over the superset `to` (nt). */
+static uint8_t expand(uint8_t tt, const int *from, int nf, const int *to, int nt)
+{
+    int pos[3] = {0, 0, 0};
+    for (int i = 0; i < nf; i++)
+        for (int j = 0; j < nt; j++)
+            if (from[i] == to[j])
+                pos[i] = j;
+    uint8_t out = 0;
+    for (int r = 0; r < 8; r++) {
+        int idx = 0;
+        for (int i = 0; i < nf; i++)
+            if ((PAT[pos[i]] >> r) & 1)
+                idx |= 1 << (2 - i);
+        /* idx: the row of tt where leaf i has the value it has in row r of `to` */
+        if ((tt >> idx) & 1)
+            out |= (uint8_t)(1u << r);
+    }
+    return out;
+}
+
+static int merge_leaves(const Cut *x, const Cut *y, int *out)
+{
+    int n = 0;
+    for (int i = 0; i < x->n; i++)
+        out[n++] = x->leaf[i];
+    for (int j = 0; j < y->n; j++) {
+        int dup = 0;
+        for (int i = 0; i < x->n; i++)
+            dup |= x->leaf[i] == y->leaf[j];
+        if (!dup) {
+            if (n == 3)
+                return -1;
+            out[n++] = y->leaf[j];
+        }
+    }
+    /* sort */
+    for (int i = 1; i < n; i++)
+        for (int j = i; j > 0 && out[j - 1] > out[j]; j--) {
+            int s = out[j];
+            out[j] = out[j - 1];
+            out[j - 1] = s;
+        }
+    return n;
+}
+
+static float leaf_flow(const TcNet *t, int l)
+{
+    const TcNode *x = &t->node[l];
+    if (x->kind == TN_LEAF || x->kind == TN_CONST)
+        return 0.f;
+    return t->flow[l] / (float)(t->refs[l] > 0 ? t->refs[l] : 1);
+}
+
+static void add_cut(TcNet *t, int n, const Cut *c)
+{
+    Cut *cs = &t->cuts[(size_t)n * PRIO];
+    int k = t->ncut[n];
+    for (int i = 0; i < k; i++)
+        if (cs[i].n == c->n && !memcmp(cs[i].leaf, c->leaf, (size_t)c->n * sizeof(int)))
+            return;
+    if (k < PRIO) {
+        cs[k] = *c;
+        t->ncut[n] = k + 1;
+    } else {
+        int worst = 0;
+        for (int i = 1; i < k; i++)
+            if (cs[i].flow > cs[worst].flow)
+                worst = i;
+        if (c->flow < cs[worst].flow)
+            cs[worst] = *c;
+    }
+}
+
+static void cuts_of(TcNet *t, int n)
+{
+    const TcNode *x = &t->node[n];
+    t->ncut[n] = 0;
+    if (x->kind == TN_CONST || x->kind == TN_LEAF) {
+        Cut c = {{n, 0, 0}, 1, 0xf0, 0.f};
+        t->cuts[(size_t)n * PRIO] = c;
+        t->ncut[n] = 1;
+        t->flow[n] = 0.f;
+        return;
+    }
+    if (x->kind == TN_NOT) {
+        const Cut *ca = &t->cuts[(size_t)x->a * PRIO];
+        for (int i = 0; i < t->ncut[x->a]; i++) {
+            Cut c = ca[i];
+            if (c.n == 1 && c.leaf[0] == x->a && t->node[x->a].kind != TN_LEAF &&
+                t->node[x->a].kind != TN_CONST) {
+                /* the trivial cut of the fanin: NOT over it */
+            }
+            c.tt = (uint8_t)~c.tt;
+            c.flow = 1.f;
+            for (int j = 0; j < c.n; j++)
+                c.flow += leaf_flow(t, c.leaf[j]);
+            add_cut(t, n, &c);
+        }
+    } else {
+        const Cut *ca = &t->cuts[(size_t)x->a * PRIO], *cb = &t->cuts[(size_t)x->b * PRIO];
+        for (int i = 0; i < t->ncut[x->a]; i++)
+            for (int j = 0; j < t->ncut[x->b]; j++) {
+                Cut c;
+                c.n = merge_leaves(&ca[i], &cb[j], c.leaf);
+                if (c.n < 0)
+                    continue;
+                uint8_t ta = expand(ca[i].tt, ca[i].leaf, ca[i].n, c.leaf, c.n);
+                uint8_t tb = expand(cb[j].tt, cb[j].leaf, cb[j].n, c.leaf, c.n);
+                c.tt = (uint8_t)~(ta & tb);
+                c.flow = 1.f;
+                for (int k = 0; k < c.n; k++)
+                    c.flow += leaf_flow(t, c.leaf[k]);
+                add_cut(t, n, &c);
+            }
+    }
+    float best = 1e30f;
+    for (int i = 0; i < t->ncut[n]; i++)
+        if (t->cuts[(size_t)n * PRIO + i].flow < best)
+            best = t->cuts[(size_t)n * PRIO + i].flow;
+    t->flow[n] = best;
+    /* the node as a leaf of its fanouts' cuts */
+    Cut self = {{n, 0, 0}, 1, 0xf0, 0.f};
+    /* keep the trivial cut last-resort: it does not count toward this node's own flow */
+    Cut *cs = &t->cuts[(size_t)n * PRIO];
+    if (t->ncut[n] < PRIO) {
+        cs[t->ncut[n]++] = self;
+    } else {
+        int worst = 0;
+        for (int i = 1; i < PRIO; i++)
+            if (cs[i].flow > cs[worst].flow)
+                worst = i;
+        cs[worst] = self;
+    }
+}
+
+int tc_net_map(TcNet *t, const int *outputs, int nout, int *order, int *norder)
+{
+    int n = t->n;
+    t->cuts = tc_xrealloc(t->cuts, (size_t)n * PRIO * sizeof *t->cuts);
+    t->ncut = tc_xrealloc(t->ncut, (size_t)n * sizeof *t->ncut);
+    t->refs = tc_xcalloc((size_t)n, sizeof *t->refs);
+    t->flow = tc_xcalloc((size_t)n, sizeof *t->flow);
+    t->best = tc_xcalloc((size_t)n, sizeof *t->best);
+    t->need = tc_xcalloc((size_t)n, 1);
+    for (int i = 0; i < n; i++) {
+        if (t->node[i].kind == TN_NAND) {
+            t->refs[t->node[i].a]++;
+            t->refs[t->node[i].b]++;
+        } else if (t->node[i].kind == TN_NOT) {
+            t->refs[t->node[i].a]++;
+        }
+    }
+    for (int i = 0; i < nout; i++)
+        t->refs[outputs[i]]++;
+    for (int i = 0; i < n; i++)
+        cuts_of(t, i);
+    /* the cover: outputs first, then the leaves of every chosen cut */
+    for (int i = 0; i < nout; i++)
+        t->need[outputs[i]] = 1;
+    int luts = 0;
+    for (int i = n - 1; i >= 0; i--) {
+        if (!t->need[i] || t->node[i].kind == TN_LEAF || t->node[i].kind == TN_CONST)
+            continue;
+        const Cut *cs = &t->cuts[(size_t)i * PRIO];
+        int b = -1;
+        for (int k = 0; k < t->ncut[i]; k++) {
+            if (cs[k].n == 1 && cs[k].leaf[0] == i)
+                continue;  /* the trivial cut cannot implement the node itself */
+            if (b < 0 || cs[k].flow < cs[b].flow)
+                b = k;
+        }
+        t->best[i] = b;
+        for (int k = 0; k < cs[b].n; k++)
+            t->need[cs[b].leaf[k]] = 1;
+        luts++;
+    }
+    int m = 0;
+    for (int i = 0; i < n; i++)
+        if (t->need[i] && t->node[i].kind != TN_LEAF && t->node[i].kind != TN_CONST)
+            order[m++] = i;
+    *norder = m;
+    return luts;
+}
+
+void tc_net_lut(const TcNet *t, int node, int *leaves, int *nleaves, uint8_t *tt)
+{
+    const Cut *c = &t->cuts[(size_t)node * PRIO + t->best[node]];
+    for (int i = 0; i < c->n; i++)
+        leaves[i] = c->leaf[i];
+    *nleaves = c->n;
+    *tt = c->tt;
+}

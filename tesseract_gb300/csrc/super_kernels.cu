@@ -1,0 +1,361 @@
+// The superoptimizer on the GPU: iterative deepening over the budget; for each budget the host
+// expands the top of the search tree to a frontier of states, and every GPU thread runs an
+// explicit-stack depth-first search of frontier subtrees taken from a work queue.  The search
+// model and its pruning are in super_search.cuh; the first thread to reach the goal records its
+// state and raises a flag the others poll, as the reference's threads share one stop flag
+// (src/super.c:770-896).
+#include <cuda_runtime.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "engine.h"
+#include "super_search.cuh"
+
+#define DEV_LEVELS 44      // deepest level a device search reaches (budgets up to 44)
+#define POLL 1024          // nodes between looks at the stop flag
+
+struct SpFrontier {
+    SpState  *states;
+    size_t    n, cap;
+    uint64_t  nodes;
+    int       depth, found;
+    SpState   sol;
+};
+
+// ---- host: the top of the tree ---------------------------------------------------------------
+
+static void host_node(const SpSpec *sp, SpState *x, int budget, SpFrontier *f);
+
+static void host_after_nand(const SpSpec *sp, SpState *x, int budget, SpFrontier *f)
+{
+    int8_t list[SP_CELLS];
+    int k = sp_hits(sp, x, list);
+    for (int mask = 0; mask < (1 << k) && !f->found; mask++) {
+        uint32_t readable = x->readable, written = x->written;
+        int cost = x->cost;
+        sp_write(sp, x, list, mask);
+        host_node(sp, x, budget, f);
+        x->readable = readable;
+        x->written = written;
+        x->cost = cost;
+    }
+}
+
+static void host_node(const SpSpec *sp, SpState *x, int budget, SpFrontier *f)
+{
+    f->nodes++;
+    int a = sp_arrive(sp, x, budget);
+    if (a == 2) {
+        f->found = 1;
+        f->sol = *x;
+        return;
+    }
+    if (a == 1)
+        return;
+    if (x->n == f->depth) {
+        if (f->n == f->cap) {
+            f->cap = f->cap ? 2 * f->cap : 4096;
+            f->states = (SpState *)tc_xrealloc(f->states, f->cap * sizeof(SpState));
+        }
+        f->states[f->n++] = *x;
+        return;
+    }
+    SpCand cand[SP_CANDS];
+    int m = sp_build(sp, x, cand);
+    for (int i = 0; i < m && !f->found; i++) {
+        uint32_t used = x->used;
+        if (!sp_nand(sp, x, &cand[i], budget))
+            continue;
+        host_after_nand(sp, x, budget, f);
+        if (cand[i].kind == SK_LAZY)
+            x->stored[cand[i].ref] = 0;
+        x->cost -= 1 + cand[i].extra;
+        x->n--;
+        x->used = used;
+    }
+}
+
+// ---- device: depth-first search of one subtree -------------------------------------------------
+
+// Raw operand sources: 0 ZERO, 1 ONE, 2 + c cell c, 18 + j RR value hist[j].
+__device__ __forceinline__ int raw_cand(const SpSpec *sp, const SpState *x, int i, SpCand *c)
+{
+    if (i == 0) {
+        c->v = 0; c->kind = SK_ZERO; c->extra = 0; c->ref = 0;
+        return 1;
+    }
+    if (i == 1) {
+        c->v = sp->mask; c->kind = SK_ONE; c->extra = 0; c->ref = 0;
+        return 1;
+    }
+    if (i < 2 + SP_CELLS) {
+        int cc = i - 2;
+        if (cc >= sp->ncells || !((x->readable >> cc) & 1))
+            return 0;
+        int prev = sp->sym_prev[cc];
+        if (prev >= 0 && !((x->used >> prev) & 1))
+            return 0;
+        c->v = sp_cell_value(sp, x, cc); c->kind = SK_CELL; c->extra = 0; c->ref = (int8_t)cc;
+        return 1;
+    }
+    int j = i - 2 - SP_CELLS;
+    if (j > x->n || (j == 0 && !x->def0))
+        return 0;
+    c->v = x->hist[j];
+    c->kind = x->stored[j] ? SK_TEMP : SK_LAZY;
+    c->extra = (uint8_t)!x->stored[j];
+    c->ref = (int8_t)j;
+    return 1;
+}
+
+// The operands of the node as a set of raw sources: one per value, the cheapest.
+__device__ uint64_t survivors(const SpSpec *sp, const SpState *x)
+{
+    uint64_t keep = 0;
+    uint64_t val[2 + SP_CELLS + DEV_LEVELS + 1];
+    uint8_t extra[2 + SP_CELLS + DEV_LEVELS + 1];
+    int idx[2 + SP_CELLS + DEV_LEVELS + 1], m = 0;
+    int top = 2 + SP_CELLS + x->n;
+    for (int i = 0; i <= top; i++) {
+        SpCand c;
+        if (!raw_cand(sp, x, i, &c))
+            continue;
+        int k = 0;
+        while (k < m && val[k] != c.v)
+            k++;
+        if (k == m) {
+            val[m] = c.v;
+            extra[m] = c.extra;
+            idx[m++] = i;
+        } else if (c.extra < extra[k]) {
+            extra[k] = c.extra;
+            idx[k] = i;
+        }
+    }
+    for (int k = 0; k < m; k++)
+        keep |= 1ull << idx[k];
+    return keep;
+}
+
+struct SpDev {
+    const SpSpec *spec;
+    const SpState *frontier;
+    unsigned long long nfront;
+    int budget;
+    unsigned long long *next;
+    int *found;
+    SpState *sol;
+    unsigned long long *nodes;
+};
+
+__global__ void __launch_bounds__(128) tc_super_kernel(SpDev d)
+{
+    __shared__ SpSpec sp_s;
+    if (threadIdx.x == 0)
+        sp_s = *d.spec;
+    __syncthreads();
+    const SpSpec *sp = &sp_s;
+    SpState x;
+    uint64_t keep[DEV_LEVELS + 1];
+    uint8_t ci[DEV_LEVELS + 1], k_at[DEV_LEVELS + 1];
+    uint16_t wmask[DEV_LEVELS + 1];
+    uint32_t w_readable[DEV_LEVELS + 1], w_written[DEV_LEVELS + 1], used_before[DEV_LEVELS + 1];
+    int w_cost[DEV_LEVELS + 1];
+    unsigned long long nodes = 0, polled = 0;
+    const int budget = d.budget;
+    for (;;) {
+        const unsigned long long f = atomicAdd(d.next, 1ull);
+        if (f >= d.nfront || *(volatile int *)d.found)
+            break;
+        x = d.frontier[f];
+        const int n0 = x.n;
+        int L = n0;
+        keep[L] = survivors(sp, &x);
+        ci[L] = 0;
+        bool expand = true;
+        for (;;) {
+            if (nodes - polled >= POLL) {
+                polled = nodes;
+                if (*(volatile int *)d.found)
+                    break;
+            }
+            if (expand) {
+                const uint64_t rest = keep[L] & (~0ull << ci[L]);
+                if (!rest) {  // every operand tried at this level
+                    if (L == n0)
+                        break;
+                    x.readable = w_readable[L];
+                    x.written = w_written[L];
+                    x.cost = w_cost[L];
+                    wmask[L]++;
+                    expand = false;
+                    continue;
+                }
+                const int i = __ffsll((long long)rest) - 1;
+                ci[L] = (uint8_t)(i + 1);
+                SpCand c;
+                raw_cand(sp, &x, i, &c);
+                const uint32_t used = x.used;
+                if (L + 1 > DEV_LEVELS || !sp_nand(sp, &x, &c, budget))
+                    continue;
+                L++;
+                used_before[L] = used;
+                int8_t list[SP_CELLS];
+                k_at[L] = (uint8_t)sp_hits(sp, &x, list);
+                wmask[L] = 0;
+                expand = false;
+                continue;
+            }
+            // the output writes after NAND L
+            if (wmask[L] >= (1u << k_at[L])) {  // all tried: take the NAND back
+                if (x.op_kind[L] == SK_LAZY)
+                    x.stored[x.op_ref[L]] = 0;
+                x.cost -= 1 + (x.op_kind[L] == SK_LAZY);
+                x.used = used_before[L];
+                x.n--;
+                L--;
+                expand = true;
+                continue;
+            }
+            int8_t list[SP_CELLS];
+            sp_hits(sp, &x, list);
+            w_readable[L] = x.readable;
+            w_written[L] = x.written;
+            w_cost[L] = x.cost;
+            sp_write(sp, &x, list, wmask[L]);
+            nodes++;
+            const int a = sp_arrive(sp, &x, budget);
+            if (a == 2) {
+                if (atomicCAS(d.found, 0, 1) == 0)
+                    *d.sol = x;
+                break;
+            }
+            if (a == 0) {
+                keep[L] = survivors(sp, &x);
+                ci[L] = 0;
+                expand = true;
+                continue;
+            }
+            x.readable = w_readable[L];
+            x.written = w_written[L];
+            x.cost = w_cost[L];
+            wmask[L]++;
+        }
+        if (*(volatile int *)d.found)
+            break;
+    }
+    atomicAdd(d.nodes, nodes);
+}
+
+// ---- the driver ----------------------------------------------------------------------------------
+
+extern "C" int tc_super_run(const SpSpec *sp, int max_cost, int lb, int *found, int *cost,
+                            int *below, SpState *sol, unsigned long long *nodes, double *seconds,
+                            int quiet, char *err, size_t errlen)
+{
+    if (!cuda_engine_init(0, err, errlen))
+        return 0;
+    double t0 = tc_now();
+    *found = 0;
+    *below = lb;
+    *nodes = 0;
+    SpSpec *d_spec = nullptr;
+    int *d_found = nullptr;
+    SpState *d_sol = nullptr;
+    unsigned long long *d_next = nullptr, *d_nodes = nullptr;
+    int ok = tc_cu_check(cudaMalloc(&d_spec, sizeof(SpSpec)), "cudaMalloc", err, errlen) &&
+             tc_cu_check(cudaMalloc(&d_found, sizeof(int)), "cudaMalloc", err, errlen) &&
+             tc_cu_check(cudaMalloc(&d_sol, sizeof(SpState)), "cudaMalloc", err, errlen) &&
+             tc_cu_check(cudaMalloc(&d_next, 8), "cudaMalloc", err, errlen) &&
+             tc_cu_check(cudaMalloc(&d_nodes, 8), "cudaMalloc", err, errlen) &&
+             tc_cu_check(cudaMemcpy(d_spec, sp, sizeof(SpSpec), cudaMemcpyHostToDevice), "copy",
+                         err, errlen);
+    int per_sm = 0;
+    if (ok)
+        ok = tc_cu_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_super_kernel,
+                                                                       128, 0),
+                         "occupancy", err, errlen);
+    const size_t threads = (size_t)tc_engine.sms * (per_sm > 0 ? per_sm : 1) * 128;
+    SpState *d_front = nullptr;
+    size_t d_cap = 0;
+    for (int budget = lb; ok && budget <= max_cost && !*found; budget++) {
+        if (budget > DEV_LEVELS) {
+            tc_fail(err, errlen, "budget %d is deeper than the device search goes (%d)", budget,
+                    DEV_LEVELS);
+            ok = 0;
+            break;
+        }
+        SpFrontier fr;
+        memset(&fr, 0, sizeof fr);
+        for (int depth = 1;; depth++) {
+            fr.n = 0;
+            fr.depth = depth;
+            fr.nodes = 0;
+            SpState root;
+            sp_reset(sp, &root);
+            host_after_nand(sp, &root, budget, &fr);
+            if (fr.found || fr.n >= 16 * threads || depth >= budget || depth >= 12)
+                break;
+        }
+        *nodes += fr.nodes;
+        if (fr.found) {
+            *found = 1;
+            *cost = fr.sol.cost;
+            *sol = fr.sol;
+            free(fr.states);
+            break;
+        }
+        if (fr.n) {
+            if (fr.n > d_cap) {
+                cudaFree(d_front);
+                d_cap = fr.n;
+                ok = tc_cu_check(cudaMalloc(&d_front, d_cap * sizeof(SpState)), "cudaMalloc", err,
+                                 errlen);
+            }
+            ok = ok &&
+                 tc_cu_check(cudaMemcpy(d_front, fr.states, fr.n * sizeof(SpState),
+                                        cudaMemcpyHostToDevice), "copy", err, errlen) &&
+                 tc_cu_check(cudaMemset(d_found, 0, sizeof(int)), "memset", err, errlen) &&
+                 tc_cu_check(cudaMemset(d_next, 0, 8), "memset", err, errlen) &&
+                 tc_cu_check(cudaMemset(d_nodes, 0, 8), "memset", err, errlen);
+            if (ok) {
+                SpDev d = {d_spec, d_front, (unsigned long long)fr.n, budget, d_next, d_found,
+                           d_sol, d_nodes};
+                unsigned blocks = (unsigned)((fr.n + 127) / 128);
+                unsigned maxb = (unsigned)(tc_engine.sms * (per_sm > 0 ? per_sm : 1));
+                if (blocks > maxb)
+                    blocks = maxb;
+                tc_super_kernel<<<blocks, 128, 0, tc_engine.stream>>>(d);
+                ok = tc_cu_check(cudaStreamSynchronize(tc_engine.stream), "super search", err,
+                                 errlen);
+            }
+            int f = 0;
+            unsigned long long dn = 0;
+            ok = ok && tc_cu_check(cudaMemcpy(&f, d_found, sizeof f, cudaMemcpyDeviceToHost),
+                                   "copy", err, errlen) &&
+                 tc_cu_check(cudaMemcpy(&dn, d_nodes, 8, cudaMemcpyDeviceToHost), "copy", err,
+                             errlen);
+            *nodes += dn;
+            if (ok && f) {
+                ok = tc_cu_check(cudaMemcpy(sol, d_sol, sizeof(SpState), cudaMemcpyDeviceToHost),
+                                 "copy", err, errlen);
+                *found = 1;
+                *cost = sol->cost;
+            }
+        }
+        free(fr.states);
+        if (ok && !*found)
+            *below = budget + 1;
+        if (ok && !quiet)
+            fprintf(stderr, "  cost %d: %s (%.3g nodes so far, %.1f s)\n", budget,
+                    *found ? "found" : "none", (double)*nodes, tc_now() - t0);
+    }
+    cudaFree(d_front);
+    cudaFree(d_spec);
+    cudaFree(d_found);
+    cudaFree(d_sol);
+    cudaFree(d_next);
+    cudaFree(d_nodes);
+    *seconds = tc_now() - t0;
+    return ok;
+}
