@@ -9,8 +9,11 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <pthread.h>
+
 #include "batch.h"
 #include "engine.h"
+#include "lutmap.h"
 
 
 int tc_batch_launch(const struct TcBatchDev *d, int slots, cudaStream_t stream, int *grid_out,
@@ -85,12 +88,182 @@ static void clear_list(Vec *lists, const Program *p, unsigned base, const unsign
 }
 
 typedef struct {
-    Vec jobs, code, lists, rpn, vars;
+    Vec jobs, code, luts, lists, rpn, vars;
     uint32_t units;
     int      slots;
 } Pack;
 
-static int pack_job(Pack *pk, const Enum *e, char *err, size_t errlen)
+/* ---- LUT jobs: one tick, the pass mapped onto 3-input LUTs ------------------------------------ */
+
+typedef struct {
+    uint32_t *ops;        /* four words per LUT */
+    int       nops, slots, ok;
+    uint16_t *in_slot;    /* slot of input k */
+    uint16_t *cmp;        /* the compare list, in the bundle format's layout */
+    int       ncmp;       /* entries */
+} LutJob;
+
+/* Maps job e onto LUTs and gives every value a slot (linear scan: a slot is free again after
+   the last op that reads it).  lj->ok = 0 when it does not fit 255 slots. */
+static void lut_job(const Enum *e, const int *in_map, const int *out_map, LutJob *lj)
+{
+    const Program *a = e->a, *b = e->b;
+    size_t n = a->ninputs;
+    memset(lj, 0, sizeof *lj);
+    TcNet *net = tc_net_new();
+    int *leaf = tc_xmalloc((n + 1) * sizeof *leaf);
+    for (size_t k = 0; k < n; k++)
+        leaf[k] = tc_net_leaf(net, (int)k);
+    int *cur_a = tc_xmalloc((a->ncells + 1) * sizeof *cur_a), *cur_b = NULL;
+    tc_net_pass(net, a, a->inputs, n, leaf, cur_a);
+    const TcSpec *sp = (const TcSpec *)e->spec;
+    int *want = tc_xmalloc(((size_t)a->noutputs * 2 + 66) * sizeof *want), nwant = 0;
+    if (e->mode == EN_EQUIV) {
+        uint32_t *b_in = tc_xmalloc((n + 1) * sizeof *b_in);
+        for (size_t k = 0; k < n; k++)
+            b_in[k] = b->inputs[in_map[k]];
+        cur_b = tc_xmalloc((b->ncells + 1) * sizeof *cur_b);
+        tc_net_pass(net, b, b_in, n, leaf, cur_b);
+        free(b_in);
+        for (size_t o = 0; o < a->noutputs; o++) {
+            want[nwant++] = cur_a[a->outputs[o]];
+            want[nwant++] = cur_b[b->outputs[out_map[o]]];
+        }
+    } else {
+        for (int i = 0; i < sp->width; i++)
+            want[nwant++] = cur_a[sp->out[i]];
+    }
+    int size = tc_net_size(net);
+    int *order = tc_xmalloc(((size_t)size + 1) * sizeof *order), norder = 0;
+    tc_net_map(net, want, nwant, order, &norder);
+    /* last use of every value: the position of the last op reading it; outputs live to the end */
+    int *last = tc_xmalloc(((size_t)size + 1) * sizeof *last);
+    for (int i = 0; i < size; i++)
+        last[i] = -1;
+    int leaves[3], nl;
+    uint8_t tt;
+    for (int p = 0; p < norder; p++) {
+        tc_net_lut(net, order[p], leaves, &nl, &tt);
+        for (int j = 0; j < nl; j++)
+            last[leaves[j]] = p;
+    }
+    for (int i = 0; i < nwant; i++)
+        last[want[i]] = norder;
+    int *slot = tc_xmalloc(((size_t)size + 1) * sizeof *slot);
+    for (int i = 0; i < size; i++)
+        slot[i] = -1;
+    slot[0] = 0;
+    slot[1] = 1;
+    for (size_t k = 0; k < n; k++)
+        slot[leaf[k]] = 2 + (int)k;
+    int next = 2 + (int)n, *freed = tc_xmalloc(((size_t)norder + 1) * sizeof *freed), nfree = 0;
+    lj->ops = tc_xmalloc(((size_t)norder + 1) * 4 * sizeof *lj->ops);
+    lj->ok = next <= TC_BATCH_MAX_SLOTS;
+    for (int p = 0; p < norder && lj->ok; p++) {
+        tc_net_lut(net, order[p], leaves, &nl, &tt);
+        int opslot[3];
+        for (int j = 0; j < 3; j++)
+            opslot[j] = j < nl ? slot[leaves[j]] : 0;
+        for (int j = 0; j < nl; j++) {  /* operands read for the last time free their slots */
+            int v = leaves[j];
+            const TcNode *x = tc_net_node(net, v);
+            int dup = 0;
+            for (int q = 0; q < j; q++)
+                dup |= leaves[q] == v;
+            if (!dup && last[v] == p && x->kind != TN_LEAF && x->kind != TN_CONST)
+                freed[nfree++] = slot[v];
+        }
+        int d = nfree ? freed[--nfree] : next++;
+        if (d > TC_BATCH_MAX_SLOTS - 1) {
+            lj->ok = 0;
+            break;
+        }
+        slot[order[p]] = d;
+        uint32_t *o = lj->ops + 4 * (size_t)p;
+        o[0] = (uint32_t)opslot[0] * TC_BATCH_BLOCK * 4;
+        o[1] = (uint32_t)opslot[1] * TC_BATCH_BLOCK * 4;
+        o[2] = (uint32_t)opslot[2] * TC_BATCH_BLOCK * 4;
+        o[3] = (uint32_t)d * TC_BATCH_BLOCK * 4 | (uint32_t)tt << 24;
+    }
+    lj->nops = norder;
+    lj->slots = next;
+    if (lj->ok) {
+        lj->in_slot = tc_xmalloc((n + 1) * sizeof *lj->in_slot);
+        for (size_t k = 0; k < n; k++)
+            lj->in_slot[k] = (uint16_t)(2 + k);
+        lj->cmp = tc_xmalloc(((size_t)nwant * 2 + 2) * sizeof *lj->cmp);
+        if (e->mode == EN_EQUIV) {
+            for (int i = 0; i < nwant; i++)
+                lj->cmp[lj->ncmp++] = (uint16_t)slot[want[i]];
+        } else if (e->mode == EN_SEARCH) {
+            uint64_t target = cuda_spec_value(e->spec, 0);
+            for (int i = 0; i < nwant; i++) {
+                lj->cmp[lj->ncmp++] = (uint16_t)slot[want[i]];
+                lj->cmp[lj->ncmp++] = (uint16_t)((target >> i) & 1);
+            }
+        } else {
+            for (int i = 0; i < nwant; i++)
+                lj->cmp[lj->ncmp++] = (uint16_t)slot[want[i]];
+        }
+    }
+    free(freed);
+    free(slot);
+    free(last);
+    free(order);
+    free(want);
+    free(cur_a);
+    free(cur_b);
+    free(leaf);
+    tc_net_free(net);
+}
+
+typedef struct {
+    const Enum *const *jobs;
+    LutJob           *out;
+    int               njobs;
+    int               next;
+    pthread_mutex_t   lock;
+} LutWork;
+
+static void *lut_worker(void *arg)
+{
+    LutWork *w = arg;
+    for (;;) {
+        pthread_mutex_lock(&w->lock);
+        int i = w->next++;
+        pthread_mutex_unlock(&w->lock);
+        if (i >= w->njobs)
+            break;
+        const Enum *e = w->jobs[i];
+        memset(&w->out[i], 0, sizeof w->out[i]);
+        if (e->ticks != 1 || !e->a)
+            continue;
+        size_t n = e->a->ninputs;
+        int *in_map = tc_xcalloc(n + 1, sizeof *in_map);
+        int *out_map = tc_xcalloc(e->a->noutputs + 1, sizeof *out_map);
+        char err[256];
+        if (tc_enum_prepare(e, in_map, out_map, err, sizeof err) && e->parts == 1)
+            lut_job(e, in_map, out_map, &w->out[i]);
+        free(in_map);
+        free(out_map);
+    }
+    return NULL;
+}
+
+static void map_jobs(const Enum *const *jobs, int njobs, LutJob *out)
+{
+    LutWork w = {jobs, out, njobs, 0, PTHREAD_MUTEX_INITIALIZER};
+    int threads = 16;
+    if (threads > njobs)
+        threads = njobs;
+    pthread_t tid[16];
+    for (int t = 0; t < threads; t++)
+        pthread_create(&tid[t], NULL, lut_worker, &w);
+    for (int t = 0; t < threads; t++)
+        pthread_join(tid[t], NULL);
+}
+
+static int pack_job(Pack *pk, const Enum *e, const LutJob *lj, char *err, size_t errlen)
 {
     const Program *a = e->a, *b = e->b;
     size_t n = a->ninputs;
@@ -108,11 +281,6 @@ static int pack_job(Pack *pk, const Enum *e, char *err, size_t errlen)
         goto done;
     }
     unsigned slots = a->ncells + (e->mode == EN_EQUIV ? b->ncells : 0);
-    if (slots > TC_BATCH_MAX_SLOTS) {
-        tc_fail(err, errlen, "%u cells: more than the batched engine's %d slots", slots,
-                TC_BATCH_MAX_SLOTS);
-        goto done;
-    }
     const TcSpec *sp = (const TcSpec *)e->spec;
     if (e->mode == EN_VERIFY && sp->max_depth > 24) {
         tc_fail(err, errlen, "the batched engine evaluates specs nested at most 24 deep");
@@ -121,6 +289,57 @@ static int pack_job(Pack *pk, const Enum *e, char *err, size_t errlen)
     TcBatchJob J;
     memset(&J, 0, sizeof J);
     J.space = 1ull << n;
+    if (lj && lj->ok) {
+        J.words = (J.space + 31) / 32;
+        J.mode = (uint8_t)e->mode;
+        J.ticks = 1;
+        J.lut = 1;
+        J.slots = (uint16_t)lj->slots;
+        J.one_a = CELL_ONE;
+        J.code_a = (uint32_t)(pk->luts.n / 4);
+        J.nb_a = (uint32_t)lj->nops;
+        vpush(&pk->luts, lj->ops, (size_t)lj->nops * 4);
+        J.lists = (uint32_t)pk->lists.n;
+        J.n_in = (uint16_t)n;
+        for (size_t k = 0; k < n; k++) {
+            uint16_t s2[2] = {lj->in_slot[k], 0};
+            vpush(&pk->lists, s2, 2);
+        }
+        vpush(&pk->lists, lj->cmp, (size_t)lj->ncmp);
+        J.n_cmp = (uint16_t)(e->mode == EN_EQUIV ? lj->ncmp / 2
+                             : e->mode == EN_SEARCH ? lj->ncmp / 2 : lj->ncmp);
+        if (e->mode == EN_VERIFY) {
+            J.rpn = (uint32_t)pk->rpn.n;
+            J.nrpn = (uint16_t)sp->nrpn;
+            for (int i = 0; i < sp->nrpn; i++) {
+                TcBatchRpn it = {(uint32_t)sp->rpn[i].op, 0, sp->rpn[i].v};
+                vpush(&pk->rpn, &it, 1);
+            }
+            J.vars = (uint32_t)pk->vars.n;
+            J.nvars = (uint16_t)sp->nvars;
+            for (int k = 0; k < sp->nvars; k++) {
+                uint8_t d[65];
+                memset(d, 0, sizeof d);
+                d[0] = (uint8_t)sp->var_bits[k];
+                for (int bit = 0; bit < sp->var_bits[k]; bit++)
+                    d[1 + bit] = (uint8_t)sp->var_pos[k][bit];
+                vpush(&pk->vars, d, 65);
+            }
+        }
+        J.first_unit = pk->units;
+        J.units = (uint32_t)((J.words + TC_BATCH_UNIT_WORDS - 1) / TC_BATCH_UNIT_WORDS);
+        pk->units += J.units;
+        if ((int)J.slots > pk->slots)
+            pk->slots = (int)J.slots;
+        vpush(&pk->jobs, &J, 1);
+        ok = 1;
+        goto done;
+    }
+    if (slots > TC_BATCH_MAX_SLOTS) {
+        tc_fail(err, errlen, "%u cells: more than the batched engine's %d slots", slots,
+                TC_BATCH_MAX_SLOTS);
+        goto done;
+    }
     J.words = (J.space + 31) / 32;
     J.mode = (uint8_t)e->mode;
     J.ticks = (uint8_t)e->ticks;
@@ -228,19 +447,30 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
     memset(&pk, 0, sizeof pk);
     pk.jobs.elem = sizeof(TcBatchJob);
     pk.code.elem = 8;
+    pk.luts.elem = 4;
     pk.lists.elem = 2;
     pk.rpn.elem = sizeof(TcBatchRpn);
     pk.vars.elem = 1;
     int ok = 1;
+    LutJob *lj = tc_xcalloc((size_t)njobs, sizeof *lj);
+    if (!getenv("TESSERACT_BATCH_BUNDLES"))
+        map_jobs(jobs, njobs, lj);
     for (int i = 0; i < njobs && ok; i++) {
         memset(&results[i], 0, sizeof results[i]);
         char e2[400];
-        if (!pack_job(&pk, jobs[i], e2, sizeof e2)) {
+        if (!pack_job(&pk, jobs[i], &lj[i], e2, sizeof e2)) {
             tc_fail(err, errlen, "job %d: %s", i, e2);
             ok = 0;
         }
     }
+    for (int i = 0; i < njobs; i++) {
+        free(lj[i].ops);
+        free(lj[i].in_slot);
+        free(lj[i].cmp);
+    }
+    free(lj);
     uint32_t *unit_job = NULL;
+    void *d_luts = NULL;
     void *d_jobs = NULL, *d_code = NULL, *d_lists = NULL, *d_rpn = NULL, *d_vars = NULL;
     void *d_unit_job = NULL, *d_next = NULL, *d_hits = NULL, *d_uhits = NULL, *d_ucount = NULL;
     unsigned long long *hits = NULL, *uhits = NULL;
@@ -254,6 +484,7 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
         Vec uj = {unit_job, pk.units, pk.units, 4};
         d_jobs = upload(&pk.jobs, &ok, err, errlen);
         d_code = upload(&pk.code, &ok, err, errlen);
+        d_luts = upload(&pk.luts, &ok, err, errlen);
         d_lists = upload(&pk.lists, &ok, err, errlen);
         d_rpn = upload(&pk.rpn, &ok, err, errlen);
         d_vars = upload(&pk.vars, &ok, err, errlen);
@@ -271,7 +502,7 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
     float ms = 0;
     int grid = 0;
     if (ok) {
-        struct TcBatchDev d = {d_jobs, d_code, d_lists, d_rpn, d_vars, d_unit_job, pk.units,
+        struct TcBatchDev d = {d_jobs, d_code, d_luts, d_lists, d_rpn, d_vars, d_unit_job, pk.units,
                                d_next, d_hits, d_uhits, d_ucount};
         ok = tc_cu_check(cudaEventRecord(tc_engine.ev0, tc_engine.stream), "event", err, errlen) &&
              tc_batch_launch(&d, pk.slots, tc_engine.stream, &grid, err, errlen) &&
@@ -320,6 +551,7 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
     }
     cudaFree(d_jobs);
     cudaFree(d_code);
+    cudaFree(d_luts);
     cudaFree(d_lists);
     cudaFree(d_rpn);
     cudaFree(d_vars);
@@ -334,6 +566,7 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
     free(unit_job);
     free(pk.jobs.p);
     free(pk.code.p);
+    free(pk.luts.p);
     free(pk.lists.p);
     free(pk.rpn.p);
     free(pk.vars.p);

@@ -33,7 +33,8 @@ typedef struct {
     uint16_t one_a, one_b;   /* the ONE slots */
     uint8_t  mode;           /* EN_VERIFY, EN_EQUIV, EN_SEARCH */
     uint8_t  ticks;
-    uint8_t  pad[2];
+    uint8_t  lut;            /* 1: code_a/nb_a are LOP3 ops (four words each, see below) */
+    uint8_t  pad;
     uint32_t rpn;            /* verify: first item in the RPN array */
     uint16_t nrpn, nvars;
     uint32_t vars;           /* verify: first entry (per var: bits, then positions) */
@@ -47,10 +48,16 @@ typedef struct {
     uint64_t v;
 } TcBatchRpn;
 
+/* A LUT job (lut = 1, one tick) is the pass mapped onto 3-input LUTs (lutmap.c): op i is four
+   words: the byte offsets in shared memory of its three operands, then the destination's byte
+   offset with the truth table in the top 8 bits.  Its slots are values, not cells: slot 0 holds
+   0, slot 1 ~0, slots 2.. the inputs, the others LUT results, reused once dead. */
+
 /* The device arrays of one batch, passed to the kernel by value. */
 struct TcBatchDev {
     const TcBatchJob   *jobs;
     const uint64_t     *code;
+    const uint32_t     *luts;
     const uint16_t     *lists;
     const TcBatchRpn   *rpn;
     const uint8_t      *vars;

@@ -50,6 +50,41 @@ __device__ __forceinline__ uint32_t run_program(uint32_t *S, const uint64_t *cod
     return r;
 }
 
+// A 3-input LUT with a truth table known only at run time: the table is the same for the whole
+// block, so a jump on it is uniform and each case is one lop3.b32 with that immediate.
+#define TC_L(t)                                                                              \
+    case 0x##t:                                                                              \
+        asm("lop3.b32 %0, %1, %2, %3, 0x" #t ";" : "=r"(r) : "r"(x), "r"(y), "r"(z));        \
+        break;
+#define TC_L16(h)                                                                            \
+    TC_L(h##0) TC_L(h##1) TC_L(h##2) TC_L(h##3) TC_L(h##4) TC_L(h##5) TC_L(h##6) TC_L(h##7)  \
+    TC_L(h##8) TC_L(h##9) TC_L(h##a) TC_L(h##b) TC_L(h##c) TC_L(h##d) TC_L(h##e) TC_L(h##f)
+
+__device__ __forceinline__ uint32_t lut3(uint32_t tt, uint32_t x, uint32_t y, uint32_t z)
+{
+    uint32_t r = 0;
+    switch (tt) {
+        TC_L16(0) TC_L16(1) TC_L16(2) TC_L16(3) TC_L16(4) TC_L16(5) TC_L16(6) TC_L16(7)
+        TC_L16(8) TC_L16(9) TC_L16(a) TC_L16(b) TC_L16(c) TC_L16(d) TC_L16(e) TC_L16(f)
+    }
+    return r;
+}
+
+// One pass of a LUT job: every op reads three slots and writes one.
+__device__ __forceinline__ void run_luts(char *Sb, const uint4 *ops, uint32_t n)
+{
+    uint4 next = n ? __ldg(ops) : make_uint4(0, 0, 0, 0);
+    for (uint32_t i = 0; i < n; i++) {
+        const uint4 op = next;
+        if (i + 1 < n)
+            next = __ldg(ops + i + 1);
+        const uint32_t x = *(const uint32_t *)(Sb + op.x);
+        const uint32_t y = *(const uint32_t *)(Sb + op.y);
+        const uint32_t z = *(const uint32_t *)(Sb + op.z);
+        *(uint32_t *)(Sb + (op.w & 0xffffffu)) = lut3(op.w >> 24, x, y, z);
+    }
+}
+
 // 32 x 32 bit transpose: A[l] bit b -> A[b] bit l
 __device__ __forceinline__ void transpose32(uint32_t *A)
 {
@@ -136,29 +171,37 @@ __global__ void __launch_bounds__(B) tc_batch_kernel(TcBatchDev d)
             uint32_t valid = 0;
             if (w < w1)
                 valid = J.space - x0 >= 32 ? 0xffffffffu : (1u << (uint32_t)(J.space - x0)) - 1u;
-            // the power-on state: cleared cells, constants, inputs from the assignment number
             const uint16_t *zero = L + 2 * J.n_in;
-            for (uint32_t z = 0; z < J.n_zero; z++)
-                S[zero[z] * B] = 0u;
-            S[(J.one_a - 1u) * B] = 0u;  /* ZERO and ONE of each program */
-            S[J.one_a * B] = 0xffffffffu;
-            if (J.mode == EN_EQUIV) {
-                S[(J.one_b - 1u) * B] = 0u;
-                S[J.one_b * B] = 0xffffffffu;
-            }
-            for (uint32_t k = 0; k < J.n_in; k++) {
-                const uint32_t v = lane_word(w, J.n_in - 1 - k);
-                S[L[2 * k] * B] = v;
-                if (J.mode == EN_EQUIV)
-                    S[L[2 * k + 1] * B] = v;
-            }
-            uint32_t r = 0;
-            for (uint32_t t = 0; t < J.ticks; t++)
-                r = run_program(S, d.code + J.code_a, J.nb_a, r);
-            if (J.mode == EN_EQUIV) {
-                uint32_t rb = 0;
+            if (J.lut) {
+                S[0] = 0u;
+                S[B] = 0xffffffffu;
+                for (uint32_t k = 0; k < J.n_in; k++)
+                    S[L[2 * k] * B] = lane_word(w, J.n_in - 1 - k);
+                run_luts((char *)S, (const uint4 *)d.luts + J.code_a, J.nb_a);
+            } else {
+                // the power-on state: cleared cells, constants, inputs from the assignment number
+                for (uint32_t z = 0; z < J.n_zero; z++)
+                    S[zero[z] * B] = 0u;
+                S[(J.one_a - 1u) * B] = 0u;  /* ZERO and ONE of each program */
+                S[J.one_a * B] = 0xffffffffu;
+                if (J.mode == EN_EQUIV) {
+                    S[(J.one_b - 1u) * B] = 0u;
+                    S[J.one_b * B] = 0xffffffffu;
+                }
+                for (uint32_t k = 0; k < J.n_in; k++) {
+                    const uint32_t v = lane_word(w, J.n_in - 1 - k);
+                    S[L[2 * k] * B] = v;
+                    if (J.mode == EN_EQUIV)
+                        S[L[2 * k + 1] * B] = v;
+                }
+                uint32_t r = 0;
                 for (uint32_t t = 0; t < J.ticks; t++)
-                    rb = run_program(S, d.code + J.code_b, J.nb_b, rb);
+                    r = run_program(S, d.code + J.code_a, J.nb_a, r);
+                if (J.mode == EN_EQUIV) {
+                    uint32_t rb = 0;
+                    for (uint32_t t = 0; t < J.ticks; t++)
+                        rb = run_program(S, d.code + J.code_b, J.nb_b, rb);
+                }
             }
             const uint16_t *cmp = zero + J.n_zero;
             uint32_t m = 0;

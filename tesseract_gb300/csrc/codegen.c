@@ -134,26 +134,6 @@ typedef struct {
     int    norder;
 } Mapped;
 
-/* One pass of p from power-on with input k in leaf k: the network of every cell's final value.
-   cur[c] gets the node holding cell c at the end of the pass. */
-static void build_pass(TcNet *net, const Program *p, const uint32_t *in_cells, size_t n,
-                       const int *leaf_of_input, int *cur)
-{
-    for (uint32_t c = 0; c < p->ncells; c++)
-        cur[c] = 0;
-    cur[CELL_ONE] = 1;
-    for (size_t k = 0; k < n; k++)
-        cur[in_cells[k]] = leaf_of_input[k];
-    int rr = 0;
-    for (size_t i = 0; i < p->len; i++) {
-        Instr in = p->code[i];
-        if (in.op == OP_NAND)
-            rr = tc_net_nand(net, rr, cur[in.addr]);
-        else if (in.addr >= CELL_FIRST_FREE)
-            cur[in.addr] = rr;
-    }
-}
-
 static void node_name(char *buf, size_t len, const TcNet *net, int node)
 {
     const TcNode *x = tc_net_node(net, node);
@@ -317,9 +297,9 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
             leaf[k] = tc_net_leaf(net, (int)k);
         int *cur_a = tc_xmalloc((a->ncells + 1) * sizeof *cur_a);
         int *cur_b = g->b ? tc_xmalloc((g->b->ncells + 1) * sizeof *cur_b) : NULL;
-        build_pass(net, a, a->inputs, n, leaf, cur_a);
+        tc_net_pass(net, a, a->inputs, n, leaf, cur_a);
         if (g->mode == EN_EQUIV)
-            build_pass(net, g->b, g->b_inputs, n, leaf, cur_b);
+            tc_net_pass(net, g->b, g->b_inputs, n, leaf, cur_b);
         int *want = tc_xmalloc(((size_t)a->noutputs * 2 + 65) * sizeof *want), nwant = 0;
         if (g->mode == EN_EQUIV)
             for (size_t k = 0; k < a->noutputs; k++) {

@@ -357,3 +357,23 @@ void tc_net_lut(const TcNet *t, int node, int *leaves, int *nleaves, uint8_t *tt
     *nleaves = c->n;
     *tt = c->tt;
 }
+
+/* One pass of p from power-on (cells 0, ONE ~0, RR 0) with input k held by node leaves[k]:
+   cur[c] gets the node of cell c's value at the end of the pass. */
+void tc_net_pass(TcNet *net, const Program *p, const uint32_t *in_cells, size_t n,
+                 const int *leaves, int *cur)
+{
+    for (uint32_t c = 0; c < p->ncells; c++)
+        cur[c] = 0;
+    cur[CELL_ONE] = 1;
+    for (size_t k = 0; k < n; k++)
+        cur[in_cells[k]] = leaves[k];
+    int rr = 0;
+    for (size_t i = 0; i < p->len; i++) {
+        Instr in = p->code[i];
+        if (in.op == OP_NAND)
+            rr = tc_net_nand(net, rr, cur[in.addr]);
+        else if (in.addr >= CELL_FIRST_FREE)
+            cur[in.addr] = rr;
+    }
+}

@@ -34,6 +34,11 @@ int  tc_net_map(TcNet *t, const int *outputs, int nout, int *order, int *norder)
    lop3.b32 patterns 0xf0, 0xcc, 0xaa of leaves 0, 1, 2. */
 void tc_net_lut(const TcNet *t, int node, int *leaves, int *nleaves, uint8_t *tt);
 
+/* One pass of a program without id or link cells from power-on, input k in node leaves[k];
+   cur[c] gets the node of cell c at the end. */
+void tc_net_pass(TcNet *net, const Program *p, const uint32_t *in_cells, size_t n,
+                 const int *leaves, int *cur);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,8 +66,11 @@ def test_batch_mixed_modes_same_alone_and_in_the_mix():
 
 
 def test_batch_refuses_what_it_cannot_run():
-    big = T.Program.random(300, 100, 1)
+    big = T.Program.random(300, 100, 1)  # two ticks: the cell interpreter, 600 cells
     with pytest.raises(T.EngineError, match="slots"):
-        T.batch_run([dict(mode=T.EN_EQUIV, a=big, b=big)])
+        T.batch_run([dict(mode=T.EN_EQUIV, a=big, b=big, ticks=2)])
+    # one tick: the LUT path needs slots for live values only, so this one runs
+    r = T.batch_run([dict(mode=T.EN_EQUIV, a=big, b=big.rewrite(3))])[0]
+    assert r["hits"] == 0
     m = T.Program.gen_mul(4)
     assert T.batch_run([]) == []
