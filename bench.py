@@ -122,6 +122,9 @@ def cpu_sample(seconds_target=12.0):
 
 
 def run_reference(args):
+    """The reference arm: the reference's own enumerator where it was built from its sources on
+    this host (oracle/_ref/alpha, x86 only: `alpha verify ... --part i/64 --raw`, a 1/64 share of
+    the space per step), otherwise the oracle's C port of it on every host core."""
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
@@ -129,33 +132,57 @@ def run_reference(args):
     import tesseract_gb300 as T
     from tesseract_gb300 import build
     build.build(reference=False)
-    p = T.Program.gen_mul(16)
-    s = T.Spec(p, "p = a * b")
     threads = os.cpu_count() or 1
-    base, _, dt = cpu_sample(seconds_target=4.0)
-    chunks = int(base["sample"].split()[0])
-    for _ in range(args.warmup):
-        O.enum_run(T.EN_VERIFY, p, spec=s, threads=threads, limit_chunks=max(1, chunks // 8))
-    ops = 0
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r = O.enum_run(T.EN_VERIFY, p, spec=s, threads=threads, limit_chunks=chunks)
-        assert r["hits"] == 0
-        ops += r["ops"]
-    dt = time.perf_counter() - t0
+    if O.have_reference():
+        import tempfile
+        with tempfile.TemporaryDirectory() as d:
+            prog = os.path.join(d, "mul16.asm")
+            with open(prog, "w") as f:
+                f.write(subprocess.run([O.REF_BIN, "gen", "mul", "--bits", "16"], check=True,
+                                       capture_output=True, text=True).stdout)
+            def step(i):
+                out = subprocess.run([O.REF_BIN, "verify", prog, "--spec", "p = a * b", "--part",
+                                      "%d/64" % (i % 64), "--raw"], check=True,
+                                     capture_output=True, text=True).stdout
+                f = out.split("\n")[0].split()
+                assert f[0] == "EN" and int(f[4]) == 0
+                return int(f[7])
+            for i in range(args.warmup):
+                step(i)
+            ops = 0
+            t0 = time.perf_counter()
+            for i in range(args.steps):
+                ops += step(args.warmup + i)
+            dt = time.perf_counter() - t0
+        kind, sample = "reference", "alpha verify --part i/64 (2^26 assignments) per step"
+    else:
+        p = T.Program.gen_mul(16)
+        s = T.Spec(p, "p = a * b")
+        base, _, _ = cpu_sample(seconds_target=4.0)
+        chunks = int(base["sample"].split()[0])
+        for _ in range(args.warmup):
+            O.enum_run(T.EN_VERIFY, p, spec=s, threads=threads, limit_chunks=max(1, chunks // 8))
+        ops = 0
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r = O.enum_run(T.EN_VERIFY, p, spec=s, threads=threads, limit_chunks=chunks)
+            assert r["hits"] == 0
+            ops += r["ops"]
+        dt = time.perf_counter() - t0
+        kind, sample = "port", f"{chunks} chunks of 32768 assignments per step"
     v = ops / dt
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "lane-ops/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample_per_step": f"{chunks} chunks of 32768 "
-                                                               "assignments"},
-            "cpu_baseline": {"value": v, "unit": "lane-ops/s", "cores": threads, "kind": "port",
-                             "sample": f"{chunks} chunks of 32768 assignments per step"},
+            "config": {"workload": WORKLOAD, "sample_per_step": sample},
+            "cpu_baseline": {"value": v, "unit": "lane-ops/s", "cores": threads, "kind": kind,
+                             "sample": sample},
             "e2e": {"value": v, "unit": "lane-ops/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0},
-            "note": "the reference's AVX2 lane engine and x86 JIT do not build on aarch64; "
-                    "this is the oracle's portable C port of its enumerator"}
+                    "d2h_bytes_per_step": 0}}
+    if kind == "port":
+        line["note"] = ("the reference's AVX2 lane engine and x86 JIT do not build on this host; "
+                        "this is the oracle's portable C port of its enumerator")
     print(json.dumps(line), flush=True)
     return 0
 
@@ -250,6 +277,68 @@ def bench_batch(args):
     return 0 if (same and not bad_equal) else 3
 
 
+def bench_super(args):
+    """Config 4: the shortest NAND/STO full adder (19, nothing of 18 or fewer) and XOR (7)."""
+    import tesseract_gb300 as T
+    from tesseract_gb300 import build
+    build.build(reference=False)
+    out = {"config": "super", "metric": "proven shortest programs", "results": []}
+    for text, want in (("RR = RR ^ x", 7), ("s{a,b} = a ^ b ^ c; c = a&b | a&c | b&c", 19)):
+        t0 = time.perf_counter()
+        r = T.super_search(text, max_cost=24, quiet=False)
+        out["results"].append({"spec": text, "cost": r["cost"], "below": r["below"],
+                               "expected": want, "nodes": r["nodes"],
+                               "seconds": time.perf_counter() - t0, "checked": r["checked"],
+                               "program": [" ".join(x) for x in r["program"]]})
+    ok = all(x["cost"] == x["expected"] == x["below"] and x["checked"] for x in out["results"])
+    out["reference_here"] = "alpha super FA: 19, nothing <= 18, 1.2e10 nodes, 87.2 s on 8 threads"
+    print(json.dumps(out), flush=True)
+    return 0 if ok else 3
+
+
+def bench_serve(args):
+    """Config 5: a Poisson stream (2,000 jobs/s, seed 1) of mixed verify / equiv / search jobs,
+    served with continuous batching; p50/p99 latency and jobs/s, against the plain engine
+    (one NVRTC-compiled kernel per job) on a sample of the same stream."""
+    import statistics as S
+    import tesseract_gb300 as T
+    from tesseract_gb300 import build
+    from tesseract_gb300.workloads import serve_stream
+    build.build(reference=False)
+    n = args.jobs if args.jobs != 4096 else 400
+    lines = []
+    for label, wmax in (("config", 34), ("light", 22)):
+        jobs, arrivals = serve_stream(n, rate=2000.0, seed=1, max_width=wmax)
+        T.serve_run(jobs[:8], [0.0] * 8)  # warm-up
+        t0 = time.perf_counter()
+        res, start, finish = T.serve_run(jobs, arrivals)
+        wall = time.perf_counter() - t0
+        lat = sorted(f - a for f, a in zip(finish, arrivals))
+        ops = sum(r["ops"] for r in res)
+        q = lambda p: lat[min(len(lat) - 1, int(p * len(lat)))]
+        span = max(finish) - min(arrivals)
+        lines.append({"stream": label, "jobs": n, "max_width": wmax,
+                      "offered_jobs_per_s": 2000.0, "served_jobs_per_s": n / span,
+                      "p50_s": q(0.50), "p99_s": q(0.99), "wall_s": wall,
+                      "lane_ops": ops, "lane_ops_per_s": ops / span,
+                      "offered_lane_ops_per_s": ops / (arrivals[-1] - arrivals[0])})
+    # the plain engine on the first jobs of the light stream, in arrival order
+    jobs, arrivals = serve_stream(n, rate=2000.0, seed=1, max_width=22)
+    sample = jobs[:24]
+    t0 = time.perf_counter()
+    plain = [T.enum_run(j["mode"], j["a"], j.get("b"), j.get("spec")) for j in sample]
+    plain_s = time.perf_counter() - t0
+    served, _, _ = T.serve_run(sample, [0.0] * len(sample))
+    same = all(p[k] == q[k] for p, q in zip(plain, served)
+               for k in ("space", "tried", "hits", "hit", "ops"))
+    out = {"config": "serve", "metric": "served jobs/s, p50/p99 latency", "streams": lines,
+           "plain_jobs_per_s_with_compile": len(sample) / plain_s,
+           "served_vs_plain_light": lines[1]["served_jobs_per_s"] / (len(sample) / plain_s),
+           "sample_identical_to_plain": same}
+    print(json.dumps(out), flush=True)
+    return 0 if same else 3
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -259,7 +348,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--share", type=int, default=1,
                     help="verify only share 0 of this many (a small case for profiling)")
-    ap.add_argument("--config", default="verify", choices=["verify", "life", "batch"],
+    ap.add_argument("--config", default="verify",
+                    choices=["verify", "life", "batch", "super", "serve"],
                     help="verify: the headline; life: cube Life 2^16 machines, 1000 "
                          "generations; batch: 4,096 equivalence jobs in one launch")
     ap.add_argument("--jobs", type=int, default=4096, help="batch: number of jobs")
@@ -271,6 +361,10 @@ def main():
         return bench_life(args)
     if args.config == "batch":
         return bench_batch(args)
+    if args.config == "super":
+        return bench_super(args)
+    if args.config == "serve":
+        return bench_serve(args)
 
     world, rank, local = dist_env()
     dist = None

@@ -16,8 +16,11 @@
 #include "lutmap.h"
 
 
-int tc_batch_launch(const struct TcBatchDev *d, int slots, cudaStream_t stream, int *grid_out,
-                    char *err, size_t errlen);
+int tc_batch_launch(const struct TcBatchDev *d, int slots, cudaStream_t stream, double share,
+                    int *grid_out, char *err, size_t errlen);
+
+typedef struct TcWave TcWave;
+void tc_wave_free(TcWave *w);
 
 typedef struct {
     void  *p;
@@ -418,7 +421,7 @@ done:
     return ok;
 }
 
-static void *upload(const Vec *v, int *ok, char *err, size_t errlen)
+static __attribute__((unused)) void *upload(const Vec *v, int *ok, char *err, size_t errlen)
 {
     void *d = NULL;
     size_t bytes = (v->n ? v->n : 1) * v->elem;
@@ -434,31 +437,48 @@ static void *upload(const Vec *v, int *ok, char *err, size_t errlen)
     return d;
 }
 
-/* Runs every job in one persistent launch.  results[i] is job i's EnumResult; seconds is the
-   device time of the whole batch. */
-int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char *err,
-                   size_t errlen)
+/* ---- waves: a set of jobs packed, launched on a stream, finished job by job ----------------- */
+
+struct TcWave {
+    int                 njobs;
+    const Enum *const  *jobs;
+    Pack                pk;
+    uint32_t           *unit_job;
+    void               *dev;        /* one device allocation for everything */
+    void               *host;       /* one mapped host allocation: unit lists, results, flags */
+    unsigned long long *h_uhits, *h_hits;
+    uint32_t           *h_ucount;
+    volatile uint32_t  *h_done;
+    cudaStream_t        stream;
+    cudaEvent_t         ev0, ev1;
+    int                 grid, launched;
+    size_t              dev_bytes;
+};
+
+static size_t align256(size_t n)
 {
-    if (njobs <= 0)
-        return 1;
-    if (!cuda_engine_init(0, err, errlen))
-        return 0;
-    Pack pk;
-    memset(&pk, 0, sizeof pk);
-    pk.jobs.elem = sizeof(TcBatchJob);
-    pk.code.elem = 8;
-    pk.luts.elem = 4;
-    pk.lists.elem = 2;
-    pk.rpn.elem = sizeof(TcBatchRpn);
-    pk.vars.elem = 1;
-    int ok = 1;
-    LutJob *lj = tc_xcalloc((size_t)njobs, sizeof *lj);
+    return (n + 255) & ~(size_t)255;
+}
+
+/* Maps and packs the jobs (no device work yet). */
+int tc_wave_prepare(TcWave **out, const Enum *const *jobs, int njobs, char *err, size_t errlen)
+{
+    TcWave *w = tc_xcalloc(1, sizeof *w);
+    w->njobs = njobs;
+    w->jobs = jobs;
+    w->pk.jobs.elem = sizeof(TcBatchJob);
+    w->pk.code.elem = 8;
+    w->pk.luts.elem = 4;
+    w->pk.lists.elem = 2;
+    w->pk.rpn.elem = sizeof(TcBatchRpn);
+    w->pk.vars.elem = 1;
+    LutJob *lj = tc_xcalloc((size_t)njobs + 1, sizeof *lj);
     if (!getenv("TESSERACT_BATCH_BUNDLES"))
         map_jobs(jobs, njobs, lj);
+    int ok = 1;
     for (int i = 0; i < njobs && ok; i++) {
-        memset(&results[i], 0, sizeof results[i]);
         char e2[400];
-        if (!pack_job(&pk, jobs[i], &lj[i], e2, sizeof e2)) {
+        if (!pack_job(&w->pk, jobs[i], &lj[i], e2, sizeof e2)) {
             tc_fail(err, errlen, "job %d: %s", i, e2);
             ok = 0;
         }
@@ -469,106 +489,199 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
         free(lj[i].cmp);
     }
     free(lj);
-    uint32_t *unit_job = NULL;
-    void *d_luts = NULL;
-    void *d_jobs = NULL, *d_code = NULL, *d_lists = NULL, *d_rpn = NULL, *d_vars = NULL;
-    void *d_unit_job = NULL, *d_next = NULL, *d_hits = NULL, *d_uhits = NULL, *d_ucount = NULL;
-    unsigned long long *hits = NULL, *uhits = NULL;
-    uint32_t *ucount = NULL;
-    if (ok) {
-        unit_job = tc_xmalloc(pk.units * sizeof *unit_job);
-        const TcBatchJob *J = pk.jobs.p;
-        for (int i = 0; i < njobs; i++)
-            for (uint32_t u = 0; u < J[i].units; u++)
-                unit_job[J[i].first_unit + u] = (uint32_t)i;
-        Vec uj = {unit_job, pk.units, pk.units, 4};
-        d_jobs = upload(&pk.jobs, &ok, err, errlen);
-        d_code = upload(&pk.code, &ok, err, errlen);
-        d_luts = upload(&pk.luts, &ok, err, errlen);
-        d_lists = upload(&pk.lists, &ok, err, errlen);
-        d_rpn = upload(&pk.rpn, &ok, err, errlen);
-        d_vars = upload(&pk.vars, &ok, err, errlen);
-        d_unit_job = upload(&uj, &ok, err, errlen);
+    if (!ok) {
+        tc_wave_free(w);
+        return 0;
     }
+    w->unit_job = tc_xmalloc(((size_t)w->pk.units + 1) * sizeof *w->unit_job);
+    const TcBatchJob *J = w->pk.jobs.p;
+    for (int i = 0; i < njobs; i++)
+        for (uint32_t u = 0; u < J[i].units; u++)
+            w->unit_job[J[i].first_unit + u] = (uint32_t)i;
+    *out = w;
+    return 1;
+}
+
+size_t tc_wave_bytes(const TcWave *w)
+{
+    const Pack *pk = &w->pk;
+    return align256(pk->jobs.n * pk->jobs.elem) + align256(pk->code.n * 8) +
+           align256(pk->luts.n * 4) + align256(pk->lists.n * 2) +
+           align256(pk->rpn.n * pk->rpn.elem) + align256(pk->vars.n) +
+           align256((size_t)pk->units * 4) + 256 + align256((size_t)w->njobs * 8) +
+           align256((size_t)w->njobs * 4);
+}
+
+/* Uploads and launches on `stream`; the grid takes `share` of the GPU's resident blocks. */
+int tc_wave_launch(TcWave *w, cudaStream_t stream, double share, char *err, size_t errlen)
+{
+    Pack *pk = &w->pk;
+    int n = w->njobs;
+    size_t off[10], at = 0;
+    size_t sizes[10] = {pk->jobs.n * pk->jobs.elem, pk->code.n * 8, pk->luts.n * 4,
+                        pk->lists.n * 2, pk->rpn.n * pk->rpn.elem, pk->vars.n,
+                        (size_t)pk->units * 4, 4, (size_t)n * 8, (size_t)n * 4};
+    for (int i = 0; i < 10; i++) {
+        off[i] = at;
+        at += align256(sizes[i] ? sizes[i] : 1);
+    }
+    w->dev_bytes = at;
+    size_t hsz[4] = {(size_t)pk->units * TC_BATCH_SHOW * 8, (size_t)pk->units * 4,
+                     (size_t)n * 8, (size_t)n * 4};
+    size_t hoff[4], hat = 0;
+    for (int i = 0; i < 4; i++) {
+        hoff[i] = hat;
+        hat += align256(hsz[i] ? hsz[i] : 1);
+    }
+    w->stream = stream;
+    if (!tc_cu_check(cudaMallocAsync(&w->dev, at, stream), "cudaMallocAsync", err, errlen) ||
+        !tc_cu_check(cudaHostAlloc(&w->host, hat, cudaHostAllocMapped), "cudaHostAlloc", err,
+                     errlen))
+        return 0;
+    memset(w->host, 0, hat);
+    char *h = w->host;
+    w->h_uhits = (unsigned long long *)(h + hoff[0]);
+    w->h_ucount = (uint32_t *)(h + hoff[1]);
+    w->h_hits = (unsigned long long *)(h + hoff[2]);
+    w->h_done = (volatile uint32_t *)(h + hoff[3]);
+    char *hd;
+    if (!tc_cu_check(cudaHostGetDevicePointer((void **)&hd, w->host, 0), "mapped memory", err,
+                     errlen))
+        return 0;
+    char *d = w->dev;
+    const void *src[7] = {pk->jobs.p, pk->code.p, pk->luts.p, pk->lists.p, pk->rpn.p, pk->vars.p,
+                          w->unit_job};
+    for (int i = 0; i < 7; i++)
+        if (sizes[i] && !tc_cu_check(cudaMemcpyAsync(d + off[i], src[i], sizes[i],
+                                                     cudaMemcpyHostToDevice, stream),
+                                     "upload", err, errlen))
+            return 0;
+    /* units left per job */
+    uint32_t *rem = tc_xmalloc((size_t)n * 4 + 4);
+    const TcBatchJob *J = pk->jobs.p;
+    for (int i = 0; i < n; i++)
+        rem[i] = J[i].units;
+    int ok = tc_cu_check(cudaMemcpyAsync(d + off[9], rem, (size_t)n * 4, cudaMemcpyHostToDevice,
+                                         stream), "upload", err, errlen) &&
+             tc_cu_check(cudaMemsetAsync(d + off[7], 0, 4, stream), "memset", err, errlen) &&
+             tc_cu_check(cudaMemsetAsync(d + off[8], 0, (size_t)n * 8, stream), "memset", err,
+                         errlen);
+    /* the host buffer must outlive the asynchronous copy: wait for it */
     if (ok)
-        ok = tc_cu_check(cudaMalloc(&d_next, 4), "cudaMalloc", err, errlen) &&
-             tc_cu_check(cudaMalloc(&d_hits, (size_t)njobs * 8), "cudaMalloc", err, errlen) &&
-             tc_cu_check(cudaMalloc(&d_uhits, (size_t)pk.units * TC_BATCH_SHOW * 8), "cudaMalloc",
-                         err, errlen) &&
-             tc_cu_check(cudaMalloc(&d_ucount, (size_t)pk.units * 4), "cudaMalloc", err, errlen) &&
-             tc_cu_check(cudaMemsetAsync(d_next, 0, 4, tc_engine.stream), "memset", err, errlen) &&
-             tc_cu_check(cudaMemsetAsync(d_hits, 0, (size_t)njobs * 8, tc_engine.stream),
-                         "memset", err, errlen);
+        ok = tc_cu_check(cudaStreamSynchronize(stream), "upload", err, errlen);
+    free(rem);
+    if (!ok)
+        return 0;
+    struct TcBatchDev dv = {(const TcBatchJob *)(d + off[0]), (const uint64_t *)(d + off[1]),
+                            (const uint32_t *)(d + off[2]), (const uint16_t *)(d + off[3]),
+                            (const TcBatchRpn *)(d + off[4]), (const uint8_t *)(d + off[5]),
+                            (const uint32_t *)(d + off[6]), pk->units, (uint32_t *)(d + off[7]),
+                            (unsigned long long *)(d + off[8]),
+                            (unsigned long long *)(hd + hoff[0]), (uint32_t *)(hd + hoff[1]),
+                            (uint32_t *)(d + off[9]), (unsigned long long *)(hd + hoff[2]),
+                            (uint32_t *)(hd + hoff[3])};
+    if (!tc_cu_check(cudaEventCreate(&w->ev0), "event", err, errlen) ||
+        !tc_cu_check(cudaEventCreate(&w->ev1), "event", err, errlen) ||
+        !tc_cu_check(cudaEventRecord(w->ev0, stream), "event", err, errlen) ||
+        !tc_batch_launch(&dv, pk->slots, stream, share, &w->grid, err, errlen) ||
+        !tc_cu_check(cudaEventRecord(w->ev1, stream), "event", err, errlen))
+        return 0;
+    w->launched = 1;
+    return 1;
+}
+
+int tc_wave_job_done(const TcWave *w, int i)
+{
+    return w->h_done[i] != 0;
+}
+
+/* 1 when the wave's kernel has finished (0 still running, -1 error) */
+int tc_wave_finished(const TcWave *w)
+{
+    cudaError_t e = cudaEventQuery(w->ev1);
+    return e == cudaSuccess ? 1 : e == cudaErrorNotReady ? 0 : -1;
+}
+
+float tc_wave_ms(const TcWave *w)
+{
     float ms = 0;
-    int grid = 0;
-    if (ok) {
-        struct TcBatchDev d = {d_jobs, d_code, d_luts, d_lists, d_rpn, d_vars, d_unit_job, pk.units,
-                               d_next, d_hits, d_uhits, d_ucount};
-        ok = tc_cu_check(cudaEventRecord(tc_engine.ev0, tc_engine.stream), "event", err, errlen) &&
-             tc_batch_launch(&d, pk.slots, tc_engine.stream, &grid, err, errlen) &&
-             tc_cu_check(cudaEventRecord(tc_engine.ev1, tc_engine.stream), "event", err, errlen) &&
-             tc_cu_check(cudaEventSynchronize(tc_engine.ev1), "batch", err, errlen);
-        if (ok)
-            cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
+    cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+    return ms;
+}
+
+/* Job i's result, valid once tc_wave_job_done(w, i). */
+void tc_wave_result(const TcWave *w, int i, EnumResult *r)
+{
+    const TcBatchJob *J = w->pk.jobs.p;
+    const Enum *e = w->jobs[i];
+    memset(r, 0, sizeof *r);
+    r->space = J[i].space;
+    r->tried = J[i].space;
+    uint64_t passes = (J[i].space + 511) / 512;
+    r->ops = passes * 512 * e->ticks * (e->a->len + (e->mode == EN_EQUIV ? e->b->len : 0));
+    r->hits = w->h_hits[i];
+    r->threads = w->grid * TC_BATCH_BLOCK;
+    for (uint32_t u = 0; u < J[i].units && r->nhit < EN_SHOW && r->hits; u++) {
+        uint32_t c = w->h_ucount[J[i].first_unit + u];
+        for (uint32_t h = 0; h < c; h++)
+            cuda_enum_add_hit(r, w->h_uhits[(size_t)(J[i].first_unit + u) * TC_BATCH_SHOW + h]);
     }
-    if (ok) {
-        hits = tc_xmalloc((size_t)njobs * 8);
-        ucount = tc_xmalloc((size_t)pk.units * 4);
-        ok = tc_cu_check(cudaMemcpy(hits, d_hits, (size_t)njobs * 8, cudaMemcpyDeviceToHost),
-                         "download", err, errlen) &&
-             tc_cu_check(cudaMemcpy(ucount, d_ucount, (size_t)pk.units * 4,
-                                    cudaMemcpyDeviceToHost), "download", err, errlen);
+}
+
+int tc_wave_njobs(const TcWave *w)
+{
+    return w->njobs;
+}
+
+void tc_wave_free(TcWave *w)
+{
+    if (!w)
+        return;
+    if (w->dev)
+        cudaFreeAsync(w->dev, w->stream);
+    if (w->host) {
+        if (w->launched)
+            cudaEventSynchronize(w->ev1);
+        cudaFreeHost(w->host);
     }
+    if (w->ev0)
+        cudaEventDestroy(w->ev0);
+    if (w->ev1)
+        cudaEventDestroy(w->ev1);
+    free(w->unit_job);
+    free(w->pk.jobs.p);
+    free(w->pk.code.p);
+    free(w->pk.luts.p);
+    free(w->pk.lists.p);
+    free(w->pk.rpn.p);
+    free(w->pk.vars.p);
+    free(w);
+}
+
+/* Runs every job in one persistent launch.  results[i] is job i's EnumResult; seconds is the
+   device time of the whole batch. */
+int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char *err,
+                   size_t errlen)
+{
+    if (njobs <= 0)
+        return 1;
+    if (!cuda_engine_init(0, err, errlen))
+        return 0;
+    TcWave *w;
+    if (!tc_wave_prepare(&w, jobs, njobs, err, errlen))
+        return 0;
+    int ok = tc_wave_launch(w, tc_engine.stream, 1.0, err, errlen) &&
+             tc_cu_check(cudaEventSynchronize(w->ev1), "batch", err, errlen);
     if (ok) {
-        const TcBatchJob *J = pk.jobs.p;
-        for (int i = 0; i < njobs && ok; i++) {
-            const Enum *e = jobs[i];
-            EnumResult *r = &results[i];
-            r->space = J[i].space;
-            r->tried = J[i].space;
-            uint64_t passes = (J[i].space + 511) / 512;
-            r->ops = passes * 512 * e->ticks *
-                     (e->a->len + (e->mode == EN_EQUIV ? e->b->len : 0));
-            r->hits = hits[i];
-            r->seconds = ms / 1e3;
-            r->threads = grid * TC_BATCH_BLOCK;
-            for (uint32_t u = 0; u < J[i].units && r->nhit < EN_SHOW && r->hits; u++) {
-                uint32_t c = ucount[J[i].first_unit + u];
-                if (!c)
-                    continue;
-                unsigned long long got[TC_BATCH_SHOW];
-                ok = tc_cu_check(cudaMemcpy(got, (char *)d_uhits + (size_t)(J[i].first_unit + u) *
-                                                                       TC_BATCH_SHOW * 8,
-                                            (size_t)c * 8, cudaMemcpyDeviceToHost),
-                                 "download", err, errlen);
-                for (uint32_t h = 0; ok && h < c; h++)
-                    cuda_enum_add_hit(r, got[h]);
-            }
+        float ms = tc_wave_ms(w);
+        for (int i = 0; i < njobs; i++) {
+            tc_wave_result(w, i, &results[i]);
+            results[i].seconds = ms / 1e3;
         }
         tc_engine.last_kernel_ms = ms;
-        tc_engine.last_grid = (unsigned)grid;
+        tc_engine.last_grid = (unsigned)w->grid;
         tc_engine.last_block = TC_BATCH_BLOCK;
     }
-    cudaFree(d_jobs);
-    cudaFree(d_code);
-    cudaFree(d_luts);
-    cudaFree(d_lists);
-    cudaFree(d_rpn);
-    cudaFree(d_vars);
-    cudaFree(d_unit_job);
-    cudaFree(d_next);
-    cudaFree(d_hits);
-    cudaFree(d_uhits);
-    cudaFree(d_ucount);
-    free(hits);
-    free(uhits);
-    free(ucount);
-    free(unit_job);
-    free(pk.jobs.p);
-    free(pk.code.p);
-    free(pk.luts.p);
-    free(pk.lists.p);
-    free(pk.rpn.p);
-    free(pk.vars.p);
+    tc_wave_free(w);
     return ok;
 }

@@ -67,6 +67,9 @@ struct TcBatchDev {
     unsigned long long *hits;        /* per job */
     unsigned long long *unit_hits;   /* per unit, TC_BATCH_SHOW each */
     uint32_t           *unit_count;  /* per unit */
+    uint32_t           *remaining;   /* per job: units not finished yet */
+    unsigned long long *hits_out;    /* per job, host-mapped: the final count */
+    uint32_t           *done;        /* per job, host-mapped: 1 once every unit is finished */
 };
 
 #endif

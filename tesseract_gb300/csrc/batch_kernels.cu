@@ -250,16 +250,26 @@ __global__ void __launch_bounds__(B) tc_batch_kernel(TcBatchDev d)
             atomicAdd(&block_hits, hits);
         __syncthreads();
         if (tid == 0) {
+            const uint32_t j = d.unit_job[unit];
             d.unit_count[unit] = recorded;
             if (block_hits)
-                atomicAdd(d.hits + d.unit_job[unit], block_hits);
+                atomicAdd(d.hits + j, block_hits);
+            // the last unit of a job publishes its result to the host: every unit's writes are
+            // made visible system-wide before it counts itself finished
+            __threadfence_system();
+            if (atomicSub(d.remaining + j, 1u) == 1u) {
+                __threadfence();
+                d.hits_out[j] = atomicAdd(d.hits + j, 0ull);
+                __threadfence_system();
+                *(volatile uint32_t *)(d.done + j) = 1u;
+            }
         }
         __syncthreads();
     }
 }
 
-extern "C" int tc_batch_launch(const TcBatchDev *d, int slots, cudaStream_t stream, int *grid_out,
-                               char *err, size_t errlen)
+extern "C" int tc_batch_launch(const TcBatchDev *d, int slots, cudaStream_t stream, double share,
+                               int *grid_out, char *err, size_t errlen)
 {
     const size_t smem = (size_t)slots * B * sizeof(uint32_t);
     if (!tc_cu_check(cudaFuncSetAttribute(tc_batch_kernel,
@@ -273,7 +283,7 @@ extern "C" int tc_batch_launch(const TcBatchDev *d, int slots, cudaStream_t stre
         return 0;
     if (per_sm < 1)
         return tc_fail(err, errlen, "the batch needs %zu bytes of shared memory per block", smem);
-    int grid = tc_engine.sms * per_sm;
+    int grid = (int)(tc_engine.sms * per_sm * share);
     if ((uint32_t)grid > d->nunits)
         grid = (int)d->nunits;
     if (grid < 1)

@@ -375,6 +375,103 @@ static int plan_enum(const Enum *e, EnumPlan *pl, char *err, size_t errlen)
     return 1;
 }
 
+/* ---- the generated-kernel cache, keyed by what the code generator reads ---------------------- */
+
+typedef struct {
+    uint64_t h1, h2;
+} Key;
+
+static void mix_bytes(Key *k, const void *p, size_t n)
+{
+    const unsigned char *b = p;
+    for (size_t i = 0; i < n; i++) {
+        k->h1 = (k->h1 ^ b[i]) * 0x100000001b3ull;
+        k->h2 = (k->h2 + b[i] + 0x9E3779B97F4A7C15ull) * 0xff51afd7ed558ccdull;
+        k->h2 ^= k->h2 >> 29;
+    }
+}
+
+static void mix_program(Key *k, const Program *p)
+{
+    for (size_t i = 0; i < p->len; i++) {
+        uint32_t w = p->code[i].addr << 1 | p->code[i].op;
+        mix_bytes(k, &w, 4);
+    }
+    mix_bytes(k, &p->len, sizeof p->len);
+    mix_bytes(k, &p->ncells, sizeof p->ncells);
+    mix_bytes(k, p->inputs, p->ninputs * sizeof *p->inputs);
+    mix_bytes(k, &p->ninputs, sizeof p->ninputs);
+    mix_bytes(k, p->outputs, p->noutputs * sizeof *p->outputs);
+    mix_bytes(k, &p->noutputs, sizeof p->noutputs);
+}
+
+static void enum_key(const TcGenEnum *g, uint64_t *k1, uint64_t *k2)
+{
+    Key k = {0xcbf29ce484222325ull, 0x6a09e667f3bcc909ull};
+    int head[4] = {g->mode, (int)g->ticks, g->block, g->no_map};
+    mix_bytes(&k, head, sizeof head);
+    mix_program(&k, g->a);
+    if (g->b) {
+        mix_program(&k, g->b);
+        mix_bytes(&k, g->b_inputs, g->a->ninputs * sizeof *g->b_inputs);
+        mix_bytes(&k, g->out_map, g->a->noutputs * sizeof *g->out_map);
+    }
+    if (g->spec) {
+        const TcSpec *s = g->spec;
+        mix_bytes(&k, &s->width, sizeof s->width);
+        mix_bytes(&k, s->out, (size_t)s->width * sizeof s->out[0]);
+        mix_bytes(&k, &s->nvars, sizeof s->nvars);
+        mix_bytes(&k, s->var_bits, (size_t)s->nvars * sizeof s->var_bits[0]);
+        for (int v = 0; v < s->nvars; v++)
+            mix_bytes(&k, s->var_pos[v], (size_t)s->var_bits[v] * sizeof s->var_pos[v][0]);
+        mix_bytes(&k, &s->nrpn, sizeof s->nrpn);
+        for (int i = 0; i < s->nrpn; i++) {
+            mix_bytes(&k, &s->rpn[i].op, sizeof s->rpn[i].op);
+            mix_bytes(&k, &s->rpn[i].v, sizeof s->rpn[i].v);
+        }
+    }
+    mix_bytes(&k, &g->target, sizeof g->target);
+    *k1 = k.h1;
+    *k2 = k.h2;
+}
+
+typedef struct {
+    uint64_t k1, k2;
+    TcModule m;
+} EnumEntry;
+
+static EnumEntry *enum_cache;
+static size_t nenum, capenum;
+
+static int lookup_enum(uint64_t k1, uint64_t k2, TcModule *m)
+{
+    int hit = 0;
+    pthread_mutex_lock(&engine_lock);
+    for (size_t i = 0; i < nenum; i++)
+        if (enum_cache[i].k1 == k1 && enum_cache[i].k2 == k2) {
+            *m = enum_cache[i].m;
+            m->info.cached = 1;
+            hit = 1;
+            break;
+        }
+    pthread_mutex_unlock(&engine_lock);
+    return hit;
+}
+
+static void remember_enum(uint64_t k1, uint64_t k2, const TcModule *m)
+{
+    pthread_mutex_lock(&engine_lock);
+    if (nenum == capenum) {
+        capenum = capenum ? 2 * capenum : 64;
+        enum_cache = tc_xrealloc(enum_cache, capenum * sizeof *enum_cache);
+    }
+    enum_cache[nenum].k1 = k1;
+    enum_cache[nenum].k2 = k2;
+    enum_cache[nenum].m = *m;
+    nenum++;
+    pthread_mutex_unlock(&engine_lock);
+}
+
 char *tc_codegen_enum_for(const Enum *e, size_t *len, char *err, size_t errlen)
 {
     EnumPlan pl;
@@ -402,11 +499,16 @@ int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
     if (!cuda_engine_init(0, err, errlen))
         goto done;
     size_t len;
-    src = tc_codegen_enum(&pl.g, &len);
     static const char *const names[] = {"tc_enum"};
     TcModule m;
-    if (!tc_module(src, len, names, 1, NULL, &m, err, errlen))
-        goto done;
+    uint64_t k1, k2;
+    enum_key(&pl.g, &k1, &k2);
+    if (!lookup_enum(k1, k2, &m)) {
+        src = tc_codegen_enum(&pl.g, &len);
+        if (!tc_module(src, len, names, 1, NULL, &m, err, errlen))
+            goto done;
+        remember_enum(k1, k2, &m);
+    }
 
     uint64_t space = 1ull << n, sel, tried, pruns;
     tc_enum_shares(e, space, &sel, &tried, &pruns);

@@ -1,6 +1,7 @@
 """Regenerates the golden fixtures in this directory from the reference itself.
 
-    python tests/golden/make_golden.py [path/to/alpha]
+    python tests/golden/make_golden.py [path/to/alpha]          # programs.json, enum.json
+    python tests/golden/make_golden.py --cli [path/to/alpha]    # cli.json
 
 Needs the reference's `alpha` binary built from its sources (oracle/Makefile builds it into
 oracle/_ref/alpha on an x86 host that has the sources).  Programs come from the reference's own
@@ -12,6 +13,7 @@ output (src/work.c:435-443): "EN mode space tried hits seconds threads ops" and 
 Outputs:
     programs.json   sha256 of the reference's generator output for each (kind, parameters)
     enum.json       enumeration cases and the reference's results
+    cli.json        the reference's stdout and exit code for command lines of the hot path
 """
 from __future__ import annotations
 
@@ -26,7 +28,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-ALPHA = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "oracle", "_ref", "alpha")
+ARGS = [a for a in sys.argv[1:] if not a.startswith("--")]
+ALPHA = ARGS[0] if ARGS else os.path.join(ROOT, "oracle", "_ref", "alpha")
 
 
 def run(args, stdin=None):
@@ -180,5 +183,56 @@ def main():
         json.dump(results, f, indent=1)
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--cli" not in sys.argv:
     main()
+
+
+# ---- the command line: the reference's stdout for the same commands -------------------------
+
+CLI_CASES = [
+    (["verify", "{mul4}", "--spec", "p = a * b"], None),
+    (["verify", "{mul4}", "--spec", "p = a * b + 1"], None),
+    (["verify", "{mul6}", "--spec", "p = a * b ^ 1", "--part", "0/3"], None),
+    (["verify", "{mul6}", "--spec", "p = a * b ^ (a >> 2)", "--raw"], None),
+    (["equiv", "{ra}", "{rb}"], None),
+    (["equiv", "{ra}", "{rc}"], None),
+    (["search", "{hash16}", "--want", "h = 34272"], None),
+    (["search", "{hash16}", "--want", "h = 34272", "--raw"], None),
+    (["verify", "{mul5}", "--spec", "p = a * b", "--ticks", "2"], None),
+]
+
+
+def cli_programs(tmp):
+    import tesseract_gb300 as T
+    progs = {}
+    for name, text in (("mul4", gen_text("mul", {"bits": 4})), ("mul5", gen_text("mul", {"bits": 5})),
+                       ("mul6", gen_text("mul", {"bits": 6})),
+                       ("hash16", gen_text("hash", {"bits": 16, "rounds": 5}))):
+        progs[name] = text
+    a = T.Program.random_in(12, 10, 200, 424242)
+    progs["ra"] = a.text()
+    progs["rb"] = a.rewrite(5).text()
+    progs["rc"] = a.rewrite(5, mutate=True).text()
+    paths = {}
+    for k, v in progs.items():
+        paths[k] = os.path.join(tmp, k + ".asm")
+        with open(paths[k], "w") as f:
+            f.write(v)
+    return progs, paths
+
+
+def cli_main():
+    out = []
+    with tempfile.TemporaryDirectory() as tmp:
+        progs, paths = cli_programs(tmp)
+        for args, _ in CLI_CASES:
+            real = [a.format(**paths) for a in args]
+            rc, stdout, stderr = run(real)
+            text = stdout.replace(tmp + "/", "")
+            out.append({"args": args, "rc": rc, "stdout": text})
+    with open(os.path.join(HERE, "cli.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__" and "--cli" in sys.argv:
+    cli_main()
