@@ -441,7 +441,7 @@ static __attribute__((unused)) void *upload(const Vec *v, int *ok, char *err, si
 
 struct TcWave {
     int                 njobs;
-    const Enum *const  *jobs;
+    const Enum        **jobs;       /* the wave's own copy: a caller may reuse its array */
     Pack                pk;
     uint32_t           *unit_job;
     void               *dev;        /* one device allocation for everything */
@@ -465,7 +465,8 @@ int tc_wave_prepare(TcWave **out, const Enum *const *jobs, int njobs, char *err,
 {
     TcWave *w = tc_xcalloc(1, sizeof *w);
     w->njobs = njobs;
-    w->jobs = jobs;
+    w->jobs = tc_xmalloc(((size_t)njobs + 1) * sizeof *w->jobs);
+    memcpy(w->jobs, jobs, (size_t)njobs * sizeof *w->jobs);
     w->pk.jobs.elem = sizeof(TcBatchJob);
     w->pk.code.elem = 8;
     w->pk.luts.elem = 4;
@@ -649,6 +650,7 @@ void tc_wave_free(TcWave *w)
     if (w->ev1)
         cudaEventDestroy(w->ev1);
     free(w->unit_job);
+    free(w->jobs);
     free(w->pk.jobs.p);
     free(w->pk.code.p);
     free(w->pk.luts.p);

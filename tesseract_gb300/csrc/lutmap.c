@@ -14,7 +14,7 @@
 
 #include "lutmap.h"
 
-#define PRIO 8  /* cuts kept per node */
+#define PRIO 12  /* cuts kept per node */
 
 typedef struct {
     int     leaf[3];
@@ -300,6 +300,47 @@ static void cuts_of(TcNet *t, int n)
     }
 }
 
+static int is_gate(const TcNet *t, int n)
+{
+    return t->node[n].kind == TN_NAND || t->node[n].kind == TN_NOT;
+}
+
+static const Cut *chosen(const TcNet *t, int n)
+{
+    return &t->cuts[(size_t)n * PRIO + t->best[n]];
+}
+
+/* Reference counting of the cover: taking cut c for node n references its leaves; a leaf whose
+   count rises from 0 enters the cover with its own chosen cut.  Both return the LUTs entering
+   (or leaving) the cover. */
+static int cover_ref(TcNet *t, const Cut *c)
+{
+    int area = 1;
+    for (int i = 0; i < c->n; i++) {
+        int l = c->leaf[i];
+        if (is_gate(t, l) && t->refs[l]++ == 0)
+            area += cover_ref(t, chosen(t, l));
+    }
+    return area;
+}
+
+static int cover_deref(TcNet *t, const Cut *c)
+{
+    int area = 1;
+    for (int i = 0; i < c->n; i++) {
+        int l = c->leaf[i];
+        if (is_gate(t, l) && --t->refs[l] == 0)
+            area += cover_deref(t, chosen(t, l));
+    }
+    return area;
+}
+
+static int usable(const TcNet *t, int n, int k)
+{
+    const Cut *c = &t->cuts[(size_t)n * PRIO + k];
+    return !(c->n == 1 && c->leaf[0] == n);  /* the trivial cut cannot implement n itself */
+}
+
 int tc_net_map(TcNet *t, const int *outputs, int nout, int *order, int *norder)
 {
     int n = t->n;
@@ -309,6 +350,7 @@ int tc_net_map(TcNet *t, const int *outputs, int nout, int *order, int *norder)
     t->flow = tc_xcalloc((size_t)n, sizeof *t->flow);
     t->best = tc_xcalloc((size_t)n, sizeof *t->best);
     t->need = tc_xcalloc((size_t)n, 1);
+    /* fanouts, for the area flow of the cuts */
     for (int i = 0; i < n; i++) {
         if (t->node[i].kind == TN_NAND) {
             t->refs[t->node[i].a]++;
@@ -321,32 +363,85 @@ int tc_net_map(TcNet *t, const int *outputs, int nout, int *order, int *norder)
         t->refs[outputs[i]]++;
     for (int i = 0; i < n; i++)
         cuts_of(t, i);
-    /* the cover: outputs first, then the leaves of every chosen cut */
-    for (int i = 0; i < nout; i++)
-        t->need[outputs[i]] = 1;
-    int luts = 0;
-    for (int i = n - 1; i >= 0; i--) {
-        if (!t->need[i] || t->node[i].kind == TN_LEAF || t->node[i].kind == TN_CONST)
+    /* first choice: the least area flow */
+    for (int i = 0; i < n; i++) {
+        if (!is_gate(t, i))
             continue;
-        const Cut *cs = &t->cuts[(size_t)i * PRIO];
         int b = -1;
-        for (int k = 0; k < t->ncut[i]; k++) {
-            if (cs[k].n == 1 && cs[k].leaf[0] == i)
-                continue;  /* the trivial cut cannot implement the node itself */
-            if (b < 0 || cs[k].flow < cs[b].flow)
+        for (int k = 0; k < t->ncut[i]; k++)
+            if (usable(t, i, k) &&
+                (b < 0 || t->cuts[(size_t)i * PRIO + k].flow < t->cuts[(size_t)i * PRIO + b].flow))
                 b = k;
-        }
         t->best[i] = b;
-        for (int k = 0; k < cs[b].n; k++)
-            t->need[cs[b].leaf[k]] = 1;
-        luts++;
     }
+    /* area flow again with the fanouts the cover really has (blended with the estimate before),
+       twice: cuts that absorb a shared node into several LUTs lose their false advantage */
+    float *est = tc_xmalloc((size_t)n * sizeof *est);
+    for (int i = 0; i < n; i++)
+        est[i] = (float)(t->refs[i] > 0 ? t->refs[i] : 1);
+    for (int round = 0; round < 3; round++) {
+        memset(t->refs, 0, (size_t)n * sizeof *t->refs);
+        for (int i = 0; i < nout; i++)
+            if (is_gate(t, outputs[i]) && t->refs[outputs[i]]++ == 0)
+                cover_ref(t, chosen(t, outputs[i]));
+        for (int i = 0; i < n; i++)
+            est[i] = 0.5f * est[i] + 0.5f * (float)(t->refs[i] > 0 ? t->refs[i] : 1);
+        for (int i = 0; i < n; i++) {
+            if (!is_gate(t, i))
+                continue;
+            float bestf = 1e30f;
+            for (int k = 0; k < t->ncut[i]; k++) {
+                if (!usable(t, i, k))
+                    continue;
+                const Cut *c = &t->cuts[(size_t)i * PRIO + k];
+                float f = 1.f;
+                for (int j = 0; j < c->n; j++)
+                    if (is_gate(t, c->leaf[j]))
+                        f += t->flow[c->leaf[j]] / est[c->leaf[j]];
+                if (f < bestf) {
+                    bestf = f;
+                    t->best[i] = k;
+                }
+            }
+            t->flow[i] = bestf;
+        }
+    }
+    free(est);
+    /* the cover of the outputs, reference counted */
+    memset(t->refs, 0, (size_t)n * sizeof *t->refs);
+    for (int i = 0; i < nout; i++)
+        if (is_gate(t, outputs[i]) && t->refs[outputs[i]]++ == 0)
+            cover_ref(t, chosen(t, outputs[i]));
+    /* area recovery: each node in the cover takes the cut that brings the fewest LUTs in */
+    for (int pass = 0; pass < 6; pass++)
+        for (int j = 0; j < n; j++) {
+            int i = pass & 1 ? n - 1 - j : j;
+            if (!is_gate(t, i) || t->refs[i] == 0)
+                continue;
+            cover_deref(t, chosen(t, i));
+            int b = t->best[i], least = 1 << 30;
+            for (int k = 0; k < t->ncut[i]; k++) {
+                if (!usable(t, i, k))
+                    continue;
+                const Cut *c = &t->cuts[(size_t)i * PRIO + k];
+                int a = cover_ref(t, c);
+                cover_deref(t, c);
+                if (a < least) {
+                    least = a;
+                    b = k;
+                }
+            }
+            t->best[i] = b;
+            cover_ref(t, chosen(t, i));
+        }
     int m = 0;
     for (int i = 0; i < n; i++)
-        if (t->need[i] && t->node[i].kind != TN_LEAF && t->node[i].kind != TN_CONST)
+        if (is_gate(t, i) && t->refs[i] > 0) {
+            t->need[i] = 1;
             order[m++] = i;
+        }
     *norder = m;
-    return luts;
+    return m;
 }
 
 void tc_net_lut(const TcNet *t, int node, int *leaves, int *nleaves, uint8_t *tt)
