@@ -193,6 +193,17 @@ void cuda_free(CudaCode *c);
 int  cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen);
 void cuda_enum_add_hit(EnumResult *r, uint64_t x);   /* enum_add_hit, src/enum.c:31-46 */
 
+/* cuda_enum_run without allocation: the same job, kernel and results, with the workspace (hit
+   counter, per-warp hit lists and counts) in a fixed 2.1 MB device array for at most 16,384
+   warps instead of buffers grown by cudaMalloc.  For callers that cannot allocate: a serving loop
+   whose device memory is handed out to admitted jobs, or one with kernels in flight on other
+   streams that a cudaFree would wait for.  It compiles nothing: the job's kernel must have been
+   loaded by an earlier cuda_enum_run of the same job, else it fails with an error; so does a
+   launch needing more warps than the array holds.  The first call on a device looks up the
+   array's address (make it before any stream capture).  Calls share the array: calls that
+   overlap on the GPU race.  No counterpart in the reference. */
+int  cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, size_t errlen);
+
 /* Batches.  Runs every job of an array of enumerations (verify, equiv, search; whole spaces, no
    --part) in one persistent launch of a precompiled interpreter kernel fed from a device work
    queue, and writes one EnumResult per job with the same fields as cuda_enum_run.  No per-program

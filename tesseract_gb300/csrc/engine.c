@@ -482,6 +482,23 @@ char *tc_codegen_enum_for(const Enum *e, size_t *len, char *err, size_t errlen)
     return src;
 }
 
+/* The loaded kernel of an enumeration, only when an earlier cuda_enum_run of the same job compiled
+   and loaded it: no code generation, no compilation, no module load.  For cuda_enum_run_static,
+   whose callers cannot allocate. */
+int tc_enum_cached(const Enum *e, TcModule *m, char *err, size_t errlen)
+{
+    EnumPlan pl;
+    if (!plan_enum(e, &pl, err, errlen))
+        return 0;
+    uint64_t k1, k2;
+    enum_key(&pl.g, &k1, &k2);
+    plan_free(&pl);
+    if (!lookup_enum(k1, k2, m))
+        return tc_fail(err, errlen, "cuda_enum_run_static: this job's kernel is not loaded; run the "
+                       "same job once through cuda_enum_run first");
+    return 1;
+}
+
 void tc_free(void *p)
 {
     free(p);

@@ -65,6 +65,7 @@ int    tc_scratch(TcBuf *b, size_t bytes, char *err, size_t errlen);
 int    tc_module(const char *src, size_t len, const char *const *kernels, int nkernels,
                  const char *extra_opt, TcModule *out, char *err, size_t errlen);
 int    tc_enum_prepare(const Enum *e, int *in_map, int *out_map, char *err, size_t errlen);
+int    tc_enum_cached(const Enum *e, TcModule *m, char *err, size_t errlen);
 void   tc_enum_shares(const Enum *e, uint64_t space, uint64_t *sel_chunks, uint64_t *tried,
                       uint64_t *passes_run);
 
