@@ -36,6 +36,10 @@
 
 /* 1: cube kernels are LOP3-mapped networks (lutmap.c); 0: the instructions as written */
 int tc_cube_map = 1;
+/* the most warps per word a mapped kernel splits its written cells over, and the fewest cells a
+   warp gets */
+int tc_cube_groups = 8;
+int tc_cube_min_cells = 16;
 
 struct CudaCube {
     Program     p;
@@ -45,6 +49,7 @@ struct CudaCube {
     unsigned    nk, nseg;
     int         loop;       /* one kernel, passes loop inside it */
     cudaKernel_t *fn;
+    unsigned    *warps;     /* warps per word of kernel k */
     cudaGraphExec_t graph;
     unsigned    graph_passes;
 };
@@ -213,10 +218,13 @@ static void chunk_body(Src *o, Chunk *k, size_t from, size_t to)
    the start of the chunk (variable c<cell>), RR (variable r), id patterns, and link reads: a
    read across dimensions 0..9 is an opaque leaf computed from the source cell's value at that
    instruction (which is then kept in the cover), a read across 10 and up a load of the
-   segment-start value.  At the end every written cell and RR get their new values. */
+   segment-start value. */
 typedef struct {
-    char  **expr;   /* per node: the expression of a leaf, or NULL */
-    size_t  n, cap;
+    char         **expr;  /* per node: the expression of a leaf, or NULL */
+    int           *cell;  /* per node: the cell whose start value the leaf is, else -1 */
+    int           *src;   /* per node: the node a near link read takes its value from, else -1 */
+    unsigned char *far;   /* per node: a far load */
+    size_t         n, cap;
 } Leaves;
 
 static int leaf(TcNet *net, Leaves *L, const char *expr)
@@ -228,7 +236,14 @@ static int leaf(TcNet *net, Leaves *L, const char *expr)
         while (cap <= (size_t)node)
             cap *= 2;
         L->expr = tc_xrealloc(L->expr, cap * sizeof *L->expr);
-        memset(L->expr + L->cap, 0, (cap - L->cap) * sizeof *L->expr);
+        L->cell = tc_xrealloc(L->cell, cap * sizeof *L->cell);
+        L->src = tc_xrealloc(L->src, cap * sizeof *L->src);
+        L->far = tc_xrealloc(L->far, cap);
+        for (size_t i = L->cap; i < cap; i++) {
+            L->expr[i] = NULL;
+            L->cell[i] = L->src[i] = -1;
+            L->far[i] = 0;
+        }
         L->cap = cap;
     }
     L->expr[node] = tc_xstrdup(expr);
@@ -236,7 +251,12 @@ static int leaf(TcNet *net, Leaves *L, const char *expr)
     return node;
 }
 
-static void name_of(char *buf, size_t len, const TcNet *net, int node)
+static int is_leaf(const Leaves *L, int node)
+{
+    return node >= 0 && (size_t)node < L->cap && L->expr[node];
+}
+
+static void name_of(char *buf, size_t len, int node)
 {
     if (node == 0)
         snprintf(buf, len, "0u");
@@ -244,23 +264,33 @@ static void name_of(char *buf, size_t len, const TcNet *net, int node)
         snprintf(buf, len, "TC_ONES");
     else
         snprintf(buf, len, "n%d", node);
-    (void)net;
 }
 
-static void mapped_body(Src *o, Chunk *k, size_t from, size_t to)
+typedef struct {
+    TcNet  *net;
+    Leaves  L;
+    int    *cur, *start;         /* per cell: its value's node now, its start-value leaf (or -1) */
+    int     rr;                  /* RR's node at the end */
+    int    *order, norder, luts; /* the chosen LUTs in topological order */
+    unsigned char *mapped;       /* per node: a chosen LUT */
+} ChunkNet;
+
+/* Builds and maps the network of instructions from .. to-1 (marks the cells written). */
+static void chunk_net(Chunk *k, size_t from, size_t to, ChunkNet *cn)
 {
     const Program *p = k->p;
-    TcNet *net = tc_net_new();
-    Leaves L = {0};
-    int *cur = tc_xmalloc((p->ncells + 1) * sizeof *cur);
-    int *start = tc_xmalloc((p->ncells + 1) * sizeof *start);
+    memset(cn, 0, sizeof *cn);
+    TcNet *net = cn->net = tc_net_new();
+    Leaves *L = &cn->L;
+    int *cur = cn->cur = tc_xmalloc((p->ncells + 1) * sizeof *cur);
+    int *start = cn->start = tc_xmalloc((p->ncells + 1) * sizeof *start);
     int *need = tc_xmalloc(((to - from) + p->ncells + 4) * sizeof *need), nneed = 0;
     char buf[160];
     for (uint32_t c = 0; c < p->ncells; c++)
         cur[c] = start[c] = -1;
     cur[CELL_ZERO] = 0;
     cur[CELL_ONE] = 1;
-    int rr = leaf(net, &L, "r");
+    int rr = leaf(net, L, "r");
     for (size_t i = from; i < to; i++) {
         Instr in = p->code[i];
         if (in.op != OP_NAND) {
@@ -279,25 +309,27 @@ static void mapped_body(Src *o, Chunk *k, size_t from, size_t to)
             Src t = {0};
             unsigned d = p->special[c].dim;
             id_word(&t, d, (mask >> d) & 1);
-            v = leaf(net, &L, t.s);
+            v = leaf(net, L, t.s);
             free(t.s);
         } else {
             unsigned hi = mask >> 5, lo = mask & 31;
             if (hi < 32 && cur[c] < 0) {  /* first use: the value loaded at the chunk start */
-                use_cell(o, k, c);
                 snprintf(buf, sizeof buf, "c%u", (unsigned)c);
-                cur[c] = start[c] = leaf(net, &L, buf);
+                cur[c] = start[c] = leaf(net, L, buf);
+                L->cell[cur[c]] = (int)c;
             }
             if (hi == 0 && lo == 0) {
                 v = cur[c];
             } else {
                 char src[96];
+                int from_node = -1;
                 if (hi >= 32) {
                     snprintf(src, sizeof src, "mem[%uu * W + (w ^ %uu)]", (unsigned)c, hi);
                 } else {
+                    from_node = cur[c];
                     need[nneed++] = cur[c];  /* the source value must exist as a register */
                     char nm[32];
-                    name_of(nm, sizeof nm, net, cur[c]);
+                    name_of(nm, sizeof nm, cur[c]);
                     if (hi)
                         snprintf(src, sizeof src, "__shfl_xor_sync(TC_FULL, %s, %uu)", nm, hi);
                     else
@@ -307,57 +339,255 @@ static void mapped_body(Src *o, Chunk *k, size_t from, size_t to)
                     snprintf(buf, sizeof buf, "tc_perm(%s, %uu)", src, lo);
                 else
                     snprintf(buf, sizeof buf, "%s", src);
-                v = leaf(net, &L, buf);
+                v = leaf(net, L, buf);
+                L->src[v] = from_node;
+                L->far[v] = hi >= 32;
             }
         }
         rr = tc_net_nand(net, rr, v);
     }
+    cn->rr = rr;
     for (uint32_t c = CELL_FIRST_FREE; c < p->ncells; c++)
         if (k->written[c])
             need[nneed++] = cur[c];
     need[nneed++] = rr;
-    int *order = tc_xmalloc(((size_t)tc_net_size(net) + 1) * sizeof *order), norder = 0;
-    int luts = tc_net_map(net, need, nneed, order, &norder);
-    emit(o, "    // %d LOP3 for %zu NAND/STO instructions\n", luts, to - from);
-    /* leaves and LUTs interleaved in node order: a link leaf comes after its source */
-    int oi = 0;
-    for (int node = 2; node < tc_net_size(net); node++) {
-        if ((size_t)node < L.cap && L.expr[node]) {
-            emit(o, "    const u32 n%d = %s;\n", node, L.expr[node]);
+    int n = tc_net_size(net);
+    cn->order = tc_xmalloc(((size_t)n + 1) * sizeof *cn->order);
+    cn->luts = tc_net_map(net, need, nneed, cn->order, &cn->norder);
+    cn->mapped = tc_xcalloc((size_t)n + 1, 1);
+    for (int i = 0; i < cn->norder; i++)
+        cn->mapped[cn->order[i]] = 1;
+    free(need);
+}
+
+static void chunk_net_free(ChunkNet *cn)
+{
+    for (size_t i = 0; i < cn->L.cap; i++)
+        free(cn->L.expr[i]);
+    free(cn->L.expr);
+    free(cn->L.cell);
+    free(cn->L.src);
+    free(cn->L.far);
+    free(cn->order);
+    free(cn->mapped);
+    free(cn->cur);
+    free(cn->start);
+    tc_net_free(cn->net);
+}
+
+static void emit_lut(Src *o, const ChunkNet *cn, int node, const char *indent)
+{
+    int lv[3], nl;
+    uint8_t tt;
+    tc_net_lut(cn->net, node, lv, &nl, &tt);
+    char a[32], b[32], c[32];
+    name_of(a, sizeof a, lv[0]);
+    name_of(b, sizeof b, nl > 1 ? lv[1] : 0);
+    name_of(c, sizeof c, nl > 2 ? lv[2] : 0);
+    emit(o, "%su32 n%d; TC_LOP3(n%d, %s, %s, %s, 0x%02x);\n", indent, node, node, a, b, c,
+         (unsigned)tt);
+}
+
+/* One warp's code in a split kernel: the cone of `outs` (cells, plus RR when own_rr) in node
+   order.  Every load comes first (start values and far reads, all in flight at once), then a
+   barrier of the whole block, then the LUTs with each cell's store right after its new value, so
+   values do not stay live to the end (a Life generation's last segment writes 1,023 cells).
+   The barrier makes storing safe: the other warps of the block, the only ones that read these
+   words' cells, have loaded every start value they use; inside a segment no written cell is read
+   across a far dimension, so no other block reads them. */
+static void emit_group(Src *o, Chunk *k, const ChunkNet *cn, const uint32_t *outs, int nouts,
+                       int own_rr, unsigned char *in_cone, int *stack, int *store_at,
+                       int *store_next)
+{
+    const Program *p = k->p;
+    int n = tc_net_size(cn->net);
+    memset(in_cone, 0, (size_t)n + 1);
+    int sp = 0;
+    for (int i = 0; i < nouts; i++)
+        stack[sp++] = cn->cur[outs[i]];
+    if (own_rr)
+        stack[sp++] = cn->rr;
+    while (sp) {
+        int v = stack[--sp];
+        if (v < 2 || in_cone[v])
+            continue;
+        in_cone[v] = 1;
+        if (is_leaf(&cn->L, v)) {
+            if (cn->L.src[v] >= 0)
+                stack[sp++] = cn->L.src[v];
             continue;
         }
-        if (oi < norder && order[oi] == node) {
-            int lv[3], nl;
-            uint8_t tt;
-            tc_net_lut(net, node, lv, &nl, &tt);
-            char a[32], b[32], c[32];
-            name_of(a, sizeof a, net, lv[0]);
-            name_of(b, sizeof b, net, nl > 1 ? lv[1] : 0);
-            name_of(c, sizeof c, net, nl > 2 ? lv[2] : 0);
-            emit(o, "    u32 n%d; TC_LOP3(n%d, %s, %s, %s, 0x%02x);\n", node, node, a, b, c,
-                 (unsigned)tt);
-            oi++;
+        int lv[3], nl;
+        uint8_t tt;
+        tc_net_lut(cn->net, v, lv, &nl, &tt);
+        for (int j = 0; j < nl; j++)
+            stack[sp++] = lv[j];
+    }
+    for (int i = 0; i <= n; i++)
+        store_at[i] = -1;
+    for (int i = 0; i < nouts; i++) {
+        int at = cn->cur[outs[i]] < 2 ? n : cn->cur[outs[i]];
+        store_next[outs[i]] = store_at[at];
+        store_at[at] = (int)outs[i];
+    }
+    char nm[32];
+    for (int v = 2; v < n; v++)
+        if (in_cone[v] && is_leaf(&cn->L, v) && cn->L.cell[v] >= 0)
+            emit(o, "        const u32 c%d = m[%du * W];\n", cn->L.cell[v], cn->L.cell[v]);
+    for (int v = 2; v < n; v++)
+        if (in_cone[v] && is_leaf(&cn->L, v) && cn->L.far[v])
+            emit(o, "        const u32 n%d = %s;\n", v, cn->L.expr[v]);
+    /* every warp of the block has read the words' start values before any warp stores; the
+       non-.aligned barrier may be reached from different code, once per warp */
+    emit(o, "        asm volatile(\"barrier.sync 0;\" ::: \"memory\");\n");
+    int luts = 0;
+    for (int v = 2; v <= n; v++) {
+        if (v < n && in_cone[v]) {
+            if (is_leaf(&cn->L, v)) {
+                if (!cn->L.far[v])
+                    emit(o, "        const u32 n%d = %s;\n", v, cn->L.expr[v]);
+            } else if (cn->mapped[v]) {
+                emit_lut(o, cn, v, "        ");
+                luts++;
+            }
+        }
+        for (int c = store_at[v]; c >= 0; c = store_next[c]) {
+            name_of(nm, sizeof nm, cn->cur[c]);
+            emit(o, "        if (t < W) m[%uu * W] = %s;\n", (unsigned)c, nm);
+            k->written[c] = 2;
         }
     }
+    if (own_rr) {
+        name_of(nm, sizeof nm, cn->rr);
+        emit(o, "        if (t < W) rr[w] = %s;\n", nm);
+    }
+    emit(o, "        // %d LOP3\n", luts);
+    (void)p;
+}
+
+/* Warps per word for a chunk kernel: its written cells split into groups of at least
+   tc_cube_min_cells, at most tc_cube_groups groups (1 for kernels that loop over passes). */
+static unsigned chunk_groups(const Program *p, size_t from, size_t to, int loop)
+{
+    if (loop || !tc_cube_map)
+        return 1;
+    unsigned char *w = tc_xcalloc(p->ncells + 1, 1);
+    unsigned nw = 0;
+    for (size_t i = from; i < to; i++)
+        if (p->code[i].op != OP_NAND && !tc_program_readonly(p, p->code[i].addr) &&
+            !w[p->code[i].addr]) {
+            w[p->code[i].addr] = 1;
+            nw++;
+        }
+    free(w);
+    unsigned g = nw / (unsigned)(tc_cube_min_cells > 0 ? tc_cube_min_cells : 1);
+    if (g > (unsigned)tc_cube_groups)
+        g = (unsigned)tc_cube_groups;
+    return g ? g : 1;
+}
+
+/* The mapped body of a kernel that does not loop: `groups` warps per word, warp y computing the
+   cone of the y-th share of the written cells (RR with the last), so a chunk runs on `groups`
+   times as many warps; nodes that several cones share are computed in each. */
+static void split_body(Src *o, Chunk *k, size_t from, size_t to, unsigned groups)
+{
+    const Program *p = k->p;
+    ChunkNet cn;
+    chunk_net(k, from, to, &cn);
+    uint32_t *outs = tc_xmalloc((p->ncells + 1) * sizeof *outs);
+    int nouts = 0;
+    for (uint32_t c = CELL_FIRST_FREE; c < p->ncells; c++)
+        if (k->written[c])
+            outs[nouts++] = c;
+    int n = tc_net_size(cn.net);
+    unsigned char *in_cone = tc_xmalloc((size_t)n + 1);
+    int *stack = tc_xmalloc((((size_t)n + 1) * 3 + p->ncells + 2) * sizeof *stack);
+    int *store_at = tc_xmalloc(((size_t)n + 1) * sizeof *store_at);
+    int *store_next = tc_xmalloc(((size_t)p->ncells + 1) * sizeof *store_next);
+    emit(o, "    // %d LOP3 for %zu NAND/STO instructions, %u group(s)\n", cn.luts, to - from,
+         groups);
+    /* each output's own cone size (LUTs, at least 1), then contiguous shares of about equal
+       total size */
+    double *weight = tc_xmalloc(((size_t)nouts + 1) * sizeof *weight), total = 0;
+    int *stamp = tc_xcalloc((size_t)n + 1, sizeof *stamp);
+    for (int i = 0; i < nouts; i++) {
+        int sp = 0, size = 0;
+        stack[sp++] = cn.cur[outs[i]];
+        while (sp) {
+            int v = stack[--sp];
+            if (v < 2 || stamp[v] == i + 1)
+                continue;
+            stamp[v] = i + 1;
+            if (is_leaf(&cn.L, v)) {
+                if (cn.L.src[v] >= 0)
+                    stack[sp++] = cn.L.src[v];
+                continue;
+            }
+            int lv[3], nl;
+            uint8_t tt;
+            tc_net_lut(cn.net, v, lv, &nl, &tt);
+            size++;
+            for (int j = 0; j < nl; j++)
+                stack[sp++] = lv[j];
+        }
+        weight[i] = size > 0 ? size : 1;
+        total += weight[i];
+    }
+    free(stamp);
+    int *cut = tc_xmalloc(((size_t)groups + 1) * sizeof *cut);
+    cut[0] = 0;
+    double acc = 0;
+    unsigned gi = 1;
+    for (int i = 0; i < nouts && gi < groups; i++) {
+        acc += weight[i];
+        if (acc >= total * gi / groups && nouts - (i + 1) >= (int)(groups - gi))
+            cut[gi++] = i + 1;
+    }
+    while (gi <= groups)
+        cut[gi++] = nouts;
+    free(weight);
+    for (unsigned g = 0; g < groups; g++) {
+        int lo = cut[g], hi = cut[g + 1];
+        emit(o, "    if (threadIdx.y == %uu) {\n", g);
+        emit_group(o, k, &cn, outs + lo, hi - lo, g + 1 == groups, in_cone, stack, store_at,
+                   store_next);
+        emit(o, "    }\n");
+    }
+    free(cut);
+    free(outs);
+    free(in_cone);
+    free(stack);
+    free(store_at);
+    free(store_next);
+    chunk_net_free(&cn);
+}
+
+/* The mapped body of a kernel that loops over passes: cells are the loop-carried variables
+   c<cell>, assigned their new values at the end of each pass. */
+static void loop_body(Src *o, Chunk *k, size_t from, size_t to)
+{
+    const Program *p = k->p;
+    ChunkNet cn;
+    chunk_net(k, from, to, &cn);
+    emit(o, "    // %d LOP3 for %zu NAND/STO instructions\n", cn.luts, to - from);
+    int n = tc_net_size(cn.net);
+    for (int v = 2; v < n; v++) {
+        if (is_leaf(&cn.L, v)) {
+            if (cn.L.cell[v] >= 0)
+                use_cell(o, k, (uint32_t)cn.L.cell[v]);  /* a cell the pass only reads */
+            emit(o, "    const u32 n%d = %s;\n", v, cn.L.expr[v]);
+        } else if (cn.mapped[v])
+            emit_lut(o, &cn, v, "    ");
+    }
+    char nm[32];
     for (uint32_t c = CELL_FIRST_FREE; c < p->ncells; c++)
         if (k->written[c]) {
-            if (!k->loaded[c]) {
-                emit(o, "    u32 c%u;\n", (unsigned)c);
-                k->loaded[c] = 1;
-            }
-            name_of(buf, sizeof buf, net, cur[c]);
-            emit(o, "    c%u = %s;\n", (unsigned)c, buf);
+            name_of(nm, sizeof nm, cn.cur[c]);
+            emit(o, "    c%u = %s;\n", (unsigned)c, nm);
         }
-    name_of(buf, sizeof buf, net, rr);
-    emit(o, "    r = %s;\n", buf);
-    for (size_t i = 0; i < L.cap; i++)
-        free(L.expr[i]);
-    free(L.expr);
-    free(order);
-    free(need);
-    free(cur);
-    free(start);
-    tc_net_free(net);
+    name_of(nm, sizeof nm, cn.rr);
+    emit(o, "    r = %s;\n", nm);
+    chunk_net_free(&cn);
 }
 
 /* One kernel for instructions from .. to-1; with loop != 0 the whole pass, `passes` times. */
@@ -365,12 +595,20 @@ static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size
                         int loop)
 {
     Chunk k = {p, W, tc_xcalloc(p->ncells + 1, 1), tc_xcalloc(p->ncells + 1, 1)};
-    emit(o, "extern \"C\" __global__ void __launch_bounds__(%d) tc_cube_%u(u32 *__restrict__ mem, "
-            "u32 *__restrict__ rr, const u32 passes)\n{\n", TC_CUBE_BLOCK, idx);
+    unsigned groups = chunk_groups(p, from, to, loop);
+    emit(o, "extern \"C\" __global__ void __launch_bounds__(%u) tc_cube_%u(u32 *__restrict__ mem, "
+            "u32 *__restrict__ rr, const u32 passes)\n{\n", TC_CUBE_BLOCK * groups, idx);
     emit(o, "    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;\n");
     emit(o, "    const u32 w = t & (W - 1u);\n");
     emit(o, "    u32 *const m = mem + w;\n");
     emit(o, "    u32 r = rr[w];\n");
+    if (tc_cube_map && !loop) {
+        split_body(o, &k, from, to, groups);
+        emit(o, "}\n");
+        free(k.loaded);
+        free(k.written);
+        return;
+    }
     if (loop) {
         /* every cell the pass touches is loop-carried: load before the loop */
         for (size_t i = from; i < to; i++) {
@@ -383,14 +621,14 @@ static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size
         emit(o, "#pragma unroll 1\n    for (u32 pass = 0; pass < passes; pass++) {\n");
     }
     if (tc_cube_map)
-        mapped_body(o, &k, from, to);
+        loop_body(o, &k, from, to);
     else
         chunk_body(o, &k, from, to);
     if (loop)
         emit(o, "    }\n");
     emit(o, "    if (t < W) {\n");
     for (uint32_t c = CELL_FIRST_FREE; c < p->ncells; c++)
-        if (k.written[c])
+        if (k.written[c] == 1)
             emit(o, "        m[%uu * W] = c%u;\n", (unsigned)c, (unsigned)c);
     emit(o, "        rr[w] = r;\n    }\n}\n");
     free(k.loaded);
@@ -481,6 +719,7 @@ void cuda_cube_free(CudaCube *c)
     cudaFree(c->rr);
     free(c->first);
     free(c->fn);
+    free(c->warps);
     tc_program_free(&c->p);
     free(c);
 }
@@ -512,6 +751,9 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
     free(cuts);
     c->loop = c->nk == 1 && c->dims <= FAR_DIM;
     c->fn = tc_xcalloc(c->nk, sizeof *c->fn);
+    c->warps = tc_xcalloc(c->nk, sizeof *c->warps);
+    for (unsigned k = 0; k < c->nk; k++)
+        c->warps[k] = chunk_groups(p, c->first[k], c->first[k + 1], c->loop);
     size_t words = (size_t)c->W * (p->ncells + 1);
     if (!tc_cu_check(cudaMalloc((void **)&c->mem, words * 4), "cudaMalloc", err, errlen) ||
         !tc_cu_check(cudaMalloc((void **)&c->rr, (size_t)c->W * 4), "cudaMalloc", err, errlen))
@@ -622,8 +864,9 @@ static int launch_pass(CudaCube *c, cudaStream_t s, unsigned passes)
     for (unsigned k = 0; k < c->nk; k++) {
         uint32_t *mem = c->mem, *rr = c->rr;
         void *args[] = {&mem, &rr, &passes};
-        if (cudaLaunchKernel((const void *)c->fn[k], dim3u(grid), dim3u(block), args, 0, s) !=
-            cudaSuccess)
+        dim3 b = dim3u(block);
+        b.y = c->warps[k];
+        if (cudaLaunchKernel((const void *)c->fn[k], dim3u(grid), b, args, 0, s) != cudaSuccess)
             return 0;
     }
     return 1;

@@ -57,6 +57,37 @@ def test_check_random_link_programs(seed, dims):
     assert r["compared"] == (1 << dims) * 5
 
 
+@pytest.fixture
+def split_every_cell():
+    """Kernels split over as many warps per word as they can (one written cell per warp, up to
+    8), so that the block barrier and the per-warp cones are exercised on small programs."""
+    import ctypes as C
+    groups = C.c_int.in_dll(T.lib(), "tc_cube_groups")
+    cells = C.c_int.in_dll(T.lib(), "tc_cube_min_cells")
+    old = groups.value, cells.value
+    groups.value, cells.value = 8, 1
+    yield
+    groups.value, cells.value = old
+
+
+@pytest.mark.parametrize("seed,dims", [(s, d) for s in range(6) for d in (11, 12, 13)])
+def test_check_random_link_programs_split(seed, dims, split_every_cell):
+    text = random_link_program(seed * 57 + dims, dims, cells=10 + seed * 6, links=6 + seed * 3,
+                               length=200 + seed * 150)
+    p = T.Program.from_asm(text)
+    r = T.check(p, seed=seed + 11, ticks=4)
+    assert r["ok"], (r, text)
+
+
+@pytest.mark.parametrize("dims,rbits,w,h", [(12, 6, 8, 8), (14, 7, 16, 8)])
+def test_life_cube_small_split(dims, rbits, w, h, split_every_cell):
+    L = LifeCube(dims, rbits, w=w, h=h)
+    L.seed(9)
+    start = L.board()
+    L.run(7)
+    assert (L.board() == life_reference(start, 7)).all()
+
+
 @pytest.mark.parametrize("w,h,rb,cb", [(4, 4, 5, 5), (3, 5, 6, 6), (2, 2, 4, 5)])
 def test_check_life_cube_programs(w, h, rb, cb):
     p = T.Program.gen_life_cube(w, h, rb, cb)
