@@ -224,24 +224,38 @@ int  cuda_super_search(const SuperSpec *sp, const SuperOpts *o, SuperResult *r, 
                        size_t errlen);
 int  cuda_super_check(const SuperSpec *sp, const SuperProg *p, char *err, size_t errlen);
 
-/* Serving.  Jobs arrive at arrival[i] seconds after the call starts (sorted); they are admitted
-   while fewer than max_inflight_jobs are on the device and their packed footprint fits
-   max_device_bytes, and run in waves of up to max_wave_jobs: each wave is one persistent launch
-   of the batched engine on one of `streams` streams, taking `share` of the GPU's resident blocks,
-   so waves overlap on the device.  start[i] / finish[i] get the seconds (from the call's start)
-   when job i was launched and when its result was known on the host; results[i] its result,
-   the same as cuda_enum_run's.  Zero fields take defaults (4 streams, 4096 jobs, 8 GiB, 1024,
-   0.5).  No counterpart in the reference. */
+/* Serving.  Jobs arrive at arrival[i] seconds after the call starts (sorted) and each runs on
+   one of two engines, chosen when it arrives (`route`; automatic by default: the generated-kernel
+   engine when the GPU time it saves over the interpreter outweighs the job's compile time spread
+   over the compile threads):
+   - the batched interpreter: jobs are admitted while fewer than max_inflight_jobs are on the
+     device and their packed footprint fits max_device_bytes, and run in waves of up to
+     max_wave_jobs, each one persistent launch on one of `streams` streams taking `share` of the
+     GPU's resident blocks, so waves overlap on the device;
+   - the generated-kernel engine of cuda_enum_run: compile_threads host threads generate and
+     compile (cached by what the generator reads) while earlier jobs run; up to compiled_slots
+     compiled jobs are on the device at once, each on its own stream and preallocated workspace.
+   start[i] / finish[i] get the seconds (from the call's start) when job i was launched and when
+   its result was known on the host; results[i] its result, the same as cuda_enum_run's;
+   engine_used[i] (may be NULL) 0 for the interpreter, 1 for generated code.  Zero fields take
+   defaults (4 streams, 4096 jobs, 8 GiB, 1024 jobs, 0.5, 12 threads, 4 slots, automatic
+   routing).  No counterpart in the reference. */
+#define CUDA_SERVE_AUTO        0
+#define CUDA_SERVE_INTERPRETER 1
+#define CUDA_SERVE_COMPILED    2
 typedef struct {
     int    streams;
     int    max_inflight_jobs;
     size_t max_device_bytes;
     int    max_wave_jobs;
     double share;
+    int    compile_threads;
+    int    compiled_slots;
+    int    route;
 } CudaServeOpts;
 int  cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
                     const CudaServeOpts *opts, double *start, double *finish,
-                    EnumResult *results, char *err, size_t errlen);
+                    EnumResult *results, int *engine_used, char *err, size_t errlen);
 
 /* Random-state parity against the reference semantics.  Replaces
    check_lanes(p, jit, seed, ticks, 0, r) (src/check.h:25, src/check.c:52-113): every machine of

@@ -388,16 +388,22 @@ def batch_run(jobs) -> list:
     return [res[i].as_dict() for i in range(n)]
 
 
+SERVE_AUTO, SERVE_INTERPRETER, SERVE_COMPILED = 0, 1, 2
+
+
 class ServeOpts(C.Structure):
     _fields_ = [("streams", C.c_int), ("max_inflight_jobs", C.c_int),
                 ("max_device_bytes", C.c_size_t), ("max_wave_jobs", C.c_int),
-                ("share", C.c_double)]
+                ("share", C.c_double), ("compile_threads", C.c_int),
+                ("compiled_slots", C.c_int), ("route", C.c_int)]
 
 
 def serve_run(jobs, arrivals, streams=4, max_inflight_jobs=0, max_device_bytes=0,
-              max_wave_jobs=0, share=0.0):
+              max_wave_jobs=0, share=0.0, compile_threads=0, compiled_slots=0,
+              route=SERVE_AUTO, engines=None):
     """Continuous-batching serving (cuda_serve_run): job i arrives arrivals[i] seconds after
-    the call starts.  Returns (results, start, finish), times in seconds from the start."""
+    the call starts.  Returns (results, start, finish), times in seconds from the start; a list
+    passed as `engines` gets each job's engine (0 interpreter, 1 generated code)."""
     jobs = list(jobs)
     n = len(jobs)
     structs = [make_enum(j["mode"], j["a"], j.get("b"), j.get("spec"), j.get("ticks", 1))
@@ -407,16 +413,21 @@ def serve_run(jobs, arrivals, streams=4, max_inflight_jobs=0, max_device_bytes=0
     start = (C.c_double * max(n, 1))()
     finish = (C.c_double * max(n, 1))()
     res = (EnumResult * max(n, 1))()
-    o = ServeOpts(streams, max_inflight_jobs, max_device_bytes, max_wave_jobs, share)
+    used = (C.c_int * max(n, 1))()
+    o = ServeOpts(streams, max_inflight_jobs, max_device_bytes, max_wave_jobs, share,
+                  compile_threads, compiled_slots, route)
     err = _err()
     L = lib()
     L.cuda_serve_run.restype = C.c_int
     L.cuda_serve_run.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(ServeOpts),
-                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]
+                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p,
+                                 C.c_size_t]
     if not L.cuda_serve_run(C.cast(arr, C.c_void_p), C.cast(at, C.c_void_p), n, C.byref(o),
                             C.cast(start, C.c_void_p), C.cast(finish, C.c_void_p),
-                            C.cast(res, C.c_void_p), err, len(err)):
+                            C.cast(res, C.c_void_p), C.cast(used, C.c_void_p), err, len(err)):
         raise EngineError(err.value.decode())
+    if engines is not None:
+        engines[:] = list(used[:n])
     return [res[i].as_dict() for i in range(n)], list(start[:n]), list(finish[:n])
 
 

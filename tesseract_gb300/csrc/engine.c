@@ -504,38 +504,39 @@ void tc_free(void *p)
     free(p);
 }
 
-int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
+/* ---- one enumeration in steps ---------------------------------------------------------------- */
+
+/* Workspace of a launch: the hit counter, then 16 hits per warp, then a count per warp. */
+#define WS_LIST 256u
+
+int tc_enum_job_prepare(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
 {
-    memset(r, 0, sizeof *r);
+    memset(j, 0, sizeof *j);
     EnumPlan pl;
-    char *src = NULL;
-    int ok = 0;
     if (!plan_enum(e, &pl, err, errlen))
         return 0;
-    size_t n = e->a->ninputs;
+    int ok = 0;
+    char *src = NULL;
     if (!cuda_engine_init(0, err, errlen))
         goto done;
-    size_t len;
     static const char *const names[] = {"tc_enum"};
-    TcModule m;
     uint64_t k1, k2;
     enum_key(&pl.g, &k1, &k2);
-    if (!lookup_enum(k1, k2, &m)) {
+    if (!lookup_enum(k1, k2, &j->m)) {
+        size_t len;
         src = tc_codegen_enum(&pl.g, &len);
-        if (!tc_module(src, len, names, 1, NULL, &m, err, errlen))
+        if (!tc_module(src, len, names, 1, NULL, &j->m, err, errlen))
             goto done;
-        remember_enum(k1, k2, &m);
+        remember_enum(k1, k2, &j->m);
     }
-
-    uint64_t space = 1ull << n, sel, tried, pruns;
+    uint64_t space = 1ull << e->a->ninputs, sel, tried, pruns;
     tc_enum_shares(e, space, &sel, &tried, &pruns);
-    r->space = space;
-    r->tried = tried;
-    r->ops = pruns * 512 * e->ticks * (e->a->len + (e->mode == EN_EQUIV ? e->b->len : 0));
-
+    j->base.space = space;
+    j->base.tried = tried;
+    j->base.ops = pruns * 512 * e->ticks * (e->a->len + (e->mode == EN_EQUIV ? e->b->len : 0));
     int per_sm = 0;
-    if (!tc_cu_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)m.fn[0],
-                                                                     TC_ENUM_BLOCK, 0),
+    if (!tc_cu_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                         &per_sm, (const void *)j->m.fn[0], TC_ENUM_BLOCK, 0),
                      "occupancy", err, errlen))
         goto done;
     if (per_sm < 1)
@@ -551,70 +552,129 @@ int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
     per_warp = (per_warp + 31) / 32 * 32;
     if (!per_warp)
         per_warp = 32;
+    j->blocks = blocks;
+    j->warps = warps;
+    j->words = words;
+    j->space = space;
+    j->per_warp = per_warp;
+    j->parts = (uint32_t)e->parts;
+    j->part = (uint32_t)e->part;
+    j->nsel = (uint32_t)(e->part_end - e->part + 1);
+    ok = 1;
+done:
+    free(src);
+    plan_free(&pl);
+    return ok;
+}
+
+size_t tc_enum_job_ws_bytes(const TcEnumJob *j)
+{
+    return WS_LIST + (size_t)j->warps * (16 * 8 + 4);
+}
+
+size_t tc_enum_job_ws_max(void)
+{
+    /* at most 2,048 threads per SM: 64 warps */
+    return WS_LIST + (size_t)tc_engine.sms * 64 * (16 * 8 + 4);
+}
+
+static int launch_enum(const TcEnumJob *j, void *hits, void *list, void *count, cudaStream_t st,
+                       char *err, size_t errlen)
+{
+    EnumArgs args;
+    memset(&args, 0, sizeof args);
+    args.words = j->words;
+    args.space = j->space;
+    args.per_warp = j->per_warp;
+    args.parts = j->parts;
+    args.part = j->part;
+    args.nsel = j->nsel;
+    args.hits = hits;
+    args.list = list;
+    args.count = count;
+    void *params[] = {&args};
+    return tc_cu_check(cudaMemsetAsync(hits, 0, 8, st), "memset", err, errlen) &&
+           tc_cu_check(cudaLaunchKernel((const void *)j->m.fn[0], dim3u((unsigned)j->blocks),
+                                        dim3u(TC_ENUM_BLOCK), params, 0, st),
+                       "launch tc_enum", err, errlen);
+}
+
+int tc_enum_job_launch(const TcEnumJob *j, void *dev_ws, void *host_ws, cudaStream_t st, char *err,
+                       size_t errlen)
+{
+    char *d = dev_ws;
+    return launch_enum(j, d, d + WS_LIST, d + WS_LIST + (size_t)j->warps * 16 * 8, st, err,
+                       errlen) &&
+           tc_cu_check(cudaMemcpyAsync(host_ws, dev_ws, tc_enum_job_ws_bytes(j),
+                                       cudaMemcpyDeviceToHost, st),
+                       "workspace copy", err, errlen);
+}
+
+void tc_enum_job_result(const TcEnumJob *j, const void *host_ws, EnumResult *r)
+{
+    const char *h = host_ws;
+    const uint64_t *list = (const uint64_t *)(h + WS_LIST);
+    const uint32_t *count = (const uint32_t *)(h + WS_LIST + (size_t)j->warps * 16 * 8);
+    *r = j->base;
+    memcpy(&r->hits, h, 8);
+    r->threads = (int)(j->blocks * TC_ENUM_BLOCK);
+    for (uint64_t w = 0; w < j->warps && r->hits && r->nhit < EN_SHOW; w++)
+        for (uint32_t i = 0; i < count[w]; i++)
+            cuda_enum_add_hit(r, list[w * 16 + i]);
+}
+
+int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
+{
+    memset(r, 0, sizeof *r);
+    TcEnumJob j;
+    if (!tc_enum_job_prepare(e, &j, err, errlen))
+        return 0;
+    uint64_t warps = j.warps;
     if (!tc_scratch(&tc_engine.ws_hits, 8, err, errlen) ||
         !tc_scratch(&tc_engine.ws_list, warps * 16 * 8, err, errlen) ||
         !tc_scratch(&tc_engine.ws_count, warps * 4, err, errlen))
-        goto done;
-    CU(cudaMemsetAsync(tc_engine.ws_hits.ptr, 0, 8, tc_engine.stream), "memset");
-    EnumArgs args;
-    memset(&args, 0, sizeof args);
-    args.words = words;
-    args.space = space;
-    args.per_warp = per_warp;
-    args.parts = (uint32_t)e->parts;
-    args.part = (uint32_t)e->part;
-    args.nsel = (uint32_t)(e->part_end - e->part + 1);
-    args.hits = tc_engine.ws_hits.ptr;
-    args.list = tc_engine.ws_list.ptr;
-    args.count = tc_engine.ws_count.ptr;
-    void *params[] = {&args};
-    CU(cudaEventRecord(tc_engine.ev0, tc_engine.stream), "event");
-    CU(cudaLaunchKernel((const void *)m.fn[0], dim3u((unsigned)blocks), dim3u(TC_ENUM_BLOCK),
-                        params, 0, tc_engine.stream),
-       "launch tc_enum");
-    CU(cudaEventRecord(tc_engine.ev1, tc_engine.stream), "event");
+        return 0;
+    cudaStream_t st = tc_engine.stream;
+    if (!tc_cu_check(cudaEventRecord(tc_engine.ev0, st), "event", err, errlen) ||
+        !launch_enum(&j, tc_engine.ws_hits.ptr, tc_engine.ws_list.ptr, tc_engine.ws_count.ptr, st,
+                     err, errlen) ||
+        !tc_cu_check(cudaEventRecord(tc_engine.ev1, st), "event", err, errlen))
+        return 0;
+    *r = j.base;
     uint64_t hits = 0;
     uint32_t *count = tc_xmalloc(warps * 4);
-    uint64_t *list = tc_xmalloc(warps * 16 * 8);
-    cudaError_t rc = cudaMemcpyAsync(&hits, tc_engine.ws_hits.ptr, 8, cudaMemcpyDeviceToHost,
-                                     tc_engine.stream);
+    cudaError_t rc = cudaMemcpyAsync(&hits, tc_engine.ws_hits.ptr, 8, cudaMemcpyDeviceToHost, st);
     if (rc == cudaSuccess)
-        rc = cudaMemcpyAsync(count, tc_engine.ws_count.ptr, warps * 4, cudaMemcpyDeviceToHost,
-                             tc_engine.stream);
+        rc = cudaMemcpyAsync(count, tc_engine.ws_count.ptr, warps * 4, cudaMemcpyDeviceToHost, st);
     if (rc == cudaSuccess)
-        rc = cudaStreamSynchronize(tc_engine.stream);
+        rc = cudaStreamSynchronize(st);
     if (rc != cudaSuccess) {
         free(count);
-        free(list);
-        tc_cu_check(rc, "tc_enum", err, errlen);
-        goto done;
+        return tc_cu_check(rc, "tc_enum", err, errlen);
     }
     /* only the warps that recorded something; lists are short */
-    for (uint64_t w = 0; w < warps && r->nhit < EN_SHOW + 0; w++) {
+    for (uint64_t w = 0; w < warps && r->nhit < EN_SHOW; w++) {
         if (!count[w])
             continue;
         uint64_t got[16];
-        CU(cudaMemcpy(got, (char *)tc_engine.ws_list.ptr + w * 16 * 8, (size_t)count[w] * 8,
-                      cudaMemcpyDeviceToHost),
-           "hits");
+        rc = cudaMemcpy(got, (char *)tc_engine.ws_list.ptr + w * 16 * 8, (size_t)count[w] * 8,
+                        cudaMemcpyDeviceToHost);
+        if (rc != cudaSuccess) {
+            free(count);
+            return tc_cu_check(rc, "hits", err, errlen);
+        }
         for (uint32_t i = 0; i < count[w]; i++)
             cuda_enum_add_hit(r, got[i]);
     }
+    free(count);
     float ms = 0;
     cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
     r->seconds = ms / 1e3;
     r->hits = hits;
-    r->threads = (int)(blocks * TC_ENUM_BLOCK);
-    tc_engine.last = m.info;
+    r->threads = (int)(j.blocks * TC_ENUM_BLOCK);
+    tc_engine.last = j.m.info;
     tc_engine.last_kernel_ms = ms;
-    tc_engine.last_grid = (unsigned)blocks;
+    tc_engine.last_grid = (unsigned)j.blocks;
     tc_engine.last_block = TC_ENUM_BLOCK;
-    free(count);
-    free(list);
-    ok = 1;
-done:
-fail:
-    free(src);
-    plan_free(&pl);
-    return ok;
+    return 1;
 }

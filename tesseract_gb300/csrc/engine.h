@@ -66,6 +66,25 @@ int    tc_module(const char *src, size_t len, const char *const *kernels, int nk
                  const char *extra_opt, TcModule *out, char *err, size_t errlen);
 int    tc_enum_prepare(const Enum *e, int *in_map, int *out_map, char *err, size_t errlen);
 int    tc_enum_cached(const Enum *e, TcModule *m, char *err, size_t errlen);
+
+/* One enumeration on the generated-kernel engine in steps, for callers that overlap many
+   (serving): prepare (refusals, code generation, NVRTC and module load through the cache, the
+   launch shape; no device work; safe from several host threads at once), launch on a stream into
+   a caller's device workspace of tc_enum_job_ws_bytes (at most tc_enum_job_ws_max) with the
+   workspace copied behind it into the caller's pinned host memory, and the result from that copy
+   once the stream has passed it. */
+typedef struct {
+    TcModule   m;
+    uint64_t   words, space, per_warp, blocks, warps;
+    uint32_t   parts, part, nsel;
+    EnumResult base;  /* space, tried, ops */
+} TcEnumJob;
+int    tc_enum_job_prepare(const Enum *e, TcEnumJob *j, char *err, size_t errlen);
+size_t tc_enum_job_ws_bytes(const TcEnumJob *j);
+size_t tc_enum_job_ws_max(void);
+int    tc_enum_job_launch(const TcEnumJob *j, void *dev_ws, void *host_ws, cudaStream_t st,
+                          char *err, size_t errlen);
+void   tc_enum_job_result(const TcEnumJob *j, const void *host_ws, EnumResult *r);
 void   tc_enum_shares(const Enum *e, uint64_t space, uint64_t *sel_chunks, uint64_t *tried,
                       uint64_t *passes_run);
 

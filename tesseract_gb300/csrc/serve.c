@@ -1,13 +1,20 @@
 /* Serving with continuous batching: jobs arrive over time (an arrival time per job), are admitted
-   by footprint as device memory and in-flight slots free up, and run in waves: each wave is the
-   batched engine's persistent kernel over the jobs admitted together, on one of several streams,
-   with a share of the GPU's blocks so that a newer wave starts while older ones still run.  A job
-   is finished the moment its last work unit is (the kernel raises a flag in host-mapped memory),
-   not when its wave ends, so a small job that shares a wave with a large one is not held back.
+   by footprint as device memory and in-flight slots free up, and run on one of two engines,
+   chosen per job when it arrives:
 
-   The host loop never blocks on the device: it admits, launches, polls the flags and frees.
-   Compilation is the LUT mapping of the batched engine, done per wave in host threads; a job's
-   mapped program is the same whoever shares its wave, so results do not depend on the mix. */
+   - waves of the batched interpreter: the jobs admitted together run in one persistent kernel,
+     on one of several streams, with a share of the GPU's blocks so that a newer wave starts
+     while older ones still run.  A job is finished the moment its last work unit is (the kernel
+     raises a flag in host-mapped memory), not when its wave ends;
+   - the generated-kernel engine of cuda_enum_run, for jobs whose work is large enough that the
+     GPU time compiled code saves outweighs their share of the compile threads: host threads
+     generate and compile (NVRTC, cached by what the generator reads), and the main loop
+     launches each compiled job on a stream of its own into a preallocated workspace.
+
+   The host loop never blocks on the device: it admits, launches, polls the flags and events and
+   frees.  A job's result does not depend on the engine, the wave or the mix: both engines
+   compute the whole enumeration of that one job. */
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
@@ -25,14 +32,83 @@ size_t tc_wave_bytes(const TcWave *w);
 void   tc_wave_free(TcWave *w);
 
 #define MAX_STREAMS 8
+#define MAX_COMPILED 8       /* compiled jobs on the device at once, one stream each */
+#define MAX_THREADS 64
+
+/* Rates for routing, measured on GB300: the batched interpreter's whole-GPU throughput on the
+   4,096-job equivalence batch, and generated code's on random programs, in NAND/STO lane-ops/s;
+   NVRTC's time for a generated kernel as a constant plus a cost per NAND/STO instruction. */
+#define RATE_INTERP 9.0e13
+#define RATE_COMPILED 2.0e15
+#define COMPILE_S0 0.2
+#define COMPILE_S_PER_INSTR 8.0e-5
 
 typedef struct {
     TcWave *w;
     int    *ids;      /* job numbers of the wave */
     int     n, left;  /* jobs, jobs not finished */
     size_t  bytes;
-    int     stream;
 } Flight;
+
+/* ---- the compile threads -------------------------------------------------------------------- */
+
+typedef struct {
+    pthread_mutex_t     mu;
+    pthread_cond_t      cv;
+    const Enum *const  *jobs;
+    TcEnumJob          *prep;            /* per job */
+    int                *queue, qhead, qtail;
+    int                *ready, rhead, rtail;
+    int                 stop, failed;
+    char                err[512];
+} Compiler;
+
+static void *compile_worker(void *arg)
+{
+    Compiler *c = arg;
+    for (;;) {
+        pthread_mutex_lock(&c->mu);
+        while (c->qhead == c->qtail && !c->stop)
+            pthread_cond_wait(&c->cv, &c->mu);
+        if (c->qhead == c->qtail) {
+            pthread_mutex_unlock(&c->mu);
+            return NULL;
+        }
+        int id = c->queue[c->qhead++];
+        pthread_mutex_unlock(&c->mu);
+        char e2[512];
+        int ok = tc_enum_job_prepare(c->jobs[id], &c->prep[id], e2, sizeof e2);
+        pthread_mutex_lock(&c->mu);
+        if (ok) {
+            c->ready[c->rtail++] = id;
+        } else if (!c->failed) {
+            c->failed = 1;
+            snprintf(c->err, sizeof c->err, "job %d: %s", id, e2);
+        }
+        pthread_mutex_unlock(&c->mu);
+    }
+}
+
+typedef struct {
+    int          id;          /* -1: free */
+    cudaStream_t st;
+    cudaEvent_t  done;
+    void        *dev, *host;  /* workspace and its pinned host copy */
+} Slot;
+
+/* Compiled code for job e when the GPU time it saves over the interpreter is worth more than its
+   compile time spread over the compile threads. */
+static int route_compiled(const Enum *e, const CudaServeOpts *o, int threads)
+{
+    if (o->route == CUDA_SERVE_INTERPRETER || threads < 1)
+        return 0;
+    if (o->route == CUDA_SERVE_COMPILED)
+        return 1;
+    double instrs = (double)e->a->len + (e->mode == EN_EQUIV ? (double)e->b->len : 0.0);
+    double work = (double)(1ull << e->a->ninputs) * (double)e->ticks * instrs;
+    double saved = work / RATE_INTERP - work / RATE_COMPILED;
+    return saved > (COMPILE_S0 + COMPILE_S_PER_INSTR * instrs) / threads;
+}
 
 static void nap(void)
 {
@@ -42,7 +118,7 @@ static void nap(void)
 
 int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
                    const CudaServeOpts *opts, double *start, double *finish, EnumResult *results,
-                   char *err, size_t errlen)
+                   int *engine_used, char *err, size_t errlen)
 {
     if (njobs <= 0)
         return 1;
@@ -61,17 +137,61 @@ int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
         o.max_wave_jobs = 1024;
     if (o.share <= 0 || o.share > 1)
         o.share = 0.5;
+    int threads = o.compile_threads == 0 ? 12 : o.compile_threads;
+    if (threads > MAX_THREADS)
+        threads = MAX_THREADS;
+    if (o.route == CUDA_SERVE_COMPILED && threads < 1)
+        threads = 1;
+    if (o.route == CUDA_SERVE_INTERPRETER)
+        threads = 0;
+    int nslots = threads > 0 ? (o.compiled_slots > 0 ? o.compiled_slots : 4) : 0;
+    if (nslots > MAX_COMPILED)
+        nslots = MAX_COMPILED;
+
+    int ok = 1;
     cudaStream_t st[MAX_STREAMS];
     int busy[MAX_STREAMS];
-    for (int s = 0; s < o.streams; s++) {
-        busy[s] = 0;
-        if (!tc_cu_check(cudaStreamCreateWithFlags(&st[s], cudaStreamNonBlocking), "stream", err,
-                         errlen))
-            return 0;
+    int nst = 0;
+    for (; nst < o.streams; nst++) {
+        busy[nst] = 0;
+        if (!tc_cu_check(cudaStreamCreateWithFlags(&st[nst], cudaStreamNonBlocking), "stream",
+                         err, errlen)) {
+            ok = 0;
+            break;
+        }
     }
+    /* compiled-job slots: the largest workspace any launch on this device can need */
+    Slot slot[MAX_COMPILED];
+    memset(slot, 0, sizeof slot);
+    size_t ws_max = tc_enum_job_ws_max();
+    int nsl = 0;
+    for (; ok && nsl < nslots; nsl++) {
+        slot[nsl].id = -1;
+        ok = tc_cu_check(cudaStreamCreateWithFlags(&slot[nsl].st, cudaStreamNonBlocking),
+                         "stream", err, errlen) &&
+             tc_cu_check(cudaEventCreateWithFlags(&slot[nsl].done, cudaEventDisableTiming),
+                         "event", err, errlen) &&
+             tc_cu_check(cudaMalloc(&slot[nsl].dev, ws_max), "cudaMalloc", err, errlen) &&
+             tc_cu_check(cudaHostAlloc(&slot[nsl].host, ws_max, cudaHostAllocDefault),
+                         "cudaHostAlloc", err, errlen);
+    }
+    Compiler cc;
+    memset(&cc, 0, sizeof cc);
+    pthread_mutex_init(&cc.mu, NULL);
+    pthread_cond_init(&cc.cv, NULL);
+    cc.jobs = jobs;
+    cc.prep = tc_xcalloc((size_t)njobs, sizeof *cc.prep);
+    cc.queue = tc_xmalloc((size_t)njobs * sizeof *cc.queue);
+    cc.ready = tc_xmalloc((size_t)njobs * sizeof *cc.ready);
+    pthread_t tid[MAX_THREADS];
+    int nthreads = 0;
+    for (; ok && nthreads < threads; nthreads++)
+        if (pthread_create(&tid[nthreads], NULL, compile_worker, &cc) != 0)
+            break;
+
     Flight fl[MAX_STREAMS];
     memset(fl, 0, sizeof fl);
-    int next = 0, finished = 0, inflight = 0, ok = 1;
+    int next = 0, finished = 0, inflight = 0;
     size_t bytes = 0;
     int *ready = tc_xmalloc((size_t)njobs * sizeof *ready), nready = 0, rhead = 0;
     const Enum **wj = tc_xmalloc((size_t)njobs * sizeof *wj);
@@ -81,11 +201,69 @@ int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
     double t0 = tc_now();
     while (ok && finished < njobs) {
         double now = tc_now() - t0;
-        while (next < njobs && arrival[next] <= now)
-            ready[nready++] = next++;
+        int progress = 0;
+        /* arrivals: to the interpreter's queue or the compile threads */
+        while (next < njobs && arrival[next] <= now) {
+            int compiled = route_compiled(jobs[next], &o, nthreads);
+            if (engine_used)
+                engine_used[next] = compiled;
+            if (compiled) {
+                pthread_mutex_lock(&cc.mu);
+                cc.queue[cc.qtail++] = next;
+                pthread_cond_signal(&cc.cv);
+                pthread_mutex_unlock(&cc.mu);
+            } else {
+                ready[nready++] = next;
+            }
+            next++;
+        }
+        /* compiled jobs: launch into free slots, collect finished ones */
+        if (nsl) {
+            pthread_mutex_lock(&cc.mu);
+            if (cc.failed) {
+                ok = tc_fail(err, errlen, "%s", cc.err);
+                pthread_mutex_unlock(&cc.mu);
+                break;
+            }
+            for (int s = 0; s < nsl && cc.rhead < cc.rtail; s++) {
+                if (slot[s].id >= 0)
+                    continue;
+                int id = cc.ready[cc.rhead++];
+                if (!tc_enum_job_launch(&cc.prep[id], slot[s].dev, slot[s].host, slot[s].st,
+                                        err, errlen) ||
+                    !tc_cu_check(cudaEventRecord(slot[s].done, slot[s].st), "event", err,
+                                 errlen)) {
+                    ok = 0;
+                    break;
+                }
+                slot[s].id = id;
+                start[id] = tc_now() - t0;
+                progress = 1;
+            }
+            pthread_mutex_unlock(&cc.mu);
+            for (int s = 0; ok && s < nsl; s++) {
+                if (slot[s].id < 0)
+                    continue;
+                cudaError_t q = cudaEventQuery(slot[s].done);
+                if (q == cudaErrorNotReady)
+                    continue;
+                if (!tc_cu_check(q, "compiled job", err, errlen)) {
+                    ok = 0;
+                    break;
+                }
+                int id = slot[s].id;
+                tc_enum_job_result(&cc.prep[id], slot[s].host, &results[id]);
+                finish[id] = tc_now() - t0;
+                slot[s].id = -1;
+                finished++;
+                progress = 1;
+            }
+            if (!ok)
+                break;
+        }
         /* a free stream and admissible jobs: a new wave */
         int s = -1;
-        for (int i = 0; i < o.streams; i++)
+        for (int i = 0; i < nst; i++)
             if (!busy[i]) {
                 s = i;
                 break;
@@ -118,7 +296,6 @@ int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
             memcpy(fl[s].ids, ready + rhead, (size_t)n * sizeof(int));
             fl[s].n = fl[s].left = n;
             fl[s].bytes = pending_need;
-            fl[s].stream = s;
             for (int i = 0; i < n; i++)
                 start[ready[rhead + i]] = at;
             busy[s] = 1;
@@ -126,10 +303,10 @@ int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
             inflight += n;
             bytes += pending_need;
             pending = NULL;
+            progress = 1;
         }
         /* finished jobs, finished waves */
-        int progress = 0;
-        for (int i = 0; i < o.streams; i++) {
+        for (int i = 0; i < nst; i++) {
             if (!busy[i])
                 continue;
             Flight *f = &fl[i];
@@ -164,8 +341,15 @@ int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
         if (!progress)
             nap();
     }
+    pthread_mutex_lock(&cc.mu);
+    cc.stop = 1;
+    cc.qhead = cc.qtail;  /* nothing more to compile */
+    pthread_cond_broadcast(&cc.cv);
+    pthread_mutex_unlock(&cc.mu);
+    for (int i = 0; i < nthreads; i++)
+        pthread_join(tid[i], NULL);
     tc_wave_free(pending);
-    for (int i = 0; i < o.streams; i++) {
+    for (int i = 0; i < nst; i++) {
         if (busy[i]) {
             tc_wave_free(fl[i].w);
             free(fl[i].ids);
@@ -173,6 +357,23 @@ int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
         cudaStreamSynchronize(st[i]);
         cudaStreamDestroy(st[i]);
     }
+    for (int i = 0; i < MAX_COMPILED; i++) {
+        if (slot[i].st) {
+            cudaStreamSynchronize(slot[i].st);
+            cudaStreamDestroy(slot[i].st);
+        }
+        if (slot[i].done)
+            cudaEventDestroy(slot[i].done);
+        if (slot[i].dev)
+            cudaFree(slot[i].dev);
+        if (slot[i].host)
+            cudaFreeHost(slot[i].host);
+    }
+    pthread_mutex_destroy(&cc.mu);
+    pthread_cond_destroy(&cc.cv);
+    free(cc.prep);
+    free(cc.queue);
+    free(cc.ready);
     free(ready);
     free(wj);
     return ok;
