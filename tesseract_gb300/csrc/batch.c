@@ -106,8 +106,36 @@ typedef struct {
     int       ncmp;       /* entries */
 } LutJob;
 
+static int net_or(TcNet *t, int a, int b)
+{
+    return tc_net_nand(t, tc_net_not(t, a), tc_net_not(t, b));
+}
+
+static int net_xor(TcNet *t, int a, int b)
+{
+    int n = tc_net_nand(t, a, b);
+    return tc_net_nand(t, tc_net_nand(t, a, n), tc_net_nand(t, b, n));
+}
+
+typedef struct {
+    int    node;
+    double key;
+} Keyed;
+
+static int by_key(const void *x, const void *y)
+{
+    const Keyed *a = x, *b = y;
+    return a->key < b->key ? -1 : a->key > b->key ? 1 : a->node - b->node;
+}
+
 /* Maps job e onto LUTs and gives every value a slot (linear scan: a slot is free again after
-   the last op that reads it).  lj->ok = 0 when it does not fit 255 slots. */
+   the last op that reads it).  lj->ok = 0 when it does not fit 255 slots.
+
+   Equiv and search fold their compare into the network: an accumulator ORs in each output's
+   mismatch (a ^ b for a pair, v ^ target bit for search) as soon as the output's final value
+   exists, so outputs do not stay live to the end of the pass (random programs output every
+   cell), and the LUTs run in program order with each accumulator step placed right after the
+   later of its operands.  The kernel then reads one mismatch word. */
 static void lut_job(const Enum *e, const int *in_map, const int *out_map, LutJob *lj)
 {
     const Program *a = e->a, *b = e->b;
@@ -119,6 +147,7 @@ static void lut_job(const Enum *e, const int *in_map, const int *out_map, LutJob
         leaf[k] = tc_net_leaf(net, (int)k);
     int *cur_a = tc_xmalloc((a->ncells + 1) * sizeof *cur_a), *cur_b = NULL;
     tc_net_pass(net, a, a->inputs, n, leaf, cur_a);
+    int a_end = tc_net_size(net), b_end = a_end;
     const TcSpec *sp = (const TcSpec *)e->spec;
     int *want = tc_xmalloc(((size_t)a->noutputs * 2 + 66) * sizeof *want), nwant = 0;
     if (e->mode == EN_EQUIV) {
@@ -127,6 +156,7 @@ static void lut_job(const Enum *e, const int *in_map, const int *out_map, LutJob
             b_in[k] = b->inputs[in_map[k]];
         cur_b = tc_xmalloc((b->ncells + 1) * sizeof *cur_b);
         tc_net_pass(net, b, b_in, n, leaf, cur_b);
+        b_end = tc_net_size(net);
         free(b_in);
         for (size_t o = 0; o < a->noutputs; o++) {
             want[nwant++] = cur_a[a->outputs[o]];
@@ -136,9 +166,65 @@ static void lut_job(const Enum *e, const int *in_map, const int *out_map, LutJob
         for (int i = 0; i < sp->width; i++)
             want[nwant++] = cur_a[sp->out[i]];
     }
+    if (e->mode != EN_VERIFY) {
+        /* outputs in the order their values were made; the accumulator follows them */
+        Keyed *ko = tc_xmalloc(((size_t)nwant + 1) * sizeof *ko);
+        int nk = 0;
+        if (e->mode == EN_EQUIV) {
+            for (int i = 0; i < nwant; i += 2) {
+                ko[nk].node = i;
+                ko[nk++].key = want[i] > want[i + 1] ? want[i] : want[i + 1];
+            }
+        } else {
+            for (int i = 0; i < nwant; i++) {
+                ko[nk].node = i;
+                ko[nk++].key = want[i];
+            }
+        }
+        qsort(ko, (size_t)nk, sizeof *ko, by_key);
+        uint64_t target = e->mode == EN_SEARCH ? cuda_spec_value(e->spec, 0) : 0;
+        int acc = 0;
+        for (int k = 0; k < nk; k++) {
+            int i = ko[k].node;
+            if (e->mode == EN_EQUIV && want[i] == want[i + 1])
+                continue;  /* the same node: equal by construction */
+            int d = e->mode == EN_EQUIV ? net_xor(net, want[i], want[i + 1])
+                    : ((target >> i) & 1) ? tc_net_not(net, want[i]) : want[i];
+            acc = net_or(net, acc, d);
+        }
+        free(ko);
+        want[0] = acc;
+        nwant = 1;
+    }
     int size = tc_net_size(net);
     int *order = tc_xmalloc(((size_t)size + 1) * sizeof *order), norder = 0;
     tc_net_map(net, want, nwant, order, &norder);
+    {
+        /* the two programs side by side, each LUT at its place in its own program (the
+           fraction of that program's network before it), and never before its operands, so an
+           accumulator LUT comes right after the later of its operands */
+        double *key = tc_xcalloc((size_t)size + 1, sizeof *key);
+        Keyed *ko = tc_xmalloc(((size_t)norder + 1) * sizeof *ko);
+        int lv[3], nlv;
+        uint8_t t8;
+        for (int q = 0; q < norder; q++) {
+            int v = order[q];
+            double k = v < a_end ? (double)v / a_end
+                     : v < b_end ? (double)(v - a_end) / (b_end - a_end) : 0.0;
+            tc_net_lut(net, v, lv, &nlv, &t8);
+            for (int j = 0; j < nlv; j++)
+                if (key[lv[j]] + 1e-9 > k)
+                    k = key[lv[j]] + 1e-9;
+            key[v] = k;
+            ko[q].node = v;
+            ko[q].key = k;
+        }
+        qsort(ko, (size_t)norder, sizeof *ko, by_key);
+        for (int q = 0; q < norder; q++)
+            order[q] = ko[q].node;
+        free(ko);
+        free(key);
+    }
     /* last use of every value: the position of the last op reading it; outputs live to the end */
     int *last = tc_xmalloc(((size_t)size + 1) * sizeof *last);
     for (int i = 0; i < size; i++)
@@ -159,7 +245,8 @@ static void lut_job(const Enum *e, const int *in_map, const int *out_map, LutJob
     slot[1] = 1;
     for (size_t k = 0; k < n; k++)
         slot[leaf[k]] = 2 + (int)k;
-    int next = 2 + (int)n, *freed = tc_xmalloc(((size_t)norder + 1) * sizeof *freed), nfree = 0;
+    int next = 2 + (int)n, nfree = 0;
+    int *freed = tc_xmalloc(((size_t)norder + n + 1) * sizeof *freed);  /* values and inputs */
     lj->ops = tc_xmalloc(((size_t)norder + 1) * 4 * sizeof *lj->ops);
     lj->ok = next <= TC_BATCH_MAX_SLOTS;
     for (int p = 0; p < norder && lj->ok; p++) {
@@ -173,8 +260,8 @@ static void lut_job(const Enum *e, const int *in_map, const int *out_map, LutJob
             int dup = 0;
             for (int q = 0; q < j; q++)
                 dup |= leaves[q] == v;
-            if (!dup && last[v] == p && x->kind != TN_LEAF && x->kind != TN_CONST)
-                freed[nfree++] = slot[v];
+            if (!dup && last[v] == p && x->kind != TN_CONST)
+                freed[nfree++] = slot[v];  /* inputs too: they are rewritten every word */
         }
         int d = nfree ? freed[--nfree] : next++;
         if (d > TC_BATCH_MAX_SLOTS - 1) {
@@ -196,14 +283,13 @@ static void lut_job(const Enum *e, const int *in_map, const int *out_map, LutJob
             lj->in_slot[k] = (uint16_t)(2 + k);
         lj->cmp = tc_xmalloc(((size_t)nwant * 2 + 2) * sizeof *lj->cmp);
         if (e->mode == EN_EQUIV) {
-            for (int i = 0; i < nwant; i++)
-                lj->cmp[lj->ncmp++] = (uint16_t)slot[want[i]];
+            /* one pair: the mismatch accumulator against the constant-0 slot */
+            lj->cmp[lj->ncmp++] = (uint16_t)slot[want[0]];
+            lj->cmp[lj->ncmp++] = 0;
         } else if (e->mode == EN_SEARCH) {
-            uint64_t target = cuda_spec_value(e->spec, 0);
-            for (int i = 0; i < nwant; i++) {
-                lj->cmp[lj->ncmp++] = (uint16_t)slot[want[i]];
-                lj->cmp[lj->ncmp++] = (uint16_t)((target >> i) & 1);
-            }
+            /* hits where the accumulator is 0: its complement, as target bit 0 */
+            lj->cmp[lj->ncmp++] = (uint16_t)slot[want[0]];
+            lj->cmp[lj->ncmp++] = 0;
         } else {
             for (int i = 0; i < nwant; i++)
                 lj->cmp[lj->ncmp++] = (uint16_t)slot[want[i]];
@@ -632,6 +718,12 @@ void tc_wave_result(const TcWave *w, int i, EnumResult *r)
 int tc_wave_njobs(const TcWave *w)
 {
     return w->njobs;
+}
+
+/* Shared-memory slots job i uses (each is 4 bytes per thread). */
+int tc_wave_job_slots(const TcWave *w, int i)
+{
+    return ((const TcBatchJob *)w->pk.jobs.p)[i].slots;
 }
 
 void tc_wave_free(TcWave *w)

@@ -7,9 +7,11 @@
    this is exactly the reference's Line layout (lane k at bit k % 64 of u64 word k / 64), so a
    group's lines copy in and out with one strided copy.
 
-   One thread runs one word (32 machines) through straight-line generated code; cells are loaded
-   into registers at their first use in a kernel and written back at its end.  A read across a
-   link from machine m reaches machine m ^ M:
+   A word (32 machines) runs through straight-line generated code, LOP3-mapped: a kernel's
+   written cells are shared out over up to tc_cube_groups warps of a block, each computing the
+   cone of its share from the cells' values loaded at the kernel's start, so a cube of 2,048
+   words (Life on 65,536 machines) runs on up to 512 warps instead of 64.  A
+   read across a link from machine m reaches machine m ^ M:
      M bits 0..4   move lanes inside the word (bit swaps, byte permutes, a 16-bit rotate)
      M bits 5..9   another lane of the same warp: __shfl_xor_sync on the register
      M bits 10..15 another warp: a load of that word from the cell's memory
@@ -17,7 +19,7 @@
    for groups: wherever a segment would both write a cell and read it across a dimension of 10 or
    more.  Each segment is its own kernel launch; inside a segment every far read sees the value the
    cell had when the segment started, which is what lockstep shows it.  Long segments are split
-   into kernels of at most TC_CUBE_CHUNK instructions that hand their cells over through memory,
+   into kernels of at most tc_cube_chunk instructions that hand their cells over through memory,
    so no single kernel is too large for the compiler.  When the whole pass is one kernel and no
    read crosses warps (at most 1024 machines), the passes loop inside the kernel. */
 #include <pthread.h>
@@ -31,7 +33,6 @@
 #include "ref_host.h"
 
 #define TC_CUBE_BLOCK 32
-#define TC_CUBE_CHUNK 12000
 #define FAR_DIM 10
 
 /* 1: cube kernels are LOP3-mapped networks (lutmap.c); 0: the instructions as written */
@@ -40,6 +41,11 @@ int tc_cube_map = 1;
    warp gets */
 int tc_cube_groups = 8;
 int tc_cube_min_cells = 16;
+/* the most instructions in one kernel: longer segments are split.  Fewer, longer kernels win
+   once they are split over warps (Life on 65,536 machines: 3 kernels of up to 125,722
+   instructions run 36-38k generations/s, 13 kernels of 12,000 run 29k), at the price of a longer
+   compile (7 s against 0.5 s) */
+int tc_cube_chunk = 140000;
 
 struct CudaCube {
     Program     p;
@@ -737,12 +743,13 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
     c->W = c->machines / 32;
     size_t *cuts = tc_xmalloc((p->len + 2) * sizeof *cuts);
     c->nseg = find_cuts(p, cuts);
-    /* split long segments into kernels of at most TC_CUBE_CHUNK instructions */
-    c->first = tc_xmalloc((p->len / TC_CUBE_CHUNK + c->nseg + 2) * sizeof *c->first);
+    /* split long segments into kernels of at most tc_cube_chunk instructions */
+    size_t chunk = tc_cube_chunk > 0 ? (size_t)tc_cube_chunk : 12000;
+    c->first = tc_xmalloc((p->len / chunk + c->nseg + 2) * sizeof *c->first);
     c->nk = 0;
     for (unsigned s = 0; s < c->nseg; s++)
         for (size_t i = cuts[s]; i < cuts[s + 1] || (i == cuts[s] && cuts[s] == cuts[s + 1]);
-             i += TC_CUBE_CHUNK) {
+             i += chunk) {
             c->first[c->nk++] = i;
             if (cuts[s] == cuts[s + 1])
                 break;
