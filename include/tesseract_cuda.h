@@ -257,6 +257,45 @@ int  cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
                     const CudaServeOpts *opts, double *start, double *finish,
                     EnumResult *results, int *engine_used, char *err, size_t errlen);
 
+/* Truth tables.  Replaces table_lanes (src/main.c:297-322) for `run --table --engine cuda`:
+   every row of a program without id or link cells (1 to 20 .in cells; the first .in cell is the
+   row's high bit) from the reset state, `ticks` passes, then the .out cells, or RR when there are
+   none (src/main.c:219-258).  vals gets 2^ninputs rows of max(noutputs, 1) bytes, each 0 or 1. */
+int  cuda_table(const Program *p, unsigned ticks, uint8_t *vals, char *err, size_t errlen);
+
+/* Tester 1: what do random 1-bit computers do?  The reference's configuration and result
+   (src/tester.h:7-51, same layout, its include guard), and cuda_t1_run in place of t1_run
+   (src/tester.h:55, src/tester.c:235-275): every random program of every size runs from 512
+   random states on the GPU and Brent's algorithm finds the cycle each run ends in.  Returns the
+   wall seconds (-1 with a message in err); *threads gets 1.  With cfg->programs > 0 the
+   histograms, pass counts and longest cycles equal a one-thread reference run's. */
+#ifndef ALPHA_TESTER_H
+#define ALPHA_TESTER_H
+#define T1_BUCKETS 64  /* bucket b: cycle length in (2^(b-1), 2^b]; the last one: not found */
+#define T1_SIZES   32
+typedef struct {
+    uint32_t cells;
+    size_t   len;
+    uint64_t programs, starts, passes;
+    uint64_t unfinished;
+    uint64_t hist[T1_BUCKETS];
+    uint64_t longest, longest_seed;
+} T1Size;
+typedef struct {
+    uint32_t             cells[T1_SIZES];
+    int                  nsizes;
+    double               ratio;
+    uint64_t             programs;
+    double               seconds;
+    uint64_t             max_passes;
+    uint64_t             seed;
+    int                  threads;
+    int                  idle;
+    const unsigned char *excluded;
+} T1Config;
+#endif
+double cuda_t1_run(const T1Config *cfg, T1Size *out, int *threads, char *err, size_t errlen);
+
 /* Random-state parity against the reference semantics.  Replaces
    check_lanes(p, jit, seed, ticks, 0, r) (src/check.h:25, src/check.c:52-113): every machine of
    the program's cube gets the same random state from splitmix64(seed) as there, runs `ticks`
@@ -287,6 +326,20 @@ int  cuda_cube_read_words(const CudaCube *c, uint32_t *mem, uint32_t *rr, char *
 int  cuda_cube_write_words(CudaCube *c, const uint32_t *mem, const uint32_t *rr, char *err,
                            size_t errlen);
 unsigned cuda_cube_kernels(const CudaCube *c);
+
+/* `alpha cube DEMO --dims D` (src/cubedemo.c:549-623) on the GPU cube: builds demo any, rank,
+   sort or life for 2^dims machines (dims 9..16), runs `checks` rounds of random inputs one pass
+   each and checks every machine against plain C (a sorted array, prefix counts, plain Life),
+   then times passes for about `seconds`.  r->ok is 0 when a check failed. */
+typedef struct {
+    char     what[96];
+    size_t   instr;
+    unsigned segs, kernels;
+    int      ok;
+    double   pass_seconds, passes_per_second;
+} CudaDemoResult;
+int  cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaDemoResult *r,
+                    char *err, size_t errlen);
 
 #ifdef __cplusplus
 }

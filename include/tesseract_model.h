@@ -39,6 +39,13 @@ int      tc_gen_hash(Program *p, int bits, int rounds);
 uint64_t tc_toyhash(uint64_t x, int bits, int rounds);
 void     tc_gen_life(Program *p, int w, int h, uint32_t *board);
 void     tc_gen_life_cube(Program *p, int w, int h, int rbits, int cbits, uint32_t *board);
+/* The big-cube demos of `alpha cube --dims D` (src/cubedemo.c:398-548), for 2^dims machines:
+   any (.in x, .out r: the OR of x over all machines), rank (.in x, .out p0.. t0..: how many
+   machines below this one, and in all, have x = 1), sort (.in/.out v0..v7: bitonic sort, machine
+   k ends with the k-th smallest byte). */
+void     tc_gen_cube_any(Program *p, int dims);
+void     tc_gen_cube_rank(Program *p, int dims);
+void     tc_gen_cube_sort(Program *p, int dims);
 unsigned tc_grid_machine(unsigned row, unsigned col, int cbits);
 void     tc_random_program(Program *p, uint32_t cells, size_t len, uint64_t seed);
 /* Random program with `width` input cells (.in w0.., never written) beside `cells` working cells

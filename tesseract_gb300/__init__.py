@@ -254,6 +254,17 @@ class Program:
         return cls._made(lib().tc_random_program, cells, length, seed)
 
     @classmethod
+    def gen_cube_demo(cls, name: str, dims: int):
+        """The big-cube demo `name` (any, rank, sort) for 2^dims machines."""
+        fn = {"any": "tc_gen_cube_any", "rank": "tc_gen_cube_rank", "sort": "tc_gen_cube_sort"}
+        p = cls()
+        f = getattr(lib(), fn[name])
+        f.argtypes = [C.POINTER(ProgramStruct), C.c_int]
+        f.restype = None
+        f(C.byref(p.s), dims)
+        return p
+
+    @classmethod
     def random_in(cls, cells: int, width: int, length: int, seed: int):
         return cls._made(lib().tc_random_program_in, cells, width, length, seed)
 
@@ -354,6 +365,21 @@ def enum_run(mode, a: Program, b: Program | None = None, spec: Spec | None = Non
     if not lib().cuda_enum_run(C.byref(e), C.byref(r), err, len(err)):
         raise EngineError(err.value.decode())
     return r.as_dict()
+
+
+def table(p: Program, ticks: int = 1):
+    """`run --table --engine cuda` (cuda_table): every row's output columns (.out cells, or RR
+    when there are none) as a list of rows of 0/1."""
+    rows, cols = 1 << p.s.ninputs, max(p.s.noutputs, 1)
+    vals = (C.c_uint8 * (rows * cols))() if 0 < p.s.ninputs <= 20 else (C.c_uint8 * 1)()
+    err = _err()
+    L = lib()
+    L.cuda_table.restype = C.c_int
+    L.cuda_table.argtypes = [C.POINTER(ProgramStruct), C.c_uint, C.c_void_p, C.c_char_p,
+                             C.c_size_t]
+    if not L.cuda_table(p.ptr, ticks, C.cast(vals, C.c_void_p), err, len(err)):
+        raise EngineError(err.value.decode())
+    return [list(vals[r * cols:(r + 1) * cols]) for r in range(rows)]
 
 
 def last_launch() -> dict:
@@ -477,6 +503,25 @@ def check(program: Program, seed: int = 1, ticks: int = 8) -> dict:
     if not lib().cuda_check(program.ptr, seed, ticks, C.byref(r), err, len(err)):
         raise EngineError(err.value.decode())
     return {f: getattr(r, f) for f, _ in CheckResult._fields_}
+
+
+class DemoResult(C.Structure):
+    _fields_ = [("what", C.c_char * 96), ("instr", C.c_size_t), ("segs", C.c_uint),
+                ("kernels", C.c_uint), ("ok", C.c_int), ("pass_seconds", C.c_double),
+                ("passes_per_second", C.c_double)]
+
+
+def cube_demo(name: str, dims: int, checks: int = 3, seconds: float = 0.2) -> dict:
+    """`alpha cube DEMO --dims D` (cuda_cube_demo): checked rounds, then passes per second."""
+    r, e = DemoResult(), _err()
+    L = lib()
+    L.cuda_cube_demo.restype = C.c_int
+    L.cuda_cube_demo.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_double,
+                                 C.POINTER(DemoResult), C.c_char_p, C.c_size_t]
+    if not L.cuda_cube_demo(name.encode(), dims, checks, seconds, C.byref(r), e, len(e)):
+        raise EngineError(e.value.decode())
+    return {f: (getattr(r, f).decode() if f == "what" else getattr(r, f))
+            for f, _ in DemoResult._fields_}
 
 
 class Cube:

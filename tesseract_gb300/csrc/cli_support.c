@@ -1,7 +1,8 @@
 /* What the command-line tool needs beyond the engine's entry points: running one assignment on
    the reference machine to show a counterexample (src/work.c:284-339 re-runs hits on `ref`), and
    `life --dims D`, which like src/work.c:490-701 runs the board on the engine and checks it
-   against plain C Life. */
+   against plain C Life, and `cube DEMO --dims D` (cuda_cube_demo), which like
+   src/cubedemo.c:549-623 runs a demo on the cube and checks every machine against plain C. */
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -160,6 +161,182 @@ int tc_life_cube_run(int dims, int rbits, int size, unsigned long long gens, uin
             }
     }
     free(big);
+    free(mem);
+    free(rr);
+    free(board);
+    cuda_cube_free(c);
+    tc_program_free(&p);
+    return okay;
+}
+
+/* ---- cube demos over 2^dims machines (src/cubedemo.c:398-623) ------------------------------- */
+
+static void mset(uint32_t *mem, unsigned W, uint32_t cell, unsigned k, unsigned v)
+{
+    uint32_t *w = &mem[(size_t)cell * W + (k >> 5)];
+    *w = (*w & ~(1u << (k & 31))) | ((v & 1u) << (k & 31));
+}
+
+static unsigned mget(const uint32_t *mem, unsigned W, uint32_t cell, unsigned k)
+{
+    return (mem[(size_t)cell * W + (k >> 5)] >> (k & 31)) & 1u;
+}
+
+static void vput(uint32_t *mem, unsigned W, const uint32_t *cells, int n, unsigned k, uint64_t x)
+{
+    for (int b = 0; b < n; b++)
+        mset(mem, W, cells[b], k, (unsigned)((x >> b) & 1));
+}
+
+static uint64_t vget(const uint32_t *mem, unsigned W, const uint32_t *cells, int n, unsigned k)
+{
+    uint64_t x = 0;
+    for (int b = 0; b < n; b++)
+        x |= (uint64_t)mget(mem, W, cells[b], k) << b;
+    return x;
+}
+
+static int cmp_u64(const void *a, const void *b)
+{
+    uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+    return x < y ? -1 : x > y;
+}
+
+static int find_cells(const Program *p, const char *stem, int n, uint32_t *cells)
+{
+    for (int i = 0; i < n; i++) {
+        char name[32];
+        snprintf(name, sizeof name, "%s%d", stem, i);
+        if (!tc_program_find_cell(p, name, &cells[i]))
+            return 0;
+    }
+    return 1;
+}
+
+int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaDemoResult *r,
+                   char *err, size_t errlen)
+{
+    memset(r, 0, sizeof *r);
+    if (dims < CUBE_DIMS || dims > CUBE_MAX_DIMS)
+        return tc_fail(err, errlen, "--dims must be %d to %d", CUBE_DIMS, CUBE_MAX_DIMS);
+    unsigned n = 1u << dims, W = n / 32;
+    Program p;
+    uint32_t *board = NULL;
+    int rbits = dims / 2, cbits = dims - rbits, T = 32;
+    if (!strcmp(name, "any")) {
+        snprintf(r->what, sizeof r->what, "OR of one bit over all %u machines", n);
+        tc_gen_cube_any(&p, dims);
+    } else if (!strcmp(name, "rank")) {
+        snprintf(r->what, sizeof r->what, "running count of %u bits, %d-bit results", n, dims + 1);
+        tc_gen_cube_rank(&p, dims);
+    } else if (!strcmp(name, "sort")) {
+        snprintf(r->what, sizeof r->what, "sort %u bytes (bitonic, %d rounds)", n,
+                 dims * (dims + 1) / 2);
+        tc_gen_cube_sort(&p, dims);
+    } else if (!strcmp(name, "life")) {
+        snprintf(r->what, sizeof r->what, "Life: one %d x %d board, one generation", T << rbits,
+                 T << cbits);
+        board = tc_xmalloc((size_t)T * T * sizeof *board);
+        tc_gen_life_cube(&p, T, T, rbits, cbits, board);
+    } else {
+        return tc_fail(err, errlen, "unknown demo '%s' (any, rank, sort, life)", name);
+    }
+    r->instr = p.len;
+    CudaCube *c;
+    if (!cuda_cube_new(&p, &c, err, errlen)) {
+        free(board);
+        tc_program_free(&p);
+        return 0;
+    }
+    r->segs = cuda_cube_segments(c);
+    r->kernels = cuda_cube_kernels(c);
+    uint32_t *mem = tc_xcalloc((size_t)W * p.ncells, 4), *rr = tc_xcalloc(W, 4);
+    uint64_t *want = tc_xcalloc((size_t)n + 1, 8), s = 42;
+    uint32_t x[CUBE_MAX_DIMS + 2], pv[CUBE_MAX_DIMS + 2], tv[CUBE_MAX_DIMS + 2];
+    int okay = 1, ok = 1, rounds = !strcmp(name, "life") && checks > 2 ? 2 : checks;
+    int gw = T << cbits, gh = T << rbits, w64 = gw / 64;
+    uint64_t *big = board ? tc_xcalloc((size_t)w64 * gh, 8) : NULL;
+    for (int round = 0; round < rounds && ok && okay; round++) {
+        /* power-on state (src/lanes.c:176-192): cells 0, ONE 1, RR 0; then the inputs */
+        memset(mem, 0, (size_t)W * p.ncells * 4);
+        memset(rr, 0, (size_t)W * 4);
+        for (unsigned w = 0; w < W; w++)
+            mem[(size_t)CELL_ONE * W + w] = 0xffffffffu;
+        unsigned one = 0;
+        uint64_t count = 0;
+        if (!strcmp(name, "any")) {
+            tc_program_find_cell(&p, "x", &x[0]);
+            one = (unsigned)(tc_splitmix64(&s) % (2ull * n));  /* sometimes none */
+            for (unsigned k = 0; k < n; k++)
+                mset(mem, W, x[0], k, k == one);
+        } else if (!strcmp(name, "rank")) {
+            tc_program_find_cell(&p, "x", &x[0]);
+            for (unsigned k = 0; k < n; k++) {
+                unsigned v = tc_splitmix64(&s) % 10 < 3;
+                mset(mem, W, x[0], k, v);
+                want[k] = count;
+                count += v;
+            }
+        } else if (!strcmp(name, "sort")) {
+            find_cells(&p, "v", 8, x);
+            for (unsigned k = 0; k < n; k++)
+                vput(mem, W, x, 8, k, want[k] = tc_splitmix64(&s) & 255);
+            qsort(want, n, sizeof *want, cmp_u64);
+        } else {
+            memset(big, 0, (size_t)w64 * gh * 8);
+            for (int R = 0; R < gh; R++)
+                for (int C = 0; C < gw; C++) {
+                    unsigned v = tc_splitmix64(&s) % 3 == 0;
+                    unsigned m = tc_grid_machine((unsigned)(R / T), (unsigned)(C / T), cbits);
+                    mset(mem, W, board[(R % T) * T + C % T], m, v);
+                    if (v)
+                        big[(size_t)R * w64 + C / 64] |= 1ull << (C % 64);
+                }
+            plain_life(big, w64, gh, 1);
+        }
+        okay = cuda_cube_write_words(c, mem, rr, err, errlen) && cuda_cube_run(c, 1, err, errlen) &&
+               cuda_cube_read_words(c, mem, rr, err, errlen);
+        if (!okay)
+            break;
+        if (!strcmp(name, "any")) {
+            uint32_t rc;
+            tc_program_find_cell(&p, "r", &rc);
+            for (unsigned k = 0; k < n && ok; k++)
+                ok = mget(mem, W, rc, k) == (one < n);
+        } else if (!strcmp(name, "rank")) {
+            find_cells(&p, "p", dims + 1, pv);
+            find_cells(&p, "t", dims + 1, tv);
+            for (unsigned k = 0; k < n && ok; k++)
+                ok = vget(mem, W, pv, dims + 1, k) == want[k] &&
+                     vget(mem, W, tv, dims + 1, k) == count;
+        } else if (!strcmp(name, "sort")) {
+            for (unsigned k = 0; k < n && ok; k++)
+                ok = vget(mem, W, x, 8, k) == want[k];
+        } else {
+            for (int R = 0; R < gh && ok; R++)
+                for (int C = 0; C < gw && ok; C++) {
+                    unsigned m = tc_grid_machine((unsigned)(R / T), (unsigned)(C / T), cbits);
+                    ok = mget(mem, W, board[(R % T) * T + C % T], m) ==
+                         ((big[(size_t)R * w64 + C / 64] >> (C % 64)) & 1);
+                }
+        }
+    }
+    r->ok = ok;
+    /* timing: double the passes until a run takes a quarter of `seconds` */
+    for (uint64_t passes = 1; okay; passes *= 2) {
+        double t0 = tc_now();
+        okay = cuda_cube_run(c, passes, err, errlen) && cuda_cube_read_words(c, mem, rr, err, errlen);
+        double t = tc_now() - t0;
+        if (t > seconds / 4 || passes >= (1ull << 30)) {
+            CudaLaunchStats st;
+            cuda_last_launch(&st);
+            r->pass_seconds = st.kernel_ms / 1e3 / (double)passes;
+            r->passes_per_second = 1.0 / r->pass_seconds;
+            break;
+        }
+    }
+    free(big);
+    free(want);
     free(mem);
     free(rr);
     free(board);

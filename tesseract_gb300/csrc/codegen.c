@@ -433,3 +433,65 @@ char *tc_codegen_enum(const TcGenEnum *g, size_t *len)
         *len = o.len;
     return o.s;
 }
+
+/* ---- truth tables (run --table) ------------------------------------------------------------ */
+
+/* CUDA C for `tc_table`: thread w runs rows 32w .. 32w + 31 of program p from the reset state
+   (input k of n is bit n-1-k of the row: the first .in cell is the high bit), `ticks` passes,
+   and stores each output column's word at out[col * words + w]; with no .out cells the one
+   column is RR (src/main.c:219-258). */
+char *tc_codegen_table(const Program *p, unsigned ticks, int block, size_t *len)
+{
+    Src o = {0};
+    size_t n = p->ninputs;
+    emit(&o, "// generated by the tesseract GB300 engine: truth table over %zu inputs, %u tick(s)\n",
+         n, ticks);
+    emit(&o, "#define TC_BLOCK %d\n", block);
+    emit(&o, "%s", PRELUDE);
+    emit(&o, "extern \"C\" __global__ void __launch_bounds__(TC_BLOCK) tc_table(u32 *out, "
+             "const u64 words)\n{\n");
+    emit(&o, "    const u64 word = (u64)blockIdx.x * blockDim.x + threadIdx.x;\n");
+    emit(&o, "    if (word >= words)\n        return;\n");
+    for (size_t k = 0; k < n; k++) {
+        int j = (int)(n - 1 - k);
+        if (j < 5)
+            emit(&o, "    const u32 in%zu = TC_PAT%d;\n", k, j);
+        else
+            emit(&o, "    const u32 in%zu = 0u - (u32)((word >> %d) & 1ull);\n", k, j - 5);
+    }
+    char (*val)[24] = tc_xcalloc(p->ncells + 2, sizeof *val);
+    if (ticks == 1 && p->noutputs) {
+        TcNet *net = tc_net_new();
+        int *leaf = tc_xmalloc((n + 1) * sizeof *leaf);
+        for (size_t k = 0; k < n; k++)
+            leaf[k] = tc_net_leaf(net, (int)k);
+        int *cur = tc_xmalloc((p->ncells + 1) * sizeof *cur);
+        tc_net_pass(net, p, p->inputs, n, leaf, cur);
+        int *want = tc_xmalloc((p->noutputs + 1) * sizeof *want);
+        for (size_t i = 0; i < p->noutputs; i++)
+            want[i] = cur[p->outputs[i]];
+        int luts = emit_luts(&o, net, want, (int)p->noutputs);
+        emit(&o, "    // %d LOP3 for %zu NAND/STO instructions\n", luts, p->len);
+        for (uint32_t c = 0; c < p->ncells; c++)
+            node_name(val[c], sizeof val[c], net, cur[c]);
+        free(want);
+        free(cur);
+        free(leaf);
+        tc_net_free(net);
+    } else {
+        body(&o, p, "a", p->inputs, n, ticks);
+        for (uint32_t c = 0; c < p->ncells; c++)
+            snprintf(val[c], sizeof val[c], c == 0 ? "0u" : c == 1 ? "TC_ONES" : "a%u", c);
+        snprintf(val[p->ncells], sizeof val[p->ncells], "ar");
+    }
+    if (p->noutputs)
+        for (size_t i = 0; i < p->noutputs; i++)
+            emit(&o, "    out[%zuull * words + word] = %s;\n", i, val[p->outputs[i]]);
+    else
+        emit(&o, "    out[word] = %s;\n", val[p->ncells]);
+    emit(&o, "}\n");
+    free(val);
+    if (len)
+        *len = o.len;
+    return o.s;
+}

@@ -25,6 +25,9 @@ typedef struct {
    can compile the same text for the host. */
 char *tc_codegen_enum(const TcGenEnum *g, size_t *len);
 
+/* CUDA C for the truth-table kernel `tc_table` of a program without id or link cells. */
+char *tc_codegen_table(const Program *p, unsigned ticks, int block, size_t *len);
+
 /* CUDA C for the cube kernels of a program with id/link cells (cube.c). */
 char *tc_codegen_cube(const Program *p, const size_t *seg_first, unsigned nseg, int block,
                       size_t *len);

@@ -678,3 +678,52 @@ int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
     tc_engine.last_block = TC_ENUM_BLOCK;
     return 1;
 }
+
+/* ---- truth tables --------------------------------------------------------------------------- */
+
+int cuda_table(const Program *p, unsigned ticks, uint8_t *vals, char *err, size_t errlen)
+{
+    if (!p)
+        return tc_fail(err, errlen, "no program");
+    if (p->special)
+        return tc_fail(err, errlen, "this program's machines read each other (id or link cells), "
+                       "so they run as a cube: --table and --engine do not apply");
+    if (p->ninputs == 0 || p->ninputs > 20)
+        return tc_fail(err, errlen, "--table needs between 1 and 20 .in cells, this program has "
+                       "%zu", p->ninputs);
+    if (ticks < 1)
+        return tc_fail(err, errlen, "--ticks must be at least 1");
+    if (!cuda_engine_init(0, err, errlen))
+        return 0;
+    size_t len;
+    char *src = tc_codegen_table(p, ticks, TC_ENUM_BLOCK, &len);
+    static const char *const names[] = {"tc_table"};
+    TcModule m;
+    int ok = tc_module(src, len, names, 1, NULL, &m, err, errlen);
+    free(src);
+    if (!ok)
+        return 0;
+    uint64_t rows = 1ull << p->ninputs, words = (rows + 31) / 32;
+    size_t cols = p->noutputs ? p->noutputs : 1;
+    size_t bytes = cols * words * 4;
+    uint32_t *d = NULL, *h = tc_xmalloc(bytes);
+    cudaStream_t st = tc_engine.stream;
+    void *params[] = {&d, &words};
+    ok = tc_cu_check(cudaMalloc((void **)&d, bytes), "cudaMalloc", err, errlen) &&
+         tc_cu_check(cudaLaunchKernel((const void *)m.fn[0],
+                                      dim3u((unsigned)((words + TC_ENUM_BLOCK - 1) / TC_ENUM_BLOCK)),
+                                      dim3u(TC_ENUM_BLOCK), params, 0, st),
+                     "launch tc_table", err, errlen) &&
+         tc_cu_check(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, st), "table", err,
+                     errlen) &&
+         tc_cu_check(cudaStreamSynchronize(st), "tc_table", err, errlen);
+    if (d)
+        cudaFree(d);
+    if (ok)
+        for (uint64_t r = 0; r < rows; r++)
+            for (size_t c = 0; c < cols; c++)
+                vals[r * cols + c] = (uint8_t)((h[c * words + (r >> 5)] >> (r & 31)) & 1u);
+    free(h);
+    tc_engine.last = m.info;
+    return ok;
+}

@@ -90,6 +90,17 @@ static uint32_t bcellf(Bld *b, const char *fmt, int i, int j)
     return bcell(b, name);
 }
 
+/* A name from a format with one number (in a small ring of buffers, for immediate use). */
+static const char *bname(Bld *b, const char *fmt, int i)
+{
+    static __thread char ring[4][48];
+    static __thread int at;
+    char *s = ring[at++ & 3];
+    snprintf(s, 48, fmt, i);
+    (void)b;
+    return s;
+}
+
 static int bhas(const Bld *b, const char *name)
 {
     return b->slots[bslot(b, name)] != 0;
@@ -607,6 +618,130 @@ void tc_gen_life_cube(Program *p, int w, int h, int rbits, int cbits, uint32_t *
     }
     life_generation(b, board, halo, w, h);
     free(halo);
+    bfinish(b, p);
+}
+
+/* ---- cube demos (the big-cube demos of src/cubedemo.c:398-623) ------------------------------
+
+   The reference builds these from its assembly library (lib/cube.inc: OR_DIM, CMPX8, ...) and
+   checks them against plain C; here they are built with the same gate builder from the same
+   algorithms, and checked against plain C the same way.  Every step reads its neighbours across
+   one dimension into cells of its own before it writes anything, because all machines run each
+   instruction together (lockstep): a link read sees the neighbour's cell as it is at that
+   instruction. */
+
+/* r = OR of x over all 2^dims machines: r = x, then r |= r across each dimension. */
+void tc_gen_cube_any(Program *p, int dims)
+{
+    Bld *b = bnew();
+    uint32_t x = bcell(b, "x"), r = bcell(b, "r");
+    binput(b, x);
+    boutput(b, r);
+    gate1(b, G_BUF, r, x);
+    for (int d = 0; d < dims; d++) {
+        uint32_t l = blink(b, bname(b, "lr%d", d), r, d);
+        gate2(b, G_OR, r, r, l);
+    }
+    bfinish(b, p);
+}
+
+/* b-bit ripple add: s += a (cells s[0..n-1], a[0..n-1]); carry is a scratch cell. */
+static void add_into(Bld *b, const uint32_t *s, const uint32_t *a, int n, uint32_t carry)
+{
+    half_add(b, s[0], carry, s[0], a[0]);
+    for (int i = 1; i < n; i++)
+        full_add(b, s[i], carry, s[i], a[i], carry);
+}
+
+/* p = how many machines below k have x = 1, t = how many have it in all (dims + 1 bits each,
+   bit 0 first): the hypercube prefix sum.  Each machine keeps t, the count of its subcube so
+   far; across dimension d it reads the neighbour's t, adds it to t, and to p when bit d of the
+   machine number is 1 (the neighbour holds the lower half). */
+void tc_gen_cube_rank(Program *p, int dims)
+{
+    Bld *b = bnew();
+    int n = dims + 1;
+    uint32_t x = bcell(b, "x"), carry = bcell(b, "cy");
+    uint32_t pv[CUBE_MAX_DIMS + 1], tv[CUBE_MAX_DIMS + 1], nb[CUBE_MAX_DIMS + 1],
+        ad[CUBE_MAX_DIMS + 1];
+    binput(b, x);
+    for (int i = 0; i < n; i++)
+        pv[i] = bcell(b, bname(b, "p%d", i));
+    for (int i = 0; i < n; i++)
+        tv[i] = bcell(b, bname(b, "t%d", i));
+    for (int i = 0; i < n; i++)
+        boutput(b, pv[i]);
+    for (int i = 0; i < n; i++)
+        boutput(b, tv[i]);
+    for (int i = 0; i < n; i++) {
+        nb[i] = bcell(b, bname(b, "n%d", i));
+        ad[i] = bcell(b, bname(b, "m%d", i));
+        gate1(b, G_BUF, pv[i], CELL_ZERO);
+        gate1(b, G_BUF, tv[i], i == 0 ? x : CELL_ZERO);
+    }
+    for (int d = 0; d < dims; d++) {
+        uint32_t id = bcell(b, bname(b, "ID%d", d));
+        int w = d + 1 < n ? d + 1 : n;  /* a subcube of 2^d machines counts to 2^d: d + 1 bits */
+        for (int i = 0; i < w; i++) {
+            char ln[32];
+            snprintf(ln, sizeof ln, "lt%d_%d", i, d);
+            gate1(b, G_BUF, nb[i], blink(b, ln, tv[i], d));
+        }
+        for (int i = w; i < n; i++)
+            gate1(b, G_BUF, nb[i], CELL_ZERO);
+        for (int i = 0; i < n; i++)
+            gate2(b, G_AND, ad[i], nb[i], id);
+        add_into(b, pv, ad, n, carry);
+        add_into(b, tv, nb, n, carry);
+    }
+    bfinish(b, p);
+}
+
+/* Bitonic sort of one 8-bit value per machine (v0..v7, bit 0 first): afterwards machine k holds
+   the k-th smallest.  Stage st = 1 .. dims sorts blocks of 2^st machines, up or down by bit st
+   of the machine number (the last stage up); each step compare-exchanges across dimension j:
+   the machine with bit j = 0 keeps the smaller value, unless the direction bit is 1. */
+void tc_gen_cube_sort(Program *p, int dims)
+{
+    Bld *b = bnew();
+    uint32_t v[8], o[8], nv[8];
+    for (int i = 0; i < 8; i++)
+        v[i] = bcell(b, bname(b, "v%d", i));
+    for (int i = 0; i < 8; i++)
+        binput(b, v[i]);
+    for (int i = 0; i < 8; i++)
+        boutput(b, v[i]);
+    for (int i = 0; i < 8; i++) {
+        o[i] = bcell(b, bname(b, "o%d", i));
+        nv[i] = bcell(b, bname(b, "w%d", i));
+    }
+    uint32_t carry = bcell(b, "cy"), sum = bcell(b, "sm"), keep = bcell(b, "km"),
+             sel = bcell(b, "se"), dif = bcell(b, "df");
+    for (int st = 1; st <= dims; st++)
+        for (int j = st - 1; j >= 0; j--) {
+            uint32_t idj = bcell(b, bname(b, "ID%d", j));
+            uint32_t dir = st < dims ? bcell(b, bname(b, "ID%d", st)) : CELL_ZERO;
+            for (int i = 0; i < 8; i++) {
+                char ln[32];
+                snprintf(ln, sizeof ln, "lv%d_%d", i, j);
+                uint32_t l = bhas(b, ln) ? bcell(b, ln) : blink(b, ln, v[i], j);
+                gate1(b, G_BUF, o[i], l);
+            }
+            /* carry out of o + ~v + 1 is (o >= v): o < v is its complement */
+            gate1(b, G_BUF, carry, CELL_ONE);
+            for (int i = 0; i < 8; i++) {
+                gate1(b, G_NOT, nv[i], v[i]);
+                full_add(b, sum, carry, o[i], nv[i], carry);
+            }
+            /* take o when keeping the minimum and o < v, or keeping the maximum and o >= v */
+            gate2(b, G_XNOR, keep, idj, dir);
+            gate2(b, G_XOR, sel, keep, carry);
+            for (int i = 0; i < 8; i++) {
+                gate2(b, G_XOR, dif, o[i], v[i]);
+                gate2(b, G_AND, dif, dif, sel);
+                gate2(b, G_XOR, v[i], v[i], dif);
+            }
+        }
     bfinish(b, p);
 }
 

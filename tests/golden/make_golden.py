@@ -2,6 +2,7 @@
 
     python tests/golden/make_golden.py [path/to/alpha]          # programs.json, enum.json
     python tests/golden/make_golden.py --cli [path/to/alpha]    # cli.json
+    python tests/golden/make_golden.py --tester1 [path/to/alpha]  # tester1.json
 
 Needs the reference's `alpha` binary built from its sources (oracle/Makefile builds it into
 oracle/_ref/alpha on an x86 host that has the sources).  Programs come from the reference's own
@@ -14,6 +15,7 @@ Outputs:
     programs.json   sha256 of the reference's generator output for each (kind, parameters)
     enum.json       enumeration cases and the reference's results
     cli.json        the reference's stdout and exit code for command lines of the hot path
+    tester1.json    the reference's `tester1 --raw` histogram lines for a few configurations
 """
 from __future__ import annotations
 
@@ -183,7 +185,7 @@ def main():
         json.dump(results, f, indent=1)
 
 
-if __name__ == "__main__" and "--cli" not in sys.argv:
+if __name__ == "__main__" and "--cli" not in sys.argv and "--tester1" not in sys.argv:
     main()
 
 
@@ -199,7 +201,15 @@ CLI_CASES = [
     (["search", "{hash16}", "--want", "h = 34272"], None),
     (["search", "{hash16}", "--want", "h = 34272", "--raw"], None),
     (["verify", "{mul5}", "--spec", "p = a * b", "--ticks", "2"], None),
+    # run --table (src/main.c:422-445): the truth table, .out columns or RR
+    (["run", "{mul3}", "--table"], None),
+    (["run", "{rt}", "--table"], None),
+    (["run", "{rt}", "--table", "--ticks", "3"], None),
+    (["run", "{rr}", "--table", "--ticks", "2"], None),
 ]
+
+RR_ONLY = ".in x y z\nNAND x\nNAND y\nSTO t\nNAND z\nNAND t\nSTO x\n"
+
 
 
 def cli_programs(tmp):
@@ -213,6 +223,9 @@ def cli_programs(tmp):
     progs["ra"] = a.text()
     progs["rb"] = a.rewrite(5).text()
     progs["rc"] = a.rewrite(5, mutate=True).text()
+    progs["mul3"] = gen_text("mul", {"bits": 3})
+    progs["rt"] = T.Program.random_in(6, 5, 40, 7).text()
+    progs["rr"] = RR_ONLY
     paths = {}
     for k, v in progs.items():
         paths[k] = os.path.join(tmp, k + ".asm")
@@ -236,3 +249,29 @@ def cli_main():
 
 if __name__ == "__main__" and "--cli" in sys.argv:
     cli_main()
+
+
+# ---- tester1: the reference's raw histogram lines (one thread, so the order is fixed) --------
+
+T1_CASES = [
+    ["--programs", "16"],
+    ["--cells", "8,100,500,1000", "--programs", "8", "--max-passes", "4096", "--seed", "7"],
+    ["--cells", "20,40", "--ratio", "2", "--programs", "32", "--max-passes", "64"],
+    ["--cells", "3,5", "--ratio", "9", "--programs", "40", "--seed", "12345"],
+]
+
+
+def t1_main():
+    out = []
+    for args in T1_CASES:
+        rc, stdout, stderr = run(["tester1"] + args + ["--raw", "--threads", "1"])
+        if rc != 0:
+            raise RuntimeError(stderr)
+        lines = [l for l in stdout.splitlines() if l.startswith("T1 ")]
+        out.append({"args": args, "t1": lines})
+    with open(os.path.join(HERE, "tester1.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__" and "--tester1" in sys.argv:
+    t1_main()

@@ -20,7 +20,9 @@ def programs(tmp):
     a = T.Program.random_in(12, 10, 200, 424242)
     progs = {"mul4": T.Program.gen_mul(4).text(), "mul5": T.Program.gen_mul(5).text(),
              "mul6": T.Program.gen_mul(6).text(), "hash16": T.Program.gen_hash(16, 5).text(),
-             "ra": a.text(), "rb": a.rewrite(5).text(), "rc": a.rewrite(5, mutate=True).text()}
+             "ra": a.text(), "rb": a.rewrite(5).text(), "rc": a.rewrite(5, mutate=True).text(),
+             "mul3": T.Program.gen_mul(3).text(), "rt": T.Program.random_in(6, 5, 40, 7).text(),
+             "rr": ".in x y z\nNAND x\nNAND y\nSTO t\nNAND z\nNAND t\nSTO x\n"}
     paths = {}
     for k, v in progs.items():
         paths[k] = os.path.join(tmp, k + ".asm")
