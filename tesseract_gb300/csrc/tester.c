@@ -2,9 +2,11 @@
    (src/tester.c:57-81, seeded by t1_program_seed, src/tester.c:51-55) runs from 512 random
    states and the cycle length of every run goes into the size's histogram, as t1_work
    (src/tester.c:182-223) adds it up.  The programs of one size run as one launch of the
-   tester kernel, one block each; sizes and chunks go in the reference's order (programs k = 0,
-   1, ... of each size), so the histogram, the pass count and the longest cycle with its
-   program are the reference's.  With a time limit (programs = 0) whole chunks run until the
+   tester kernel, one block each, which makes its program and its starting states itself and adds
+   its runs to the size's histogram on the device; the host only adds up the passes and finds
+   the first program with the longest cycle, in the reference's order (programs k = 0, 1, ... of
+   each size), so the histogram, the pass count and the longest cycle with its program are the
+   reference's.  With a time limit (programs = 0) whole chunks run until the
    time is up: no program is cut off, so `unfinished` stays 0. */
 #include <stdlib.h>
 #include <string.h>
@@ -12,10 +14,10 @@
 #include "engine.h"
 #include "tester.h"
 
-int tc_t1_launch(const TcT1Dev *d, uint32_t nprogs, uint32_t max_cells, cudaStream_t stream,
-                 char *err, size_t errlen);
+int tc_t1_launch(const TcT1Dev *d, uint32_t nprogs, cudaStream_t stream, char *err,
+                 size_t errlen);
 
-#define CHUNK 8192  /* programs per launch */
+#define CHUNK 65536  /* programs per launch */
 
 uint64_t tc_t1_program_seed(uint64_t seed, uint32_t cells, uint64_t k)
 {
@@ -29,96 +31,59 @@ static size_t program_len(const T1Config *cfg, uint32_t cells)
     return len ? len : 1;
 }
 
-static int bucket(uint64_t lam)
-{
-    int b = 0;
-    while (b < T1_BUCKETS - 2 && ((uint64_t)1 << b) < lam)
-        b++;
-    return b;
-}
+/* Device buffers of one run: the histogram, then passes and longest cycle per program. */
+typedef struct {
+    uint64_t *dev, *hist, *passes, *longest;
+} Bufs;
 
 /* Programs k0 .. k0 + n - 1 of size cells: one launch; their results go into st. */
-static int run_chunk(const T1Config *cfg, uint32_t cells, uint64_t k0, uint32_t n, T1Size *st,
-                     char *err, size_t errlen)
+static int run_chunk(const T1Config *cfg, const Bufs *b, uint32_t cells, uint64_t k0, uint32_t n,
+                     T1Size *st, char *err, size_t errlen)
 {
     size_t len = program_len(cfg, cells);
-    uint32_t ncells = cells + CELL_FIRST_FREE, writable = cells;
-    uint32_t nsample = writable < 64 ? writable : 64;
-    size_t code_n = (size_t)n * len, jobs_b = (size_t)n * sizeof(TcT1Job);
-    size_t code_b = code_n * 4, sample_b = (size_t)nsample * 4;
-    size_t lam_b = (size_t)n * 512 * 8, passes_b = (size_t)n * 8;
-    TcT1Job *jobs = tc_xcalloc(n, sizeof *jobs);
-    uint32_t *code = tc_xmalloc(code_b + 4), sample[64];
-    for (uint32_t i = 0; i < nsample; i++)
-        sample[i] = CELL_FIRST_FREE + (uint32_t)((uint64_t)i * writable / nsample);
-    for (uint32_t i = 0; i < n; i++) {
-        uint64_t ps = tc_t1_program_seed(cfg->seed, cells, k0 + i);
-        Program p;
-        tc_random_program(&p, cells, len, ps);
-        for (size_t q = 0; q < len; q++)
-            code[(size_t)i * len + q] = p.code[q].addr << 1 | p.code[q].op;
-        tc_program_free(&p);
-        jobs[i].seed = ps;
-        jobs[i].ncells = ncells;
-        jobs[i].len = (uint32_t)len;
-        jobs[i].code = (uint32_t)((size_t)i * len);
-        jobs[i].sample = 0;
-        jobs[i].nsample = nsample;
-    }
-    size_t o_code = 0, o_jobs = (code_b + 255) & ~(size_t)255;
-    size_t o_sample = o_jobs + ((jobs_b + 255) & ~(size_t)255);
-    size_t o_lam = o_sample + 256, o_passes = o_lam + ((lam_b + 255) & ~(size_t)255);
-    size_t total = o_passes + passes_b;
-    char *dev = NULL;
-    uint64_t *lam = tc_xmalloc(lam_b), *passes = tc_xmalloc(passes_b);
-    cudaStream_t s = tc_engine.stream;
+    if (len > 0xffffffffu)
+        return tc_fail(err, errlen, "%zu instructions per program: too many", len);
     TcT1Dev d;
-    int ok = tc_cu_check(cudaMalloc((void **)&dev, total), "cudaMalloc", err, errlen);
-    if (ok) {
-        d.jobs = (const TcT1Job *)(dev + o_jobs);
-        d.code = (const uint32_t *)(dev + o_code);
-        d.sample = (const uint32_t *)(dev + o_sample);
-        d.lam = (uint64_t *)(dev + o_lam);
-        d.passes = (uint64_t *)(dev + o_passes);
-        d.max_passes = cfg->max_passes;
-        ok = tc_cu_check(cudaMemcpyAsync(dev + o_code, code, code_b, cudaMemcpyHostToDevice, s),
+    memset(&d, 0, sizeof d);
+    d.seed = cfg->seed;
+    d.k0 = k0;
+    d.max_passes = cfg->max_passes;
+    d.cells = cells;
+    d.len = (uint32_t)len;
+    d.nsample = cells < 64 ? cells : 64;
+    d.hist = b->hist;
+    d.passes = b->passes;
+    d.longest = b->longest;
+    uint64_t hist[T1_BUCKETS];
+    uint64_t *passes = tc_xmalloc((size_t)n * 8), *longest = tc_xmalloc((size_t)n * 8);
+    cudaStream_t s = tc_engine.stream;
+    int ok = tc_cu_check(cudaMemsetAsync(b->hist, 0, sizeof hist, s), "memset", err, errlen) &&
+             tc_t1_launch(&d, n, s, err, errlen) &&
+             tc_cu_check(cudaMemcpyAsync(hist, b->hist, sizeof hist, cudaMemcpyDeviceToHost, s),
                          "copy", err, errlen) &&
-             tc_cu_check(cudaMemcpyAsync(dev + o_jobs, jobs, jobs_b, cudaMemcpyHostToDevice, s),
+             tc_cu_check(cudaMemcpyAsync(passes, b->passes, (size_t)n * 8,
+                                         cudaMemcpyDeviceToHost, s),
                          "copy", err, errlen) &&
-             tc_cu_check(cudaMemcpyAsync(dev + o_sample, sample, sample_b ? sample_b : 4,
-                                         cudaMemcpyHostToDevice, s),
-                         "copy", err, errlen) &&
-             tc_t1_launch(&d, n, ncells, s, err, errlen) &&
-             tc_cu_check(cudaMemcpyAsync(lam, dev + o_lam, lam_b, cudaMemcpyDeviceToHost, s),
-                         "copy", err, errlen) &&
-             tc_cu_check(cudaMemcpyAsync(passes, dev + o_passes, passes_b,
+             tc_cu_check(cudaMemcpyAsync(longest, b->longest, (size_t)n * 8,
                                          cudaMemcpyDeviceToHost, s),
                          "copy", err, errlen) &&
              tc_cu_check(cudaStreamSynchronize(s), "tester1", err, errlen);
-    }
-    if (dev)
-        cudaFree(dev);
-    for (uint32_t i = 0; ok && i < n; i++) {  /* as t1_work adds one program up */
-        st->passes += passes[i];
-        st->programs++;
-        st->starts += 512;
-        for (int l = 0; l < 512; l++) {
-            uint64_t v = lam[(size_t)i * 512 + l];
-            if (!v) {
-                st->hist[T1_BUCKETS - 1]++;
-                continue;
-            }
-            st->hist[bucket(v)]++;
-            if (v > st->longest) {
-                st->longest = v;
-                st->longest_seed = jobs[i].seed;
+    if (ok) {
+        /* as t1_work adds each program up, in program order: the first longest cycle wins */
+        for (int i = 0; i < T1_BUCKETS; i++)
+            st->hist[i] += hist[i];
+        for (uint32_t i = 0; i < n; i++) {
+            st->passes += passes[i];
+            st->programs++;
+            st->starts += 512;
+            if (longest[i] > st->longest) {
+                st->longest = longest[i];
+                st->longest_seed = tc_t1_program_seed(cfg->seed, cells, k0 + i);
             }
         }
     }
-    free(lam);
     free(passes);
-    free(jobs);
-    free(code);
+    free(longest);
     return ok;
 }
 
@@ -137,22 +102,32 @@ double cuda_t1_run(const T1Config *cfg, T1Size *out, int *threads, char *err, si
         out[si].cells = cfg->cells[si];
         out[si].len = program_len(cfg, cfg->cells[si]);
     }
+    Bufs b;
+    memset(&b, 0, sizeof b);
+    if (!tc_cu_check(cudaMalloc((void **)&b.dev, (T1_BUCKETS + 2 * (size_t)CHUNK) * 8),
+                     "cudaMalloc", err, errlen))
+        return -1;
+    b.hist = b.dev;
+    b.passes = b.dev + T1_BUCKETS;
+    b.longest = b.passes + CHUNK;
     double t0 = tc_now();
     uint64_t next[T1_SIZES] = {0};
+    uint32_t chunk = cfg->programs ? CHUNK : 4096;  /* timed runs check the clock more often */
+    int ok = 1;
     for (;;) {
         int any = 0;
-        for (int si = 0; si < cfg->nsizes; si++) {
-            uint64_t left = cfg->programs ? cfg->programs - next[si] : CHUNK;
+        for (int si = 0; si < cfg->nsizes && ok; si++) {
+            uint64_t left = cfg->programs ? cfg->programs - next[si] : chunk;
             if (!left)
                 continue;
-            uint32_t n = left < CHUNK ? (uint32_t)left : CHUNK;
-            if (!run_chunk(cfg, cfg->cells[si], next[si], n, &out[si], err, errlen))
-                return -1;
+            uint32_t n = left < chunk ? (uint32_t)left : chunk;
+            ok = run_chunk(cfg, &b, cfg->cells[si], next[si], n, &out[si], err, errlen);
             next[si] += n;
             any = 1;
         }
-        if (!any || (!cfg->programs && tc_now() - t0 >= cfg->seconds))
+        if (!ok || !any || (!cfg->programs && tc_now() - t0 >= cfg->seconds))
             break;
     }
-    return tc_now() - t0;
+    cudaFree(b.dev);
+    return ok ? tc_now() - t0 : -1;
 }
