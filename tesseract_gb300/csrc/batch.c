@@ -90,10 +90,17 @@ static void clear_list(Vec *lists, const Program *p, unsigned base, const unsign
     free(seen);
 }
 
+#define MAX_CLASSES 16
+
 typedef struct {
     Vec jobs, code, luts, lists, rpn, vars;
     uint32_t units;
     int      slots;
+    /* units in launch order: class by class (jobs needing few shared-memory slots first), each
+       class one launch with its own slot count, so light jobs run with more blocks per SM */
+    int      nclass;
+    uint32_t class_end[MAX_CLASSES];  /* units of classes 0..i end at class_end[i] */
+    int      class_slots[MAX_CLASSES];
 } Pack;
 
 /* ---- LUT jobs: one tick, the pass mapped onto 3-input LUTs ------------------------------------ */
@@ -507,22 +514,6 @@ done:
     return ok;
 }
 
-static __attribute__((unused)) void *upload(const Vec *v, int *ok, char *err, size_t errlen)
-{
-    void *d = NULL;
-    size_t bytes = (v->n ? v->n : 1) * v->elem;
-    if (!*ok)
-        return NULL;
-    if (!tc_cu_check(cudaMalloc(&d, bytes), "cudaMalloc", err, errlen) ||
-        (v->n && !tc_cu_check(cudaMemcpy(d, v->p, bytes, cudaMemcpyHostToDevice), "upload", err,
-                              errlen))) {
-        *ok = 0;
-        cudaFree(d);
-        return NULL;
-    }
-    return d;
-}
-
 /* ---- waves: a set of jobs packed, launched on a stream, finished job by job ----------------- */
 
 struct TcWave {
@@ -546,6 +537,58 @@ static size_t align256(size_t n)
     return (n + 255) & ~(size_t)255;
 }
 
+/* Blocks of the interpreter an SM holds when a block needs `slots` slots (shared memory is the
+   limit; 16 blocks of 128 threads fill an SM). */
+static int blocks_per_sm(int slots)
+{
+    int b = (int)(233472 / ((size_t)slots * TC_BATCH_BLOCK * 4 + 1024));
+    return b < 1 ? 1 : b > 16 ? 16 : b;
+}
+
+/* Gives the jobs' units their launch order: jobs grouped by how many blocks per SM their slots
+   allow (fewest slots first), a group too small to fill the GPU about twice merged into the
+   next; within a group, job order. */
+static void order_units(Pack *pk)
+{
+    TcBatchJob *J = pk->jobs.p;
+    int n = (int)pk->jobs.n, sms = tc_engine.sms > 0 ? tc_engine.sms : 152;
+    uint32_t units_at[17] = {0};
+    for (int i = 0; i < n; i++)
+        units_at[blocks_per_sm(J[i].slots)] += J[i].units;
+    /* classes from 16 blocks per SM down to 1; small ones join the next */
+    int cls_of[17], nclass = 0;
+    uint32_t pending = 0;
+    for (int b = 16; b >= 1; b--) {
+        cls_of[b] = nclass;
+        pending += units_at[b];
+        if (pending && (pending >= (uint32_t)(2 * sms * b) || b == 1)) {
+            nclass++;
+            pending = 0;
+        }
+    }
+    if (pending || !nclass)
+        nclass++;
+    for (int b = 1; b <= 16; b++)
+        if (cls_of[b] >= nclass)
+            cls_of[b] = nclass - 1;
+    /* first units, class by class */
+    uint32_t at = 0;
+    for (int c = 0; c < nclass; c++) {
+        pk->class_slots[c] = 1;
+        for (int i = 0; i < n; i++) {
+            int b = blocks_per_sm(J[i].slots);
+            if (cls_of[b] != c)
+                continue;
+            J[i].first_unit = at;
+            at += J[i].units;
+            if (J[i].slots > pk->class_slots[c])
+                pk->class_slots[c] = J[i].slots;
+        }
+        pk->class_end[c] = at;
+    }
+    pk->nclass = nclass;
+}
+
 /* Maps and packs the jobs (no device work yet). */
 int tc_wave_prepare(TcWave **out, const Enum *const *jobs, int njobs, char *err, size_t errlen)
 {
@@ -560,8 +603,7 @@ int tc_wave_prepare(TcWave **out, const Enum *const *jobs, int njobs, char *err,
     w->pk.rpn.elem = sizeof(TcBatchRpn);
     w->pk.vars.elem = 1;
     LutJob *lj = tc_xcalloc((size_t)njobs + 1, sizeof *lj);
-    if (!getenv("TESSERACT_BATCH_BUNDLES"))
-        map_jobs(jobs, njobs, lj);
+    map_jobs(jobs, njobs, lj);
     int ok = 1;
     for (int i = 0; i < njobs && ok; i++) {
         char e2[400];
@@ -580,6 +622,7 @@ int tc_wave_prepare(TcWave **out, const Enum *const *jobs, int njobs, char *err,
         tc_wave_free(w);
         return 0;
     }
+    order_units(&w->pk);
     w->unit_job = tc_xmalloc(((size_t)w->pk.units + 1) * sizeof *w->unit_job);
     const TcBatchJob *J = w->pk.jobs.p;
     for (int i = 0; i < njobs; i++)
@@ -607,7 +650,7 @@ int tc_wave_launch(TcWave *w, cudaStream_t stream, double share, char *err, size
     size_t off[10], at = 0;
     size_t sizes[10] = {pk->jobs.n * pk->jobs.elem, pk->code.n * 8, pk->luts.n * 4,
                         pk->lists.n * 2, pk->rpn.n * pk->rpn.elem, pk->vars.n,
-                        (size_t)pk->units * 4, 4, (size_t)n * 8, (size_t)n * 4};
+                        (size_t)pk->units * 4, MAX_CLASSES * 4, (size_t)n * 8, (size_t)n * 4};
     for (int i = 0; i < 10; i++) {
         off[i] = at;
         at += align256(sizes[i] ? sizes[i] : 1);
@@ -650,7 +693,8 @@ int tc_wave_launch(TcWave *w, cudaStream_t stream, double share, char *err, size
         rem[i] = J[i].units;
     int ok = tc_cu_check(cudaMemcpyAsync(d + off[9], rem, (size_t)n * 4, cudaMemcpyHostToDevice,
                                          stream), "upload", err, errlen) &&
-             tc_cu_check(cudaMemsetAsync(d + off[7], 0, 4, stream), "memset", err, errlen) &&
+             tc_cu_check(cudaMemsetAsync(d + off[7], 0, MAX_CLASSES * 4, stream), "memset", err,
+                         errlen) &&
              tc_cu_check(cudaMemsetAsync(d + off[8], 0, (size_t)n * 8, stream), "memset", err,
                          errlen);
     /* the host buffer must outlive the asynchronous copy: wait for it */
@@ -662,16 +706,30 @@ int tc_wave_launch(TcWave *w, cudaStream_t stream, double share, char *err, size
     struct TcBatchDev dv = {(const TcBatchJob *)(d + off[0]), (const uint64_t *)(d + off[1]),
                             (const uint32_t *)(d + off[2]), (const uint16_t *)(d + off[3]),
                             (const TcBatchRpn *)(d + off[4]), (const uint8_t *)(d + off[5]),
-                            (const uint32_t *)(d + off[6]), pk->units, (uint32_t *)(d + off[7]),
+                            (const uint32_t *)(d + off[6]), 0, pk->units, (uint32_t *)(d + off[7]),
                             (unsigned long long *)(d + off[8]),
                             (unsigned long long *)(hd + hoff[0]), (uint32_t *)(hd + hoff[1]),
                             (uint32_t *)(d + off[9]), (unsigned long long *)(hd + hoff[2]),
                             (uint32_t *)(hd + hoff[3])};
     if (!tc_cu_check(cudaEventCreate(&w->ev0), "event", err, errlen) ||
         !tc_cu_check(cudaEventCreate(&w->ev1), "event", err, errlen) ||
-        !tc_cu_check(cudaEventRecord(w->ev0, stream), "event", err, errlen) ||
-        !tc_batch_launch(&dv, pk->slots, stream, share, &w->grid, err, errlen) ||
-        !tc_cu_check(cudaEventRecord(w->ev1, stream), "event", err, errlen))
+        !tc_cu_check(cudaEventRecord(w->ev0, stream), "event", err, errlen))
+        return 0;
+    /* one launch per class, each with its own counter and slot count */
+    w->grid = 0;
+    for (int c = 0; c < pk->nclass; c++) {
+        int grid = 0;
+        dv.unit_base = c ? pk->class_end[c - 1] : 0;
+        dv.nunits = pk->class_end[c];
+        dv.next_unit = (uint32_t *)(d + off[7]) + c;
+        if (dv.nunits == dv.unit_base)
+            continue;
+        if (!tc_batch_launch(&dv, pk->class_slots[c], stream, share, &grid, err, errlen))
+            return 0;
+        if (grid > w->grid)
+            w->grid = grid;
+    }
+    if (!tc_cu_check(cudaEventRecord(w->ev1, stream), "event", err, errlen))
         return 0;
     w->launched = 1;
     return 1;

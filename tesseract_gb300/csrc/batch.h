@@ -62,6 +62,7 @@ struct TcBatchDev {
     const TcBatchRpn   *rpn;
     const uint8_t      *vars;
     const uint32_t     *unit_job;
+    uint32_t            unit_base;   /* this launch takes units unit_base .. nunits - 1 */
     uint32_t            nunits;
     uint32_t           *next_unit;
     unsigned long long *hits;        /* per job */

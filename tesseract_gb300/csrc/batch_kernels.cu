@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(B) tc_batch_kernel(TcBatchDev d)
     uint32_t *S = smem + tid;
     for (;;) {
         if (tid == 0) {
-            unit_s = atomicAdd(d.next_unit, 1u);
+            unit_s = d.unit_base + atomicAdd(d.next_unit, 1u);
             block_hits = 0;
         }
         __syncthreads();
@@ -284,8 +284,8 @@ extern "C" int tc_batch_launch(const TcBatchDev *d, int slots, cudaStream_t stre
     if (per_sm < 1)
         return tc_fail(err, errlen, "the batch needs %zu bytes of shared memory per block", smem);
     int grid = (int)(tc_engine.sms * per_sm * share);
-    if ((uint32_t)grid > d->nunits)
-        grid = (int)d->nunits;
+    if ((uint32_t)grid > d->nunits - d->unit_base)
+        grid = (int)(d->nunits - d->unit_base);
     if (grid < 1)
         grid = 1;
     *grid_out = grid;
