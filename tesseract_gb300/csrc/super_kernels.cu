@@ -146,7 +146,66 @@ struct SpDev {
     int *found;
     SpState *sol;
     unsigned long long *nodes;
+    ulonglong2 *tt;             // the transposition table, shared by every thread
+    unsigned long long tt_mask;
+    int tt_min_rem;             // states with fewer instructions left are not looked up
 };
+
+// Subtrees with fewer instructions left than this are searched again rather than looked up:
+// a lookup is a random global-memory access and a key over every operand value.
+extern "C" {
+int tc_super_tt_min_rem = 4;
+}
+
+// ---- the transposition table ------------------------------------------------------------------
+//
+// States searched in full without a program, as the reference's per-thread table keeps them
+// (src/super.c:408-418, 641-716): the same state is reached in many orders, and its future
+// depends only on RR, the readable, written and used cells, and the values a NAND could read with
+// what each costs.  Here one table serves every thread, and it is kept from budget to budget.  An
+// entry is two 64-bit words: the state's first key, and its second key with the low byte
+// replaced by the instructions that were left when it was searched; a state arriving with `rem`
+// left is pruned when an entry holds both its keys and at least `rem`.  An entry torn between two
+// writers matches only when both wrote this state (the rem is then a true one) or by a 120-bit
+// coincidence, which the reference's 128-bit keys also rule out in practice.
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// The state's keys (src/super.c:626-641): RR, the cell masks, and the operand values as a set.
+__device__ void state_key(const SpSpec *sp, const SpState *x, uint64_t keep, uint64_t *k1,
+                          uint64_t *k2)
+{
+    uint64_t a = mix64(x->hist[x->n] ^ (uint64_t)sp_rr_def(x) << 63), b = mix64(a + 0x1234567);
+    const uint64_t f = (uint64_t)x->readable | (uint64_t)x->written << 21 |
+                       (uint64_t)x->used << 42;
+    a += mix64(f + 0x9E3779B97F4A7C15ull);
+    b ^= mix64(f * 3 + 77);
+    for (uint64_t rest = keep; rest; rest &= rest - 1) {
+        SpCand c;
+        raw_cand(sp, x, __ffsll((long long)rest) - 1, &c);
+        const uint64_t v = c.v * 2 + c.extra;
+        a += mix64(v + 0x51ED27);
+        b += mix64(v * 0x2545F4914F6CDD1Dull + 0xABCDEF);
+    }
+    *k1 = a;
+    *k2 = b;
+}
+
+__device__ __forceinline__ bool tt_seen(const SpDev &d, uint64_t k1, uint64_t k2, int rem)
+{
+    const ulonglong2 e = d.tt[k1 & d.tt_mask];
+    return e.x == k1 && (e.y & ~0xFFull) == (k2 & ~0xFFull) && (int)(e.y & 0xFFull) >= rem;
+}
+
+__device__ __forceinline__ void tt_store(const SpDev &d, uint64_t k1, uint64_t k2, int rem)
+{
+    d.tt[k1 & d.tt_mask] = make_ulonglong2(k1, (k2 & ~0xFFull) | (uint64_t)rem);
+}
 
 __global__ void __launch_bounds__(128) tc_super_kernel(SpDev d)
 {
@@ -161,6 +220,8 @@ __global__ void __launch_bounds__(128) tc_super_kernel(SpDev d)
     uint16_t wmask[DEV_LEVELS + 1];
     uint32_t w_readable[DEV_LEVELS + 1], w_written[DEV_LEVELS + 1], used_before[DEV_LEVELS + 1];
     int w_cost[DEV_LEVELS + 1];
+    uint64_t key1[DEV_LEVELS + 1], key2[DEV_LEVELS + 1];
+    int8_t key_rem[DEV_LEVELS + 1];  // rem of the node at this level, or -1: not in the table
     unsigned long long nodes = 0, polled = 0;
     const int budget = d.budget;
     for (;;) {
@@ -172,6 +233,7 @@ __global__ void __launch_bounds__(128) tc_super_kernel(SpDev d)
         int L = n0;
         keep[L] = survivors(sp, &x);
         ci[L] = 0;
+        key_rem[L] = -1;
         bool expand = true;
         for (;;) {
             if (nodes - polled >= POLL) {
@@ -184,6 +246,8 @@ __global__ void __launch_bounds__(128) tc_super_kernel(SpDev d)
                 if (!rest) {  // every operand tried at this level
                     if (L == n0)
                         break;
+                    if (key_rem[L] >= 0)  // searched in full, nothing found
+                        tt_store(d, key1[L], key2[L], key_rem[L]);
                     x.readable = w_readable[L];
                     x.written = w_written[L];
                     x.cost = w_cost[L];
@@ -233,8 +297,19 @@ __global__ void __launch_bounds__(128) tc_super_kernel(SpDev d)
             if (a == 0) {
                 keep[L] = survivors(sp, &x);
                 ci[L] = 0;
-                expand = true;
-                continue;
+                key_rem[L] = -1;
+                const int rem = budget - x.cost;
+                bool seen = false;
+                if (rem >= d.tt_min_rem) {  // small subtrees: cheaper to search again
+                    state_key(sp, &x, keep[L], &key1[L], &key2[L]);
+                    seen = tt_seen(d, key1[L], key2[L], rem);
+                    key_rem[L] = (int8_t)rem;
+                }
+                if (!seen) {
+                    expand = true;
+                    continue;
+                }
+                key_rem[L] = -1;  // searched before with at least this much left: nothing there
             }
             x.readable = w_readable[L];
             x.written = w_written[L];
@@ -278,6 +353,12 @@ extern "C" int tc_super_run(const SpSpec *sp, int max_cost, int lb, int *found, 
     const size_t threads = (size_t)tc_engine.sms * (per_sm > 0 ? per_sm : 1) * 128;
     SpState *d_front = nullptr;
     size_t d_cap = 0;
+    // the transposition table: 2^25 entries of 16 bytes, kept from budget to budget
+    const unsigned long long tt_entries = 1ull << 25;
+    ulonglong2 *d_tt = nullptr;
+    ok = ok && tc_cu_check(cudaMalloc(&d_tt, tt_entries * sizeof(ulonglong2)), "cudaMalloc", err,
+                           errlen) &&
+         tc_cu_check(cudaMemset(d_tt, 0, tt_entries * sizeof(ulonglong2)), "memset", err, errlen);
     for (int budget = lb; ok && budget <= max_cost && !*found; budget++) {
         if (budget > DEV_LEVELS) {
             tc_fail(err, errlen, "budget %d is deeper than the device search goes (%d)", budget,
@@ -320,7 +401,8 @@ extern "C" int tc_super_run(const SpSpec *sp, int max_cost, int lb, int *found, 
                  tc_cu_check(cudaMemset(d_nodes, 0, 8), "memset", err, errlen);
             if (ok) {
                 SpDev d = {d_spec, d_front, (unsigned long long)fr.n, budget, d_next, d_found,
-                           d_sol, d_nodes};
+                           d_sol, d_nodes, d_tt, tt_entries - 1,
+                           tc_super_tt_min_rem > 0 ? tc_super_tt_min_rem : 1};
                 unsigned blocks = (unsigned)((fr.n + 127) / 128);
                 unsigned maxb = (unsigned)(tc_engine.sms * (per_sm > 0 ? per_sm : 1));
                 if (blocks > maxb)
@@ -351,6 +433,7 @@ extern "C" int tc_super_run(const SpSpec *sp, int max_cost, int lb, int *found, 
                     *found ? "found" : "none", (double)*nodes, tc_now() - t0);
     }
     cudaFree(d_front);
+    cudaFree(d_tt);
     cudaFree(d_spec);
     cudaFree(d_found);
     cudaFree(d_sol);
