@@ -39,8 +39,10 @@
 int tc_cube_map = 1;
 /* the most warps per word a mapped kernel splits its written cells over, and the fewest cells a
    warp gets */
-int tc_cube_groups = 8;
+int tc_cube_groups = 32;
 int tc_cube_min_cells = 16;
+/* warps per block of a group-major kernel (0: never group-major) */
+int tc_cube_gm_warps = 4;
 /* the most instructions in one kernel: longer segments are split.  Fewer, longer kernels win
    once they are split over warps (Life on 65,536 machines: 3 kernels of up to 125,722
    instructions run 36-38k generations/s, 13 kernels of 12,000 run 29k), at the price of a longer
@@ -55,7 +57,8 @@ struct CudaCube {
     unsigned    nk, nseg;
     int         loop;       /* one kernel, passes loop inside it */
     cudaKernel_t *fn;
-    unsigned    *warps;     /* warps per word of kernel k */
+    unsigned    *warps;     /* warp groups of kernel k */
+    int         *gmajor;    /* kernel k is group-major (one group per block) */
     cudaGraphExec_t graph;
     unsigned    graph_passes;
 };
@@ -394,18 +397,10 @@ static void emit_lut(Src *o, const ChunkNet *cn, int node, const char *indent)
          (unsigned)tt);
 }
 
-/* One warp's code in a split kernel: the cone of `outs` (cells, plus RR when own_rr) in node
-   order.  Every load comes first (start values and far reads, all in flight at once), then a
-   barrier of the whole block, then the LUTs with each cell's store right after its new value, so
-   values do not stay live to the end (a Life generation's last segment writes 1,023 cells).
-   The barrier makes storing safe: the other warps of the block, the only ones that read these
-   words' cells, have loaded every start value they use; inside a segment no written cell is read
-   across a far dimension, so no other block reads them. */
-static void emit_group(Src *o, Chunk *k, const ChunkNet *cn, const uint32_t *outs, int nouts,
-                       int own_rr, unsigned char *in_cone, int *stack, int *store_at,
-                       int *store_next)
+/* Marks in in_cone the nodes warp group needs for `outs` (and RR when own_rr). */
+static void cone_of(const ChunkNet *cn, const uint32_t *outs, int nouts, int own_rr,
+                    unsigned char *in_cone, int *stack)
 {
-    const Program *p = k->p;
     int n = tc_net_size(cn->net);
     memset(in_cone, 0, (size_t)n + 1);
     int sp = 0;
@@ -429,6 +424,21 @@ static void emit_group(Src *o, Chunk *k, const ChunkNet *cn, const uint32_t *out
         for (int j = 0; j < nl; j++)
             stack[sp++] = lv[j];
     }
+}
+
+/* One warp group's code in a split kernel: the cone of `outs` (cells, plus RR when own_rr) in
+   node order.  Every load comes first (start values and far reads, all in flight at once), then
+   with `barrier` a barrier of the whole block, then the LUTs with each cell's store right after
+   its new value, so values do not stay live to the end (a Life generation's last segment writes
+   1,023 cells).  The barrier makes storing safe when another group of the block reads a start
+   value this group overwrites; without such a conflict there is none and the groups need not
+   share a block.  Inside a segment no written cell is read across a far dimension, so no other
+   word's warps read these cells. */
+static void emit_group(Src *o, Chunk *k, const ChunkNet *cn, const uint32_t *outs, int nouts,
+                       int own_rr, const unsigned char *in_cone, int barrier, int *store_at,
+                       int *store_next)
+{
+    int n = tc_net_size(cn->net);
     for (int i = 0; i <= n; i++)
         store_at[i] = -1;
     for (int i = 0; i < nouts; i++) {
@@ -443,9 +453,9 @@ static void emit_group(Src *o, Chunk *k, const ChunkNet *cn, const uint32_t *out
     for (int v = 2; v < n; v++)
         if (in_cone[v] && is_leaf(&cn->L, v) && cn->L.far[v])
             emit(o, "        const u32 n%d = %s;\n", v, cn->L.expr[v]);
-    /* every warp of the block has read the words' start values before any warp stores; the
-       non-.aligned barrier may be reached from different code, once per warp */
-    emit(o, "        asm volatile(\"barrier.sync 0;\" ::: \"memory\");\n");
+    /* the non-.aligned barrier may be reached from different code, once per warp */
+    if (barrier)
+        emit(o, "        asm volatile(\"barrier.sync 0;\" ::: \"memory\");\n");
     int luts = 0;
     for (int v = 2; v <= n; v++) {
         if (v < n && in_cone[v]) {
@@ -468,7 +478,6 @@ static void emit_group(Src *o, Chunk *k, const ChunkNet *cn, const uint32_t *out
         emit(o, "        if (t < W) rr[w] = %s;\n", nm);
     }
     emit(o, "        // %d LOP3\n", luts);
-    (void)p;
 }
 
 /* Warps per word for a chunk kernel: its written cells split into groups of at least
@@ -492,10 +501,19 @@ static unsigned chunk_groups(const Program *p, size_t from, size_t to, int loop)
     return g ? g : 1;
 }
 
-/* The mapped body of a kernel that does not loop: `groups` warps per word, warp y computing the
-   cone of the y-th share of the written cells (RR with the last), so a chunk runs on `groups`
-   times as many warps; nodes that several cones share are computed in each. */
-static void split_body(Src *o, Chunk *k, size_t from, size_t to, unsigned groups)
+/* The mapped body of a kernel that does not loop: `groups` warp groups per word, group y
+   computing the cone of the y-th share of the written cells (RR with the last), so a chunk runs
+   on `groups` times as many warps; nodes that several cones share are computed in each.
+
+   A cell one group overwrites while another group reads its start value would be a conflict,
+   so outputs that read a written cell's start value are kept in that cell's group (and the same
+   for RR).  When that leaves the groups balanced the kernel is "group-major": each block runs
+   tc_cube_gm_warps warps of ONE group over as many words, so the warps on an SM share their
+   instructions, and no barrier is needed.  Otherwise the shares ignore the conflicts, and every
+   block holds all groups of 32 words and waits at a barrier between loads and stores.
+   *group_major gets the choice. */
+static void split_body(Src *o, Chunk *k, size_t from, size_t to, unsigned groups,
+                       int *group_major)
 {
     const Program *p = k->p;
     ChunkNet cn;
@@ -506,25 +524,46 @@ static void split_body(Src *o, Chunk *k, size_t from, size_t to, unsigned groups
         if (k->written[c])
             outs[nouts++] = c;
     int n = tc_net_size(cn.net);
-    unsigned char *in_cone = tc_xmalloc((size_t)n + 1);
     int *stack = tc_xmalloc((((size_t)n + 1) * 3 + p->ncells + 2) * sizeof *stack);
     int *store_at = tc_xmalloc(((size_t)n + 1) * sizeof *store_at);
     int *store_next = tc_xmalloc(((size_t)p->ncells + 1) * sizeof *store_next);
-    emit(o, "    // %d LOP3 for %zu NAND/STO instructions, %u group(s)\n", cn.luts, to - from,
-         groups);
-    /* each output's own cone size (LUTs, at least 1), then contiguous shares of about equal
-       total size */
-    double *weight = tc_xmalloc(((size_t)nouts + 1) * sizeof *weight), total = 0;
+    /* Each output's own cone: its size (LUTs, at least 1) for the balance, and the start values
+       it reads.  An output that reads the start value of a cell this kernel writes must be in
+       that cell's group (the writer would otherwise overwrite it under the reader): such
+       outputs are joined (union-find; RR is output nouts, its start value the first leaf). */
+    int nall = nouts + 1, rr_leaf = 2;
+    double *weight = tc_xmalloc(((size_t)nall + 1) * sizeof *weight), total = 0;
     int *stamp = tc_xcalloc((size_t)n + 1, sizeof *stamp);
-    for (int i = 0; i < nouts; i++) {
+    int *out_of = tc_xmalloc(((size_t)p->ncells + 1) * sizeof *out_of);  /* cell -> output */
+    int *root = tc_xmalloc(((size_t)nall + 1) * sizeof *root);
+    for (uint32_t c = 0; c < p->ncells; c++)
+        out_of[c] = -1;
+    for (int i = 0; i < nouts; i++)
+        out_of[outs[i]] = i;
+    for (int i = 0; i < nall; i++)
+        root[i] = i;
+#define FIND(x)                                                                                \
+    ({                                                                                         \
+        int r_ = (x);                                                                          \
+        while (root[r_] != r_)                                                                 \
+            r_ = root[r_] = root[root[r_]];                                                    \
+        r_;                                                                                    \
+    })
+    for (int i = 0; i < nall; i++) {
         int sp = 0, size = 0;
-        stack[sp++] = cn.cur[outs[i]];
+        stack[sp++] = i < nouts ? cn.cur[outs[i]] : cn.rr;
         while (sp) {
             int v = stack[--sp];
             if (v < 2 || stamp[v] == i + 1)
                 continue;
             stamp[v] = i + 1;
             if (is_leaf(&cn.L, v)) {
+                int j = cn.L.cell[v] >= 0 ? out_of[cn.L.cell[v]] : v == rr_leaf ? nouts : -1;
+                if (j >= 0 && j != i) {
+                    int a = FIND(i), b = FIND(j);
+                    if (a != b)
+                        root[a < b ? b : a] = a < b ? a : b;
+                }
                 if (cn.L.src[v] >= 0)
                     stack[sp++] = cn.L.src[v];
                 continue;
@@ -540,28 +579,78 @@ static void split_body(Src *o, Chunk *k, size_t from, size_t to, unsigned groups
         total += weight[i];
     }
     free(stamp);
-    int *cut = tc_xmalloc(((size_t)groups + 1) * sizeof *cut);
-    cut[0] = 0;
-    double acc = 0;
-    unsigned gi = 1;
-    for (int i = 0; i < nouts && gi < groups; i++) {
-        acc += weight[i];
-        if (acc >= total * gi / groups && nouts - (i + 1) >= (int)(groups - gi))
-            cut[gi++] = i + 1;
+    /* joined outputs go together; whole clusters to groups in output order, about equal total
+       size each */
+    double *cw = tc_xcalloc((size_t)nall + 1, sizeof *cw), biggest = 0;
+    for (int i = 0; i < nall; i++)
+        cw[FIND(i)] += weight[i];
+    for (int i = 0; i < nall; i++)
+        if (cw[i] > biggest)
+            biggest = cw[i];
+    int *cgroup = tc_xmalloc(((size_t)nall + 1) * sizeof *cgroup);
+    for (int i = 0; i < nall; i++)
+        cgroup[i] = -1;
+    int *owner = tc_xmalloc(((size_t)nall + 1) * sizeof *owner);
+    {
+        double acc = 0;
+        unsigned g = 0;
+        for (int i = 0; i < nall; i++) {
+            int r0 = FIND(i);
+            if (cgroup[r0] < 0) {
+                cgroup[r0] = (int)g;
+                acc += cw[r0];
+                if (g + 1 < groups && acc >= total * (g + 1) / groups)
+                    g++;
+            }
+            owner[i] = cgroup[r0];
+        }
     }
-    while (gi <= groups)
-        cut[gi++] = nouts;
+#undef FIND
+    /* a cluster much larger than a share leaves the groups unbalanced: then word-major */
+    int conflicts = biggest > 1.5 * total / groups;
+    if (conflicts) {  /* contiguous shares, ignoring the clusters */
+        double acc = 0;
+        unsigned g = 0;
+        for (int i = 0; i < nall; i++) {
+            owner[i] = (int)g;
+            acc += weight[i];
+            if (g + 1 < groups && acc >= total * (g + 1) / groups &&
+                nall - (i + 1) >= (int)(groups - g - 1))
+                g++;
+        }
+    }
     free(weight);
+    free(cw);
+    free(cgroup);
+    free(root);
+    free(out_of);
+    int rr_owner = owner[nouts];
+    /* per group: its outputs and its cone */
+    uint32_t *gouts = tc_xmalloc(((size_t)nouts + 1) * groups * sizeof *gouts);
+    int *gn = tc_xcalloc(groups, sizeof *gn);
+    unsigned char *cone = tc_xmalloc(((size_t)n + 1) * groups);
+#define GROUP_CONE(g) (cone + (size_t)(g) * ((size_t)n + 1))
     for (unsigned g = 0; g < groups; g++) {
-        int lo = cut[g], hi = cut[g + 1];
-        emit(o, "    if (threadIdx.y == %uu) {\n", g);
-        emit_group(o, k, &cn, outs + lo, hi - lo, g + 1 == groups, in_cone, stack, store_at,
-                   store_next);
+        for (int i = 0; i < nouts; i++)
+            if (owner[i] == (int)g)
+                gouts[(size_t)g * nouts + gn[g]++] = outs[i];
+        cone_of(&cn, gouts + (size_t)g * nouts, gn[g], rr_owner == (int)g, GROUP_CONE(g), stack);
+    }
+    *group_major = conflicts == 0 && groups > 1 && tc_cube_gm_warps > 0;
+    emit(o, "    // %d LOP3 for %zu NAND/STO instructions, %u group(s), %s\n", cn.luts, to - from,
+         groups, *group_major ? "group-major" : "word-major with a barrier");
+    for (unsigned g = 0; g < groups; g++) {
+        emit(o, "    if (%s == %uu) {\n", *group_major ? "group" : "threadIdx.y", g);
+        emit_group(o, k, &cn, gouts + (size_t)g * nouts, gn[g], rr_owner == (int)g,
+                   GROUP_CONE(g), !*group_major, store_at, store_next);
         emit(o, "    }\n");
     }
-    free(cut);
+#undef GROUP_CONE
+    free(gouts);
+    free(gn);
+    free(cone);
+    free(owner);
     free(outs);
-    free(in_cone);
     free(stack);
     free(store_at);
     free(store_next);
@@ -597,24 +686,54 @@ static void loop_body(Src *o, Chunk *k, size_t from, size_t to)
 }
 
 /* One kernel for instructions from .. to-1; with loop != 0 the whole pass, `passes` times. */
+/* Blocks of a group-major kernel over W words: tc_cube_gm_warps warps (at most enough for W). */
+static unsigned gm_warps(unsigned W)
+{
+    unsigned wpb = (unsigned)(tc_cube_gm_warps > 0 ? tc_cube_gm_warps : 1);
+    while (wpb > 1 && 32 * wpb > W)
+        wpb /= 2;
+    return wpb;
+}
+
 static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size_t from, size_t to,
-                        int loop)
+                        int loop, int *group_major)
 {
     Chunk k = {p, W, tc_xcalloc(p->ncells + 1, 1), tc_xcalloc(p->ncells + 1, 1)};
     unsigned groups = chunk_groups(p, from, to, loop);
+    int gm = 0;
+    if (tc_cube_map && !loop) {
+        Src body = {0};
+        split_body(&body, &k, from, to, groups, &gm);
+        unsigned wpb = gm_warps(W), nwb = (W + 32 * wpb - 1) / (32 * wpb);
+        emit(o, "extern \"C\" __global__ void __launch_bounds__(%u) tc_cube_%u(u32 *__restrict__ "
+                "mem, u32 *__restrict__ rr, const u32 passes)\n{\n",
+             gm ? 32 * wpb : TC_CUBE_BLOCK * groups, idx);
+        if (gm) {
+            emit(o, "    const u32 group = blockIdx.x / %uu;\n", nwb);
+            emit(o, "    const u32 t = (blockIdx.x %% %uu) * %uu + threadIdx.y * 32u + threadIdx.x;\n",
+                 nwb, 32 * wpb);
+        } else {
+            emit(o, "    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;\n");
+        }
+        emit(o, "    const u32 w = t & (W - 1u);\n");
+        emit(o, "    u32 *const m = mem + w;\n");
+        emit(o, "    u32 r = rr[w];\n");
+        emit(o, "%.*s}\n", (int)body.len, body.s ? body.s : "");
+        free(body.s);
+        free(k.loaded);
+        free(k.written);
+        if (group_major)
+            *group_major = gm;
+        return;
+    }
+    if (group_major)
+        *group_major = 0;
     emit(o, "extern \"C\" __global__ void __launch_bounds__(%u) tc_cube_%u(u32 *__restrict__ mem, "
             "u32 *__restrict__ rr, const u32 passes)\n{\n", TC_CUBE_BLOCK * groups, idx);
     emit(o, "    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;\n");
     emit(o, "    const u32 w = t & (W - 1u);\n");
     emit(o, "    u32 *const m = mem + w;\n");
     emit(o, "    u32 r = rr[w];\n");
-    if (tc_cube_map && !loop) {
-        split_body(o, &k, from, to, groups);
-        emit(o, "}\n");
-        free(k.loaded);
-        free(k.written);
-        return;
-    }
     if (loop) {
         /* every cell the pass touches is loop-carried: load before the loop */
         for (size_t i = from; i < to; i++) {
@@ -653,7 +772,7 @@ char *tc_codegen_cube(const Program *p, const size_t *first, unsigned nk, int bl
     emit(&o, "#define W %uu\n", W);
     emit(&o, "%s", CUBE_PRELUDE);
     for (unsigned k = 0; k < nk; k++)
-        emit_kernel(&o, p, W, k, first[k], first[k + 1], loop);
+        emit_kernel(&o, p, W, k, first[k], first[k + 1], loop, NULL);
     if (len)
         *len = o.len;
     return o.s;
@@ -685,7 +804,8 @@ static void *compile_job(void *arg)
     emit(&o, "#define W %uu\n", c->W);
     emit(&o, "%s", CUBE_PRELUDE);
     for (unsigned k = 0; k < nk; k++)
-        emit_kernel(&o, &c->p, c->W, j->k0 + k, first[k], first[k + 1], loop);
+        emit_kernel(&o, &c->p, c->W, j->k0 + k, first[k], first[k + 1], loop,
+                    &c->gmajor[j->k0 + k]);
     len = o.len;
     char **names = tc_xmalloc(nk * sizeof *names);
     for (unsigned k = 0; k < nk; k++) {
@@ -726,6 +846,7 @@ void cuda_cube_free(CudaCube *c)
     free(c->first);
     free(c->fn);
     free(c->warps);
+    free(c->gmajor);
     tc_program_free(&c->p);
     free(c);
 }
@@ -759,6 +880,7 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
     c->loop = c->nk == 1 && c->dims <= FAR_DIM;
     c->fn = tc_xcalloc(c->nk, sizeof *c->fn);
     c->warps = tc_xcalloc(c->nk, sizeof *c->warps);
+    c->gmajor = tc_xcalloc(c->nk, sizeof *c->gmajor);
     for (unsigned k = 0; k < c->nk; k++)
         c->warps[k] = chunk_groups(p, c->first[k], c->first[k + 1], c->loop);
     size_t words = (size_t)c->W * (p->ncells + 1);
@@ -871,9 +993,15 @@ static int launch_pass(CudaCube *c, cudaStream_t s, unsigned passes)
     for (unsigned k = 0; k < c->nk; k++) {
         uint32_t *mem = c->mem, *rr = c->rr;
         void *args[] = {&mem, &rr, &passes};
-        dim3 b = dim3u(block);
-        b.y = c->warps[k];
-        if (cudaLaunchKernel((const void *)c->fn[k], dim3u(grid), b, args, 0, s) != cudaSuccess)
+        dim3 b = dim3u(block), g = dim3u(grid);
+        if (c->gmajor[k]) {  /* blocks of one group: gm_warps warps of 32 words */
+            unsigned wpb = gm_warps(c->W);
+            b.y = wpb;
+            g.x = ((c->W + 32 * wpb - 1) / (32 * wpb)) * c->warps[k];
+        } else {
+            b.y = c->warps[k];
+        }
+        if (cudaLaunchKernel((const void *)c->fn[k], g, b, args, 0, s) != cudaSuccess)
             return 0;
     }
     return 1;

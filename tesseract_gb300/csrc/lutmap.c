@@ -6,9 +6,12 @@
    LUTs that cover the network.  This file builds the network with constant folding and
    structural hashing, enumerates the 3-feasible cuts of every node bottom up (keeping the best
    few by area flow, the usual priority-cuts method of FPGA mapping), selects a cover from the
-   required outputs down, and lists the chosen LUTs in topological order with their truth tables.
-   A full adder's sum and carry, for example, become one LUT each over (x, y, c), where the
-   19-instruction NAND/STO form needs eight or more 2-input operations. */
+   required outputs down, improves it by exact-area moves (one node at a time, then groups of
+   nodes whose cuts share their leaves), and lists the chosen LUTs in topological order with
+   their truth tables.  A full adder's sum and carry, for example, become one LUT each over
+   (x, y, c), where the 19-instruction NAND/STO form needs eight or more 2-input operations; in
+   an array multiplier that takes moving both at once, since each alone keeps the shared
+   x ^ y node alive. */
 #include <stdlib.h>
 #include <string.h>
 
@@ -341,6 +344,129 @@ static int usable(const TcNet *t, int n, int k)
     return !(c->n == 1 && c->leaf[0] == n);  /* the trivial cut cannot implement n itself */
 }
 
+/* Area recovery: each node in the cover takes the cut that brings the fewest LUTs in. */
+static void exact_area(TcNet *t, int passes)
+{
+    int n = t->n;
+    for (int pass = 0; pass < passes; pass++)
+        for (int j = 0; j < n; j++) {
+            int i = pass & 1 ? n - 1 - j : j;
+            if (!is_gate(t, i) || t->refs[i] == 0)
+                continue;
+            cover_deref(t, chosen(t, i));
+            int b = t->best[i], least = 1 << 30;
+            for (int k = 0; k < t->ncut[i]; k++) {
+                if (!usable(t, i, k))
+                    continue;
+                const Cut *c = &t->cuts[(size_t)i * PRIO + k];
+                int a = cover_ref(t, c);
+                cover_deref(t, c);
+                if (a < least) {
+                    least = a;
+                    b = k;
+                }
+            }
+            t->best[i] = b;
+            cover_ref(t, chosen(t, i));
+        }
+}
+
+/* The cover from scratch: the outputs' chosen cuts and, recursively, their leaves'. */
+static void recount(TcNet *t, const int *outputs, int nout)
+{
+    memset(t->refs, 0, (size_t)t->n * sizeof *t->refs);
+    for (int i = 0; i < nout; i++)
+        if (is_gate(t, outputs[i]) && t->refs[outputs[i]]++ == 0)
+            cover_ref(t, chosen(t, outputs[i]));
+}
+
+static int cut_has(const Cut *c, int node)
+{
+    for (int j = 0; j < c->n; j++)
+        if (c->leaf[j] == node)
+            return 1;
+    return 0;
+}
+
+typedef struct {
+    uint64_t key;  /* the leaf set */
+    int      node, cut;
+} LeafSet;
+
+static int by_leafset(const void *x, const void *y)
+{
+    const LeafSet *a = x, *b = y;
+    return a->key < b->key ? -1 : a->key > b->key ? 1 : a->node - b->node;
+}
+
+/* One sweep of joint moves; returns how many groups moved. */
+static int joint_moves(TcNet *t)
+{
+    int n = t->n, moved = 0;
+    size_t cap = 0, m = 0;
+    LeafSet *ls = NULL;
+    for (int i = 0; i < n; i++) {
+        if (!is_gate(t, i) || t->refs[i] == 0)
+            continue;
+        for (int k = 0; k < t->ncut[i]; k++) {
+            const Cut *c = &t->cuts[(size_t)i * PRIO + k];
+            if (!usable(t, i, k) || c->n < 2 || k == t->best[i])
+                continue;
+            if (m == cap) {
+                cap = cap ? 2 * cap : 1024;
+                ls = tc_xrealloc(ls, cap * sizeof *ls);
+            }
+            uint64_t key = 0;
+            for (int j = 0; j < c->n; j++)
+                key = key * 0x100000001b3ull + (uint64_t)(c->leaf[j] + 1);
+            ls[m].key = key ^ (uint64_t)c->n << 60;
+            ls[m].node = i;
+            ls[m].cut = k;
+            m++;
+        }
+    }
+    qsort(ls, m, sizeof *ls, by_leafset);
+    for (size_t a = 0; a < m;) {
+        size_t b = a + 1;
+        while (b < m && ls[b].key == ls[a].key)
+            b++;
+        if (b - a >= 2) {
+            /* the group's nodes as they are, then all switched */
+            int before = 0, after = 0, ok = 1, old[8], cnt = (int)(b - a < 8 ? b - a : 8);
+            for (int q = 0; q < cnt; q++) {
+                ok &= t->refs[ls[a + q].node] > 0;
+                for (int r = 0; r < cnt; r++)  /* no member a leaf of another's cuts */
+                    ok &= !cut_has(chosen(t, ls[a + q].node), ls[a + r].node) &&
+                          !cut_has(&t->cuts[(size_t)ls[a + q].node * PRIO + ls[a + q].cut],
+                                   ls[a + r].node);
+            }
+            if (ok) {
+                for (int q = 0; q < cnt; q++) {
+                    old[q] = t->best[ls[a + q].node];
+                    before += cover_deref(t, chosen(t, ls[a + q].node));
+                }
+                for (int q = 0; q < cnt; q++) {
+                    t->best[ls[a + q].node] = ls[a + q].cut;
+                    after += cover_ref(t, chosen(t, ls[a + q].node));
+                }
+                if (after >= before) {  /* no gain: back as it was */
+                    for (int q = 0; q < cnt; q++)
+                        cover_deref(t, chosen(t, ls[a + q].node));
+                    for (int q = 0; q < cnt; q++) {
+                        t->best[ls[a + q].node] = old[q];
+                        cover_ref(t, chosen(t, ls[a + q].node));
+                    }
+                } else {
+                    moved++;
+                }
+            }
+        }
+        a = b;
+    }
+    free(ls);
+    return moved;
+}
+
 int tc_net_map(TcNet *t, const int *outputs, int nout, int *order, int *norder)
 {
     int n = t->n;
@@ -412,28 +538,18 @@ int tc_net_map(TcNet *t, const int *outputs, int nout, int *order, int *norder)
     for (int i = 0; i < nout; i++)
         if (is_gate(t, outputs[i]) && t->refs[outputs[i]]++ == 0)
             cover_ref(t, chosen(t, outputs[i]));
-    /* area recovery: each node in the cover takes the cut that brings the fewest LUTs in */
-    for (int pass = 0; pass < 6; pass++)
-        for (int j = 0; j < n; j++) {
-            int i = pass & 1 ? n - 1 - j : j;
-            if (!is_gate(t, i) || t->refs[i] == 0)
-                continue;
-            cover_deref(t, chosen(t, i));
-            int b = t->best[i], least = 1 << 30;
-            for (int k = 0; k < t->ncut[i]; k++) {
-                if (!usable(t, i, k))
-                    continue;
-                const Cut *c = &t->cuts[(size_t)i * PRIO + k];
-                int a = cover_ref(t, c);
-                cover_deref(t, c);
-                if (a < least) {
-                    least = a;
-                    b = k;
-                }
-            }
-            t->best[i] = b;
-            cover_ref(t, chosen(t, i));
-        }
+    exact_area(t, 6);
+    /* joint moves: cover nodes that each have a cut over the same leaves (a full adder's sum
+       and carry over its three inputs) switch to those cuts together when that shrinks the
+       cover, which no single node's move shows; then the single moves again */
+    for (int round = 0; round < 3; round++) {
+        int moved = joint_moves(t);
+        recount(t, outputs, nout);
+        if (!moved)
+            break;
+        exact_area(t, 2);
+    }
+    recount(t, outputs, nout);
     int m = 0;
     for (int i = 0; i < n; i++)
         if (is_gate(t, i) && t->refs[i] > 0) {
