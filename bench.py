@@ -374,10 +374,14 @@ def main():
 
     world, rank, local = dist_env()
     dist = None
+    device = 0
     if world > 1:
         import torch.distributed as dist  # barrier only; the engine itself uses no torch
         dist.init_process_group("gloo")
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if world > 1 else None
+        if "CUDA_VISIBLE_DEVICES" not in os.environ:
+            os.environ["CUDA_VISIBLE_DEVICES"] = str(local)  # this rank sees its GPU as 0
+        elif len(os.environ["CUDA_VISIBLE_DEVICES"].split(",")) > local:
+            device = local  # all GPUs visible: take this rank's
 
     import tesseract_gb300 as T
     from tesseract_gb300 import build
@@ -385,6 +389,9 @@ def main():
         build.build(reference=False)
     if dist:
         dist.barrier()
+    err = T._err()
+    if not T.lib().cuda_engine_init(device, err, len(err)):
+        raise T.EngineError(err.value.decode())
     p = T.Program.gen_mul(16)
     s = T.Spec(p, "p = a * b")
     info = T.device_info()
@@ -401,7 +408,8 @@ def main():
     if dist:
         dist.barrier()
     kernel_s, ops, results = 0.0, 0, []
-    with Clocks(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or 0)) as clk:
+    visible = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")
+    with Clocks(int(visible[min(device, len(visible) - 1)] or 0)) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
             r = T.enum_run(T.EN_VERIFY, p, spec=s, **share)

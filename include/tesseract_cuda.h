@@ -192,6 +192,9 @@ void cuda_free(CudaCode *c);
    the device work. */
 int  cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen);
 void cuda_enum_add_hit(EnumResult *r, uint64_t x);   /* enum_add_hit, src/enum.c:31-46 */
+/* Adds the result of one share (--part) into a total, as merge_raw does (src/work.c:341-371):
+   the host side of running shares on several GPUs or machines.  Needs no GPU. */
+void cuda_enum_merge(EnumResult *into, const EnumResult *part);
 
 /* cuda_enum_run without allocation: the same job, kernel and results, with the workspace (hit
    counter, per-warp hit lists and counts) in a fixed 2.1 MB device array for at most 16,384

@@ -258,6 +258,21 @@ void cuda_enum_add_hit(EnumResult *r, uint64_t x)
     r->hit[i] = x;
 }
 
+/* Adds one share's result into a total, as merge_raw does with --raw lines
+   (src/work.c:341-371): counts add up, the slowest share's seconds, the 16 smallest hits. */
+void cuda_enum_merge(EnumResult *into, const EnumResult *part)
+{
+    into->space = part->space;
+    into->tried += part->tried;
+    into->hits += part->hits;
+    into->ops += part->ops;
+    into->threads += part->threads;
+    if (part->seconds > into->seconds)
+        into->seconds = part->seconds;
+    for (int i = 0; i < part->nhit; i++)
+        cuda_enum_add_hit(into, part->hit[i]);
+}
+
 static int match_names(const Program *a, const uint32_t *la, size_t na, const Program *b,
                        const uint32_t *lb, size_t nb, int *map, const char *what, char *err,
                        size_t errlen)

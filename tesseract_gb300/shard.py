@@ -1,0 +1,54 @@
+"""Enumeration across ranks: the assignment space split by the reference's share rule (chunks of
+64 passes of 512 assignments, chunk c in share c mod parts, src/enum.c:11,215-242), one share per
+rank, and the shares' results merged on the host as merge_raw merges --raw lines
+(src/work.c:341-371, here cuda_enum_merge).  Nothing crosses ranks on the data path: each rank
+enumerates its own chunks; the only exchange is the small result record, gathered once.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import tesseract_gb300 as T
+
+
+def share(rank: int, world: int) -> dict:
+    """The --part arguments of rank's share: part rank of world."""
+    if not 0 <= rank < world:
+        raise ValueError("rank %d of %d" % (rank, world))
+    return dict(part=rank, part_end=rank, parts=world)
+
+
+def _struct(d: dict) -> T.EnumResult:
+    r = T.EnumResult()
+    r.space, r.tried, r.hits, r.ops = d["space"], d["tried"], d["hits"], d["ops"]
+    r.seconds, r.threads = d.get("seconds", 0.0), d.get("threads", 0)
+    r.nhit = len(d["hit"])
+    for i, x in enumerate(d["hit"]):
+        r.hit[i] = x
+    return r
+
+
+def merge(results) -> dict:
+    """The total of several shares' result dicts (cuda_enum_merge)."""
+    L = T.lib()
+    L.cuda_enum_merge.restype = None
+    L.cuda_enum_merge.argtypes = [C.POINTER(T.EnumResult), C.POINTER(T.EnumResult)]
+    total = T.EnumResult()
+    for d in results:
+        part = _struct(d)
+        L.cuda_enum_merge(C.byref(total), C.byref(part))
+    return total.as_dict()
+
+
+def gather_merge(local: dict, group=None) -> dict:
+    """Every rank's share result, gathered over torch.distributed and merged (all ranks get
+    the total)."""
+    import torch.distributed as dist
+    parts = [None] * dist.get_world_size(group)
+    dist.all_gather_object(parts, local, group=group)
+    return merge(parts)
+
+
+def run_share(mode, a, b=None, spec=None, ticks=1, rank=0, world=1) -> dict:
+    """This rank's share on its GPU (cuda_enum_run with --part rank/world)."""
+    return T.enum_run(mode, a, b, spec, ticks, **share(rank, world))
