@@ -46,6 +46,19 @@ void     tc_gen_life_cube(Program *p, int w, int h, int rbits, int cbits, uint32
 void     tc_gen_cube_any(Program *p, int dims);
 void     tc_gen_cube_rank(Program *p, int dims);
 void     tc_gen_cube_sort(Program *p, int dims);
+/* max (.in v0..v7, .out m0..m7: the largest byte everywhere), anf (.in/.out f: the Möbius
+   transform of a truth table, src/cubedemo.c:194-210), walsh (.in f, .out w0..: the
+   Walsh-Hadamard spectrum, dims + 3 bits), ring (.in/.out x: one step of Rule 110 on the
+   machines as a Gray-coded ring, src/cubedemo.c:286-306). */
+void     tc_gen_cube_max(Program *p, int dims);
+void     tc_gen_cube_anf(Program *p, int dims);
+void     tc_gen_cube_walsh(Program *p, int dims);
+void     tc_gen_cube_ring(Program *p, int dims);
+/* polymul (dims 9..11): .in a0.. b0.. zf<d>_0.. zi<d>_0.., .out c0..: c = a b in
+   Z_12289[x]/(x^(2^dims) + 1), one coefficient per machine, by the number-theoretic transform
+   (the reference's demo, src/gen.c:456-669, src/cubedemo.c:253-284); zf and zi are the forward
+   and inverse twiddles of each round times 2^14 mod 12289, as cuda_cube_demo sets them. */
+void     tc_gen_cube_polymul(Program *p, int dims);
 unsigned tc_grid_machine(unsigned row, unsigned col, int cbits);
 void     tc_random_program(Program *p, uint32_t cells, size_t len, uint64_t seed);
 /* Random program with `width` input cells (.in w0.., never written) beside `cells` working cells

@@ -255,8 +255,10 @@ class Program:
 
     @classmethod
     def gen_cube_demo(cls, name: str, dims: int):
-        """The big-cube demo `name` (any, rank, sort) for 2^dims machines."""
-        fn = {"any": "tc_gen_cube_any", "rank": "tc_gen_cube_rank", "sort": "tc_gen_cube_sort"}
+        """The cube demo `name` (any, rank, sort, max, anf, walsh, ring) for 2^dims machines."""
+        fn = {"any": "tc_gen_cube_any", "rank": "tc_gen_cube_rank", "sort": "tc_gen_cube_sort",
+              "max": "tc_gen_cube_max", "anf": "tc_gen_cube_anf", "walsh": "tc_gen_cube_walsh",
+              "ring": "tc_gen_cube_ring", "polymul": "tc_gen_cube_polymul"}
         p = cls()
         f = getattr(lib(), fn[name])
         f.argtypes = [C.POINTER(ProgramStruct), C.c_int]

@@ -213,6 +213,66 @@ static int find_cells(const Program *p, const char *stem, int n, uint32_t *cells
     return 1;
 }
 
+/* polymul's numbers mod q = 12289: x^e */
+static uint64_t pow_q(uint64_t x, uint64_t e)
+{
+    uint64_t r = 1;
+    for (x %= 12289; e; e >>= 1, x = x * x % 12289)
+        if (e & 1)
+            r = r * x % 12289;
+    return r;
+}
+
+/* polymul's inputs: random a and b in 0 .. q-1, and the twiddles of each round in Montgomery
+   form (times R = 2^14): round d pairs machines u, u + 2^d with the zeta psi^brv(2^(dims-1-d) +
+   u >> (d + 1)) of the usual in-place loop, psi a primitive 2N-th root of unity; the way back
+   multiplies the upper machine by 1/zeta.  want gets the product by schoolbook. */
+static void polymul_inputs(const Program *p, int dims, uint32_t *mem, unsigned W, uint64_t *s,
+                           uint64_t *want)
+{
+    const uint64_t q = 12289, R = (1u << 14) % q;
+    unsigned n = 1u << dims;
+    uint64_t g = 2;
+    while (pow_q(g, (q - 1) / 2) == 1 || pow_q(g, (q - 1) / 3) == 1)
+        g++;
+    uint64_t psi = pow_q(g, (q - 1) / (2 * (uint64_t)n));
+    uint32_t a[14], b[14], z[14];
+    find_cells(p, "a", 14, a);
+    find_cells(p, "b", 14, b);
+    uint64_t *x = tc_xmalloc((size_t)n * 8), *y = tc_xmalloc((size_t)n * 8);
+    for (unsigned k = 0; k < n; k++) {
+        vput(mem, W, a, 14, k, x[k] = tc_splitmix64(s) % q);
+        vput(mem, W, b, 14, k, y[k] = tc_splitmix64(s) % q);
+    }
+    for (int d = 0; d < dims; d++)
+        for (int inv = 0; inv < 2; inv++) {
+            char stem[16];
+            snprintf(stem, sizeof stem, "%s%d_", inv ? "zi" : "zf", d);
+            find_cells(p, stem, 14, z);
+            for (unsigned k = 0; k < n; k++) {
+                unsigned idx = (1u << (dims - 1 - d)) + (k >> (d + 1)), rev = 0;
+                for (int i = 0; i < dims; i++)
+                    rev |= ((idx >> i) & 1) << (dims - 1 - i);
+                uint64_t zeta = pow_q(psi, rev), v;
+                if (!inv)
+                    v = zeta * R % q;
+                else
+                    v = (k >> d) & 1 ? pow_q(zeta, q - 2) * R % q : R;
+                vput(mem, W, z, 14, k, v);
+            }
+        }
+    for (unsigned k = 0; k < n; k++)
+        want[k] = 0;
+    for (unsigned i = 0; i < n; i++)  /* x^N = -1 */
+        for (unsigned j = 0; j < n; j++) {
+            uint64_t t = x[i] * y[j] % q;
+            unsigned at = (i + j) % n;
+            want[at] = (want[at] + (i + j < n ? t : q - t)) % q;
+        }
+    free(x);
+    free(y);
+}
+
 int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaDemoResult *r,
                    char *err, size_t errlen)
 {
@@ -233,13 +293,31 @@ int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaD
         snprintf(r->what, sizeof r->what, "sort %u bytes (bitonic, %d rounds)", n,
                  dims * (dims + 1) / 2);
         tc_gen_cube_sort(&p, dims);
+    } else if (!strcmp(name, "max")) {
+        snprintf(r->what, sizeof r->what, "largest of %u bytes", n);
+        tc_gen_cube_max(&p, dims);
+    } else if (!strcmp(name, "anf")) {
+        snprintf(r->what, sizeof r->what, "truth table of %d inputs -> normal form (Mobius)", dims);
+        tc_gen_cube_anf(&p, dims);
+    } else if (!strcmp(name, "walsh")) {
+        snprintf(r->what, sizeof r->what, "Walsh-Hadamard spectrum of f, %d-bit results", dims + 3);
+        tc_gen_cube_walsh(&p, dims);
+    } else if (!strcmp(name, "ring")) {
+        snprintf(r->what, sizeof r->what, "Rule 110 on a ring of %u cells, one step", n);
+        tc_gen_cube_ring(&p, dims);
+    } else if (!strcmp(name, "polymul")) {
+        if (dims > 11)
+            return tc_fail(err, errlen, "polymul needs a 2N-th root of unity mod 12289: dims 9..11");
+        snprintf(r->what, sizeof r->what, "c = a * b in Z_12289[x]/(x^%u + 1), by NTT", n);
+        tc_gen_cube_polymul(&p, dims);
     } else if (!strcmp(name, "life")) {
         snprintf(r->what, sizeof r->what, "Life: one %d x %d board, one generation", T << rbits,
                  T << cbits);
         board = tc_xmalloc((size_t)T * T * sizeof *board);
         tc_gen_life_cube(&p, T, T, rbits, cbits, board);
     } else {
-        return tc_fail(err, errlen, "unknown demo '%s' (any, rank, sort, life)", name);
+        return tc_fail(err, errlen, "unknown demo '%s' (any, rank, max, sort, anf, walsh, ring, "
+                       "polymul, life)", name);
     }
     r->instr = p.len;
     CudaCube *c;
@@ -282,6 +360,24 @@ int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaD
             for (unsigned k = 0; k < n; k++)
                 vput(mem, W, x, 8, k, want[k] = tc_splitmix64(&s) & 255);
             qsort(want, n, sizeof *want, cmp_u64);
+        } else if (!strcmp(name, "max")) {
+            find_cells(&p, "v", 8, x);
+            count = 0;  /* the largest */
+            for (unsigned k = 0; k < n; k++) {
+                uint64_t v = tc_splitmix64(&s) & 255;
+                vput(mem, W, x, 8, k, v);
+                count = v > count ? v : count;
+            }
+        } else if (!strcmp(name, "anf") || !strcmp(name, "walsh")) {
+            tc_program_find_cell(&p, "f", &x[0]);
+            for (unsigned k = 0; k < n; k++)
+                mset(mem, W, x[0], k, (unsigned)(want[k] = tc_splitmix64(&s) & 1));
+        } else if (!strcmp(name, "ring")) {
+            tc_program_find_cell(&p, "x", &x[0]);
+            for (unsigned k = 0; k < n; k++)
+                mset(mem, W, x[0], k, (unsigned)(want[k] = tc_splitmix64(&s) & 1));
+        } else if (!strcmp(name, "polymul")) {
+            polymul_inputs(&p, dims, mem, W, &s, want);
         } else {
             memset(big, 0, (size_t)w64 * gh * 8);
             for (int R = 0; R < gh; R++)
@@ -312,6 +408,47 @@ int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaD
         } else if (!strcmp(name, "sort")) {
             for (unsigned k = 0; k < n && ok; k++)
                 ok = vget(mem, W, x, 8, k) == want[k];
+        } else if (!strcmp(name, "max")) {
+            find_cells(&p, "m", 8, pv);
+            for (unsigned k = 0; k < n && ok; k++)
+                ok = vget(mem, W, pv, 8, k) == count;
+        } else if (!strcmp(name, "anf")) {
+            for (unsigned d = 1; d < n; d <<= 1)  /* the Mobius transform in plain C */
+                for (unsigned k = 0; k < n; k++)
+                    if (k & d)
+                        want[k] ^= want[k ^ d];
+            for (unsigned k = 0; k < n && ok; k++)
+                ok = mget(mem, W, x[0], k) == want[k];
+        } else if (!strcmp(name, "walsh")) {
+            /* the spectrum in plain C: the fast transform on integers */
+            int64_t *a = tc_xmalloc((size_t)n * sizeof *a);
+            for (unsigned k = 0; k < n; k++)
+                a[k] = want[k] ? -1 : 1;
+            for (unsigned d = 1; d < n; d <<= 1)
+                for (unsigned k = 0; k < n; k++)
+                    if (!(k & d)) {
+                        int64_t u = a[k], v = a[k | d];
+                        a[k] = u + v;
+                        a[k | d] = u - v;
+                    }
+            find_cells(&p, "w", dims + 3, pv);
+            for (unsigned k = 0; k < n && ok; k++)
+                ok = vget(mem, W, pv, dims + 3, k) == ((uint64_t)a[k] & ((1ull << (dims + 3)) - 1));
+            free(a);
+        } else if (!strcmp(name, "polymul")) {
+            find_cells(&p, "c", 14, pv);
+            for (unsigned k = 0; k < n && ok; k++)
+                ok = vget(mem, W, pv, 14, k) == want[k];
+        } else if (!strcmp(name, "ring")) {
+            uint64_t *nx = tc_xmalloc((size_t)n * sizeof *nx);
+            for (unsigned i = 0; i < n; i++) {  /* Rule 110, position i at machine gray(i) */
+                unsigned l = tc_grid_machine(0, (i + n - 1) % n, dims),
+                         c = tc_grid_machine(0, i, dims), rt = tc_grid_machine(0, (i + 1) % n, dims);
+                nx[c] = (110u >> ((want[l] << 2) | (want[c] << 1) | want[rt])) & 1;
+            }
+            for (unsigned k = 0; k < n && ok; k++)
+                ok = mget(mem, W, x[0], k) == nx[k];
+            free(nx);
         } else {
             for (int R = 0; R < gh && ok; R++)
                 for (int C = 0; C < gw && ok; C++) {

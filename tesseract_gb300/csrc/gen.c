@@ -537,7 +537,7 @@ unsigned tc_grid_machine(unsigned row, unsigned col, int cbits)
 static void axis_masks(Bld *b, int lo, int k, uint32_t *next, uint32_t *prev, const char *tag)
 {
     char name[32];
-    uint32_t id[CUBE_DIMS], v[4];
+    uint32_t id[CUBE_MAX_DIMS], v[4];
     for (int j = 0; j < k; j++) {
         id[j] = bcellf(b, "ID%d", lo + j, 0);
         snprintf(name, sizeof name, "%s_n%d", tag, j);
@@ -575,7 +575,7 @@ static void axis_masks(Bld *b, int lo, int k, uint32_t *next, uint32_t *prev, co
 static uint32_t axis_gather(Bld *b, const char *name, uint32_t src, int lo, int k,
                             const uint32_t *mask)
 {
-    uint32_t t[CUBE_DIMS];
+    uint32_t t[CUBE_MAX_DIMS];
     uint32_t out = bcell(b, name);
     char lname[48];
     for (int j = 0; j < k; j++) {
@@ -593,7 +593,7 @@ void tc_gen_life_cube(Program *p, int w, int h, int rbits, int cbits, uint32_t *
     Bld *b = bnew();
     int W = w + 2;
     uint32_t *halo = board_and_halo(b, w, h, board);
-    uint32_t right[CUBE_DIMS], left[CUBE_DIMS], down[CUBE_DIMS], up[CUBE_DIMS];
+    uint32_t right[CUBE_MAX_DIMS], left[CUBE_MAX_DIMS], down[CUBE_MAX_DIMS], up[CUBE_MAX_DIMS];
     char name[32];
     if (cbits)
         axis_masks(b, 0, cbits, right, left, "gc");
@@ -742,6 +742,300 @@ void tc_gen_cube_sort(Program *p, int dims)
                 gate2(b, G_XOR, v[i], v[i], dif);
             }
         }
+    bfinish(b, p);
+}
+
+/* m = the largest byte v (v0..v7) over all machines: m = v, then m = max(m, m across d) for
+   every dimension. */
+void tc_gen_cube_max(Program *p, int dims)
+{
+    Bld *b = bnew();
+    uint32_t v[8], m[8], o[8], nm[8];
+    for (int i = 0; i < 8; i++)
+        binput(b, v[i] = bcell(b, bname(b, "v%d", i)));
+    for (int i = 0; i < 8; i++)
+        boutput(b, m[i] = bcell(b, bname(b, "m%d", i)));
+    for (int i = 0; i < 8; i++) {
+        o[i] = bcell(b, bname(b, "o%d", i));
+        nm[i] = bcell(b, bname(b, "nm%d", i));
+        gate1(b, G_BUF, m[i], v[i]);
+    }
+    uint32_t carry = bcell(b, "cy"), sum = bcell(b, "sm"), dif = bcell(b, "df");
+    for (int d = 0; d < dims; d++) {
+        for (int i = 0; i < 8; i++) {
+            char ln[32];
+            snprintf(ln, sizeof ln, "lm%d_%d", i, d);
+            gate1(b, G_BUF, o[i], blink(b, ln, m[i], d));
+        }
+        /* carry out of o + ~m + 1 is (o >= m): take o then */
+        gate1(b, G_BUF, carry, CELL_ONE);
+        for (int i = 0; i < 8; i++) {
+            gate1(b, G_NOT, nm[i], m[i]);
+            full_add(b, sum, carry, o[i], nm[i], carry);
+        }
+        for (int i = 0; i < 8; i++) {
+            gate2(b, G_XOR, dif, o[i], m[i]);
+            gate2(b, G_AND, dif, dif, carry);
+            gate2(b, G_XOR, m[i], m[i], dif);
+        }
+    }
+    bfinish(b, p);
+}
+
+/* f (one bit per machine, machine k holding f(k)) becomes its algebraic normal form, the
+   Möbius transform over GF(2): across each dimension d the machines with bit d set XOR in f of
+   the machine below. */
+void tc_gen_cube_anf(Program *p, int dims)
+{
+    Bld *b = bnew();
+    uint32_t f = bcell(b, "f"), t = bcell(b, "mt");
+    binput(b, f);
+    boutput(b, f);
+    for (int d = 0; d < dims; d++) {
+        gate2(b, G_AND, t, blink(b, bname(b, "lf%d", d), f, d), bcell(b, bname(b, "ID%d", d)));
+        gate2(b, G_XOR, f, f, t);
+    }
+    bfinish(b, p);
+}
+
+/* w = the Walsh-Hadamard spectrum of f: w(k) = sum over j of (-1)^(f(j) + j.k), dims + 3 bits in
+   two's complement (bit 0 first).  Start from 1 - 2 f(k), then across each dimension the
+   machine below takes a + a', the one above a' - a (its value subtracted from the one below). */
+void tc_gen_cube_walsh(Program *p, int dims)
+{
+    Bld *b = bnew();
+    int n = dims + 3;
+    uint32_t f = bcell(b, "f"), w[CUBE_MAX_DIMS + 3], o[CUBE_MAX_DIMS + 3], y[CUBE_MAX_DIMS + 3];
+    binput(b, f);
+    for (int i = 0; i < n; i++)
+        boutput(b, w[i] = bcell(b, bname(b, "w%d", i)));
+    for (int i = 0; i < n; i++) {
+        o[i] = bcell(b, bname(b, "o%d", i));
+        y[i] = bcell(b, bname(b, "y%d", i));
+    }
+    /* 1 - 2f: f = 0 gives 1 (bit 0 set), f = 1 gives -1 (all bits set) */
+    gate1(b, G_BUF, w[0], CELL_ONE);
+    for (int i = 1; i < n; i++)
+        gate1(b, G_BUF, w[i], f);
+    uint32_t carry = bcell(b, "cy");
+    for (int d = 0; d < dims; d++) {
+        uint32_t id = bcell(b, bname(b, "ID%d", d));
+        for (int i = 0; i < n; i++) {
+            char ln[32];
+            snprintf(ln, sizeof ln, "lw%d_%d", i, d);
+            gate1(b, G_BUF, o[i], blink(b, ln, w[i], d));
+        }
+        /* below (id 0): w + o; above (id 1): o - w = o + ~w + 1 */
+        for (int i = 0; i < n; i++)
+            gate2(b, G_XOR, y[i], w[i], id);
+        gate1(b, G_BUF, carry, id);
+        for (int i = 0; i < n; i++)
+            full_add(b, w[i], carry, o[i], y[i], carry);
+    }
+    bfinish(b, p);
+}
+
+/* Rule 110 on the machines as a ring, position i being machine gray(i): one step,
+   x' = (x | right) & ~(left & x & right), the neighbours gathered over the Gray-coded axis as
+   the Life board's edges are. */
+void tc_gen_cube_ring(Program *p, int dims)
+{
+    Bld *b = bnew();
+    uint32_t x = bcell(b, "x"), next[CUBE_MAX_DIMS], prev[CUBE_MAX_DIMS];
+    binput(b, x);
+    boutput(b, x);
+    axis_masks(b, 0, dims, next, prev, "rg");
+    uint32_t left = axis_gather(b, "left", x, 0, dims, prev);
+    uint32_t right = axis_gather(b, "right", x, 0, dims, next);
+    uint32_t all3 = bcell(b, "all3"), in3[3] = {x, left, right}, t = bcell(b, "or");
+    gate(b, G_AND, all3, in3, 3);
+    gate2(b, G_OR, t, x, right);
+    gate1(b, G_NOT, all3, all3);
+    gate2(b, G_AND, x, t, all3);
+    bfinish(b, p);
+}
+
+/* ---- polynomial product mod x^N + 1 over Z_q by the number-theoretic transform ---------------
+
+   The cube's 2^dims machines hold the coefficients (dims 9..11: q - 1 = 3 * 2^12 allows a
+   2N-th root of unity for N up to 2^11).  Numbers mod q take 14 bits.  Products use Montgomery
+   reduction with R = 2^14: montmul(x, y) = x y / R mod q, so twiddles given times R come out
+   as plain products.  The algorithm is the textbook negacyclic NTT: Cooley-Tukey butterflies
+   forward (dimension dims-1 down to 0), the product point by point, Gentleman-Sande butterflies
+   back (dimension 0 up), and one last product by R^2 / N. */
+
+enum { NQ = 12289, NQB = 14 };
+
+/* out = x + y + cin over n bits (cin a cell); out may be x or y */
+static void add_bits(Bld *b, const uint32_t *out, const uint32_t *x, const uint32_t *y,
+                     uint32_t cin, int n, uint32_t carry)
+{
+    gate1(b, G_BUF, carry, cin);
+    for (int i = 0; i < n; i++)
+        full_add(b, out[i], carry, x[i], y[i], carry);
+}
+
+/* out = sel ? x1 : x0 over n bits; out may be x0 or x1 */
+static void mux_bits(Bld *b, const uint32_t *out, uint32_t sel, const uint32_t *x1,
+                     const uint32_t *x0, int n, uint32_t t)
+{
+    for (int i = 0; i < n; i++) {
+        gate2(b, G_XOR, t, x0[i], x1[i]);
+        gate2(b, G_AND, t, t, sel);
+        gate2(b, G_XOR, out[i], x0[i], t);
+    }
+}
+
+static void const_bits(uint32_t *out, uint64_t v, int n)
+{
+    for (int i = 0; i < n; i++)
+        out[i] = (v >> i) & 1 ? CELL_ONE : CELL_ZERO;
+}
+
+/* u = v mod q for v < 2q on 15 bits, into r (14 bits): v - q when it does not borrow */
+static void reduce_q(Bld *b, const uint32_t *r, const uint32_t *v, uint32_t carry)
+{
+    uint32_t k[15], d[15], mt = bcell(b, "nq_t");
+    for (int i = 0; i < 15; i++)
+        d[i] = bcell(b, bname(b, "nq_d%d", i));
+    const_bits(k, 32768 - NQ, 15);
+    add_bits(b, d, v, k, CELL_ZERO, 15, carry);  /* carry out: v >= q */
+    mux_bits(b, r, carry, d, v, NQB, mt);
+}
+
+/* r = x y / R mod q (x, y, r in 0 .. q-1; r may be x or y) */
+static void montmul(Bld *b, const uint32_t *r, const uint32_t *x, const uint32_t *y)
+{
+    uint32_t t[30], sm[NQB], m[NQB], ns[NQB], z[NQB], sh[30], u[15];
+    uint32_t carry = bcell(b, "mm_c"), k = bcell(b, "mm_k");
+    for (int i = 0; i < 30; i++)
+        t[i] = bcell(b, bname(b, "mm_t%d", i));
+    for (int i = 0; i < NQB; i++) {
+        sm[i] = bcell(b, bname(b, "mm_s%d", i));
+        m[i] = bcell(b, bname(b, "mm_m%d", i));
+        ns[i] = bcell(b, bname(b, "mm_n%d", i));
+    }
+    multiply(b, t, x, y, NQB);  /* t = x y < q^2 < 2^28 */
+    gate1(b, G_BUF, t[28], CELL_ZERO);
+    gate1(b, G_BUF, t[29], CELL_ZERO);
+    /* m = -t / q mod R: 1/q = 2^12 + 1 mod 2^14, so m = -(t + (t << 12)) mod 2^14 */
+    for (int i = 0; i < 12; i++)
+        gate1(b, G_BUF, sm[i], t[i]);
+    gate2(b, G_XOR, sm[12], t[12], t[0]);
+    gate2(b, G_AND, k, t[12], t[0]);
+    gate2(b, G_XOR, sm[13], t[13], t[1]);
+    gate2(b, G_XOR, sm[13], sm[13], k);
+    for (int i = 0; i < NQB; i++)
+        gate1(b, G_NOT, ns[i], sm[i]);
+    const_bits(z, 0, NQB);
+    add_bits(b, m, ns, z, CELL_ONE, NQB, carry);
+    /* t += m q = m + (m << 12) + (m << 13); t is then a multiple of R */
+    for (int sft = 0; sft <= 13; sft += sft == 0 ? 12 : 1) {
+        for (int i = 0; i < 30; i++)
+            sh[i] = i >= sft && i < sft + NQB ? m[i - sft] : CELL_ZERO;
+        add_bits(b, t, t, sh, CELL_ZERO, 30, carry);
+    }
+    for (int i = 0; i < 15; i++)
+        u[i] = t[NQB + i];  /* (t + m q) / R < 2q */
+    reduce_q(b, r, u, carry);
+}
+
+/* out = sel ? x - y : x + y, mod q (all in 0 .. q-1); out may be x or y */
+static void addsub_q(Bld *b, const uint32_t *out, uint32_t sel, const uint32_t *x,
+                     const uint32_t *y)
+{
+    uint32_t q[15], ny[15], neg[15], y2[15], x15[15], s[15], carry = bcell(b, "as_c"),
+             mt = bcell(b, "as_t");
+    for (int i = 0; i < 15; i++) {
+        ny[i] = bcell(b, bname(b, "as_n%d", i));
+        neg[i] = bcell(b, bname(b, "as_g%d", i));
+        y2[i] = bcell(b, bname(b, "as_y%d", i));
+        s[i] = bcell(b, bname(b, "as_s%d", i));
+        x15[i] = i < NQB ? x[i] : CELL_ZERO;
+    }
+    const_bits(q, NQ, 15);
+    for (int i = 0; i < 15; i++)
+        gate1(b, G_NOT, ny[i], i < NQB ? y[i] : CELL_ZERO);
+    add_bits(b, neg, q, ny, CELL_ONE, 15, carry);  /* q - y, in 1 .. q */
+    for (int i = 0; i < 15; i++)
+        gate1(b, G_BUF, y2[i], i < NQB ? y[i] : CELL_ZERO);
+    mux_bits(b, y2, sel, neg, y2, 15, mt);
+    add_bits(b, s, x15, y2, CELL_ZERO, 15, carry);  /* below 2q */
+    reduce_q(b, out, s, carry);
+}
+
+/* c = a b mod (x^N + 1, q), N = 2^dims; inputs a, b, and per dimension d the twiddles zf<d>_,
+   zi<d>_ (14 bits each, times R mod q) that cuda_cube_demo's polymul computes */
+void tc_gen_cube_polymul(Program *p, int dims)
+{
+    Bld *b = bnew();
+    uint32_t a[NQB], bv[NQB], c[NQB], wa[NQB], wb[NQB], f[NQB], x[NQB], y[NQB], t[NQB];
+    uint32_t zf[CUBE_MAX_DIMS][NQB], zi[CUBE_MAX_DIMS][NQB], la[NQB], lt[NQB];
+    for (int i = 0; i < NQB; i++)
+        binput(b, a[i] = bcell(b, bname(b, "a%d", i)));
+    for (int i = 0; i < NQB; i++)
+        binput(b, bv[i] = bcell(b, bname(b, "b%d", i)));
+    char name[48];
+    for (int d = 0; d < dims; d++)
+        for (int i = 0; i < NQB; i++) {
+            snprintf(name, sizeof name, "zf%d_%d", d, i);
+            binput(b, zf[d][i] = bcell(b, name));
+        }
+    for (int d = 0; d < dims; d++)
+        for (int i = 0; i < NQB; i++) {
+            snprintf(name, sizeof name, "zi%d_%d", d, i);
+            binput(b, zi[d][i] = bcell(b, name));
+        }
+    for (int i = 0; i < NQB; i++) {
+        c[i] = bcell(b, bname(b, "c%d", i));
+        wa[i] = bcell(b, bname(b, "wa%d", i));
+        wb[i] = bcell(b, bname(b, "wb%d", i));
+        x[i] = bcell(b, bname(b, "nx%d", i));
+        y[i] = bcell(b, bname(b, "ny%d", i));
+        t[i] = bcell(b, bname(b, "nt%d", i));
+        gate1(b, G_BUF, wa[i], a[i]);
+        gate1(b, G_BUF, wb[i], bv[i]);
+    }
+    uint32_t mt = bcell(b, "nm_t");
+    for (int pass = 0; pass < 2; pass++) {  /* forward transforms of a and of b */
+        uint32_t *w = pass ? wb : wa;
+        for (int d = dims - 1; d >= 0; d--) {
+            uint32_t id = bcell(b, bname(b, "ID%d", d));
+            montmul(b, t, w, zf[d]);  /* z times this machine's value: used above */
+            for (int i = 0; i < NQB; i++) {
+                snprintf(name, sizeof name, "f%c_a%d_%d", pass ? 'b' : 'a', d, i);
+                la[i] = blink(b, name, w[i], d);
+                snprintf(name, sizeof name, "f%c_t%d_%d", pass ? 'b' : 'a', d, i);
+                lt[i] = blink(b, name, t[i], d);
+            }
+            mux_bits(b, x, id, la, w, NQB, mt);  /* x = a_u */
+            mux_bits(b, y, id, t, lt, NQB, mt);  /* y = z a_v */
+            addsub_q(b, w, id, x, y);
+        }
+    }
+    montmul(b, wa, wa, wb);  /* point by point */
+    for (int d = 0; d < dims; d++) {  /* back */
+        uint32_t id = bcell(b, bname(b, "ID%d", d));
+        for (int i = 0; i < NQB; i++) {
+            snprintf(name, sizeof name, "ia_a%d_%d", d, i);
+            la[i] = blink(b, name, wa[i], d);
+        }
+        mux_bits(b, x, id, la, wa, NQB, mt);  /* x = a_u */
+        mux_bits(b, y, id, wa, la, NQB, mt);  /* y = a_v */
+        addsub_q(b, wa, id, x, y);
+        montmul(b, wa, wa, zi[d]);
+    }
+    /* R^2 / N mod q undoes the two 1/R of the point products and the N of the way back */
+    uint64_t r2 = (1ull << NQB) % NQ;
+    r2 = r2 * r2 % NQ;
+    uint64_t ninv = 1, base = (uint64_t)(1u << dims) % NQ;
+    for (uint64_t e = NQ - 2; e; e >>= 1, base = base * base % NQ)
+        if (e & 1)
+            ninv = ninv * base % NQ;
+    const_bits(f, r2 * ninv % NQ, NQB);
+    montmul(b, c, wa, f);
+    for (int i = 0; i < NQB; i++)
+        boutput(b, c[i]);
     bfinish(b, p);
 }
 

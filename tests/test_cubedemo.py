@@ -78,3 +78,104 @@ def test_sizes():
         s = T.Program.gen_cube_demo("sort", d)
         assert s.dims() == d
         assert len(s) > d * (d + 1) // 2 * 200
+
+
+@pytest.mark.parametrize("dims,seed", [(9, 5), (10, 6)])
+def test_max(dims, seed):
+    p = T.Program.gen_cube_demo("max", dims)
+    rnd = random.Random(seed)
+    n = 1 << dims
+    vs = [rnd.randrange(256) for _ in range(n)]
+    v, m = cells(p, "v", 8), cells(p, "m", 8)
+
+    def setup(c):
+        for k in range(n):
+            for b in range(8):
+                c.set(k, v[b], (vs[k] >> b) & 1)
+
+    cube = run(p, dims, setup)
+    assert all(sum(cube.get(k, m[b]) << b for b in range(8)) == max(vs) for k in range(n))
+
+
+def mobius(a):
+    a = list(a)
+    d = 1
+    while d < len(a):
+        for k in range(len(a)):
+            if k & d:
+                a[k] ^= a[k ^ d]
+        d <<= 1
+    return a
+
+
+@pytest.mark.parametrize("dims,seed", [(9, 7), (10, 8)])
+def test_anf_and_walsh(dims, seed):
+    rnd = random.Random(seed)
+    n = 1 << dims
+    fs = [rnd.randrange(2) for _ in range(n)]
+    p = T.Program.gen_cube_demo("anf", dims)
+    f = cell(p, "f")
+    cube = run(p, dims, lambda c: [c.set(k, f, fs[k]) for k in range(n)])
+    assert [cube.get(k, f) for k in range(n)] == mobius(fs)
+    p = T.Program.gen_cube_demo("walsh", dims)
+    f, w = cell(p, "f"), cells(p, "w", dims + 3)
+    cube = run(p, dims, lambda c: [c.set(k, f, fs[k]) for k in range(n)])
+    mask = (1 << (dims + 3)) - 1
+    for k in (0, 1, 5, n // 3, n - 1):
+        want = sum((-1) ** (fs[j] ^ (bin(j & k).count("1") & 1)) for j in range(n))
+        assert sum(cube.get(k, w[b]) << b for b in range(dims + 3)) == want & mask
+
+
+@pytest.mark.parametrize("dims,seed", [(9, 9), (11, 10)])
+def test_ring(dims, seed):
+    p = T.Program.gen_cube_demo("ring", dims)
+    rnd = random.Random(seed)
+    n = 1 << dims
+    xs = [rnd.randrange(2) for _ in range(n)]
+    x = cell(p, "x")
+    cube = run(p, dims, lambda c: [c.set(k, x, xs[k]) for k in range(n)])
+    gray = lambda i: i ^ (i >> 1)
+    for i in range(n):
+        l, c, r = gray((i - 1) % n), gray(i), gray((i + 1) % n)
+        assert cube.get(c, x) == (110 >> ((xs[l] << 2) | (xs[c] << 1) | xs[r])) & 1
+
+
+def test_polymul_ntt():
+    """c = a b in Z_12289[x]/(x^512 + 1) by the NTT program on the reference machine's cube,
+    its twiddles computed here from the textbook definition, against the schoolbook product."""
+    dims, q, R = 9, 12289, (1 << 14) % 12289
+    n = 1 << dims
+    p = T.Program.gen_cube_demo("polymul", dims)
+    g = 2
+    while pow(g, (q - 1) // 2, q) == 1 or pow(g, (q - 1) // 3, q) == 1:
+        g += 1
+    psi = pow(g, (q - 1) // (2 * n), q)
+    rnd = random.Random(11)
+    x = [rnd.randrange(q) for _ in range(n)]
+    y = [rnd.randrange(q) for _ in range(n)]
+    a, b, c = cells(p, "a", 14), cells(p, "b", 14), cells(p, "c", 14)
+    zf = [cells(p, "zf%d_" % d, 14) for d in range(dims)]
+    zi = [cells(p, "zi%d_" % d, 14) for d in range(dims)]
+
+    def brv(i):
+        return int(format(i, "0%db" % dims)[::-1], 2)
+
+    def setup(cube):
+        for k in range(n):
+            vals = [(a, x[k]), (b, y[k])]
+            for d in range(dims):
+                zeta = pow(psi, brv((1 << (dims - 1 - d)) + (k >> (d + 1))), q)
+                vals.append((zf[d], zeta * R % q))
+                vals.append((zi[d], pow(zeta, q - 2, q) * R % q if (k >> d) & 1 else R))
+            for cs, v in vals:
+                for i, cl in enumerate(cs):
+                    cube.set(k, cl, (v >> i) & 1)
+
+    cube = run(p, dims, setup)
+    want = [0] * n
+    for i in range(n):
+        for j in range(n):
+            t = x[i] * y[j] % q
+            want[(i + j) % n] = (want[(i + j) % n] + (t if i + j < n else q - t)) % q
+    got = [sum(cube.get(k, cl) << i for i, cl in enumerate(c)) for k in range(n)]
+    assert got == want

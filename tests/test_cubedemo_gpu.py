@@ -12,12 +12,19 @@ import tesseract_gb300 as T
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", ["any", "rank", "sort", "life"])
+@pytest.mark.parametrize("name", ["any", "rank", "max", "sort", "anf", "walsh", "ring", "life"])
 @pytest.mark.parametrize("dims", [9, 11, 16])
 def test_demo_checks(name, dims):
     r = T.cube_demo(name, dims, checks=3, seconds=0.05)
     assert r["ok"], r
     assert r["passes_per_second"] > 0
+
+
+@pytest.mark.parametrize("dims", [9, 11])
+def test_polymul_demo(dims):
+    """The NTT product mod x^N + 1 over Z_12289 against the schoolbook product."""
+    r = T.cube_demo("polymul", dims, checks=2, seconds=0.05)
+    assert r["ok"], r
 
 
 @pytest.mark.parametrize("dims", [12, 14])
@@ -46,7 +53,8 @@ def test_sort_through_the_cube_api(dims):
 
 
 @pytest.mark.parametrize("name,dims", [("any", 10), ("rank", 9), ("rank", 11), ("sort", 9),
-                                       ("sort", 10)])
+                                       ("sort", 10), ("max", 11), ("anf", 12), ("walsh", 10),
+                                       ("ring", 11)])
 def test_check_demo_programs(name, dims):
     p = T.Program.gen_cube_demo(name, dims)
     r = T.check(p, seed=dims, ticks=2)
