@@ -42,6 +42,16 @@ WORKLOAD = ("verify gen mul --bits 16 (6040 NAND/STO instructions, 72 cells) ove
 VERIFY_DRAM_BYTES = 27136  # dram__bytes_read.sum + dram__bytes_write.sum, one tc_enum launch
 
 
+def measured_peaks() -> dict:
+    """MEASURED_PEAKS.json beside this file, when the run has one."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
 def dist_env():
     return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), \
         int(os.environ.get("LOCAL_RANK", "0"))
@@ -228,6 +238,20 @@ def bench_life(args):
                         "segments": L.cube.segments, "kernels_per_pass": L.cube.kernels},
             "setup_s_incl_nvrtc": setup_s,
             "cpu_word_parallel_life_s": cpu_s, "cpu_threads": os.cpu_count()}
+    # the exchange between machines: 1,056 link reads per machine per generation (4 gathers
+    # of the tile edges), one bit each, 476 of them across 512-machine groups
+    exchange = 65536 * 1056 / 8
+    peaks = measured_peaks()
+    gbs = exchange * args.gens / (ms / 1e3) / 1e9
+    line["roofline"] = {"bound": "instruction fetch and latency (2,048 words of state; the "
+                                 "27.2 MB state stays in L2)",
+                        "exchange_bytes_per_gen": exchange, "achieved": gbs,
+                        "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                        "frac": gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None,
+                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth); the "
+                                       "exchange is served from L2, not HBM",
+                        "lane_ops_per_s": args.gens * len(n) * 65536 / (ms / 1e3),
+                        "traffic": None}
     c = clk.summary()
     if c:
         line["clocks"] = c
@@ -273,6 +297,13 @@ def bench_batch(args):
             "plain_jobs_per_s_cached": len(sample) / plain_warm,
             "speedup_vs_plain_cached": (len(jobs) / wall) / (len(sample) / plain_warm),
             "sample_identical_to_plain": same}
+    peak = T.lop3_peak() * 32
+    line["roofline"] = {"bound": "interpreter dispatch and shared-memory latency (LUT ops "
+                                  "interpreted from shared-memory slots)",
+                        "achieved": ops / (ms / 1e3), "peak": peak, "unit": "lane-op/s",
+                        "frac": ops / (ms / 1e3) / peak,
+                        "peak_source": "measured: cuda_lop3_peak (32-bit LOP3/s x 32 lanes)",
+                        "traffic": None}
     c = clk.summary()
     if c:
         line["clocks"] = c

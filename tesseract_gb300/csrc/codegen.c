@@ -279,10 +279,17 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
     const Program *a = g->a;
     size_t n = a->ninputs;
     emit(o, "TC_DEV u32 tc_word(const u64 word)\n{\n");
+    /* input k is bit j = n-1-k of x = 32 word + lane: a lane pattern for j < 5, else bit j - 5
+       of the word spread over all 32 lanes (a shift up to the sign bit and an arithmetic shift
+       down: two instructions; words fit 32 bits up to 37 inputs) */
+    if (n > 5 && n <= 37)
+        emit(o, "    const u32 wlo = (u32)word;\n");
     for (size_t k = 0; k < n; k++) {
         int j = (int)(n - 1 - k);
         if (j < 5)
             emit(o, "    const u32 in%zu = TC_PAT%d;\n", k, j);
+        else if (n <= 37)
+            emit(o, "    const u32 in%zu = (u32)((int)(wlo << %d) >> 31);\n", k, 31 - (j - 5));
         else
             emit(o, "    const u32 in%zu = 0u - (u32)((word >> %d) & 1ull);\n", k, j - 5);
     }
@@ -388,7 +395,7 @@ static const char *KERNEL =
     "    for (u64 s = s0; s < s1; s += 32) {\n"
     "        const u64 j = s >> 10;\n"
     "        const u64 chunk = a.nsel == a.parts ? j : (j / a.nsel) * a.parts + a.part + j % a.nsel;\n"
-    "        const u64 word = (chunk << 10) | ((s + lane) & 1023u);\n"
+    "        const u64 word = (chunk << 10) | (s & 992u) | lane;  /* s is a multiple of 32 */\n"
     "        const u64 x0 = word << 5;\n"
     "        u32 valid = 0u;\n"
     "        if (s + lane < s1 && x0 < a.space)\n"
