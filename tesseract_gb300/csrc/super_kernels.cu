@@ -1,7 +1,7 @@
 // The superoptimizer on the GPU: iterative deepening over the budget.  For each budget the top of
 // the search tree is expanded breadth-first on the device, one kernel per level, until the level
-// holds enough states to keep every thread busy; then every GPU thread runs an explicit-stack
-// depth-first search of frontier subtrees taken from a work queue.  The search model and its
+// holds enough states to keep every warp busy; then every warp runs an explicit-stack depth-first
+// search of frontier subtrees taken from a work queue.  The search model and its
 // pruning are in super_search.cuh; the first thread to reach the goal records its state and
 // raises a flag the others poll, as the reference's threads share one stop flag
 // (src/super.c:770-896).
@@ -11,10 +11,9 @@
 
 #include "engine.h"
 #include "super_search.cuh"
+#include "super_warp.cuh"
 
-#define DEV_LEVELS 44      // deepest level a device search reaches (budgets up to 44)
-#define POLL 1024          // nodes between looks at the stop flag
-#define FRONT_PER_THREAD 16  // frontier states per search thread, for the work queue's balance
+#define FRONT_PER_WARP 64    // frontier states per searching warp, for the work queue's balance
 #define FRONT_MAX (8u << 20) // states one frontier level may hold (776 B each: 6.5 GB)
 
 // ---- the top of the tree, breadth-first ---------------------------------------------------------
@@ -105,251 +104,10 @@ __global__ void __launch_bounds__(128) tc_super_expand(SpExpand e)
     expand_one(&sp_s, &x, e.budget, e.out, base, nullptr, nullptr, nullptr);
 }
 
-// ---- device: depth-first search of one subtree -------------------------------------------------
-
-// Raw operand sources: 0 ZERO, 1 ONE, 2 + c cell c, 18 + j RR value hist[j].
-__device__ __forceinline__ int raw_cand(const SpSpec *sp, const SpState *x, int i, SpCand *c)
-{
-    if (i == 0) {
-        c->v = 0; c->kind = SK_ZERO; c->extra = 0; c->ref = 0;
-        return 1;
-    }
-    if (i == 1) {
-        c->v = sp->mask; c->kind = SK_ONE; c->extra = 0; c->ref = 0;
-        return 1;
-    }
-    if (i < 2 + SP_CELLS) {
-        int cc = i - 2;
-        if (cc >= sp->ncells || !((x->readable >> cc) & 1))
-            return 0;
-        int prev = sp->sym_prev[cc];
-        if (prev >= 0 && !((x->used >> prev) & 1))
-            return 0;
-        c->v = sp_cell_value(sp, x, cc); c->kind = SK_CELL; c->extra = 0; c->ref = (int8_t)cc;
-        return 1;
-    }
-    int j = i - 2 - SP_CELLS;
-    if (j > x->n || (j == 0 && !x->def0))
-        return 0;
-    c->v = x->hist[j];
-    c->kind = x->stored[j] ? SK_TEMP : SK_LAZY;
-    c->extra = (uint8_t)!x->stored[j];
-    c->ref = (int8_t)j;
-    return 1;
-}
-
-// The operands of the node as a set of raw sources: one per value, the cheapest.
-__device__ uint64_t survivors(const SpSpec *sp, const SpState *x)
-{
-    uint64_t keep = 0;
-    uint64_t val[2 + SP_CELLS + DEV_LEVELS + 1];
-    uint8_t extra[2 + SP_CELLS + DEV_LEVELS + 1];
-    int idx[2 + SP_CELLS + DEV_LEVELS + 1], m = 0;
-    int top = 2 + SP_CELLS + x->n;
-    for (int i = 0; i <= top; i++) {
-        SpCand c;
-        if (!raw_cand(sp, x, i, &c))
-            continue;
-        int k = 0;
-        while (k < m && val[k] != c.v)
-            k++;
-        if (k == m) {
-            val[m] = c.v;
-            extra[m] = c.extra;
-            idx[m++] = i;
-        } else if (c.extra < extra[k]) {
-            extra[k] = c.extra;
-            idx[k] = i;
-        }
-    }
-    for (int k = 0; k < m; k++)
-        keep |= 1ull << idx[k];
-    return keep;
-}
-
-struct SpDev {
-    const SpSpec *spec;
-    const SpState *frontier;
-    unsigned long long nfront;
-    int budget;
-    unsigned long long *next;
-    int *found;
-    SpState *sol;
-    unsigned long long *nodes;
-    ulonglong2 *tt;             // the transposition table, shared by every thread
-    unsigned long long tt_mask;
-    int tt_min_rem;             // states with fewer instructions left are not looked up
-};
-
 // Subtrees with fewer instructions left than this are searched again rather than looked up:
-// a lookup is a random global-memory access and a key over every operand value.
+// a lookup is a random global-memory access.
 extern "C" {
 int tc_super_tt_min_rem = 4;
-}
-
-// ---- the transposition table ------------------------------------------------------------------
-//
-// States searched in full without a program, as the reference's per-thread table keeps them
-// (src/super.c:408-418, 641-716): the same state is reached in many orders, and its future
-// depends only on RR, the readable, written and used cells, and the values a NAND could read with
-// what each costs.  Here one table serves every thread, and it is kept from budget to budget.  An
-// entry is two 64-bit words: the state's first key, and its second key with the low byte
-// replaced by the instructions that were left when it was searched; a state arriving with `rem`
-// left is pruned when an entry holds both its keys and at least `rem`.  An entry torn between two
-// writers matches only when both wrote this state (the rem is then a true one) or by a 120-bit
-// coincidence, which the reference's 128-bit keys also rule out in practice.
-
-__device__ __forceinline__ uint64_t mix64(uint64_t z)
-{
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-
-// The state's keys (src/super.c:626-641): RR, the cell masks, and the operand values as a set.
-__device__ void state_key(const SpSpec *sp, const SpState *x, uint64_t keep, uint64_t *k1,
-                          uint64_t *k2)
-{
-    uint64_t a = mix64(x->hist[x->n] ^ (uint64_t)sp_rr_def(x) << 63), b = mix64(a + 0x1234567);
-    const uint64_t f = (uint64_t)x->readable | (uint64_t)x->written << 21 |
-                       (uint64_t)x->used << 42;
-    a += mix64(f + 0x9E3779B97F4A7C15ull);
-    b ^= mix64(f * 3 + 77);
-    for (uint64_t rest = keep; rest; rest &= rest - 1) {
-        SpCand c;
-        raw_cand(sp, x, __ffsll((long long)rest) - 1, &c);
-        const uint64_t v = c.v * 2 + c.extra;
-        a += mix64(v + 0x51ED27);
-        b += mix64(v * 0x2545F4914F6CDD1Dull + 0xABCDEF);
-    }
-    *k1 = a;
-    *k2 = b;
-}
-
-__device__ __forceinline__ bool tt_seen(const SpDev &d, uint64_t k1, uint64_t k2, int rem)
-{
-    const ulonglong2 e = d.tt[k1 & d.tt_mask];
-    return e.x == k1 && (e.y & ~0xFFull) == (k2 & ~0xFFull) && (int)(e.y & 0xFFull) >= rem;
-}
-
-__device__ __forceinline__ void tt_store(const SpDev &d, uint64_t k1, uint64_t k2, int rem)
-{
-    d.tt[k1 & d.tt_mask] = make_ulonglong2(k1, (k2 & ~0xFFull) | (uint64_t)rem);
-}
-
-__global__ void __launch_bounds__(128) tc_super_kernel(SpDev d)
-{
-    __shared__ SpSpec sp_s;
-    if (threadIdx.x == 0)
-        sp_s = *d.spec;
-    __syncthreads();
-    const SpSpec *sp = &sp_s;
-    SpState x;
-    uint64_t keep[DEV_LEVELS + 1];
-    uint8_t ci[DEV_LEVELS + 1], k_at[DEV_LEVELS + 1];
-    uint16_t wmask[DEV_LEVELS + 1];
-    uint32_t w_readable[DEV_LEVELS + 1], w_written[DEV_LEVELS + 1], used_before[DEV_LEVELS + 1];
-    int w_cost[DEV_LEVELS + 1];
-    uint64_t key1[DEV_LEVELS + 1], key2[DEV_LEVELS + 1];
-    int8_t key_rem[DEV_LEVELS + 1];  // rem of the node at this level, or -1: not in the table
-    unsigned long long nodes = 0, polled = 0;
-    const int budget = d.budget;
-    for (;;) {
-        const unsigned long long f = atomicAdd(d.next, 1ull);
-        if (f >= d.nfront || *(volatile int *)d.found)
-            break;
-        x = d.frontier[f];
-        const int n0 = x.n;
-        int L = n0;
-        keep[L] = survivors(sp, &x);
-        ci[L] = 0;
-        key_rem[L] = -1;
-        bool expand = true;
-        for (;;) {
-            if (nodes - polled >= POLL) {
-                polled = nodes;
-                if (*(volatile int *)d.found)
-                    break;
-            }
-            if (expand) {
-                const uint64_t rest = keep[L] & (~0ull << ci[L]);
-                if (!rest) {  // every operand tried at this level
-                    if (L == n0)
-                        break;
-                    if (key_rem[L] >= 0)  // searched in full, nothing found
-                        tt_store(d, key1[L], key2[L], key_rem[L]);
-                    x.readable = w_readable[L];
-                    x.written = w_written[L];
-                    x.cost = w_cost[L];
-                    wmask[L]++;
-                    expand = false;
-                    continue;
-                }
-                const int i = __ffsll((long long)rest) - 1;
-                ci[L] = (uint8_t)(i + 1);
-                SpCand c;
-                raw_cand(sp, &x, i, &c);
-                const uint32_t used = x.used;
-                if (L + 1 > DEV_LEVELS || !sp_nand(sp, &x, &c, budget))
-                    continue;
-                L++;
-                used_before[L] = used;
-                int8_t list[SP_CELLS];
-                k_at[L] = (uint8_t)sp_hits(sp, &x, list);
-                wmask[L] = 0;
-                expand = false;
-                continue;
-            }
-            // the output writes after NAND L
-            if (wmask[L] >= (1u << k_at[L])) {  // all tried: take the NAND back
-                if (x.op_kind[L] == SK_LAZY)
-                    x.stored[x.op_ref[L]] = 0;
-                x.cost -= 1 + (x.op_kind[L] == SK_LAZY);
-                x.used = used_before[L];
-                x.n--;
-                L--;
-                expand = true;
-                continue;
-            }
-            int8_t list[SP_CELLS];
-            sp_hits(sp, &x, list);
-            w_readable[L] = x.readable;
-            w_written[L] = x.written;
-            w_cost[L] = x.cost;
-            sp_write(sp, &x, list, wmask[L]);
-            nodes++;
-            const int a = sp_arrive(sp, &x, budget);
-            if (a == 2) {
-                if (atomicCAS(d.found, 0, 1) == 0)
-                    *d.sol = x;
-                break;
-            }
-            if (a == 0) {
-                keep[L] = survivors(sp, &x);
-                ci[L] = 0;
-                key_rem[L] = -1;
-                const int rem = budget - x.cost;
-                bool seen = false;
-                if (rem >= d.tt_min_rem) {  // small subtrees: cheaper to search again
-                    state_key(sp, &x, keep[L], &key1[L], &key2[L]);
-                    seen = tt_seen(d, key1[L], key2[L], rem);
-                    key_rem[L] = (int8_t)rem;
-                }
-                if (!seen) {
-                    expand = true;
-                    continue;
-                }
-                key_rem[L] = -1;  // searched before with at least this much left: nothing there
-            }
-            x.readable = w_readable[L];
-            x.written = w_written[L];
-            x.cost = w_cost[L];
-            wmask[L]++;
-        }
-        if (*(volatile int *)d.found)
-            break;
-    }
-    atomicAdd(d.nodes, nodes);
 }
 
 // ---- the driver ----------------------------------------------------------------------------------
@@ -413,9 +171,9 @@ extern "C" int tc_super_run(const SpSpec *sp, int max_cost, int lb, int *found, 
     int per_sm = 0;
     if (ok)
         ok = tc_cu_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_super_kernel,
-                                                                       128, 0),
+                                                                       WARPS * 32, 0),
                          "occupancy", err, errlen);
-    const size_t threads = (size_t)tc_engine.sms * (per_sm > 0 ? per_sm : 1) * 128;
+    const size_t warps = (size_t)tc_engine.sms * (per_sm > 0 ? per_sm : 1) * WARPS;
     SpState *lv[2] = {nullptr, nullptr};
     size_t lv_cap[2] = {0, 0};
     // the transposition table: 2^25 entries of 16 bytes, kept from budget to budget
@@ -461,7 +219,7 @@ extern "C" int tc_super_run(const SpSpec *sp, int max_cost, int lb, int *found, 
         if (*found)
             n = 0;
         // the next levels, on the device, until one keeps every search thread busy
-        for (int depth = 0; ok && n && n < FRONT_PER_THREAD * threads && depth < budget;) {
+        for (int depth = 0; ok && n && n < FRONT_PER_WARP * warps && depth < budget;) {
             SpExpand e = {d_spec, lv[cur], (unsigned long long)n, nullptr, d_count, d_nodes,
                           d_found, d_sol, budget};
             const unsigned blocks = (unsigned)((n + 127) / 128);
@@ -511,11 +269,11 @@ extern "C" int tc_super_run(const SpSpec *sp, int max_cost, int lb, int *found, 
                 SpDev d = {d_spec, lv[cur], (unsigned long long)n, budget, d_next, d_found,
                            d_sol, d_nodes, d_tt, tt_entries - 1,
                            tc_super_tt_min_rem > 0 ? tc_super_tt_min_rem : 1};
-                unsigned blocks = (unsigned)((n + 127) / 128);
+                unsigned blocks = (unsigned)((n + WARPS - 1) / WARPS);
                 unsigned maxb = (unsigned)(tc_engine.sms * (per_sm > 0 ? per_sm : 1));
                 if (blocks > maxb)
                     blocks = maxb;
-                tc_super_kernel<<<blocks, 128, 0, tc_engine.stream>>>(d);
+                tc_super_kernel<<<blocks, WARPS * 32, 0, tc_engine.stream>>>(d);
                 ok = tc_cu_check(cudaGetLastError(), "super search", err, errlen) &&
                      tc_cu_check(cudaStreamSynchronize(tc_engine.stream), "super search", err,
                                  errlen);
