@@ -208,6 +208,61 @@ __device__ int warp_arrive(const SpSpec *sp, const WNode &x, const LaneSpec &ls,
     return 0;
 }
 
+// The operands whose NAND leads to a child worth visiting: sp_nand's checks (RR defined or the
+// operand ZERO; RR changes) and the child's lower bound.  The bound is the same for every subset
+// of the outputs the child then writes (each write adds one instruction and takes one STO off
+// the bound; the outputs it writes hold RR's value, which the bound leaves out already), and a
+// child over the bound can be no goal, so such children are dropped here, in one pass over all
+// operands, instead of one visit each.
+__device__ uint64_t warp_filter(const SpSpec *sp, const WNode &x, uint64_t keep, const Ops &o,
+                                const LaneSpec &ls, uint32_t out_mask, int budget, int L)
+{
+    if (L + 1 > DEV_LEVELS)
+        return 0;
+    const int lane = threadIdx.x & 31;
+    const bool def = x.n > 0 || x.def0;
+    if (!def)
+        keep &= 1ull;  // only ZERO may be read before RR is defined
+    const uint32_t U = out_mask & ~x.written;
+    // distinct targets among the unwritten outputs
+    bool lead = false;
+    if ((U >> lane) & 1) {
+        const uint32_t m = __match_any_sync(U, ls.target);
+        lead = __ffs(m) - 1 == lane;
+    }
+    const int distinct = __popc(__ballot_sync(FULL, lead));
+    bool rrt_in_u = false;
+    uint64_t r[2];
+    bool in_u[2] = {false, false};
+    r[0] = ~(x.rr & o.vA) & sp->mask;
+    r[1] = ~(x.rr & o.vB) & sp->mask;
+    for (uint32_t u = U; u; u &= u - 1) {
+        const uint64_t t = sp->target[__ffs(u) - 1];
+        in_u[0] |= t == r[0];
+        in_u[1] |= t == r[1];
+        rrt_in_u |= t == sp->rr_target;
+    }
+    const int base_cost = x.cost + 1 + __popc(U);
+    bool pass[2];
+    for (int h = 0; h < 2; h++) {
+        const int need = distinct - in_u[h];
+        int nands = need;
+        if (sp->rr_out) {
+            if (r[h] != sp->rr_target) {
+                if (!(rrt_in_u && sp->rr_target != r[h]))
+                    nands++;
+            } else if (need) {
+                nands++;
+            }
+        }
+        const int extra = h == 0 ? !o.e0A : !o.e0B;
+        pass[h] = !(def && r[h] == x.rr) && base_cost + extra + nands <= budget;
+    }
+    const uint64_t ok = (uint64_t)__ballot_sync(FULL, pass[0]) |
+                        (uint64_t)__ballot_sync(FULL, pass[1]) << 32;
+    return keep & ok;
+}
+
 // ---- the transposition table ------------------------------------------------------------------
 //
 // States searched in full without a program, as the reference's per-thread table keeps them
@@ -308,7 +363,8 @@ __global__ void __launch_bounds__(WARPS * 32) tc_super_kernel(SpDev d)
         const int n0 = x.n;
         int L = n0;
         Ops o;
-        ws.keep[L] = warp_survivors(sp, ws, x, ls, base, o);
+        ws.keep[L] = warp_filter(sp, x, warp_survivors(sp, ws, x, ls, base, o), o, ls, out_mask,
+                                 budget, L);
         ws.ci[L] = 0;
         ws.key_rem[L] = -1;
         bool expand = true, stop = false;
@@ -434,14 +490,15 @@ __global__ void __launch_bounds__(WARPS * 32) tc_super_kernel(SpDev d)
                 break;
             }
             if (a == 0) {
-                ws.keep[L] = warp_survivors(sp, ws, x, ls, base, o);
+                const uint64_t all = warp_survivors(sp, ws, x, ls, base, o);
+                ws.keep[L] = warp_filter(sp, x, all, o, ls, out_mask, budget, L);
                 ws.ci[L] = 0;
                 ws.key_rem[L] = -1;
                 const int rem = budget - x.cost;
                 bool seen = false;
                 if (rem >= d.tt_min_rem) {  // small subtrees: cheaper to search again
                     uint64_t k1, k2;
-                    warp_key(x, ws.keep[L], o, &k1, &k2);
+                    warp_key(x, all, o, &k1, &k2);
                     ws.key1[L] = k1;
                     ws.key2[L] = k2;
                     seen = tt_seen(d, k1, k2, rem);
