@@ -153,14 +153,17 @@ __device__ void warp_key(const WNode &x, uint64_t keep, const Ops &o, uint64_t *
     const uint64_t f = (uint64_t)x.readable | (uint64_t)x.written << 21 | (uint64_t)x.used << 42;
     a += mix64(f + 0x9E3779B97F4A7C15ull);
     b ^= mix64(f * 3 + 77);
+    // an operand that costs a store is told apart by a constant XORed in (not by a shift, which
+    // would lose the top row of a 64-row table)
+    const uint64_t lazy = 0xD6E8FEB86659FD93ull;
     uint64_t ca = 0, cb = 0;
     if ((keep >> lane) & 1) {
-        const uint64_t v = o.vA * 2 + !o.e0A;
+        const uint64_t v = o.vA ^ (o.e0A ? 0ull : lazy);
         ca += mix64(v + 0x51ED27);
         cb += mix64(v * 0x2545F4914F6CDD1Dull + 0xABCDEF);
     }
     if ((keep >> (lane + 32)) & 1) {
-        const uint64_t v = o.vB * 2 + !o.e0B;
+        const uint64_t v = o.vB ^ (o.e0B ? 0ull : lazy);
         ca += mix64(v + 0x51ED27);
         cb += mix64(v * 0x2545F4914F6CDD1Dull + 0xABCDEF);
     }
