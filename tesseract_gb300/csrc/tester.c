@@ -112,7 +112,7 @@ double cuda_t1_run(const T1Config *cfg, T1Size *out, int *threads, char *err, si
     b.longest = b.passes + CHUNK;
     double t0 = tc_now();
     uint64_t next[T1_SIZES] = {0};
-    uint32_t chunk = cfg->programs ? CHUNK : 4096;  /* timed runs check the clock more often */
+    uint32_t chunk = cfg->programs ? CHUNK : 16384;  /* timed runs check the clock more often */
     int ok = 1;
     for (;;) {
         int any = 0;
