@@ -175,6 +175,11 @@ int tc_module(const char *src, size_t len, const char *const *kernels, int nkern
         opts[nopt++] = "--std=c++17";
         opts[nopt++] = "-lineinfo";
         opts[nopt++] = "--ptxas-options=-v";
+        /* ptxas -O2 rather than its default -O3: measured on the GB300, the kernels run the
+           same (mul16's verify 7.89 ms either way in alternating runs, cube Life 71,900 gen/s
+           either way) and compiling takes ~35 % less (0.77 against 1.18 s for a
+           20,000-instruction program); -O1 compiles faster still but runs Life 11 % slower */
+        opts[nopt++] = "--ptxas-options=-O2";
         if (extra_opt && *extra_opt)
             opts[nopt++] = extra_opt;
         nr = nvrtcCompileProgram(prog, nopt, opts);

@@ -40,8 +40,8 @@ void   tc_wave_free(TcWave *w);
    NVRTC's time for a generated kernel as a constant plus a cost per NAND/STO instruction. */
 #define RATE_INTERP 9.0e13
 #define RATE_COMPILED 2.0e15
-#define COMPILE_S0 0.2
-#define COMPILE_S_PER_INSTR 8.0e-5
+#define COMPILE_S0 0.1
+#define COMPILE_S_PER_INSTR 4.0e-5  /* ptxas -O2: 0.15 s at 5,000 instructions, 0.77 s at 20,000 */
 
 typedef struct {
     TcWave *w;
