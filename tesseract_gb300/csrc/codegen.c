@@ -185,16 +185,16 @@ static int spec_fits_32(const TcSpec *s)
     return 1;
 }
 
-/* The part of input vector k that comes from the word number (x with its 5 low bits zero):
-   runs of vector bits b0..b1 whose x bits descend (pos = P - b) come from one shift of the
-   bit-reversed x; other bits one at a time. */
-static void emit_var_high(Src *o, const TcSpec *s, int k)
+/* The part of input vector k that comes from the word number (y = 32 word + lane with its 5 low
+   bits zero; x bit p of the assignment is y bit sigma[p]): runs of vector bits b0..b1 whose y bits
+   descend (pos = P - b) come from one shift of the bit-reversed y; other bits one at a time. */
+static void emit_var_high(Src *o, const TcSpec *s, int k, const int *sigma)
 {
     emit(o, "    const u64 vh%d = 0ull", k);
     int w = s->var_bits[k];
     for (int b0 = 0; b0 < w;) {
-        int P = s->var_pos[k][b0] + b0, b1 = b0;
-        while (b1 + 1 < w && s->var_pos[k][b1 + 1] == P - (b1 + 1))
+        int P = sigma[s->var_pos[k][b0]] + b0, b1 = b0;
+        while (b1 + 1 < w && sigma[s->var_pos[k][b1 + 1]] == P - (b1 + 1))
             b1++;
         /* bit b of the vector = bit (63 - pos) = bit (63 - P + b) of brx */
         int sh = 63 - P;
@@ -204,25 +204,25 @@ static void emit_var_high(Src *o, const TcSpec *s, int k)
         else if (b1 > b0)
             emit(o, " | ((brx << %d) & 0x%llxull)", -sh, (unsigned long long)mask);
         else
-            emit(o, " | (((xw >> %d) & 1ull) << %d)", s->var_pos[k][b0], b0);
+            emit(o, " | (((xw >> %d) & 1ull) << %d)", sigma[s->var_pos[k][b0]], b0);
         b0 = b1 + 1;
     }
     emit(o, ";\n");
 }
 
-/* The part of input vector k that comes from lane l (x bits 0..4). */
-static uint64_t var_low(const TcSpec *s, int k, int l)
+/* The part of input vector k that comes from lane l (y bits 0..4). */
+static uint64_t var_low(const TcSpec *s, int k, int l, const int *sigma)
 {
     uint64_t v = 0;
     for (int b = 0; b < s->var_bits[k]; b++)
-        if (s->var_pos[k][b] < 5)
-            v |= (uint64_t)((l >> s->var_pos[k][b]) & 1) << b;
+        if (sigma[s->var_pos[k][b]] < 5)
+            v |= (uint64_t)((l >> sigma[s->var_pos[k][b]]) & 1) << b;
     return v;
 }
 
 /* RPN for lane l into e[l] (and eh[l] when the left side is wider than 32 bits).  Every item
    gets its own variable t<i>; a compile-time stack holds the item numbers. */
-static void emit_lane(Src *o, const TcSpec *s, int l, int narrow)
+static void emit_lane(Src *o, const TcSpec *s, int l, int narrow, const int *sigma)
 {
     const char *T = narrow ? "u32" : "u64";
     int st[TS_MAX_STACK + 2] = {0}, sp = 0;
@@ -235,7 +235,7 @@ static void emit_lane(Src *o, const TcSpec *s, int l, int narrow)
             st[sp++] = i;
         } else if (op == TS_VAR) {
             emit(o, "      const %s t%d = (%s)(vh%d + 0x%llxull);\n", T, i, T, (int)v,
-                 (unsigned long long)var_low(s, (int)v, l));
+                 (unsigned long long)var_low(s, (int)v, l, sigma));
             st[sp++] = i;
         } else if (op == TS_NOT) {
             emit(o, "      const %s t%d = ~t%d;\n", T, i, st[sp - 1]);
@@ -274,26 +274,108 @@ static void emit_lane(Src *o, const TcSpec *s, int l, int narrow)
 
 /* ---- one enumeration kernel -------------------------------------------------------------- */
 
+/* Where the assignment bits come from.  The kernel enumerates y = 32 word + lane: y bits 0..4 are
+   the bit lane (constant patterns), 5..9 the thread's lane in its warp, 10..14 the 32 steps a
+   warp takes through one chunk of 1,024 words, 15 and up the chunk.  Assignment x has y bit
+   sigma[j] at its bit j (input k is x bit n-1-k).  Only the 5 inputs on y bits 10..14 change
+   from step to step within a chunk: every LUT that depends on none of them is computed once per
+   chunk (tc_outer) and kept in registers for the 32 steps (tc_inner).  The identity puts x bits
+   10..14 there; when 5 other inputs among x bits 0..14 leave more LUTs out of the steps (an
+   array multiplier's last rows, say, whose inputs are the low x bits), sigma moves those 5 onto
+   y bits 10..14 and the x bits it displaces onto the lanes.  x bits 15 and up never move, so a
+   chunk is the same set of assignments either way and the reference's --part shares hold. */
+typedef struct {
+    int      split;     /* 1: the chunk-invariant LUTs are hoisted */
+    int      permuted;  /* 1: sigma is not the identity */
+    int      sigma[64];
+    uint64_t inner;     /* inputs (bit k) that change between steps */
+} Layout;
+
+#define SPLIT_MAX_FIELDS 48   /* values kept across the steps: registers */
+
+static int popcount64(uint64_t v)
+{
+    int c = 0;
+    for (; v; v &= v - 1)
+        c++;
+    return c;
+}
+
+/* LUTs of `order` that depend on no input of mask `vary`. */
+static int invariant_luts(const uint64_t *sup, int norder, uint64_t vary)
+{
+    int c = 0;
+    for (int i = 0; i < norder; i++)
+        c += (sup[i] & vary) == 0;
+    return c;
+}
+
+static uint64_t input_bit(size_t n, int j)  /* the input on x bit j */
+{
+    return 1ull << (n - 1 - (size_t)j);
+}
+
+/* Picks the inputs that change within a chunk (greedily, the 5 among x bits 0..14 that leave the
+   most LUTs invariant, or the identity's if that is as good) and sigma. */
+static void choose_layout(Layout *L, size_t n, const uint64_t *sup, int norder)
+{
+    memset(L, 0, sizeof *L);
+    for (int j = 0; j < 64; j++)
+        L->sigma[j] = j;
+    if (n < 15 || norder == 0)
+        return;
+    uint64_t id = 0, best = 0;
+    for (int j = 10; j < 15; j++)
+        id |= input_bit(n, j);
+    for (int step = 0; step < 5; step++) {
+        int bj = -1, bc = -1;
+        for (int j = 0; j < 15; j++) {
+            uint64_t m = input_bit(n, j);
+            if (best & m)
+                continue;
+            int c = invariant_luts(sup, norder, best | m);
+            if (c > bc) {
+                bc = c;
+                bj = j;
+            }
+        }
+        best |= input_bit(n, bj);
+    }
+    if (invariant_luts(sup, norder, best) <= invariant_luts(sup, norder, id))
+        best = id;
+    L->inner = best;
+    if (best == id)
+        return;
+    /* x bits 0..14: the chosen 5 to y bits 10..14, the rest in order to y bits 0..9 */
+    int next_lane = 0, next_step = 10;
+    for (int j = 0; j < 15; j++)
+        L->sigma[j] = (best & input_bit(n, j)) ? next_step++ : next_lane++;
+    L->permuted = 1;
+}
+
+/* Input k as y bit q: a lane pattern for q < 5, else bit q - 5 of the word spread over all 32
+   lanes (a shift up to the sign bit and an arithmetic shift down: two instructions; words fit
+   32 bits up to 37 inputs). */
+static void emit_input(Src *o, size_t k, size_t n, int q, const char *w32, const char *w64)
+{
+    if (q < 5)
+        emit(o, "    const u32 in%zu = TC_PAT%d;\n", k, q);
+    else if (n <= 37)
+        emit(o, "    const u32 in%zu = (u32)((int)(%s << %d) >> 31);\n", k, w32, 31 - (q - 5));
+    else
+        emit(o, "    const u32 in%zu = 0u - (u32)((%s >> %d) & 1ull);\n", k, w64, q - 5);
+}
+
 static void emit_word_function(Src *o, const TcGenEnum *g)
 {
     const Program *a = g->a;
     size_t n = a->ninputs;
-    emit(o, "TC_DEV u32 tc_word(const u64 word)\n{\n");
-    /* input k is bit j = n-1-k of x = 32 word + lane: a lane pattern for j < 5, else bit j - 5
-       of the word spread over all 32 lanes (a shift up to the sign bit and an arithmetic shift
-       down: two instructions; words fit 32 bits up to 37 inputs) */
-    if (n > 5 && n <= 37)
-        emit(o, "    const u32 wlo = (u32)word;\n");
-    for (size_t k = 0; k < n; k++) {
-        int j = (int)(n - 1 - k);
-        if (j < 5)
-            emit(o, "    const u32 in%zu = TC_PAT%d;\n", k, j);
-        else if (n <= 37)
-            emit(o, "    const u32 in%zu = (u32)((int)(wlo << %d) >> 31);\n", k, 31 - (j - 5));
-        else
-            emit(o, "    const u32 in%zu = 0u - (u32)((word >> %d) & 1ull);\n", k, j - 5);
-    }
     const TcSpec *s = g->spec;
+    Layout L;
+    memset(&L, 0, sizeof L);
+    for (int j = 0; j < 64; j++)
+        L.sigma[j] = j;
+    Src outer = {0}, inner = {0}, fields = {0}, stores = {0}, loads = {0};
     /* the cells compared, as (program, cell) pairs: a first */
     char (*val_a)[24] = tc_xcalloc(a->ncells + 1, sizeof *val_a);
     char (*val_b)[24] = tc_xcalloc((g->b ? g->b->ncells : 0) + 1, sizeof *val_b);
@@ -316,66 +398,178 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         else
             for (int bit = 0; bit < s->width; bit++)
                 want[nwant++] = cur_a[s->out[bit]];
-        int luts = emit_luts(o, net, want, nwant);
-        emit(o, "    // %d LOP3 for %zu + %zu NAND/STO instructions\n", luts, a->len,
-             g->b ? g->b->len : (size_t)0);
+        const int size = tc_net_size(net);
+        int *order = tc_xmalloc(((size_t)size + 1) * sizeof *order), norder = 0;
+        const int luts = tc_net_map(net, want, nwant, order, &norder);
+        /* the inputs each node depends on */
+        uint64_t *nsup = tc_xcalloc((size_t)size + 1, sizeof *nsup);
+        uint64_t *sup = tc_xmalloc(((size_t)norder + 1) * sizeof *sup);
+        int (*lv)[3] = tc_xmalloc(((size_t)norder + 1) * sizeof *lv);
+        uint8_t *tts = tc_xmalloc((size_t)norder + 1);
+        for (size_t k = 0; k < n; k++)
+            nsup[leaf[k]] = 1ull << k;
+        for (int i = 0; i < norder; i++) {
+            int nl;
+            tc_net_lut(net, order[i], lv[i], &nl, &tts[i]);
+            for (int q = nl; q < 3; q++)
+                lv[i][q] = 0;
+            nsup[order[i]] = nsup[lv[i][0]] | nsup[lv[i][1]] | nsup[lv[i][2]];
+            sup[i] = nsup[order[i]];
+        }
+        choose_layout(&L, n, sup, norder);
+        /* values of the chunk read by the steps: kept in TcInv */
+        char *field = tc_xcalloc((size_t)size + 1, 1);
+        int nfields = 0;
+#define STEADY(nd) ((nsup[nd] & L.inner) == 0 && (nd) > 1 &&                                    \
+                    !(tc_net_node(net, nd)->kind == TN_LEAF &&                                  \
+                      L.sigma[n - 1 - (size_t)tc_net_node(net, nd)->id] < 5))
+        for (int i = 0; i < norder; i++)
+            for (int q = 0; q < 3 && (sup[i] & L.inner); q++)
+                if (STEADY(lv[i][q]) && !field[lv[i][q]]) {
+                    field[lv[i][q]] = 1;
+                    nfields++;
+                }
+        for (int w = 0; w < nwant; w++)
+            if (STEADY(want[w]) && !field[want[w]]) {
+                field[want[w]] = 1;
+                nfields++;
+            }
+#undef STEADY
+        const int hoisted = invariant_luts(sup, norder, L.inner);
+        L.split = L.inner && hoisted > 0 && 5 * hoisted >= norder &&
+                  nfields <= SPLIT_MAX_FIELDS;
+        if (!L.split) {
+            memset(field, 0, (size_t)size + 1);
+            L.permuted = 0;
+            for (int j = 0; j < 64; j++)
+                L.sigma[j] = j;
+        }
+        for (size_t k = 0; k < n; k++) {
+            const int q = L.sigma[n - 1 - k];
+            if (!L.split || (L.inner >> k & 1)) {
+                emit_input(&inner, k, n, q, "wlo", "word");
+            } else {
+                emit_input(&outer, k, n, q, "clo", "cword");
+                if (q < 5)
+                    emit_input(&inner, k, n, q, "wlo", "word");
+            }
+        }
+        for (int i = 0; i < norder; i++) {
+            char x[32], y[32], z[32];
+            node_name(x, sizeof x, net, lv[i][0]);
+            node_name(y, sizeof y, net, lv[i][1]);
+            node_name(z, sizeof z, net, lv[i][2]);
+            emit(L.split && !(sup[i] & L.inner) ? &outer : &inner,
+                 "    u32 n%d; TC_LOP3(n%d, %s, %s, %s, 0x%02x);\n", order[i], order[i], x, y, z,
+                 (unsigned)tts[i]);
+        }
+        for (int nd = 0; nd <= size; nd++)
+            if (field[nd]) {
+                char f[32];
+                node_name(f, sizeof f, net, nd);
+                emit(&fields, " u32 %s;", f);
+                emit(&stores, "    v->%s = %s;\n", f, f);
+                emit(&loads, "    const u32 %s = v->%s;\n", f, f);
+            }
+        emit(&inner, "    // %d LOP3 for %zu + %zu NAND/STO instructions, %d of them once per chunk\n",
+             luts, a->len, g->b ? g->b->len : (size_t)0, L.split ? hoisted : 0);
         for (uint32_t c = 0; c < a->ncells; c++)
             node_name(val_a[c], sizeof val_a[c], net, cur_a[c]);
         for (uint32_t c = 0; g->mode == EN_EQUIV && c < g->b->ncells; c++)
             node_name(val_b[c], sizeof val_b[c], net, cur_b[c]);
+        free(field);
+        free(tts);
+        free(lv);
+        free(sup);
+        free(nsup);
+        free(order);
         free(want);
         free(cur_a);
         free(cur_b);
         free(leaf);
         tc_net_free(net);
     } else {
-        body(o, a, "a", a->inputs, n, g->ticks);
+        for (size_t k = 0; k < n; k++)
+            emit_input(&inner, k, n, (int)(n - 1 - k), "wlo", "word");
+        body(&inner, a, "a", a->inputs, n, g->ticks);
         if (g->mode == EN_EQUIV)
-            body(o, g->b, "b", g->b_inputs, n, g->ticks);
+            body(&inner, g->b, "b", g->b_inputs, n, g->ticks);
         for (uint32_t c = 0; c < a->ncells; c++)
             snprintf(val_a[c], sizeof val_a[c], c == 0 ? "0u" : c == 1 ? "TC_ONES" : "a%u", c);
         for (uint32_t c = 0; g->mode == EN_EQUIV && c < g->b->ncells; c++)
             snprintf(val_b[c], sizeof val_b[c], c == 0 ? "0u" : c == 1 ? "TC_ONES" : "b%u", c);
     }
     if (g->mode == EN_SEARCH) {
-        emit(o, "    u32 m = TC_ONES;\n");
+        emit(&inner, "    u32 m = TC_ONES;\n");
         for (int b = 0; b < s->width; b++) {
             int bit = (int)((g->target >> b) & 1);
-            emit(o, "    m &= %s%s;\n", bit ? "" : "~", val_a[s->out[b]]);
+            emit(&inner, "    m &= %s%s;\n", bit ? "" : "~", val_a[s->out[b]]);
         }
     } else if (g->mode == EN_EQUIV) {
-        emit(o, "    u32 m = 0u;\n");
+        emit(&inner, "    u32 m = 0u;\n");
         for (size_t k = 0; k < a->noutputs; k++)
-            emit(o, "    m |= %s ^ %s;\n", val_a[a->outputs[k]],
+            emit(&inner, "    m |= %s ^ %s;\n", val_a[a->outputs[k]],
                  val_b[g->b->outputs[g->out_map[k]]]);
     } else {
         int narrow = spec_fits_32(s);
-        emit(o, "    const u64 xw = word << 5;\n");
-        emit(o, "    const u64 brx = __brevll(xw);\n    (void)brx;\n");
+        emit(&inner, "    const u64 xw = word << 5;\n");
+        emit(&inner, "    const u64 brx = __brevll(xw);\n    (void)brx;\n");
         for (int k = 0; k < s->nvars; k++)
-            emit_var_high(o, s, k);
-        emit(o, "    u32 e[32];\n");
+            emit_var_high(&inner, s, k, L.sigma);
+        emit(&inner, "    u32 e[32];\n");
         if (!narrow)
-            emit(o, "    u32 eh[32];\n");
+            emit(&inner, "    u32 eh[32];\n");
         for (int l = 0; l < 32; l++)
-            emit_lane(o, s, l, narrow);
-        emit(o, "    tc_transpose32(e);\n");
+            emit_lane(&inner, s, l, narrow, L.sigma);
+        emit(&inner, "    tc_transpose32(e);\n");
         if (!narrow)
-            emit(o, "    tc_transpose32(eh);\n");
-        emit(o, "    u32 m = 0u;\n");
+            emit(&inner, "    tc_transpose32(eh);\n");
+        emit(&inner, "    u32 m = 0u;\n");
         for (int b = 0; b < s->width; b++)
-            emit(o, "    m |= %s ^ %s[%d];\n", val_a[s->out[b]], b < 32 ? "e" : "eh", b & 31);
+            emit(&inner, "    m |= %s ^ %s[%d];\n", val_a[s->out[b]], b < 32 ? "e" : "eh", b & 31);
     }
     free(val_a);
     free(val_b);
-    emit(o, "    return m;\n}\n");
+    /* what a chunk computes once (cword: the word with its step bits, 5..9, zero), what each step
+       computes, and the two together for one word */
+    emit(o, "typedef struct {%s } TcInv;\n", fields.len ? fields.s : " u32 unused_;");
+    emit(o, "TC_DEV void tc_outer(const u64 cword, TcInv *v)\n{\n");
+    emit(o, "    const u32 clo = (u32)cword;\n    (void)clo;\n    (void)v;\n");
+    emit(o, "%s%s}\n", outer.len ? outer.s : "", stores.len ? stores.s : "");
+    emit(o, "TC_DEV u32 tc_inner(const u64 word, const TcInv *v)\n{\n");
+    emit(o, "    const u32 wlo = (u32)word;\n    (void)wlo;\n    (void)v;\n");
+    emit(o, "%s%s    return m;\n}\n", loads.len ? loads.s : "", inner.s);
+    emit(o, "TC_DEV u32 tc_word(const u64 word)\n{\n    TcInv v;\n"
+            "    tc_outer(word & ~992ull, &v);\n    return tc_inner(word, &v);\n}\n");
+    /* y -> x: the assignment a hit at y stands for */
+    emit(o, "#define TC_PERMUTED %d\n", L.permuted);
+    emit(o, "TC_DEV u64 tc_unperm(const u64 y)\n{\n");
+    if (!L.permuted) {
+        emit(o, "    return y;\n}\n");
+    } else {
+        uint64_t fixed = 0;
+        for (size_t j = 0; j < 64; j++)
+            if (j >= n || L.sigma[j] == (int)j)
+                fixed |= 1ull << j;
+        emit(o, "    u64 x = y & 0x%llxull;\n", (unsigned long long)fixed);
+        for (size_t j = 0; j < n; j++)
+            if (L.sigma[j] != (int)j)
+                emit(o, "    x |= ((y >> %d) & 1ull) << %zu;\n", L.sigma[j], j);
+        emit(o, "    return x;\n}\n");
+    }
+    free(outer.s);
+    free(inner.s);
+    free(fields.s);
+    free(stores.s);
+    free(loads.s);
 }
 
 /* The kernel template: each warp takes a contiguous run of the selected words (a multiple of 32),
    32 words per step, one per lane.  Words are selected in chunks of 1024 (64 passes of 512
    lanes, the reference's hand-out unit, src/enum.c:11), chunk c belonging to share c % parts
-   (src/enum.c:232-234).  Hits are counted with popcount; the first 16 hits of each warp, which
-   are its 16 smallest because the warp's words rise, are written to list[warp]. */
+   (src/enum.c:232-234); a chunk's invariant LUTs are computed once before its 32 steps.  Hits
+   are counted with popcount; each warp's 16 smallest hits go to list[warp]: its first 16 when
+   the order is the identity (the warp's assignments rise), else a sorted insertion. */
 static const char *KERNEL =
     "#ifndef TC_HOST_EMULATION\n"
     "struct TcEnumArgs {\n"
@@ -391,18 +585,59 @@ static const char *KERNEL =
     "    const u64 s0 = warp * a.per_warp;\n"
     "    const u64 s1 = s0 + a.per_warp < a.words ? s0 + a.per_warp : a.words;\n"
     "    u32 recorded = 0;\n"
-    "    u64 hits = 0;\n"
-    "    for (u64 s = s0; s < s1; s += 32) {\n"
+    "    u64 hits = 0, thr = ~0ull;  /* thr: the 16th smallest hit kept so far */\n"
+    "    (void)thr;\n"
+    "    for (u64 s = s0; s < s1;) {\n"
     "        const u64 j = s >> 10;\n"
     "        const u64 chunk = a.nsel == a.parts ? j : (j / a.nsel) * a.parts + a.part + j % a.nsel;\n"
-    "        const u64 word = (chunk << 10) | (s & 992u) | lane;  /* s is a multiple of 32 */\n"
+    "        const u64 cbase = (chunk << 10) | lane;\n"
+    "        const u64 s_end = ((j + 1) << 10) < s1 ? ((j + 1) << 10) : s1;\n"
+    "        TcInv inv;\n"
+    "        tc_outer(cbase, &inv);  /* what stays the same for the chunk's 32 steps */\n"
+    "        for (; s < s_end; s += 32) {\n"
+    "        const u64 word = cbase | (s & 992u);  /* s is a multiple of 32 */\n"
     "        const u64 x0 = word << 5;\n"
     "        u32 valid = 0u;\n"
     "        if (s + lane < s1 && x0 < a.space)\n"
     "            valid = a.space - x0 >= 32u ? TC_ONES : (1u << (u32)(a.space - x0)) - 1u;\n"
-    "        const u32 m = tc_word(word) & valid;\n"
+    "        const u32 m = tc_inner(word, &inv) & valid;\n"
     "        hits += __popc(m);\n"
     "        u32 any = __ballot_sync(TC_ONES, m != 0u);\n"
+    "#if TC_PERMUTED\n"
+    "        /* the warp's assignments do not come in order: keep its 16 smallest, sorted.  A lane's\n"
+    "           hits rise with their bit (the bit lanes take x bits in order), so its smallest is\n"
+    "           its lowest bit; the warp's smallest goes in while it beats the 16th kept. */\n"
+    "        if (any) {\n"
+    "            const u64 bx = tc_unperm(x0);\n"
+    "            u32 mm = m;\n"
+    "            for (;;) {\n"
+    "                const u64 mine = mm ? bx | tc_unperm((u64)(__ffs(mm) - 1)) : ~0ull;\n"
+    "                u64 least = mine;\n"
+    "                for (int d = 16; d > 0; d >>= 1) {\n"
+    "                    const u64 other = __shfl_xor_sync(TC_ONES, least, d);\n"
+    "                    least = other < least ? other : least;\n"
+    "                }\n"
+    "                if (least == ~0ull || (recorded == 16u && least >= thr))\n"
+    "                    break;\n"
+    "                if (lane == 0) {\n"
+    "                    u64 *L = a.list + warp * 16u;\n"
+    "                    u32 i = recorded < 16u ? recorded : 15u;\n"
+    "                    while (i > 0 && L[i - 1] > least) {\n"
+    "                        L[i] = L[i - 1];\n"
+    "                        i--;\n"
+    "                    }\n"
+    "                    L[i] = least;\n"
+    "                }\n"
+    "                recorded = recorded < 16u ? recorded + 1u : 16u;\n"
+    "                u64 t = 0;\n"
+    "                if (lane == 0 && recorded == 16u)\n"
+    "                    t = a.list[warp * 16u + 15u];\n"
+    "                thr = __shfl_sync(TC_ONES, t, 0);\n"
+    "                if (mine == least)\n"
+    "                    mm &= mm - 1u;\n"
+    "            }\n"
+    "        }\n"
+    "#else\n"
     "        while (any && recorded < 16u) {\n"
     "            const int src = __ffs(any) - 1;\n"
     "            u32 mm = __shfl_sync(TC_ONES, m, src);\n"
@@ -414,6 +649,8 @@ static const char *KERNEL =
     "                mm &= mm - 1u;\n"
     "            }\n"
     "            any &= any - 1u;\n"
+    "        }\n"
+    "#endif\n"
     "        }\n"
     "    }\n"
     "    for (int d = 16; d > 0; d >>= 1)\n"

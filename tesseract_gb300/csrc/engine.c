@@ -638,7 +638,9 @@ void tc_enum_job_result(const TcEnumJob *j, const void *host_ws, EnumResult *r)
     *r = j->base;
     memcpy(&r->hits, h, 8);
     r->threads = (int)(j->blocks * TC_ENUM_BLOCK);
-    for (uint64_t w = 0; w < j->warps && r->hits && r->nhit < EN_SHOW; w++)
+    /* every warp's list: a kernel whose enumeration order is permuted does not find the
+       smallest hits in the first warps */
+    for (uint64_t w = 0; w < j->warps && r->hits; w++)
         for (uint32_t i = 0; i < count[w]; i++)
             cuda_enum_add_hit(r, list[w * 16 + i]);
 }
@@ -672,19 +674,20 @@ int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
         free(count);
         return tc_cu_check(rc, "tc_enum", err, errlen);
     }
-    /* only the warps that recorded something; lists are short */
-    for (uint64_t w = 0; w < warps && r->nhit < EN_SHOW; w++) {
-        if (!count[w])
-            continue;
-        uint64_t got[16];
-        rc = cudaMemcpy(got, (char *)tc_engine.ws_list.ptr + w * 16 * 8, (size_t)count[w] * 8,
-                        cudaMemcpyDeviceToHost);
+    /* every warp's list (a kernel whose enumeration order is permuted does not find the
+       smallest hits in the first warps), in one copy when there are hits */
+    if (hits) {
+        uint64_t *list = tc_xmalloc(warps * 16 * 8);
+        rc = cudaMemcpy(list, tc_engine.ws_list.ptr, warps * 16 * 8, cudaMemcpyDeviceToHost);
         if (rc != cudaSuccess) {
+            free(list);
             free(count);
             return tc_cu_check(rc, "hits", err, errlen);
         }
-        for (uint32_t i = 0; i < count[w]; i++)
-            cuda_enum_add_hit(r, got[i]);
+        for (uint64_t w = 0; w < warps; w++)
+            for (uint32_t i = 0; i < count[w]; i++)
+                cuda_enum_add_hit(r, list[w * 16 + i]);
+        free(list);
     }
     free(count);
     float ms = 0;

@@ -22,6 +22,7 @@
 // lists are read only up to those counts.  Calls that overlap on the GPU (two host threads
 // calling at once) race on the array.
 #include <cuda_runtime.h>
+#include <stdlib.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -134,27 +135,26 @@ extern "C" int cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, siz
                      err, errlen) ||
         !tc_cu_check(cudaStreamSynchronize(st), "tc_enum", err, errlen))
         return 0;
-    // The warps' first hits, in warp order (rising assignments), until 16 are kept.  Counts come
-    // over in runs of 1024 warps into this stack buffer.
+    // Every warp's hits (a kernel whose enumeration order is permuted does not find the
+    // smallest in the first warps).  Counts and lists come over in runs of 1024 warps.
     uint32_t count[1024];
-    for (uint64_t w0 = 0; hits && w0 < warps && r->nhit < EN_SHOW; w0 += 1024) {
+    uint64_t *got = hits ? (uint64_t *)tc_xmalloc(1024 * 16 * 8) : nullptr;
+    for (uint64_t w0 = 0; hits && w0 < warps; w0 += 1024) {
         uint64_t n = warps - w0 < 1024 ? warps - w0 : 1024;
         if (!tc_cu_check(cudaMemcpy(count, (uint32_t *)args.count + w0, n * 4,
                                     cudaMemcpyDeviceToHost),
-                         "hit counts", err, errlen))
+                         "hit counts", err, errlen) ||
+            !tc_cu_check(cudaMemcpy(got, (uint64_t *)args.list + w0 * 16, n * 16 * 8,
+                                    cudaMemcpyDeviceToHost),
+                         "hits", err, errlen)) {
+            free(got);
             return 0;
-        for (uint64_t i = 0; i < n && r->nhit < EN_SHOW; i++) {
-            if (!count[i])
-                continue;
-            uint64_t got[16];
-            if (!tc_cu_check(cudaMemcpy(got, (uint64_t *)args.list + (w0 + i) * 16,
-                                        (size_t)count[i] * 8, cudaMemcpyDeviceToHost),
-                             "hits", err, errlen))
-                return 0;
-            for (uint32_t k = 0; k < count[i]; k++)
-                cuda_enum_add_hit(r, got[k]);
         }
+        for (uint64_t i = 0; i < n; i++)
+            for (uint32_t k = 0; k < count[i]; k++)
+                cuda_enum_add_hit(r, got[i * 16 + k]);
     }
+    free(got);
     float ms = 0;
     cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
     r->seconds = ms / 1e3;

@@ -11,7 +11,6 @@ import os
 import subprocess
 import tempfile
 
-import numpy as np
 import pytest
 
 import tesseract_gb300 as T
@@ -25,6 +24,36 @@ void tc_host_words(unsigned long long first, unsigned long long n, unsigned *out
 {
     for (unsigned long long i = 0; i < n; i++)
         out[i] = tc_word(first + i);
+}
+
+/* every word of the space: the hit count and the 16 smallest hits, each hit's enumeration index
+   y = 32 word + lane mapped back to its assignment by tc_unperm */
+void tc_host_enum(unsigned long long words, unsigned long long space, unsigned long long *count,
+                  unsigned long long *first, int *nfirst)
+{
+    unsigned long long c = 0;
+    int nf = 0;
+    for (unsigned long long w = 0; w < words; w++) {
+        unsigned m = tc_word(w);
+        if (space < 32)
+            m &= (1u << space) - 1u;
+        while (m) {
+            const int l = __builtin_ctz(m);
+            m &= m - 1u;
+            c++;
+            const unsigned long long x = tc_unperm((w << 5) | (unsigned long long)l);
+            if (nf < 16 || x < first[15]) {
+                int i = nf < 16 ? nf++ : 15;
+                while (i > 0 && first[i - 1] > x) {
+                    first[i] = first[i - 1];
+                    i--;
+                }
+                first[i] = x;
+            }
+        }
+    }
+    *count = c;
+    *nfirst = nf;
 }
 """
 
@@ -47,24 +76,13 @@ def host_words(src: str):
 def emulate(mode, a, b, spec, kw):
     src = T.codegen_enum_source(mode, a, b, spec, kw["ticks"])
     L = host_words(src)
+    L.tc_host_enum.argtypes = [C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p]
     space = 1 << len(a.inputs)
     words = (space + 31) // 32
-    out = np.zeros(words, dtype=np.uint32)
-    L.tc_host_words(0, words, out.ctypes.data)
-    if space < 32:
-        out &= np.uint32((1 << space) - 1)
-    hits = int(sum(bin(int(w)).count("1") for w in out)) if words < 64 else \
-        int(np.unpackbits(out.view(np.uint8)).sum())
-    first = []
-    for w in np.nonzero(out)[0]:
-        v = int(out[w])
-        while v and len(first) < 16:
-            low = v & -v
-            first.append(int(w) * 32 + low.bit_length() - 1)
-            v ^= low
-        if len(first) >= 16:
-            break
-    return hits, first
+    count, nf = C.c_uint64(), C.c_int()
+    first = (C.c_uint64 * 16)()
+    L.tc_host_enum(words, space, C.byref(count), first, C.byref(nf))
+    return count.value, [int(first[i]) for i in range(nf.value)]
 
 
 @pytest.mark.parametrize("case", CASES, ids=[case_id(c) for c in CASES])
