@@ -353,6 +353,49 @@ static void choose_layout(Layout *L, size_t n, const uint64_t *sup, int norder)
     L->permuted = 1;
 }
 
+/* Is the spec a sum of a part that depends on no step input and a part that depends on no bit-lane
+   input (the x bits sigma puts on y bits 10..14 and 0..4)?  Then over a chunk's 32 steps each
+   lane's value is its value at step 0 plus a difference that is the same for all 32 lanes.  Sums,
+   differences, negations and complements of such specs are such specs; a product or a left shift
+   is one when neither factor has a bit-lane input while the other has a step input; a bitwise
+   and, or or xor when its operands together have bit-lane or step inputs but not both. */
+static int spec_separable(const TcSpec *s, const int *sigma)
+{
+    int dl[TS_MAX_STACK + 2], ds[TS_MAX_STACK + 2], ok[TS_MAX_STACK + 2], sp = 0;
+    for (int i = 0; i < s->nrpn; i++) {
+        const int op = s->rpn[i].op;
+        if (op == TS_NUM) {
+            dl[sp] = ds[sp] = 0;
+            ok[sp++] = 1;
+        } else if (op == TS_VAR) {
+            const int v = (int)s->rpn[i].v;
+            dl[sp] = ds[sp] = 0;
+            for (int b = 0; b < s->var_bits[v]; b++) {
+                const int q = sigma[s->var_pos[v][b]];
+                dl[sp] |= q < 5;
+                ds[sp] |= q >= 10 && q < 15;
+            }
+            ok[sp++] = 1;
+        } else if (op == TS_NOT || op == TS_NEG) {
+            continue;
+        } else if (op == TS_SHR || sp < 2) {
+            return 0;
+        } else {
+            const int a = sp - 2, b = sp - 1;
+            int k = ok[a] && ok[b];
+            if (op == TS_MUL || op == TS_SHL)
+                k = k && !(dl[a] && ds[b]) && !(ds[a] && dl[b]);
+            else if (op == TS_AND || op == TS_OR || op == TS_XOR)
+                k = k && !((dl[a] || dl[b]) && (ds[a] || ds[b]));
+            dl[a] |= dl[b];
+            ds[a] |= ds[b];
+            ok[a] = k;
+            sp--;
+        }
+    }
+    return sp == 1 && ok[0];
+}
+
 /* Input k as y bit q: a lane pattern for q < 5, else bit q - 5 of the word spread over all 32
    lanes (a shift up to the sign bit and an arithmetic shift down: two instructions; words fit
    32 bits up to 37 inputs). */
@@ -510,6 +553,43 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         for (size_t k = 0; k < a->noutputs; k++)
             emit(&inner, "    m |= %s ^ %s;\n", val_a[a->outputs[k]],
                  val_b[g->b->outputs[g->out_map[k]]]);
+    } else if (spec_fits_32(s) && spec_separable(s, L.sigma)) {
+        /* once per chunk: every lane's value at step 0, bit-sliced (32 words kept), and lane 0's;
+           each step: lane 0's value now minus at step 0 is every lane's difference d, added to
+           the bit-sliced values with one carry chain over the bits, each sum bit compared at once */
+        emit(&outer, "    const u64 xw = cword << 5;\n");
+        emit(&outer, "    const u64 brx = __brevll(xw);\n    (void)brx;\n");
+        for (int k = 0; k < s->nvars; k++)
+            emit_var_high(&outer, s, k, L.sigma);
+        emit(&outer, "    u32 e[32];\n");
+        for (int l = 0; l < 32; l++)
+            emit_lane(&outer, s, l, 1, L.sigma);
+        emit(&outer, "    const u32 sf0 = e[0];\n");
+        emit(&outer, "    tc_transpose32(e);\n");
+        emit(&fields, " u32 sf0;");
+        emit(&stores, "    v->sf0 = sf0;\n");
+        emit(&loads, "    const u32 sf0 = v->sf0;\n");
+        for (int b = 0; b < s->width; b++) {
+            emit(&outer, "    const u32 sp%d = e[%d];\n", b, b);
+            emit(&fields, " u32 sp%d;", b);
+            emit(&stores, "    v->sp%d = sp%d;\n", b, b);
+            emit(&loads, "    const u32 sp%d = v->sp%d;\n", b, b);
+        }
+        emit(&inner, "    const u64 xw = word << 5;\n");
+        emit(&inner, "    const u64 brx = __brevll(xw);\n    (void)brx;\n");
+        for (int k = 0; k < s->nvars; k++)
+            emit_var_high(&inner, s, k, L.sigma);
+        emit(&inner, "    u32 e[1];\n");
+        emit_lane(&inner, s, 0, 1, L.sigma);
+        emit(&inner, "    const u32 d = e[0] - sf0;\n");
+        emit(&inner, "    u32 m = 0u, c = 0u;\n    (void)c;\n");
+        for (int b = 0; b < s->width; b++) {
+            emit(&inner, "    {\n      const u32 q = (u32)((int)(d << %d) >> 31);\n", 31 - b);
+            emit(&inner, "      m |= %s ^ sp%d ^ q ^ c;\n", val_a[s->out[b]], b);
+            if (b + 1 < s->width)
+                emit(&inner, "      c = (sp%d & q) | (sp%d & c) | (q & c);\n", b, b);
+            emit(&inner, "    }\n");
+        }
     } else {
         int narrow = spec_fits_32(s);
         emit(&inner, "    const u64 xw = word << 5;\n");

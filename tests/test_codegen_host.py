@@ -99,3 +99,21 @@ def test_transpose_and_wide_spec_on_host():
     spec = T.Spec(p, "p = (a * b) >> 0 | ((a * b) >> 24 << 24)")
     hits, first = emulate(T.EN_VERIFY, p, None, spec, {"ticks": 1})
     assert hits == 0 and first == []
+
+
+@pytest.mark.parametrize("text", ["p = a * b", "p = a * b + a", "p = a * b - 3 * a + 1",
+                                  "p = a * b ^ 1"])
+def test_hoisted_chunk_and_spec_on_host(text):
+    """A 12 x 12 multiplier (24 inputs) takes the permuted layout: b's last rows change per step,
+    the rest of the LUTs run once per chunk; specs that are a sum of a step part and a lane part
+    are bit-sliced once per chunk and advanced by one difference per step.  The hits and the 16
+    smallest equal the oracle's."""
+    import oracle as O
+    p = T.Program.gen_mul(12)
+    spec = T.Spec(p, text)
+    src = T.codegen_enum_source(T.EN_VERIFY, p, None, spec, 1)
+    assert "#define TC_PERMUTED 1" in src
+    assert ("const u32 d = e[0] - sf0;" in src) == (text != "p = a * b ^ 1")
+    hits, first = emulate(T.EN_VERIFY, p, None, spec, {"ticks": 1})
+    want = O.enum_run(T.EN_VERIFY, p, spec=spec)
+    assert hits == want["hits"] and first == want["hit"]
