@@ -456,6 +456,16 @@ def main():
     assert all(h == 0 for h in results), "verify found mismatches"
     if rank != 0:
         return 0
+    # a negative control outside the timed region: a wrong spec of the same shape must fail on
+    # exactly the assignments where a != 0, so the kernel visibly checks every assignment
+    control = None
+    if args.share == 1:
+        cs = T.Spec(p, "p = a * b + a")
+        cr = T.enum_run(T.EN_VERIFY, p, spec=cs)
+        want = (1 << 32) - (1 << 16)
+        control = {"spec": "p = a * b + a", "hits": cr["hits"], "expected": want,
+                   "first_hits": cr["hit"][:4], "ok": cr["hits"] == want}
+        assert control["ok"], control
     value = world * ops / kernel_s
     e2e = world * ops / wall
     per_launch = ops / args.steps / (kernel_s / args.steps)
@@ -471,7 +481,7 @@ def main():
                    "l2": "no DRAM inputs: cell state lives in registers and every input word is "
                          "derived from the lane index, so there is nothing to flush",
                    "device": info, "parallelism": f"replicas x{world}"},
-        "result": {"mismatches": 0, "tried_per_step": r["tried"]},
+        "result": {"mismatches": 0, "tried_per_step": r["tried"], "negative_control": control},
         "roofline": {"bound": "alu-lop3", "achieved": per_launch, "peak": peak_lane_ops,
                      "unit": "lane-op/s", "frac": per_launch / peak_lane_ops,
                      "peak_source": "measured: cuda_lop3_peak microbenchmark on this GPU "

@@ -50,7 +50,7 @@ def rank_main(rank, world, port, out):
 @pytest.mark.parametrize("world", [2, 3])
 def test_shares_over_gloo_merge_to_the_whole(world):
     port = free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:  # no fork after the GPU is in use
         out = mgr.dict()
         mp.spawn(rank_main, args=(world, port, out), nprocs=world, join=True)
         results = dict(out)
