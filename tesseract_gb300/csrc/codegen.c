@@ -291,7 +291,7 @@ typedef struct {
     uint64_t inner;     /* inputs (bit k) that change between steps */
 } Layout;
 
-#define SPLIT_MAX_FIELDS 48   /* values kept across the steps: registers */
+#define SPLIT_MAX_FIELDS 64   /* values kept across the steps: registers */
 
 static int popcount64(uint64_t v)
 {

@@ -51,6 +51,18 @@ def test_hoisted_kernels_equal_oracle(text, parts):
         assert same_result(got, want), (text, part, got, want)
 
 
+@pytest.mark.parametrize("text", ["p = a * b", "p = a * b + 1"])
+def test_hoisted_kernels_40_inputs_on_shares(text):
+    """A 20 x 20 multiplier (40 inputs: words past 32 bits) with the chunk-invariant LUTs hoisted,
+    run on a few of 2^20 shares (32 chunks each) and compared with the oracle's same shares."""
+    p = T.Program.gen_mul(20)
+    spec = T.Spec(p, text)
+    for part in (0, 7, (1 << 20) - 1):
+        got = T.enum_run(T.EN_VERIFY, p, spec=spec, part=part, parts=1 << 20)
+        want = O.enum_run(T.EN_VERIFY, p, spec=spec, part=part, parts=1 << 20)
+        assert same_result(got, want), (text, part, got, want)
+
+
 def test_mul16_verify_full_space():
     p = T.Program.gen_mul(16)
     r = T.enum_run(T.EN_VERIFY, p, spec=T.Spec(p, "p = a * b"))
