@@ -359,21 +359,29 @@ static void choose_layout(Layout *L, size_t n, const uint64_t *sup, int norder)
    differences, negations and complements of such specs are such specs; a product or a left shift
    is one when neither factor has a bit-lane input while the other has a step input; a bitwise
    and, or or xor when its operands together have bit-lane or step inputs but not both. */
-static int spec_separable(const TcSpec *s, const int *sigma)
+static int spec_separable(const TcSpec *s, const int *sigma, int *step_tz)
 {
-    int dl[TS_MAX_STACK + 2], ds[TS_MAX_STACK + 2], ok[TS_MAX_STACK + 2], sp = 0;
+    /* tz: low bits known zero in the part that depends on step inputs (64: no such part) */
+    int dl[TS_MAX_STACK + 2], ds[TS_MAX_STACK + 2], ok[TS_MAX_STACK + 2], tz[TS_MAX_STACK + 2];
+    int sp = 0;
     for (int i = 0; i < s->nrpn; i++) {
         const int op = s->rpn[i].op;
         if (op == TS_NUM) {
             dl[sp] = ds[sp] = 0;
+            tz[sp] = 64;
             ok[sp++] = 1;
         } else if (op == TS_VAR) {
             const int v = (int)s->rpn[i].v;
             dl[sp] = ds[sp] = 0;
+            tz[sp] = 64;
             for (int b = 0; b < s->var_bits[v]; b++) {
                 const int q = sigma[s->var_pos[v][b]];
                 dl[sp] |= q < 5;
-                ds[sp] |= q >= 10 && q < 15;
+                if (q >= 10 && q < 15) {
+                    ds[sp] = 1;
+                    if (b < tz[sp])
+                        tz[sp] = b;
+                }
             }
             ok[sp++] = 1;
         } else if (op == TS_NOT || op == TS_NEG) {
@@ -382,17 +390,28 @@ static int spec_separable(const TcSpec *s, const int *sigma)
             return 0;
         } else {
             const int a = sp - 2, b = sp - 1;
-            int k = ok[a] && ok[b];
-            if (op == TS_MUL || op == TS_SHL)
+            int k = ok[a] && ok[b], t = tz[a] < tz[b] ? tz[a] : tz[b];
+            if (op == TS_MUL || op == TS_SHL) {
                 k = k && !(dl[a] && ds[b]) && !(ds[a] && dl[b]);
-            else if (op == TS_AND || op == TS_OR || op == TS_XOR)
+                /* x * y: the step part is (step part of one) * (the other), so its low zeros are
+                   at least the step part's; a left shift by a constant c adds c */
+                t = ds[a] ? tz[a] : tz[b];
+                if (op == TS_SHL && ds[a] && i > 0 && s->rpn[i - 1].op == TS_NUM)
+                    t += (int)(s->rpn[i - 1].v < 64 ? s->rpn[i - 1].v : 64);
+                if (ds[a] && ds[b])
+                    t = 0;
+            } else if (op == TS_AND || op == TS_OR || op == TS_XOR) {
                 k = k && !((dl[a] || dl[b]) && (ds[a] || ds[b]));
+                t = 0;  /* a bitwise part is not a sum: no known zeros claimed */
+            }
             dl[a] |= dl[b];
             ds[a] |= ds[b];
+            tz[a] = t > 64 ? 64 : t;
             ok[a] = k;
             sp--;
         }
     }
+    *step_tz = sp == 1 ? tz[0] : 0;
     return sp == 1 && ok[0];
 }
 
@@ -419,6 +438,7 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
     for (int j = 0; j < 64; j++)
         L.sigma[j] = j;
     Src outer = {0}, inner = {0}, fields = {0}, stores = {0}, loads = {0};
+    int step_tz = 0;
     /* the cells compared, as (program, cell) pairs: a first */
     char (*val_a)[24] = tc_xcalloc(a->ncells + 1, sizeof *val_a);
     char (*val_b)[24] = tc_xcalloc((g->b ? g->b->ncells : 0) + 1, sizeof *val_b);
@@ -553,7 +573,7 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         for (size_t k = 0; k < a->noutputs; k++)
             emit(&inner, "    m |= %s ^ %s;\n", val_a[a->outputs[k]],
                  val_b[g->b->outputs[g->out_map[k]]]);
-    } else if (spec_fits_32(s) && spec_separable(s, L.sigma)) {
+    } else if (spec_fits_32(s) && spec_separable(s, L.sigma, &step_tz)) {
         /* once per chunk: every lane's value at step 0, bit-sliced (32 words kept), and lane 0's;
            each step: lane 0's value now minus at step 0 is every lane's difference d, added to
            the bit-sliced values with one carry chain over the bits, each sum bit compared at once */
@@ -582,8 +602,13 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         emit(&inner, "    u32 e[1];\n");
         emit_lane(&inner, s, 0, 1, L.sigma);
         emit(&inner, "    const u32 d = e[0] - sf0;\n");
-        emit(&inner, "    u32 m = 0u, c = 0u;\n    (void)c;\n");
+        emit(&inner, "    u32 m = 0u, c = 0u;\n    (void)c;\n    (void)d;\n");
+        /* below bit step_tz, d is known to be zero: no carry, the sum bit is the kept one */
         for (int b = 0; b < s->width; b++) {
+            if (b < step_tz) {
+                emit(&inner, "    m |= %s ^ sp%d;\n", val_a[s->out[b]], b);
+                continue;
+            }
             emit(&inner, "    {\n      const u32 q = (u32)((int)(d << %d) >> 31);\n", 31 - b);
             emit(&inner, "      m |= %s ^ sp%d ^ q ^ c;\n", val_a[s->out[b]], b);
             if (b + 1 < s->width)

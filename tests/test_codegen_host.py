@@ -102,7 +102,7 @@ def test_transpose_and_wide_spec_on_host():
 
 
 @pytest.mark.parametrize("text", ["p = a * b", "p = a * b + a", "p = a * b - 3 * a + 1",
-                                  "p = a * b ^ 1"])
+                                  "p = a * b ^ 1", "p = a * b << 3", "p = a * b * 3 - b"])
 def test_hoisted_chunk_and_spec_on_host(text):
     """A 12 x 12 multiplier (24 inputs) takes the permuted layout: b's last rows change per step,
     the rest of the LUTs run once per chunk; specs that are a sum of a step part and a lane part

@@ -37,7 +37,8 @@ def test_gpu_equals_oracle_on_random_equivalences():
 
 
 @pytest.mark.parametrize("text", ["p = a * b", "p = a * b + a", "p = a * b - 3 * a + 1",
-                                  "p = a * b ^ 1", "p = (a + 1) * b"])
+                                  "p = a * b ^ 1", "p = (a + 1) * b", "p = a * b << 3",
+                                  "p = a * b * 3 - b"])
 @pytest.mark.parametrize("parts", [1, 3])
 def test_hoisted_kernels_equal_oracle(text, parts):
     """A 12 x 12 multiplier (24 inputs) runs in the permuted order with the chunk-invariant LUTs
