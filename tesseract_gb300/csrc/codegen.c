@@ -289,6 +289,7 @@ typedef struct {
     int      permuted;  /* 1: sigma is not the identity */
     int      sigma[64];
     uint64_t inner;     /* inputs (bit k) that change between steps */
+    int      step_bits; /* a stretch of 2^step_bits steps shares the hoisted values */
 } Layout;
 
 #define SPLIT_MAX_FIELDS 64   /* values kept across the steps: registers */
@@ -315,41 +316,65 @@ static uint64_t input_bit(size_t n, int j)  /* the input on x bit j */
     return 1ull << (n - 1 - (size_t)j);
 }
 
-/* Picks the inputs that change within a chunk (greedily, the 5 among x bits 0..14 that leave the
-   most LUTs invariant, or the identity's if that is as good) and sigma. */
-static void choose_layout(Layout *L, size_t n, const uint64_t *sup, int norder)
+/* Picks how many steps a stretch of words takes (2^sb, sb = 3, 4 or 5) and the sb inputs that
+   change between them: for each sb, greedily the ones among x bits 0..9+sb that leave the most
+   LUTs invariant (or the identity's, x bits 10..9+sb, if that is as good), then the sb whose
+   estimated work per word is least: the LUTs that change per step, plus the invariant ones and
+   `outer_extra` (what else runs once per stretch) spread over its 2^sb steps.  Measured on mul16
+   with the spec hoisted: 2.64 ms per 2^32 at sb = 4, 2.67 at 3, 2.77 at 5; the estimate picks 4. */
+static void choose_layout(Layout *L, size_t n, const uint64_t *sup, int norder, int outer_extra)
 {
     memset(L, 0, sizeof *L);
     for (int j = 0; j < 64; j++)
         L->sigma[j] = j;
-    if (n < 15 || norder == 0)
+    L->step_bits = 5;
+    if (n < 13 || norder == 0)
         return;
-    uint64_t id = 0, best = 0;
-    for (int j = 10; j < 15; j++)
-        id |= input_bit(n, j);
-    for (int step = 0; step < 5; step++) {
-        int bj = -1, bc = -1;
-        for (int j = 0; j < 15; j++) {
-            uint64_t m = input_bit(n, j);
-            if (best & m)
-                continue;
-            int c = invariant_luts(sup, norder, best | m);
-            if (c > bc) {
-                bc = c;
-                bj = j;
+    double best_cost = 0;
+    uint64_t best_set = 0;
+    int best_sb = 0, best_perm = 0;
+    for (int sb = 5; sb >= 3; sb--) {
+        const int top = 10 + sb;  /* x bits 0..top-1 may move */
+        if ((int)n < top)
+            continue;
+        uint64_t id = 0, set = 0;
+        for (int j = 10; j < top; j++)
+            id |= input_bit(n, j);
+        for (int step = 0; step < sb; step++) {
+            int bj = -1, bc = -1;
+            for (int j = 0; j < top; j++) {
+                uint64_t m = input_bit(n, j);
+                if (set & m)
+                    continue;
+                int c = invariant_luts(sup, norder, set | m);
+                if (c > bc) {
+                    bc = c;
+                    bj = j;
+                }
             }
+            set |= input_bit(n, bj);
         }
-        best |= input_bit(n, bj);
+        if (invariant_luts(sup, norder, set) <= invariant_luts(sup, norder, id))
+            set = id;
+        const int inv = invariant_luts(sup, norder, set);
+        const double cost = (norder - inv) + (double)(inv + outer_extra) / (1 << sb);
+        if (!best_sb || cost < best_cost) {
+            best_cost = cost;
+            best_set = set;
+            best_sb = sb;
+            best_perm = set != id;
+        }
     }
-    if (invariant_luts(sup, norder, best) <= invariant_luts(sup, norder, id))
-        best = id;
-    L->inner = best;
-    if (best == id)
+    if (!best_sb)
         return;
-    /* x bits 0..14: the chosen 5 to y bits 10..14, the rest in order to y bits 0..9 */
+    L->inner = best_set;
+    L->step_bits = best_sb;
+    if (!best_perm)
+        return;
+    /* x bits 0..9+sb: the chosen sb to y bits 10..9+sb, the rest in order to y bits 0..9 */
     int next_lane = 0, next_step = 10;
-    for (int j = 0; j < 15; j++)
-        L->sigma[j] = (best & input_bit(n, j)) ? next_step++ : next_lane++;
+    for (int j = 0; j < 10 + best_sb; j++)
+        L->sigma[j] = (best_set & input_bit(n, j)) ? next_step++ : next_lane++;
     L->permuted = 1;
 }
 
@@ -359,7 +384,7 @@ static void choose_layout(Layout *L, size_t n, const uint64_t *sup, int norder)
    differences, negations and complements of such specs are such specs; a product or a left shift
    is one when neither factor has a bit-lane input while the other has a step input; a bitwise
    and, or or xor when its operands together have bit-lane or step inputs but not both. */
-static int spec_separable(const TcSpec *s, const int *sigma, int *step_tz)
+static int spec_separable(const TcSpec *s, const int *sigma, int step_bits, int *step_tz)
 {
     /* tz: low bits known zero in the part that depends on step inputs (64: no such part) */
     int dl[TS_MAX_STACK + 2], ds[TS_MAX_STACK + 2], ok[TS_MAX_STACK + 2], tz[TS_MAX_STACK + 2];
@@ -377,7 +402,7 @@ static int spec_separable(const TcSpec *s, const int *sigma, int *step_tz)
             for (int b = 0; b < s->var_bits[v]; b++) {
                 const int q = sigma[s->var_pos[v][b]];
                 dl[sp] |= q < 5;
-                if (q >= 10 && q < 15) {
+                if (q >= 10 && q < 10 + step_bits) {
                     ds[sp] = 1;
                     if (b < tz[sp])
                         tz[sp] = b;
@@ -437,6 +462,7 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
     memset(&L, 0, sizeof L);
     for (int j = 0; j < 64; j++)
         L.sigma[j] = j;
+    L.step_bits = 5;
     Src outer = {0}, inner = {0}, fields = {0}, stores = {0}, loads = {0};
     int step_tz = 0;
     /* the cells compared, as (program, cell) pairs: a first */
@@ -479,7 +505,9 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
             nsup[order[i]] = nsup[lv[i][0]] | nsup[lv[i][1]] | nsup[lv[i][2]];
             sup[i] = nsup[order[i]];
         }
-        choose_layout(&L, n, sup, norder);
+        /* once per stretch besides the LUTs: a verify's per-lane spec and transpose */
+        const int outer_extra = g->mode == EN_VERIFY ? 64 * s->nrpn + 256 : 0;
+        choose_layout(&L, n, sup, norder, outer_extra);
         /* values of the chunk read by the steps: kept in TcInv */
         char *field = tc_xcalloc((size_t)size + 1, 1);
         int nfields = 0;
@@ -504,6 +532,7 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         if (!L.split) {
             memset(field, 0, (size_t)size + 1);
             L.permuted = 0;
+            L.step_bits = 5;
             for (int j = 0; j < 64; j++)
                 L.sigma[j] = j;
         }
@@ -573,7 +602,7 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         for (size_t k = 0; k < a->noutputs; k++)
             emit(&inner, "    m |= %s ^ %s;\n", val_a[a->outputs[k]],
                  val_b[g->b->outputs[g->out_map[k]]]);
-    } else if (spec_fits_32(s) && spec_separable(s, L.sigma, &step_tz)) {
+    } else if (spec_fits_32(s) && spec_separable(s, L.sigma, L.step_bits, &step_tz)) {
         /* once per chunk: every lane's value at step 0, bit-sliced (32 words kept), and lane 0's;
            each step: lane 0's value now minus at step 0 is every lane's difference d, added to
            the bit-sliced values with one carry chain over the bits, each sum bit compared at once */
@@ -644,8 +673,11 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
     emit(o, "TC_DEV u32 tc_inner(const u64 word, const TcInv *v)\n{\n");
     emit(o, "    const u32 wlo = (u32)word;\n    (void)wlo;\n    (void)v;\n");
     emit(o, "%s%s    return m;\n}\n", loads.len ? loads.s : "", inner.s);
+    /* a stretch: 2^TC_STEP_BITS steps of 32 words, word bits 5 .. 4 + TC_STEP_BITS */
+    emit(o, "#define TC_STEP_BITS %d\n#define TC_STEP_MASK ((32ull << TC_STEP_BITS) - 32ull)\n",
+         L.step_bits);
     emit(o, "TC_DEV u32 tc_word(const u64 word)\n{\n    TcInv v;\n"
-            "    tc_outer(word & ~992ull, &v);\n    return tc_inner(word, &v);\n}\n");
+            "    tc_outer(word & ~TC_STEP_MASK, &v);\n    return tc_inner(word, &v);\n}\n");
     /* y -> x: the assignment a hit at y stands for */
     emit(o, "#define TC_PERMUTED %d\n", L.permuted);
     emit(o, "TC_DEV u64 tc_unperm(const u64 y)\n{\n");
@@ -695,12 +727,13 @@ static const char *KERNEL =
     "    for (u64 s = s0; s < s1;) {\n"
     "        const u64 j = s >> 10;\n"
     "        const u64 chunk = a.nsel == a.parts ? j : (j / a.nsel) * a.parts + a.part + j % a.nsel;\n"
-    "        const u64 cbase = (chunk << 10) | lane;\n"
-    "        const u64 s_end = ((j + 1) << 10) < s1 ? ((j + 1) << 10) : s1;\n"
+    "        const u64 span = 32ull << TC_STEP_BITS;  /* words of a stretch */\n"
+    "        const u64 cbase = (chunk << 10) | (s & 992u & ~TC_STEP_MASK) | lane;\n"
+    "        const u64 s_end = (s / span + 1) * span < s1 ? (s / span + 1) * span : s1;\n"
     "        TcInv inv;\n"
-    "        tc_outer(cbase, &inv);  /* what stays the same for the chunk's 32 steps */\n"
+    "        tc_outer(cbase, &inv);  /* what stays the same for the stretch's steps */\n"
     "        for (; s < s_end; s += 32) {\n"
-    "        const u64 word = cbase | (s & 992u);  /* s is a multiple of 32 */\n"
+    "        const u64 word = cbase | (s & TC_STEP_MASK);  /* s is a multiple of 32 */\n"
     "        const u64 x0 = word << 5;\n"
     "        u32 valid = 0u;\n"
     "        if (s + lane < s1 && x0 < a.space)\n"
