@@ -488,12 +488,12 @@ def main():
                                     "(32-bit LOP3/s x 32 lanes)",
                      "lop3_per_s": lop3,
                      # DRAM bytes (read + write) of one full-space launch, from the ncu capture
-                     # summarised in profiles/tc_enum_verify_mul16.md (ALU pipe 96.7 % busy there)
+                     # summarised in profiles/tc_enum_verify_mul16.md (ALU pipe 97.3 % busy there)
                      "traffic": VERIFY_DRAM_BYTES if args.share == 1 else None,
-                     "traffic_unit": "bytes per launch", "alu_pipe_busy_ncu": 0.967,
+                     "traffic_unit": "bytes per launch", "alu_pipe_busy_ncu": 0.973,
                      "note": "achieved counts the reference's 6,040 NAND/STO lane-ops per "
-                             "assignment; the kernel issues 720 LOP3 for them, 485 of those once "
-                             "per 32 steps, so frac exceeds 1; the machine-level figure is "
+                             "assignment; the kernel issues 720 LOP3 for them, 532 of those once "
+                             "per 16 steps, so frac exceeds 1; the machine-level figure is "
                              "alu_pipe_busy_ncu (integer ALU pipe, share of its sustained peak)"},
         "kernel": {"regs": stats["regs"], "local_bytes": stats["local_bytes"],
                    "grid": stats["grid"], "block": stats["block"],
