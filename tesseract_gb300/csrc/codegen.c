@@ -275,17 +275,18 @@ static void emit_lane(Src *o, const TcSpec *s, int l, int narrow, const int *sig
 /* ---- one enumeration kernel -------------------------------------------------------------- */
 
 /* Where the assignment bits come from.  The kernel enumerates y = 32 word + lane: y bits 0..4 are
-   the bit lane (constant patterns), 5..9 the thread's lane in its warp, 10..14 the 32 steps a
-   warp takes through one chunk of 1,024 words, 15 and up the chunk.  Assignment x has y bit
-   sigma[j] at its bit j (input k is x bit n-1-k).  Only the 5 inputs on y bits 10..14 change
-   from step to step within a chunk: every LUT that depends on none of them is computed once per
-   chunk (tc_outer) and kept in registers for the 32 steps (tc_inner).  The identity puts x bits
-   10..14 there; when 5 other inputs among x bits 0..14 leave more LUTs out of the steps (an
-   array multiplier's last rows, say, whose inputs are the low x bits), sigma moves those 5 onto
-   y bits 10..14 and the x bits it displaces onto the lanes.  x bits 15 and up never move, so a
-   chunk is the same set of assignments either way and the reference's --part shares hold. */
+   the bit lane (constant patterns), 5..9 the thread's lane in its warp, 10..9+sb the 2^sb steps
+   a warp takes through one stretch of a chunk of 1,024 words (sb = step_bits: 3, 4 or 5), the
+   bits above that the stretch and the chunk.  Assignment x has y bit sigma[j] at its bit j
+   (input k is x bit n-1-k).  Only the sb inputs on the step bits change from step to step: every
+   LUT that depends on none of them is computed once per stretch (tc_outer) and kept in registers
+   for its steps (tc_inner).  The identity puts x bits 10..9+sb there; when other inputs among x
+   bits 0..9+sb leave more LUTs out of the steps (an array multiplier's last rows, say, whose
+   inputs are the low x bits), sigma moves those onto the step bits and the x bits it displaces
+   onto the lanes.  x bits 15 and up never move, so a chunk is the same set of assignments
+   either way and the reference's --part shares hold. */
 typedef struct {
-    int      split;     /* 1: the chunk-invariant LUTs are hoisted */
+    int      split;     /* 1: the stretch-invariant LUTs are hoisted */
     int      permuted;  /* 1: sigma is not the identity */
     int      sigma[64];
     uint64_t inner;     /* inputs (bit k) that change between steps */
@@ -379,8 +380,8 @@ static void choose_layout(Layout *L, size_t n, const uint64_t *sup, int norder, 
 }
 
 /* Is the spec a sum of a part that depends on no step input and a part that depends on no bit-lane
-   input (the x bits sigma puts on y bits 10..14 and 0..4)?  Then over a chunk's 32 steps each
-   lane's value is its value at step 0 plus a difference that is the same for all 32 lanes.  Sums,
+   input (the x bits sigma puts on the step bits and on y bits 0..4)?  Then over a stretch's steps
+   each lane's value is its value at step 0 plus a difference that is the same for all 32 lanes.  Sums,
    differences, negations and complements of such specs are such specs; a product or a left shift
    is one when neither factor has a bit-lane input while the other has a step input; a bitwise
    and, or or xor when its operands together have bit-lane or step inputs but not both. */
@@ -563,7 +564,7 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
                 emit(&stores, "    v->%s = %s;\n", f, f);
                 emit(&loads, "    const u32 %s = v->%s;\n", f, f);
             }
-        emit(&inner, "    // %d LOP3 for %zu + %zu NAND/STO instructions, %d of them once per chunk\n",
+        emit(&inner, "    // %d LOP3 for %zu + %zu NAND/STO instructions, %d of them once per stretch\n",
              luts, a->len, g->b ? g->b->len : (size_t)0, L.split ? hoisted : 0);
         for (uint32_t c = 0; c < a->ncells; c++)
             node_name(val_a[c], sizeof val_a[c], net, cur_a[c]);
@@ -603,7 +604,7 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
             emit(&inner, "    m |= %s ^ %s;\n", val_a[a->outputs[k]],
                  val_b[g->b->outputs[g->out_map[k]]]);
     } else if (spec_fits_32(s) && spec_separable(s, L.sigma, L.step_bits, &step_tz)) {
-        /* once per chunk: every lane's value at step 0, bit-sliced (32 words kept), and lane 0's;
+        /* once per stretch: every lane's value at step 0, bit-sliced (32 words kept), and lane 0's;
            each step: lane 0's value now minus at step 0 is every lane's difference d, added to
            the bit-sliced values with one carry chain over the bits, each sum bit compared at once */
         emit(&outer, "    const u64 xw = cword << 5;\n");
@@ -704,7 +705,7 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
 /* The kernel template: each warp takes a contiguous run of the selected words (a multiple of 32),
    32 words per step, one per lane.  Words are selected in chunks of 1024 (64 passes of 512
    lanes, the reference's hand-out unit, src/enum.c:11), chunk c belonging to share c % parts
-   (src/enum.c:232-234); a chunk's invariant LUTs are computed once before its 32 steps.  Hits
+   (src/enum.c:232-234); a stretch's invariant LUTs are computed once before its steps.  Hits
    are counted with popcount; each warp's 16 smallest hits go to list[warp]: its first 16 when
    the order is the identity (the warp's assignments rise), else a sorted insertion. */
 static const char *KERNEL =

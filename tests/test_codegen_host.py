@@ -105,8 +105,8 @@ def test_transpose_and_wide_spec_on_host():
                                   "p = a * b ^ 1", "p = a * b << 3", "p = a * b * 3 - b"])
 def test_hoisted_chunk_and_spec_on_host(text):
     """A 12 x 12 multiplier (24 inputs) takes the permuted layout: b's last rows change per step,
-    the rest of the LUTs run once per chunk; specs that are a sum of a step part and a lane part
-    are bit-sliced once per chunk and advanced by one difference per step.  The hits and the 16
+    the rest of the LUTs run once per stretch; specs that are a sum of a step part and a lane part
+    are bit-sliced once per stretch and advanced by one difference per step.  The hits and the 16
     smallest equal the oracle's."""
     import oracle as O
     p = T.Program.gen_mul(12)

@@ -41,7 +41,7 @@ def test_gpu_equals_oracle_on_random_equivalences():
                                   "p = a * b * 3 - b"])
 @pytest.mark.parametrize("parts", [1, 3])
 def test_hoisted_kernels_equal_oracle(text, parts):
-    """A 12 x 12 multiplier (24 inputs) runs in the permuted order with the chunk-invariant LUTs
+    """A 12 x 12 multiplier (24 inputs) runs in the permuted order with the stretch-invariant LUTs
     hoisted; the separable specs also take the bit-sliced difference path.  Hit counts, the 16
     smallest hits (sorted insertion per warp) and shares equal the oracle's."""
     p = T.Program.gen_mul(12)
@@ -54,7 +54,7 @@ def test_hoisted_kernels_equal_oracle(text, parts):
 
 @pytest.mark.parametrize("text", ["p = a * b", "p = a * b + 1"])
 def test_hoisted_kernels_40_inputs_on_shares(text):
-    """A 20 x 20 multiplier (40 inputs: words past 32 bits) with the chunk-invariant LUTs hoisted,
+    """A 20 x 20 multiplier (40 inputs: words past 32 bits) with the stretch-invariant LUTs hoisted,
     run on a few of 2^20 shares (32 chunks each) and compared with the oracle's same shares."""
     p = T.Program.gen_mul(20)
     spec = T.Spec(p, text)
