@@ -37,17 +37,32 @@ __device__ __forceinline__ uint64_t splitmix_nth(uint64_t s, uint64_t n)
     return mix64(s + n * GOLDEN);
 }
 
+__device__ __forceinline__ uint32_t run_one(uint32_t *S, uint32_t in, uint32_t r)
+{
+    uint32_t *cell = S + (in >> 1) * T1_THREADS;
+    if (in & 1u)
+        *cell = r;
+    else
+        r = ~(r & *cell);
+    return r;
+}
+
+// One pass; the instructions are read four at a time (one 16-byte shared-memory load; the code
+// starts the block's dynamic shared memory, so it is 16-byte aligned).
 __device__ __forceinline__ uint32_t run_pass(uint32_t *S, const uint32_t *code, uint32_t len,
                                              uint32_t r)
 {
-    for (uint32_t i = 0; i < len; i++) {
-        const uint32_t in = code[i];
-        uint32_t *cell = S + (in >> 1) * T1_THREADS;
-        if (in & 1u)
-            *cell = r;
-        else
-            r = ~(r & *cell);
+    const uint4 *code4 = (const uint4 *)code;
+    uint32_t i = 0;
+    for (; i + 4 <= len; i += 4) {
+        const uint4 q = code4[i >> 2];
+        r = run_one(S, q.x, r);
+        r = run_one(S, q.y, r);
+        r = run_one(S, q.z, r);
+        r = run_one(S, q.w, r);
     }
+    for (; i < len; i++)
+        r = run_one(S, code[i], r);
     return r;
 }
 
@@ -61,7 +76,7 @@ __device__ __forceinline__ int bucket(uint64_t lam)
 
 __global__ void __launch_bounds__(T1_THREADS) tc_t1_kernel(TcT1Dev d)
 {
-    extern __shared__ uint32_t smem[];
+    extern __shared__ __align__(16) uint32_t smem[];
     __shared__ unsigned long long hist[T1_BUCKETS];
     const uint32_t j = threadIdx.x;
     const uint64_t k = d.k0 + blockIdx.x;
