@@ -63,3 +63,20 @@ def case_id(c):
     if "ticks" in c:
         s += "-ticks%d" % c["ticks"]
     return s
+
+
+def random_spec(r, depth: int = 3) -> str:
+    """A random right side over a, b and small constants with + - * ^ & | << ~ and negation
+    (the spec language's operators), for differential tests of the spec paths."""
+    def expr(d):
+        if d == 0 or r.random() < 0.25:
+            return r.choice(["a", "b", str(r.randrange(1, 9))])
+        op = r.choice(["+", "-", "*", "^", "&", "|", "<<", "~", "neg"])
+        if op == "~":
+            return "~(" + expr(d - 1) + ")"
+        if op == "neg":
+            return "-(" + expr(d - 1) + ")"
+        if op == "<<":
+            return "(" + expr(d - 1) + ") << " + str(r.randrange(0, 4))
+        return "(" + expr(d - 1) + " " + op + " " + expr(d - 1) + ")"
+    return "p = " + ("a * b + " if r.random() < 0.7 else "") + expr(depth)

@@ -117,3 +117,20 @@ def test_hoisted_chunk_and_spec_on_host(text):
     hits, first = emulate(T.EN_VERIFY, p, None, spec, {"ticks": 1})
     want = O.enum_run(T.EN_VERIFY, p, spec=spec)
     assert hits == want["hits"] and first == want["hit"]
+
+
+def test_random_specs_on_host():
+    """Random specs on a 10 x 10 multiplier (20 inputs, permuted and hoisted): the separable ones
+    take the difference path, the rest the per-lane path; hits and the 16 smallest equal the
+    oracle's."""
+    import random
+    import oracle as O
+    from cases import random_spec
+    r = random.Random(2024)
+    p = T.Program.gen_mul(10)
+    for _ in range(10):
+        text = random_spec(r)
+        spec = T.Spec(p, text)
+        hits, first = emulate(T.EN_VERIFY, p, None, spec, {"ticks": 1})
+        want = O.enum_run(T.EN_VERIFY, p, spec=spec)
+        assert hits == want["hits"] and first == want["hit"], text

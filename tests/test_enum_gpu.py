@@ -64,6 +64,22 @@ def test_hoisted_kernels_40_inputs_on_shares(text):
         assert same_result(got, want), (text, part, got, want)
 
 
+def test_random_specs_equal_oracle():
+    """Forty random specs on a 12 x 12 multiplier (24 inputs, permuted and hoisted), whole space
+    and a 3-way share: the GPU's hits, 16 smallest and counts equal the oracle's."""
+    import random
+    from cases import random_spec
+    r = random.Random(77)
+    p = T.Program.gen_mul(12)
+    for i in range(40):
+        text = random_spec(r)
+        spec = T.Spec(p, text)
+        part, parts = (i % 3, 3) if i % 4 == 0 else (0, 1)
+        got = T.enum_run(T.EN_VERIFY, p, spec=spec, part=part, parts=parts)
+        want = O.enum_run(T.EN_VERIFY, p, spec=spec, part=part, parts=parts)
+        assert same_result(got, want), (text, got, want)
+
+
 def test_mul16_verify_full_space():
     p = T.Program.gen_mul(16)
     r = T.enum_run(T.EN_VERIFY, p, spec=T.Spec(p, "p = a * b"))
