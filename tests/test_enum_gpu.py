@@ -80,6 +80,23 @@ def test_random_specs_equal_oracle():
         assert same_result(got, want), (text, got, want)
 
 
+@pytest.mark.parametrize("bits", [10, 12])
+def test_hoisted_equiv_and_search_equal_oracle(bits):
+    """Equivalence of a multiplier with its identity-rewritten and mutated copies, and searches
+    for products, run with the hoisted (and permuted) layout: equal to the oracle."""
+    p = T.Program.gen_mul(bits)
+    for seed, mutate in ((3, False), (4, True), (5, True)):
+        q = p.rewrite(seed, mutate)
+        got = T.enum_run(T.EN_EQUIV, p, q)
+        want = O.enum_run(T.EN_EQUIV, p, q)
+        assert same_result(got, want), (bits, seed, mutate, got, want)
+    for target in (0, 77 * 91, (1 << (2 * bits)) - 1 - 5):
+        spec = T.Spec(p, "p = %d" % target, False)
+        got = T.enum_run(T.EN_SEARCH, p, spec=spec)
+        want = O.enum_run(T.EN_SEARCH, p, spec=spec)
+        assert same_result(got, want), (bits, target, got, want)
+
+
 def test_mul16_verify_full_space():
     p = T.Program.gen_mul(16)
     r = T.enum_run(T.EN_VERIFY, p, spec=T.Spec(p, "p = a * b"))
