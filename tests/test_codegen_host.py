@@ -134,3 +134,22 @@ def test_random_specs_on_host():
         hits, first = emulate(T.EN_VERIFY, p, None, spec, {"ticks": 1})
         want = O.enum_run(T.EN_VERIFY, p, spec=spec)
         assert hits == want["hits"] and first == want["hit"], text
+
+
+def test_hoisted_equiv_and_search_on_host():
+    """Equivalence with rewritten and mutated copies and searches for products on a 10 x 10
+    multiplier, in the hoisted (permuted) layout: equal to the oracle."""
+    import oracle as O
+    p = T.Program.gen_mul(10)
+    for seed, mutate in ((3, False), (4, True)):
+        q = p.rewrite(seed, mutate)
+        src = T.codegen_enum_source(T.EN_EQUIV, p, q, None, 1)
+        assert "#define TC_PERMUTED 1" in src
+        got = emulate(T.EN_EQUIV, p, q, None, {"ticks": 1})
+        want = O.enum_run(T.EN_EQUIV, p, q)
+        assert got == (want["hits"], want["hit"]), (seed, mutate)
+    for target in (0, 33 * 17, (1 << 20) - 6):
+        spec = T.Spec(p, "p = %d" % target, False)
+        got = emulate(T.EN_SEARCH, p, None, spec, {"ticks": 1})
+        want = O.enum_run(T.EN_SEARCH, p, spec=spec)
+        assert got == (want["hits"], want["hit"]), target
