@@ -21,8 +21,10 @@ typedef struct {
 } TcGenEnum;
 
 /* CUDA C for the enumeration kernel `tc_enum` (malloc'd; *len gets its length).  The per-word
-   function tc_word(word) -> hit mask is plain C when TC_HOST_EMULATION is defined, so the tests
-   can compile the same text for the host. */
+   functions are plain C when TC_HOST_EMULATION is defined, so the tests can compile the same
+   text for the host: tc_outer(cword, &inv) (what a stretch of steps shares), tc_inner(word, &inv)
+   -> hit mask, tc_word(word) (the two for one word) and tc_unperm(y) (the assignment that
+   enumeration index y stands for). */
 char *tc_codegen_enum(const TcGenEnum *g, size_t *len);
 
 /* CUDA C for the truth-table kernel `tc_table` of a program without id or link cells. */
