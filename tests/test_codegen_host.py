@@ -153,3 +153,20 @@ def test_hoisted_equiv_and_search_on_host():
         got = emulate(T.EN_SEARCH, p, None, spec, {"ticks": 1})
         want = O.enum_run(T.EN_SEARCH, p, spec=spec)
         assert got == (want["hits"], want["hit"]), target
+
+
+def test_layout_choice_for_multipliers():
+    """The generated enumeration code for gen mul 16: 720 LUTs, 532 of them once per stretch of
+    2^4 steps in a permuted order, the spec on the difference path with 12 carry-free low bits;
+    gen mul 20 (40-bit product) hoists its LUTs but keeps the per-lane spec."""
+    import re
+    p = T.Program.gen_mul(16)
+    src = T.codegen_enum_source(T.EN_VERIFY, p, None, T.Spec(p, "p = a * b"), 1)
+    assert re.search(r"// 720 LOP3 for 6040 \+ 0 NAND/STO instructions, 532 of them", src)
+    assert "#define TC_STEP_BITS 4" in src and "#define TC_PERMUTED 1" in src
+    assert "const u32 d = e[0] - sf0;" in src
+    assert len(re.findall(r"m \|= n\d+ \^ sp\d+;", src)) == 12
+    p = T.Program.gen_mul(20)
+    src = T.codegen_enum_source(T.EN_VERIFY, p, None, T.Spec(p, "p = a * b"), 1)
+    assert "#define TC_PERMUTED 1" in src and "sf0" not in src
+    assert int(re.search(r"NAND/STO instructions, (\d+) of them", src).group(1)) > 800
