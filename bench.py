@@ -488,7 +488,7 @@ def main():
                                     "(32-bit LOP3/s x 32 lanes)",
                      "lop3_per_s": lop3,
                      # DRAM bytes (read + write) of one full-space launch, from the ncu capture
-                     # summarised in profiles/tc_enum_verify_mul16.md (ALU pipe 97.3 % busy there)
+                     # of the same kernel (ALU pipe 97.3 % busy in that capture)
                      "traffic": VERIFY_DRAM_BYTES if args.share == 1 else None,
                      "traffic_unit": "bytes per launch", "alu_pipe_busy_ncu": 0.973,
                      "note": "achieved counts the reference's 6,040 NAND/STO lane-ops per "
