@@ -170,3 +170,24 @@ def test_layout_choice_for_multipliers():
     src = T.codegen_enum_source(T.EN_VERIFY, p, None, T.Spec(p, "p = a * b"), 1)
     assert "#define TC_PERMUTED 1" in src and "sf0" not in src
     assert int(re.search(r"NAND/STO instructions, (\d+) of them", src).group(1)) > 800
+
+
+def test_unperm_is_a_bijection_that_keeps_chunks():
+    """tc_unperm maps the kernel's enumeration index y to the assignment x: a bijection of the
+    space that moves no bit from 15 up, so every chunk of 32,768 assignments (the reference's
+    --part unit) is the same set either way."""
+    p = T.Program.gen_mul(10)
+    src = T.codegen_enum_source(T.EN_VERIFY, p, None, T.Spec(p, "p = a * b"), 1)
+    assert "#define TC_PERMUTED 1" in src
+    L = host_words(src + "\nunsigned long long tc_host_unperm(unsigned long long y) "
+                         "{ return tc_unperm(y); }\n")
+    L.tc_host_unperm.restype = C.c_uint64
+    L.tc_host_unperm.argtypes = [C.c_uint64]
+    seen = set()
+    for y in range(1 << 15):
+        x = L.tc_host_unperm(y)
+        assert x >> 15 == 0
+        seen.add(x)
+    assert len(seen) == 1 << 15
+    for y in (1 << 15, 5 << 15 | 12345, (1 << 20) - 1):
+        assert L.tc_host_unperm(y) >> 15 == y >> 15
