@@ -114,6 +114,12 @@ def cases():
         out.append({"mode": "verify", "a": mul(10), "spec": "p = a * b ^ 1", "part": part})
     # ticks > 1 on a combinational program: the same answer
     out.append({"mode": "verify", "a": mul(5), "spec": "p = a * b", "ticks": 3})
+    # specs that are a sum of a part without the fastest-changing inputs and a part without the
+    # lane inputs, on multipliers whose enumeration order the engine permutes
+    for spec in ["p = a * b + a", "p = a * b * 3 - b", "p = a * b << 3"]:
+        out.append({"mode": "verify", "a": mul(12), "spec": spec})
+    out.append({"mode": "verify", "a": mul(16), "spec": "p = a * b + a", "part": [5, 5, 4096]})
+    out.append({"mode": "verify", "a": mul(16), "spec": "p = a * b", "part": [0, 1, 4096]})
     # search: toy hash preimages (tests/test_work.c:322-376)
     for bits, rounds, x in ((3, 5, 5), (16, 5, 12345), (20, 8, 777), (24, 8, 0xabcdef)):
         out.append({"mode": "search", "a": {"kind": "hash", "params": {"bits": bits,
