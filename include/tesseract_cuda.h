@@ -220,7 +220,8 @@ int  cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, cha
    language, same SuperSpec.  cuda_super_search replaces super_search (src/super.c:821-896):
    iterative deepening over the budget from the same lower bound, the same chain-program model
    and pruning rules, every budget below the answer searched in full on the GPU, so `cost` and
-   `below` mean what they mean there (node counts differ: there is no transposition table).
+   `below` mean what they mean there.  Node counts differ: the search visits only children
+   within the bound, and its transposition table is one table shared by every warp.
    cuda_super_check replaces super_check (src/super.c:908-1001). */
 int  cuda_super_parse(const char *text, SuperSpec *sp, char *err, size_t errlen);
 int  cuda_super_search(const SuperSpec *sp, const SuperOpts *o, SuperResult *r, char *err,

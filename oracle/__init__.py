@@ -139,6 +139,17 @@ def have_reference() -> bool:
     return os.path.exists(REF_LIB) and os.path.exists(REF_BIN)
 
 
+def reference_sources() -> str | None:
+    """The reference's source tree that oracle/_ref was built from (oracle/Makefile records it
+    in oracle/_ref/SOURCE), when it is still present on this host; else None."""
+    rec = os.path.join(HERE, "_ref", "SOURCE")
+    if not os.path.exists(rec):
+        return None
+    with open(rec) as f:
+        path = f.read().strip()
+    return path if os.path.isdir(os.path.join(path, "src")) else None
+
+
 def ref_lib():
     global _ref
     if _ref is None:

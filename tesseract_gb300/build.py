@@ -28,6 +28,9 @@ BUILD = os.path.join(ROOT, "_build")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# The reference's source tree, for oracle/_ref (golden fixtures and the x86 CPU baseline only).
+# This build recipe is the one place that names where it is mounted; TESSERACT_REFERENCE
+# overrides it, and the step is skipped where the tree is absent (the GPU machine).
 REFERENCE = os.environ.get("TESSERACT_REFERENCE", "/root/reference")
 
 HOST_C = ["program", "asm", "spec", "gen", "lutmap", "codegen", "engine", "cube", "ref_host", "batch", "tester",

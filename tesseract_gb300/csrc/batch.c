@@ -735,9 +735,12 @@ int tc_wave_launch(TcWave *w, cudaStream_t stream, double share, char *err, size
     return 1;
 }
 
+/* The flag is read with acquire order: on a weakly ordered host (Grace is aarch64) the reads of
+   the job's counts and hit lists in host-mapped memory that tc_wave_result makes after it must
+   not be satisfied before the flag was seen set (the kernel fences them before the flag). */
 int tc_wave_job_done(const TcWave *w, int i)
 {
-    return w->h_done[i] != 0;
+    return __atomic_load_n((const uint32_t *)&w->h_done[i], __ATOMIC_ACQUIRE) != 0;
 }
 
 /* 1 when the wave's kernel has finished (0 still running, -1 error) */

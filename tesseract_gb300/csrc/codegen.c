@@ -710,13 +710,9 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
    the order is the identity (the warp's assignments rise), else a sorted insertion. */
 static const char *KERNEL =
     "#ifndef TC_HOST_EMULATION\n"
-    "struct TcEnumArgs {\n"
-    "    u64 words, space, per_warp;\n"
-    "    u32 parts, part, nsel, pad;\n"
-    "    u64 *hits;\n"
-    "    u64 *list;\n"
-    "    u32 *count;\n"
-    "};\n"
+    "struct TcEnumArgs {\n    "
+    TC_TEXT(TC_ENUM_ARGS_FIELDS(u64, u32))
+    "\n};\n"
     "extern \"C\" __global__ void __launch_bounds__(TC_BLOCK) tc_enum(const TcEnumArgs a)\n{\n"
     "    const u32 lane = threadIdx.x & 31u;\n"
     "    const u64 warp = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;\n"

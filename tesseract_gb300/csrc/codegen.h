@@ -20,6 +20,23 @@ typedef struct {
     int             no_map;     /* 1: keep the NAND/STO body as written (no LOP3 mapping) */
 } TcGenEnum;
 
+/* The argument block of the generated kernel `tc_enum`, in one place: the host launchers declare
+   TcEnumArgs from it with C's types, and tc_codegen_enum writes the same fields, as text, into the
+   generated source with its own names for the types (u64, u32), so the two layouts cannot drift
+   apart.  hits: one counter; list: 16 hits per warp; count: hits kept per warp. */
+#define TC_ENUM_ARGS_FIELDS(u64, u32)                                                       \
+    u64 words, space, per_warp;                                                             \
+    u32 parts, part, nsel, pad;                                                             \
+    u64 *hits;                                                                              \
+    u64 *list;                                                                              \
+    u32 *count;
+#define TC_TEXT_(...) #__VA_ARGS__
+#define TC_TEXT(...) TC_TEXT_(__VA_ARGS__)
+
+typedef struct {
+    TC_ENUM_ARGS_FIELDS(uint64_t, uint32_t)
+} TcEnumArgs;
+
 /* CUDA C for the enumeration kernel `tc_enum` (malloc'd; *len gets its length).  The per-word
    functions are plain C when TC_HOST_EMULATION is defined, so the tests can compile the same
    text for the host: tc_outer(cword, &inv) (what a stretch of steps shares), tc_inner(word, &inv)

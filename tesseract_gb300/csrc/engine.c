@@ -344,12 +344,6 @@ void tc_enum_shares(const Enum *e, uint64_t space, uint64_t *sel_chunks, uint64_
 }
 
 typedef struct {
-    uint64_t words, space, per_warp;
-    uint32_t parts, part, nsel, pad;
-    void    *hits, *list, *count;
-} EnumArgs;
-
-typedef struct {
     int       *in_map, *out_map;
     uint32_t  *b_in;
     TcGenEnum  g;
@@ -363,19 +357,13 @@ static void plan_free(EnumPlan *pl)
     memset(pl, 0, sizeof *pl);
 }
 
-/* Refusals, name matching and the code generator's input for one enumeration. */
-static int plan_enum(const Enum *e, EnumPlan *pl, char *err, size_t errlen)
+/* The code generator's input for one enumeration, into maps the caller gave pl (in_map and b_in
+   of ninputs + 1 entries, out_map of noutputs + 1), after the refusals and the name matching. */
+static int plan_fill(const Enum *e, EnumPlan *pl, char *err, size_t errlen)
 {
-    memset(pl, 0, sizeof *pl);
-    if (!e || !e->a)
-        return tc_fail(err, errlen, "no program");
     size_t n = e->a->ninputs;
-    pl->in_map = tc_xcalloc(n + 1, sizeof *pl->in_map);
-    pl->out_map = tc_xcalloc(e->a->noutputs + 1, sizeof *pl->out_map);
-    if (!tc_enum_prepare(e, pl->in_map, pl->out_map, err, errlen)) {
-        plan_free(pl);
+    if (!tc_enum_prepare(e, pl->in_map, pl->out_map, err, errlen))
         return 0;
-    }
     TcGenEnum *g = &pl->g;
     g->mode = e->mode;
     g->a = e->a;
@@ -383,7 +371,6 @@ static int plan_enum(const Enum *e, EnumPlan *pl, char *err, size_t errlen)
     g->ticks = e->ticks;
     g->block = TC_ENUM_BLOCK;
     if (e->mode == EN_EQUIV) {
-        pl->b_in = tc_xcalloc(n + 1, sizeof *pl->b_in);
         for (size_t k = 0; k < n; k++)
             pl->b_in[k] = e->b->inputs[pl->in_map[k]];
         g->b = e->b;
@@ -392,6 +379,24 @@ static int plan_enum(const Enum *e, EnumPlan *pl, char *err, size_t errlen)
     }
     if (e->mode == EN_SEARCH)
         g->target = cuda_spec_value(e->spec, 0);
+    return 1;
+}
+
+/* Refusals, name matching and the code generator's input for one enumeration (maps on the
+   heap; plan_free releases them). */
+static int plan_enum(const Enum *e, EnumPlan *pl, char *err, size_t errlen)
+{
+    memset(pl, 0, sizeof *pl);
+    if (!e || !e->a)
+        return tc_fail(err, errlen, "no program");
+    size_t n = e->a->ninputs;
+    pl->in_map = tc_xcalloc(n + 1, sizeof *pl->in_map);
+    pl->out_map = tc_xcalloc(e->a->noutputs + 1, sizeof *pl->out_map);
+    pl->b_in = tc_xcalloc(n + 1, sizeof *pl->b_in);
+    if (!plan_fill(e, pl, err, errlen)) {
+        plan_free(pl);
+        return 0;
+    }
     return 1;
 }
 
@@ -507,12 +512,23 @@ char *tc_codegen_enum_for(const Enum *e, size_t *len, char *err, size_t errlen)
    whose callers cannot allocate. */
 int tc_enum_cached(const Enum *e, TcModule *m, char *err, size_t errlen)
 {
+    /* the maps in fixed buffers: this lookup allocates nothing */
+    int in_map[EN_MAX_IN + 1], out_map[TC_CACHED_MAX_OUTPUTS + 1];
+    uint32_t b_in[EN_MAX_IN + 1];
+    if (!e || !e->a)
+        return tc_fail(err, errlen, "no program");
+    if (e->a->noutputs > TC_CACHED_MAX_OUTPUTS)
+        return tc_fail(err, errlen, "cuda_enum_run_static: %zu outputs; at most %d here",
+                       e->a->noutputs, TC_CACHED_MAX_OUTPUTS);
     EnumPlan pl;
-    if (!plan_enum(e, &pl, err, errlen))
+    memset(&pl, 0, sizeof pl);
+    pl.in_map = in_map;
+    pl.out_map = out_map;
+    pl.b_in = b_in;
+    if (!plan_fill(e, &pl, err, errlen))
         return 0;
     uint64_t k1, k2;
     enum_key(&pl.g, &k1, &k2);
-    plan_free(&pl);
     if (!lookup_enum(k1, k2, m))
         return tc_fail(err, errlen, "cuda_enum_run_static: this job's kernel is not loaded; run the "
                        "same job once through cuda_enum_run first");
@@ -601,7 +617,7 @@ size_t tc_enum_job_ws_max(void)
 static int launch_enum(const TcEnumJob *j, void *hits, void *list, void *count, cudaStream_t st,
                        char *err, size_t errlen)
 {
-    EnumArgs args;
+    TcEnumArgs args;
     memset(&args, 0, sizeof args);
     args.words = j->words;
     args.space = j->space;

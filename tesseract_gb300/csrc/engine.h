@@ -65,6 +65,10 @@ int    tc_scratch(TcBuf *b, size_t bytes, char *err, size_t errlen);
 int    tc_module(const char *src, size_t len, const char *const *kernels, int nkernels,
                  const char *extra_opt, TcModule *out, char *err, size_t errlen);
 int    tc_enum_prepare(const Enum *e, int *in_map, int *out_map, char *err, size_t errlen);
+/* The loaded kernel of a job that an earlier enumeration compiled, else an error; allocates
+   nothing (its maps are fixed buffers, so programs of more than TC_CACHED_MAX_OUTPUTS outputs
+   are refused). */
+#define TC_CACHED_MAX_OUTPUTS 4096
 int    tc_enum_cached(const Enum *e, TcModule *m, char *err, size_t errlen);
 
 /* One enumeration on the generated-kernel engine in steps, for callers that overlap many

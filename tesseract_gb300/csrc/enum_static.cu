@@ -8,10 +8,12 @@
 //     counted for a job already in flight;
 //   - callers with kernels in flight on other streams: cudaFree waits for the whole device, so
 //     growing the workspace would stall their work.
-// This entry point calls no cudaMalloc, cudaFree or other allocating routine.  Its workspace is
-// tc_enum_scratch below, sized for TC_STATIC_WARPS warps; a launch that would need more warps is
-// refused with an error.  It compiles nothing either: the job's generated kernel must already be
-// loaded by an earlier cuda_enum_run of the same job, else the call fails with an error.
+// This entry point calls no cudaMalloc, cudaFree or other allocating routine, on the device or
+// on the host.  Its device workspace is tc_enum_scratch below, sized for TC_STATIC_WARPS warps;
+// a launch that would need more warps is refused with an error.  The hit lists come back
+// through a fixed buffer on the stack, TC_STATIC_RUN warps at a time, with stream-ordered copies
+// on the engine's stream.  It compiles nothing either: the job's generated kernel must already
+// be loaded by an earlier cuda_enum_run of the same job, else the call fails with an error.
 //
 // Set-up: the first call on a device, with that device current, takes the array's address with
 // cudaGetSymbolAddress.  With CUDA's lazy module loading that first use loads this file's module
@@ -26,6 +28,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include "codegen.h"
 #include "engine.h"
 
 #define TC_STATIC_WARPS 16384u        // 16 hits of 8 bytes and one count per warp
@@ -33,18 +36,12 @@
 #define TC_STATIC_COUNT_OFF (TC_STATIC_LIST_OFF + TC_STATIC_WARPS * 16u * 8u)
 #define TC_STATIC_BYTES (TC_STATIC_COUNT_OFF + TC_STATIC_WARPS * 4u)   // 2,162,944 bytes
 #define TC_STATIC_DEVICES 64
+#define TC_STATIC_RUN 128u            // warps whose hits come back per copy (16 KB on the stack)
 
 // [0, 8): hit counter; [256, +2 MiB): hit lists; then the counts.
 static __device__ __align__(256) unsigned char tc_enum_scratch[TC_STATIC_BYTES];
 
 static void *scratch_at[TC_STATIC_DEVICES];
-
-// The kernel argument block of the generated tc_enum kernel (the TcEnumArgs of its source).
-struct StaticEnumArgs {
-    uint64_t words, space, per_warp;
-    uint32_t parts, part, nsel, pad;
-    void    *hits, *list, *count;
-};
 
 static int scratch_for_current_device(unsigned char **out, char *err, size_t errlen)
 {
@@ -110,7 +107,7 @@ extern "C" int cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, siz
         per_warp = 32;
 
     cudaStream_t st = tc_engine.stream;
-    StaticEnumArgs args;
+    TcEnumArgs args;  // the generated kernel's own argument block (codegen.h)
     memset(&args, 0, sizeof args);
     args.words = words;
     args.space = space;
@@ -118,9 +115,9 @@ extern "C" int cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, siz
     args.parts = (uint32_t)e->parts;
     args.part = (uint32_t)e->part;
     args.nsel = (uint32_t)(e->part_end - e->part + 1);
-    args.hits = ws;
-    args.list = ws + TC_STATIC_LIST_OFF;
-    args.count = ws + TC_STATIC_COUNT_OFF;
+    args.hits = (uint64_t *)ws;
+    args.list = (uint64_t *)(ws + TC_STATIC_LIST_OFF);
+    args.count = (uint32_t *)(ws + TC_STATIC_COUNT_OFF);
     void *params[] = {&args};
     if (!tc_cu_check(cudaMemsetAsync(args.hits, 0, 8, st), "memset", err, errlen) ||
         !tc_cu_check(cudaMemsetAsync(args.count, 0, warps * 4, st), "memset", err, errlen) ||
@@ -136,25 +133,24 @@ extern "C" int cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, siz
         !tc_cu_check(cudaStreamSynchronize(st), "tc_enum", err, errlen))
         return 0;
     // Every warp's hits (a kernel whose enumeration order is permuted does not find the
-    // smallest in the first warps).  Counts and lists come over in runs of 1024 warps.
-    uint32_t count[1024];
-    uint64_t *got = hits ? (uint64_t *)tc_xmalloc(1024 * 16 * 8) : nullptr;
-    for (uint64_t w0 = 0; hits && w0 < warps; w0 += 1024) {
-        uint64_t n = warps - w0 < 1024 ? warps - w0 : 1024;
-        if (!tc_cu_check(cudaMemcpy(count, (uint32_t *)args.count + w0, n * 4,
-                                    cudaMemcpyDeviceToHost),
+    // smallest in the first warps).  Counts and lists come over in runs of TC_STATIC_RUN warps,
+    // on the engine's stream; only the counts this call cleared and its kernel wrote are read.
+    uint32_t count[TC_STATIC_RUN];
+    uint64_t got[TC_STATIC_RUN * 16];
+    for (uint64_t w0 = 0; hits && w0 < warps; w0 += TC_STATIC_RUN) {
+        uint64_t n = warps - w0 < TC_STATIC_RUN ? warps - w0 : TC_STATIC_RUN;
+        if (!tc_cu_check(cudaMemcpyAsync(count, args.count + w0, n * 4, cudaMemcpyDeviceToHost,
+                                         st),
                          "hit counts", err, errlen) ||
-            !tc_cu_check(cudaMemcpy(got, (uint64_t *)args.list + w0 * 16, n * 16 * 8,
-                                    cudaMemcpyDeviceToHost),
-                         "hits", err, errlen)) {
-            free(got);
+            !tc_cu_check(cudaMemcpyAsync(got, args.list + w0 * 16, n * 16 * 8,
+                                         cudaMemcpyDeviceToHost, st),
+                         "hits", err, errlen) ||
+            !tc_cu_check(cudaStreamSynchronize(st), "hit copy", err, errlen))
             return 0;
-        }
         for (uint64_t i = 0; i < n; i++)
-            for (uint32_t k = 0; k < count[i]; k++)
+            for (uint32_t k = 0; k < count[i] && k < 16; k++)
                 cuda_enum_add_hit(r, got[i * 16 + k]);
     }
-    free(got);
     float ms = 0;
     cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
     r->seconds = ms / 1e3;

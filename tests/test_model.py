@@ -15,8 +15,8 @@ import oracle as O
 import tesseract_gb300 as T
 from cases import load
 
-REFERENCE = os.environ.get("TESSERACT_REFERENCE", "/root/reference")
-needs_ref = pytest.mark.skipif(not (O.have_reference() and os.path.isdir(REFERENCE)),
+REFERENCE = O.reference_sources() or ""
+needs_ref = pytest.mark.skipif(not (O.have_reference() and REFERENCE),
                                reason="the reference is not built here")
 
 

@@ -1,7 +1,8 @@
 """cuda_enum_run_static, the enumeration whose workspace is a fixed device array (it allocates
 nothing), against cuda_enum_run on the same jobs: equal results on two calls in a row, with jobs
-that leave many hits in the shared array run before jobs that find none.  Collected last; passes
-alone in a fresh process and after the other tests."""
+that leave many hits in the shared array run before jobs that find none, and small grids with
+hits run right after the full 2^32 grid.  Collected last; passes alone in a fresh process and
+after the other tests."""
 import ctypes as C
 
 import pytest
@@ -39,6 +40,11 @@ def jobs():
         dict(mode=T.EN_VERIFY, a=mul10, spec=T.Spec(mul10, "p = a * b ^ 1"), part=1, parts=3),
         # the whole 2^32 space: the full grid, no hits
         dict(mode=T.EN_VERIFY, a=mul16, spec=T.Spec(mul16, "p = a * b")),
+        # then a small grid with hits: its lists must not mix with the larger launch's
+        dict(mode=T.EN_VERIFY, a=mul10, spec=T.Spec(mul10, "p = a * b ^ (b & 2)")),
+        dict(mode=T.EN_VERIFY, a=mul16, spec=T.Spec(mul16, "p = a * b ^ (a & 1)")),
+        dict(mode=T.EN_VERIFY, a=mul10, spec=T.Spec(mul10, "p = a * b ^ (b & 2)"), part=2,
+             parts=5),
     ]
 
 
