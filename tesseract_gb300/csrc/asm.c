@@ -1,9 +1,19 @@
-/* The assembler: source text to Program.  The language is the reference's (docs/ISA.md,
-   "Assembly language"): .in/.out/.link/.include/.macro directives, NAND and STO, macros with
-   parameters, '#' name joining and @locals.  Cells are numbered in order of first appearance and
-   macro locals are named "@<call>:<name>", exactly as src/asm.c does, so both assemblers give the
-   same Program for the same text.  Cell lookup is a hash table here (the programs that matter on
-   the GPU have hundreds of thousands of instructions). */
+/* The assembler: source text -> Program.
+
+   The language is the reference's program format (its docs/ISA.md, src/asm.h:7-17), and the
+   Program it yields must be the reference's cell for cell: cells are numbered by first
+   appearance (ZERO, ONE, then every name as met in .in/.out/.link lines, instructions and macro
+   bodies), names keep the spelling of their first appearance, each macro call numbers its @local
+   names @<call>:<name>, and errors read "file:line: message", with " (in macro called at
+   file:line)" naming the outermost call when the line came from a macro body.  Macro expansion
+   in that language is textual: a call rewrites each body line (parameters replaced, '#' pieces
+   joined, @locals renamed, tokens with blanks quoted) into a line that is then read like any
+   other, so this assembler does the same.
+
+   The design here: one driver loop pulls lines from an explicit stack of frames -- the source
+   text, each included file, each macro call's rewritten body -- instead of recursing into
+   includes and calls; a macro definition is cut out of the frame it appears in; cells and macros
+   live in hash tables keyed by their case-folded names. */
 #include <ctype.h>
 #include <stdarg.h>
 #include <stdlib.h>
@@ -11,107 +21,135 @@
 
 #include "tc_host.h"
 
-enum { NEST_LIMIT = 64, TOKEN_LIMIT = 128 };
+#define NEST_LIMIT  64   /* frames above the source: macro calls and includes together */
+#define LINE_TOKENS 128  /* tokens on one line */
 
-typedef struct {
-    char  *name;
-    char **params;
-    int    nparams;
-    char **lines;
-    int   *line_no;
-    int    nlines;
-    char  *file, *dir;
-} Macro;
+/* ---- names ----------------------------------------------------------------------------------- */
 
-typedef struct {
-    /* the program being built */
-    Instr    *code;
-    size_t    len, cap;
-    char    **names;
-    CellInfo *info;
-    uint32_t  ncells, capcells;
-    uint32_t *slots;  /* open addressing: cell + 1, 0 = empty */
-    size_t    nslots;
-    uint32_t *in, *out;
-    size_t    nin, capin, nout, capout;
-    int       special;
-    Macro    *macros;
-    int       nmacros, capmacros;
-    unsigned  calls;  /* macro calls so far: numbers the @locals */
-    char     *err;
-    size_t    errlen;
-    int       failed;
-} Asm;
-
-typedef struct {
-    const char *file, *dir;
-    const char *from;  /* "file:line" of the outermost macro call, or NULL */
-    int         depth;
-    int         in_macro;
-} Where;
-
-typedef struct {
-    char *copy;
-    char *t[TOKEN_LIMIT];
-    int   n;
-} Toks;
-
-static void assemble_lines(Asm *a, const Where *w, char **lines, const int *nos, int n);
-
-static void error(Asm *a, const Where *w, int line, const char *fmt, ...)
+static int name_char(int c)
 {
-    if (a->failed)
-        return;
-    a->failed = 1;
-    if (!a->errlen)
-        return;
-    size_t at = 0;
-    int k = snprintf(a->err, a->errlen, "%s:%d: ", w->file, line);
-    at = k > 0 ? (size_t)k : 0;
-    if (at < a->errlen) {
-        va_list ap;
-        va_start(ap, fmt);
-        k = vsnprintf(a->err + at, a->errlen - at, fmt, ap);
-        va_end(ap);
-        if (k > 0)
-            at += (size_t)k;
-    }
-    if (w->from && at < a->errlen)
-        snprintf(a->err + at, a->errlen - at, " (in macro called at %s)", w->from);
+    return isalnum(c) || c == '_';
 }
 
-/* ---- tokens ------------------------------------------------------------------------------- */
+/* A name: letters, digits and '_', not starting with a digit. */
+static int is_name(const char *s)
+{
+    if (!isalpha((unsigned char)*s) && *s != '_')
+        return 0;
+    while (*++s)
+        if (!name_char((unsigned char)*s))
+            return 0;
+    return 1;
+}
 
-static int is_sep(char c)
+static int is_opcode(const char *s)
+{
+    return tc_same_name(s, "NAND") || tc_same_name(s, "STO");
+}
+
+/* An open-addressing table from case-folded names to indices. */
+typedef struct {
+    uint32_t *slot;  /* index + 1, 0 = empty */
+    size_t    cap;   /* a power of two */
+} NameTable;
+
+static uint64_t fold_hash(const char *s)
+{
+    uint64_t h = 0x9ae16a3b2f90404full;
+    for (; *s; s++)
+        h = (h ^ (uint64_t)tolower((unsigned char)*s)) * 0x100000001b3ull;
+    return h ^ (h >> 32);
+}
+
+/* The index of `name` (case ignored) among names[] through the table, or -1. */
+static long table_find(const NameTable *t, char *const *names, const char *name)
+{
+    if (!t->cap)
+        return -1;
+    for (size_t i = fold_hash(name) & (t->cap - 1);; i = (i + 1) & (t->cap - 1)) {
+        if (!t->slot[i])
+            return -1;
+        if (tc_same_name(names[t->slot[i] - 1], name))
+            return (long)t->slot[i] - 1;
+    }
+}
+
+/* Records names[index] (not yet present); keeps the table at most half full. */
+static void table_add(NameTable *t, char *const *names, uint32_t index)
+{
+    if (2 * (size_t)(index + 1) > t->cap) {
+        size_t cap = t->cap ? 2 * t->cap : 64;
+        free(t->slot);
+        t->slot = tc_xcalloc(cap, sizeof *t->slot);
+        t->cap = cap;
+        for (uint32_t k = 0; k < index; k++)
+            table_add(t, names, k);
+    }
+    size_t i = fold_hash(names[index]) & (t->cap - 1);
+    while (t->slot[i])
+        i = (i + 1) & (t->cap - 1);
+    t->slot[i] = index + 1;
+}
+
+/* ---- text ------------------------------------------------------------------------------------ */
+
+typedef struct {
+    char *s;
+    size_t n, cap;
+} Text;
+
+static void text_put(Text *t, const char *s, size_t n)
+{
+    if (t->n + n + 1 > t->cap) {
+        t->cap = 2 * (t->n + n + 1);
+        t->s = tc_xrealloc(t->s, t->cap);
+    }
+    memcpy(t->s + t->n, s, n);
+    t->n += n;
+    t->s[t->n] = '\0';
+}
+
+static void text_puts(Text *t, const char *s)
+{
+    text_put(t, s, strlen(s));
+}
+
+/* The tokens of one line, cut out of a private copy of it.  Blanks, tabs, carriage returns and
+   commas separate tokens; ';' ends the line; a token that starts with '"' runs to the next '"'
+   (which it does not include) and may hold any of those.  Returns NULL or an error message. */
+typedef struct {
+    char *copy;
+    char *tok[LINE_TOKENS];
+    int   n;
+} Line;
+
+static int separator(char c)
 {
     return c == ' ' || c == '\t' || c == ',' || c == '\r';
 }
 
-/* Splits a line: separators are blanks and commas, ';' starts a comment, "..." is one token.
-   Returns NULL or an error message. */
-static const char *split(const char *line, Toks *t)
+static const char *lex(const char *src, Line *l)
 {
-    char *p = t->copy = tc_xstrdup(line);
-    t->n = 0;
+    char *p = l->copy = tc_xstrdup(src);
+    l->n = 0;
     for (;;) {
-        while (is_sep(*p))
+        while (separator(*p))
             p++;
         if (!*p || *p == ';')
             return NULL;
-        if (t->n == TOKEN_LIMIT)
+        if (l->n == LINE_TOKENS)
             return "too many tokens on one line";
         if (*p == '"') {
-            t->t[t->n++] = ++p;
-            char *q = strchr(p, '"');
-            if (!q)
+            char *close = strchr(p + 1, '"');
+            if (!close)
                 return "unterminated string";
-            *q = '\0';
-            p = q + 1;
+            *close = '\0';
+            l->tok[l->n++] = p + 1;
+            p = close + 1;
             continue;
         }
-        t->t[t->n++] = p;
-        while (*p && !is_sep(*p) && *p != ';')
-            p++;
+        l->tok[l->n++] = p;
+        p += strcspn(p, " \t,\r;");
         if (*p == ';') {
             *p = '\0';
             return NULL;
@@ -121,59 +159,153 @@ static const char *split(const char *line, Toks *t)
     }
 }
 
-static int identifier(const char *s)
+static void line_free(Line *l)
 {
-    if (!isalpha((unsigned char)*s) && *s != '_')
-        return 0;
-    while (*++s)
-        if (!isalnum((unsigned char)*s) && *s != '_')
-            return 0;
-    return 1;
+    free(l->copy);
+    l->copy = NULL;
 }
 
-static int instruction_name(const char *s)
+/* UTF-16 with a byte order mark (as Windows PowerShell 5 writes files) becomes 8-bit text, each
+   character beyond ASCII a '?'; a UTF-8 byte order mark is dropped.  buf[len] is 0. */
+static void normalize(char *buf, size_t len)
 {
-    return tc_same_name(s, "NAND") || tc_same_name(s, "STO");
+    unsigned char *b = (unsigned char *)buf;
+    if (len >= 2 && (b[0] == 0xFF || b[0] == 0xFE) && b[1] == (b[0] ^ 0x01)) {
+        int hi_first = b[0] == 0xFE;
+        size_t k = 0;
+        for (size_t i = 2; i + 1 < len; i += 2) {
+            unsigned c = hi_first ? (unsigned)b[i] << 8 | b[i + 1]
+                                  : (unsigned)b[i + 1] << 8 | b[i];
+            b[k++] = c < 0x80 ? (unsigned char)c : '?';
+        }
+        b[k] = '\0';
+    } else if (len >= 3 && b[0] == 0xEF && b[1] == 0xBB && b[2] == 0xBF) {
+        memmove(b, b + 3, len - 2);
+    }
 }
 
-/* ---- cells --------------------------------------------------------------------------------- */
-
-static uint64_t name_hash(const char *s)
+static char *read_text(const char *path)
 {
-    uint64_t h = 0xcbf29ce484222325ull;
-    for (; *s; s++)
-        h = (h ^ (uint64_t)(unsigned char)tolower((unsigned char)*s)) * 0x100000001b3ull;
-    return h;
+    FILE *f = fopen(path, "rb");
+    if (!f)
+        return NULL;
+    Text t = {0};
+    char chunk[65536];
+    size_t got;
+    text_put(&t, "", 0);
+    while ((got = fread(chunk, 1, sizeof chunk, f)) > 0)
+        text_put(&t, chunk, got);
+    fclose(f);
+    normalize(t.s, t.n);
+    return t.s;
 }
 
-static size_t slot_of(const Asm *a, const char *name)
+/* The directory part of a path ('/' or '\\' separated), "." when it has none. */
+static char *parent_dir(const char *path)
 {
-    size_t i = (size_t)name_hash(name) & (a->nslots - 1);
-    while (a->slots[i] && !tc_same_name(a->names[a->slots[i] - 1], name))
-        i = (i + 1) & (a->nslots - 1);
-    return i;
+    const char *cut = NULL;
+    for (const char *p = path; *p; p++)
+        if (*p == '/' || *p == '\\')
+            cut = p;
+    if (!cut)
+        return tc_xstrdup(".");
+    size_t n = cut == path ? 1 : (size_t)(cut - path);
+    char *d = tc_xmalloc(n + 1);
+    memcpy(d, path, n);
+    d[n] = '\0';
+    return d;
 }
 
-static void grow_slots(Asm *a)
+/* ---- the assembler's state --------------------------------------------------------------------- */
+
+typedef struct {
+    char       *name;
+    char      **params;
+    int         nparams;
+    char      **body;     /* raw lines between .macro and .endm */
+    int        *body_no;  /* their line numbers */
+    int         nbody;
+    const char *file, *dir;  /* where it was defined */
+} Macro;
+
+/* Where lines come from: the source text, an included file, or one macro call's body. */
+typedef struct {
+    char      **lines;
+    int        *nos;        /* line numbers (in `file`) */
+    int         n, at;
+    const char *file, *dir;
+    const char *from;       /* the outermost macro call ("file:line"), NULL outside macros */
+    int         depth;      /* frames below this one */
+    int         local_ok;   /* a macro body: @names allowed */
+    char       *text;       /* the buffer lines[] point into, or NULL when each line is owned */
+} Frame;
+
+typedef struct {
+    /* the program */
+    Instr    *code;
+    size_t    len, capcode;
+    char    **names;
+    CellInfo *info;
+    uint32_t  ncells, capcells;
+    int       special;
+    uint32_t *in, *out;
+    size_t    nin, nout, capin, capout;
+    NameTable cells;
+    /* macros */
+    Macro    *macros;
+    char    **macro_names;
+    int       nmacros, capmacros;
+    NameTable macro_table;
+    unsigned  calls;       /* macro calls so far: numbers the @locals */
+    /* lines */
+    Frame    *frames;
+    int       nframes, capframes;
+    char    **strings;     /* file names, directories, call sites: alive until the end */
+    size_t    nstrings, capstrings;
+    /* errors */
+    char     *err;
+    size_t    errlen;
+    int       failed;
+} Asm;
+
+static const char *keep(Asm *a, char *s)  /* takes ownership of s */
 {
-    free(a->slots);
-    a->nslots = a->nslots ? 2 * a->nslots : 256;
-    a->slots = tc_xcalloc(a->nslots, sizeof *a->slots);
-    for (uint32_t c = 0; c < a->ncells; c++)
-        a->slots[slot_of(a, a->names[c])] = c + 1;
+    if (a->nstrings == a->capstrings) {
+        a->capstrings = a->capstrings ? 2 * a->capstrings : 16;
+        a->strings = tc_xrealloc(a->strings, a->capstrings * sizeof *a->strings);
+    }
+    a->strings[a->nstrings++] = s;
+    return s;
 }
 
-static int lookup(const Asm *a, const char *name)
+/* Records the first error: "file:line: message", plus the outermost macro call. */
+static void error(Asm *a, const Frame *f, int line, const char *fmt, ...)
 {
-    size_t i = slot_of(a, name);
-    return a->slots[i] ? (int)a->slots[i] - 1 : -1;
+    if (a->failed++ || !a->errlen)
+        return;
+    size_t at = 0, room = a->errlen;
+    int k = snprintf(a->err, room, "%s:%d: ", f->file, line);
+    at = k > 0 ? (size_t)k : 0;
+    if (at < room) {
+        va_list ap;
+        va_start(ap, fmt);
+        k = vsnprintf(a->err + at, room - at, fmt, ap);
+        va_end(ap);
+        at += k > 0 ? (size_t)k : 0;
+    }
+    if (f->from && at < room)
+        snprintf(a->err + at, room - at, " (in macro called at %s)", f->from);
 }
 
+/* ---- cells ------------------------------------------------------------------------------------- */
+
+/* The cell called `name`, created at the end of the numbering when new (ID0..ID15 are lane-id
+   cells). */
 static uint32_t cell(Asm *a, const char *name)
 {
-    size_t i = slot_of(a, name);
-    if (a->slots[i])
-        return a->slots[i] - 1;
+    long found = table_find(&a->cells, a->names, name);
+    if (found >= 0)
+        return (uint32_t)found;
     if (a->ncells == a->capcells) {
         a->capcells = a->capcells ? 2 * a->capcells : 64;
         a->names = tc_xrealloc(a->names, a->capcells * sizeof *a->names);
@@ -182,515 +314,497 @@ static uint32_t cell(Asm *a, const char *name)
     uint32_t c = a->ncells++;
     a->names[c] = tc_xstrdup(name);
     memset(&a->info[c], 0, sizeof a->info[c]);
-    int d = tc_program_id_name(name);
-    if (d >= 0) {
+    int bit = tc_program_id_name(name);
+    if (bit >= 0) {
         a->info[c].kind = CK_ID;
-        a->info[c].dim = (uint8_t)d;
+        a->info[c].dim = (uint8_t)bit;
         a->special = 1;
     }
-    a->slots[i] = c + 1;
-    if (2 * (size_t)a->ncells > a->nslots)
-        grow_slots(a);
+    table_add(&a->cells, a->names, c);
     return c;
 }
 
-static int readonly(const Asm *a, uint32_t c)
+static const char *readonly_kind(const Asm *a, uint32_t c)  /* NULL for a writable cell */
 {
-    return c < CELL_FIRST_FREE || a->info[c].kind != CK_PLAIN;
+    if (c < CELL_FIRST_FREE)
+        return "constant";
+    return a->info[c].kind == CK_ID ? "lane-id" : a->info[c].kind == CK_LINK ? "link" : NULL;
 }
 
-static const char *kind_text(const Asm *a, uint32_t c)
+/* A cell name in a statement: a name, or an @local (only in lines from a macro body, where the
+   call has already renamed it). */
+static int check_name(Asm *a, const Frame *f, int line, const char *tok)
 {
-    return c < CELL_FIRST_FREE ? "constant" : a->info[c].kind == CK_ID ? "lane-id" : "link";
-}
-
-static int name_ok(Asm *a, const Where *w, int line, const char *tok)
-{
-    if (tok[0] == '@') {
-        if (w->in_macro)
-            return 1;
-        error(a, w, line, "'%s': @names are only allowed inside macros", tok);
-        return 0;
-    }
-    if (identifier(tok))
+    if (tok[0] == '@' && f->local_ok)
         return 1;
-    error(a, w, line, "'%s' is not a valid cell name", tok);
-    return 0;
+    if (tok[0] == '@')
+        error(a, f, line, "'%s': @names are only allowed inside macros", tok);
+    else if (!is_name(tok))
+        error(a, f, line, "'%s' is not a valid cell name", tok);
+    return !a->failed;
 }
 
-static void io_list(Asm *a, const Where *w, int line, const Toks *t, uint32_t **list, size_t *n,
-                    size_t *cap)
+/* ---- statements -------------------------------------------------------------------------------- */
+
+static void push_cell(uint32_t **list, size_t *n, size_t *cap, uint32_t c)
 {
-    if (t->n < 2) {
-        error(a, w, line, "%s expects at least one cell name", t->t[0]);
-        return;
+    if (*n == *cap) {
+        *cap = *cap ? 2 * *cap : 16;
+        *list = tc_xrealloc(*list, *cap * sizeof **list);
     }
-    for (int i = 1; i < t->n; i++) {
-        if (!name_ok(a, w, line, t->t[i]))
+    (*list)[(*n)++] = c;
+}
+
+/* .in / .out NAME... */
+static void declare_io(Asm *a, const Frame *f, int line, const Line *l, int output)
+{
+    uint32_t **list = output ? &a->out : &a->in;
+    size_t *n = output ? &a->nout : &a->nin, *cap = output ? &a->capout : &a->capin;
+    if (l->n == 1)
+        error(a, f, line, "%s expects at least one cell name", l->tok[0]);
+    for (int i = 1; i < l->n && !a->failed; i++) {
+        const char *name = l->tok[i];
+        if (!check_name(a, f, line, name))
             return;
-        uint32_t c = cell(a, t->t[i]);
-        if (readonly(a, c)) {
-            error(a, w, line, "%s is a %s cell", t->t[i], kind_text(a, c));
+        uint32_t c = cell(a, name);
+        const char *ro = readonly_kind(a, c);
+        if (ro) {
+            error(a, f, line, "%s is a %s cell", name, ro);
             return;
         }
         for (size_t k = 0; k < *n; k++)
             if ((*list)[k] == c) {
-                error(a, w, line, "%s is declared twice", t->t[i]);
+                error(a, f, line, "%s is declared twice", name);
                 return;
             }
-        if (*n == *cap) {
-            *cap = *cap ? 2 * *cap : 16;
-            *list = tc_xrealloc(*list, *cap * sizeof **list);
-        }
-        (*list)[(*n)++] = c;
+        push_cell(list, n, cap, c);
     }
 }
 
-/* .link y = x @ d, spaces optional: the tokens are joined first. */
-static void link_line(Asm *a, const Where *w, int line, const Toks *t)
+/* .link NAME = SOURCE @ DIM, the tokens read as one string (blanks anywhere).  The dimension
+   follows the last '@' after the '='.  NAME must be a new cell, so links never form a loop. */
+static void declare_link(Asm *a, const Frame *f, int line, const Line *l)
 {
-    char buf[512];
-    size_t n = 0;
-    for (int i = 1; i < t->n; i++) {
-        size_t k = strlen(t->t[i]);
-        if (n + k + 1 > sizeof buf) {
-            error(a, w, line, ".link line too long");
+    char s[512];
+    size_t len = 0;
+    for (int i = 1; i < l->n; i++) {
+        size_t k = strlen(l->tok[i]);
+        if (len + k >= sizeof s) {
+            error(a, f, line, ".link line too long");
             return;
         }
-        memcpy(buf + n, t->t[i], k);
-        n += k;
+        memcpy(s + len, l->tok[i], k);
+        len += k;
     }
-    buf[n] = '\0';
-    char *eq = strchr(buf, '=');
-    char *at = eq ? strrchr(eq + 1, '@') : NULL;
-    if (!eq || !at) {
-        error(a, w, line, ".link expects: .link name = cell @ dimension");
+    s[len] = '\0';
+    char *eq = strchr(s, '=');
+    char *at = eq ? strrchr(eq, '@') : NULL;
+    if (!at) {
+        error(a, f, line, ".link expects: .link name = cell @ dimension");
         return;
     }
-    *eq = '\0';
-    *at = '\0';
-    const char *name = buf, *src = eq + 1, *dim = at + 1;
+    *eq = *at = '\0';
+    const char *name = s, *src = eq + 1, *dim = at + 1;
     char *end;
     long d = strtol(dim, &end, 10);
-    if (!*dim || *end || d < 0 || d >= CUBE_MAX_DIMS) {
-        error(a, w, line, "the dimension must be 0 to %d, got '%s'", CUBE_MAX_DIMS - 1, dim);
+    if (end == dim || *end || d < 0 || d >= CUBE_MAX_DIMS) {
+        error(a, f, line, "the dimension must be 0 to %d, got '%s'", CUBE_MAX_DIMS - 1, dim);
         return;
     }
-    if (!name_ok(a, w, line, name) || !name_ok(a, w, line, src))
+    if (!check_name(a, f, line, name) || !check_name(a, f, line, src))
         return;
-    if (lookup(a, name) >= 0) {
-        error(a, w, line, "%s is already a cell: declare a link before its first use", name);
+    if (table_find(&a->cells, a->names, name) >= 0)
+        error(a, f, line, "%s is already a cell: declare a link before its first use", name);
+    else if (tc_program_id_name(name) >= 0)
+        error(a, f, line, "%s is a lane-id cell", name);
+    else if (tc_same_name(name, src))
+        error(a, f, line, "a link cannot read itself");
+    if (a->failed)
         return;
-    }
-    if (tc_program_id_name(name) >= 0) {
-        error(a, w, line, "%s is a lane-id cell", name);
-        return;
-    }
-    if (tc_same_name(name, src)) {
-        error(a, w, line, "a link cannot read itself");
-        return;
-    }
-    uint32_t s = cell(a, src), y = cell(a, name);
+    uint32_t from = cell(a, src);  /* the source is numbered before the link */
+    uint32_t y = cell(a, name);
     a->info[y].kind = CK_LINK;
     a->info[y].dim = (uint8_t)d;
-    a->info[y].src = s;
+    a->info[y].src = from;
     a->special = 1;
 }
 
-/* ---- files --------------------------------------------------------------------------------- */
-
-/* UTF-16 (with a byte order mark) becomes 8-bit text, a UTF-8 byte order mark is dropped. */
-static size_t normalize(char *buf, size_t len)
+/* NAND CELL / STO CELL */
+static void instruction(Asm *a, const Frame *f, int line, const Line *l)
 {
-    unsigned char *b = (unsigned char *)buf;
-    if (len >= 2 && ((b[0] == 0xFF && b[1] == 0xFE) || (b[0] == 0xFE && b[1] == 0xFF))) {
-        int little = b[0] == 0xFF;
-        size_t n = 0;
-        for (size_t i = 2; i + 1 < len; i += 2) {
-            unsigned c = little ? (unsigned)b[i] | (unsigned)b[i + 1] << 8
-                                : (unsigned)b[i] << 8 | (unsigned)b[i + 1];
-            b[n++] = (unsigned char)(c < 128 ? c : '?');
-        }
-        b[n] = '\0';
-        return n;
+    if (l->n != 2) {
+        error(a, f, line, "%s expects exactly one cell", l->tok[0]);
+        return;
     }
-    if (len >= 3 && b[0] == 0xEF && b[1] == 0xBB && b[2] == 0xBF) {
-        memmove(b, b + 3, len - 2);
-        return len - 3;
+    if (!check_name(a, f, line, l->tok[1]))
+        return;
+    uint32_t c = cell(a, l->tok[1]);
+    int store = tc_same_name(l->tok[0], "STO");
+    const char *ro = readonly_kind(a, c);
+    if (store && ro) {
+        error(a, f, line, "cannot store to %s cell %s", ro, l->tok[1]);
+        return;
     }
-    return len;
+    if (a->len == a->capcode) {
+        a->capcode = a->capcode ? 2 * a->capcode : 256;
+        a->code = tc_xrealloc(a->code, a->capcode * sizeof *a->code);
+    }
+    a->code[a->len].op = (uint8_t)(store ? OP_STO : OP_NAND);
+    a->code[a->len].addr = c;
+    a->len++;
 }
 
-static char *slurp(const char *path)
+/* ---- frames ------------------------------------------------------------------------------------ */
+
+static Frame *push_frame(Asm *a)
 {
-    FILE *f = fopen(path, "rb");
-    if (!f)
-        return NULL;
-    size_t len = 0, cap = 1 << 16;
-    char *buf = tc_xmalloc(cap);
-    for (;;) {
-        size_t got = fread(buf + len, 1, cap - len - 1, f);
-        if (!got)
-            break;
-        len += got;
-        if (len + 1 == cap) {
-            cap *= 2;
-            buf = tc_xrealloc(buf, cap);
-        }
+    if (a->nframes == a->capframes) {
+        a->capframes = a->capframes ? 2 * a->capframes : 8;
+        a->frames = tc_xrealloc(a->frames, (size_t)a->capframes * sizeof *a->frames);
     }
-    fclose(f);
-    buf[len] = '\0';
-    normalize(buf, len);
-    return buf;
+    Frame *f = &a->frames[a->nframes++];
+    memset(f, 0, sizeof *f);
+    return f;
 }
 
-static char *directory(const char *path)
+static void pop_frame(Asm *a)
 {
-    const char *slash = NULL;
-    for (const char *p = path; *p; p++)
-        if (*p == '/' || *p == '\\')
-            slash = p;
-    if (!slash)
-        return tc_xstrdup(".");
-    size_t n = slash == path ? 1 : (size_t)(slash - path);
-    char *d = tc_xmalloc(n + 1);
-    memcpy(d, path, n);
-    d[n] = '\0';
-    return d;
+    Frame *f = &a->frames[--a->nframes];
+    if (f->text)
+        free(f->text);
+    else
+        for (int i = 0; i < f->n; i++)
+            free(f->lines[i]);
+    free(f->lines);
+    free(f->nos);
 }
 
-static void assemble_text(Asm *a, char *text, const char *file, const char *dir,
-                          const char *from, int depth)
+/* A frame over `text` (taken over), split at newlines, numbered from 1. */
+static void push_text(Asm *a, char *text, const char *file, const char *dir, const char *from,
+                      int depth)
 {
-    if ((unsigned char)text[0] == 0xEF && (unsigned char)text[1] == 0xBB &&
-        (unsigned char)text[2] == 0xBF)
-        text += 3;
+    char *start = text;
+    if ((unsigned char)start[0] == 0xEF && (unsigned char)start[1] == 0xBB &&
+        (unsigned char)start[2] == 0xBF)
+        start += 3;
     int n = 1;
-    for (const char *p = text; *p; p++)
+    for (const char *p = start; *p; p++)
         n += *p == '\n';
-    char **lines = tc_xmalloc((size_t)n * sizeof *lines);
-    int k = 0;
-    lines[k++] = text;
-    for (char *p = text; *p; p++)
-        if (*p == '\n') {
-            *p = '\0';
-            lines[k++] = p + 1;
-        }
-    Where w = {file, dir, from, depth, 0};
-    assemble_lines(a, &w, lines, NULL, n);
-    free(lines);
+    Frame *f = push_frame(a);
+    f->lines = tc_xmalloc((size_t)n * sizeof *f->lines);
+    f->nos = tc_xmalloc((size_t)n * sizeof *f->nos);
+    char *p = start;
+    for (int i = 0; i < n; i++) {
+        f->lines[i] = p;
+        f->nos[i] = i + 1;
+        p += strcspn(p, "\n");
+        if (*p)
+            *p++ = '\0';
+    }
+    f->n = n;
+    f->text = text;
+    f->file = file;
+    f->dir = dir;
+    f->from = from;
+    f->depth = depth;
 }
 
-static void include(Asm *a, const Where *w, int line, const char *name)
+/* .include "FILE", relative to the including file's directory unless absolute. */
+static void include(Asm *a, const Frame *f, int line, const char *name)
 {
-    if (w->depth >= NEST_LIMIT) {
-        error(a, w, line, "includes nested too deeply");
+    if (f->depth >= NEST_LIMIT) {
+        error(a, f, line, "includes nested too deeply");
         return;
     }
     char path[1024];
     int absolute = name[0] == '/' || name[0] == '\\' || (name[0] && name[1] == ':');
-    if (absolute)
-        snprintf(path, sizeof path, "%s", name);
-    else
-        snprintf(path, sizeof path, "%s/%s", w->dir, name);
-    char *text = slurp(path);
+    snprintf(path, sizeof path, absolute ? "%s%s" : "%s/%s", absolute ? "" : f->dir, name);
+    char *text = read_text(path);
     if (!text) {
-        error(a, w, line, "cannot open include file '%s'", path);
+        error(a, f, line, "cannot open include file '%s'", path);
         return;
     }
-    char *dir = directory(path);
-    assemble_text(a, text, path, dir, w->from, w->depth + 1);
-    free(dir);
-    free(text);
+    const char *file = keep(a, tc_xstrdup(path));
+    const char *dir = keep(a, parent_dir(path));
+    const char *from = f->from;
+    int depth = f->depth + 1;
+    push_text(a, text, file, dir, from, depth);  /* may move the frames: f is not used after */
 }
 
-/* ---- macros -------------------------------------------------------------------------------- */
+/* ---- macros ------------------------------------------------------------------------------------ */
 
-static Macro *find_macro(Asm *a, const char *name)
+static long find_macro(const Asm *a, const char *name)
 {
-    for (int i = 0; i < a->nmacros; i++)
-        if (tc_same_name(a->macros[i].name, name))
-            return &a->macros[i];
-    return NULL;
+    return table_find(&a->macro_table, a->macro_names, name);
 }
 
-static int param(const Macro *m, const char *tok)
+static int param_of(const Macro *m, const char *s)
 {
     for (int i = 0; i < m->nparams; i++)
-        if (tc_same_name(m->params[i], tok))
+        if (tc_same_name(m->params[i], s))
             return i;
     return -1;
 }
 
-/* Reads the body of a .macro starting at lines[start]; returns the index of its .endm. */
-static int define_macro(Asm *a, const Where *w, const Toks *head, char **lines, const int *nos,
-                        int start, int n)
+/* .macro NAME PARAM... at line index `head` of f: takes the lines up to .endm out of the frame
+   and defines the macro. */
+static void define_macro(Asm *a, Frame *f, const Line *head)
 {
-    int line = nos ? nos[start] : start + 1, end;
-    for (end = start + 1; end < n; end++) {
-        Toks t;
-        const char *e = split(lines[end], &t);
-        int is_end = !e && t.n > 0 && tc_same_name(t.t[0], ".endm");
-        int nested = !e && t.n > 0 && tc_same_name(t.t[0], ".macro");
-        free(t.copy);
-        if (nested) {
-            error(a, w, nos ? nos[end] : end + 1, "macros cannot be defined inside macros");
-            return n;
+    int line = f->nos[f->at - 1], end = f->at;
+    for (; end < f->n; end++) {
+        Line l;
+        const char *bad = lex(f->lines[end], &l);
+        int is_macro = !bad && l.n && tc_same_name(l.tok[0], ".macro");
+        int is_end = !bad && l.n && tc_same_name(l.tok[0], ".endm");
+        line_free(&l);
+        if (is_macro) {
+            error(a, f, f->nos[end], "macros cannot be defined inside macros");
+            return;
         }
         if (is_end)
             break;
     }
-    if (end == n) {
-        error(a, w, line, "missing .endm for macro %s", head->n > 1 ? head->t[1] : "");
-        return n;
+    if (end == f->n) {
+        error(a, f, line, "missing .endm for macro %s", head->n > 1 ? head->tok[1] : "");
+        return;
     }
-    if (head->n < 2 || !identifier(head->t[1])) {
-        error(a, w, line, ".macro expects a name");
-        return end;
+    int first = f->at;
+    f->at = end + 1;
+    const char *name = head->n > 1 ? head->tok[1] : NULL;
+    if (!name || !is_name(name)) {
+        error(a, f, line, ".macro expects a name");
+        return;
     }
-    const char *name = head->t[1];
-    if (instruction_name(name)) {
-        error(a, w, line, "cannot redefine instruction %s", name);
-        return end;
+    if (is_opcode(name)) {
+        error(a, f, line, "cannot redefine instruction %s", name);
+        return;
     }
-    if (find_macro(a, name)) {
-        error(a, w, line, "macro %s is already defined", name);
-        return end;
+    if (find_macro(a, name) >= 0) {
+        error(a, f, line, "macro %s is already defined", name);
+        return;
     }
     for (int i = 2; i < head->n; i++) {
-        if (!identifier(head->t[i]) || instruction_name(head->t[i])) {
-            error(a, w, line, "'%s' is not a valid parameter name", head->t[i]);
-            return end;
+        if (!is_name(head->tok[i]) || is_opcode(head->tok[i])) {
+            error(a, f, line, "'%s' is not a valid parameter name", head->tok[i]);
+            return;
         }
         for (int k = 2; k < i; k++)
-            if (tc_same_name(head->t[k], head->t[i])) {
-                error(a, w, line, "parameter %s is listed twice", head->t[i]);
-                return end;
+            if (tc_same_name(head->tok[k], head->tok[i])) {
+                error(a, f, line, "parameter %s is listed twice", head->tok[i]);
+                return;
             }
     }
     if (a->nmacros == a->capmacros) {
         a->capmacros = a->capmacros ? 2 * a->capmacros : 16;
         a->macros = tc_xrealloc(a->macros, (size_t)a->capmacros * sizeof *a->macros);
+        a->macro_names = tc_xrealloc(a->macro_names,
+                                     (size_t)a->capmacros * sizeof *a->macro_names);
     }
-    Macro *m = &a->macros[a->nmacros++];
+    Macro *m = &a->macros[a->nmacros];
     m->name = tc_xstrdup(name);
     m->nparams = head->n - 2;
     m->params = tc_xmalloc((size_t)(m->nparams + 1) * sizeof *m->params);
     for (int i = 0; i < m->nparams; i++)
-        m->params[i] = tc_xstrdup(head->t[i + 2]);
-    m->nlines = end - start - 1;
-    m->lines = tc_xmalloc((size_t)(m->nlines + 1) * sizeof *m->lines);
-    m->line_no = tc_xmalloc((size_t)(m->nlines + 1) * sizeof *m->line_no);
-    for (int i = 0; i < m->nlines; i++) {
-        m->lines[i] = tc_xstrdup(lines[start + 1 + i]);
-        m->line_no[i] = nos ? nos[start + 1 + i] : start + 2 + i;
+        m->params[i] = tc_xstrdup(head->tok[i + 2]);
+    m->nbody = end - first;
+    m->body = tc_xmalloc((size_t)(m->nbody + 1) * sizeof *m->body);
+    m->body_no = tc_xmalloc((size_t)(m->nbody + 1) * sizeof *m->body_no);
+    for (int i = 0; i < m->nbody; i++) {
+        m->body[i] = tc_xstrdup(f->lines[first + i]);
+        m->body_no[i] = f->nos[first + i];
     }
-    m->file = tc_xstrdup(w->file);
-    m->dir = tc_xstrdup(w->dir);
-    return end;
+    m->file = f->file;
+    m->dir = f->dir;
+    a->macro_names[a->nmacros] = m->name;
+    table_add(&a->macro_table, a->macro_names, (uint32_t)a->nmacros);
+    a->nmacros++;
 }
 
-typedef struct {
-    char  *s;
-    size_t len, cap;
-} Buf;
-
-static void buf_add(Buf *b, const char *s)
+/* One token of a body line as the call rewrites it: a parameter becomes its argument; with '#',
+   each piece that is a parameter becomes its argument and the pieces are joined (at most 299
+   characters); an @local of this call becomes @<call>:<name>.  Returns 0 after an error. */
+static int rewrite_token(Asm *a, const Frame *body, int line, const Macro *m, char *const *args,
+                         unsigned call, const char *tok, Text *out)
 {
-    size_t n = strlen(s);
-    if (b->len + n + 1 > b->cap) {
-        b->cap = 2 * (b->len + n + 1);
-        b->s = tc_xrealloc(b->s, b->cap);
+    char joined[300], local[320];
+    if (strchr(tok, '#')) {
+        size_t at = 0;
+        joined[0] = '\0';
+        for (const char *piece = tok; at < sizeof joined;) {
+            size_t n = strcspn(piece, "#");
+            char part[300];
+            snprintf(part, sizeof part, "%.*s", (int)n, piece);
+            int p = param_of(m, part);
+            int k = snprintf(joined + at, sizeof joined - at, "%s", p >= 0 ? args[p] : part);
+            at += k > 0 ? (size_t)k : 0;
+            if (!piece[n])
+                break;
+            piece += n + 1;
+        }
+        tok = joined;
+    } else {
+        int p = param_of(m, tok);
+        if (p >= 0)
+            tok = args[p];
     }
-    memcpy(b->s + b->len, s, n + 1);
-    b->len += n;
+    /* a lone '@' is .link syntax; a name holding ':' is an outer call's local already */
+    if (tok[0] == '@' && tok[1] && !strchr(tok, ':')) {
+        if (!is_name(tok + 1)) {
+            error(a, body, line, "'%s' is not a valid local name", tok);
+            return 0;
+        }
+        snprintf(local, sizeof local, "@%u:%s", call, tok + 1);
+        tok = local;
+    }
+    int quote = !*tok || strchr(tok, ' ');
+    if (quote)
+        text_puts(out, "\"");
+    text_puts(out, tok);
+    if (quote)
+        text_puts(out, "\"");
+    return 1;
 }
 
-/* One macro call: parameters substituted, pieces joined at '#', every @local renamed to
-   "@<call>:<name>" (names that already hold ':' belong to an outer call), then the body is
-   assembled in the macro's own file context. */
-static void call_macro(Asm *a, const Where *w, int line, const Macro *m, char *const *args)
+/* A call of macro mi with the tokens after the name as arguments: the rewritten body becomes a
+   new frame on top of f. */
+static void call_macro(Asm *a, Frame *f, int line, long mi, char *const *args)
 {
-    if (w->depth >= NEST_LIMIT) {
-        error(a, w, line, "macros nested too deeply (does %s call itself?)", m->name);
+    const Macro *m = &a->macros[mi];
+    if (f->depth >= NEST_LIMIT) {
+        error(a, f, line, "macros nested too deeply (does %s call itself?)", m->name);
         return;
     }
     for (int i = 0; i < m->nparams; i++) {
         size_t digits = strspn(args[i], "0123456789");
-        if (!(digits > 0 && !args[i][digits]) && !name_ok(a, w, line, args[i]))
+        if ((!digits || args[i][digits]) && !check_name(a, f, line, args[i]))
             return;
     }
-    unsigned id = ++a->calls;
-    char from[512];
-    if (!w->from)
-        snprintf(from, sizeof from, "%s:%d", w->file, line);
-    Where sub = {m->file, m->dir, w->from ? w->from : from, w->depth + 1, 1};
-
-    int n = m->nlines;
-    const int *nos = m->line_no;
-    char **body = tc_xmalloc((size_t)(n + 1) * sizeof *body);
-    for (int b = 0; b < n; b++) {
-        Toks t;
-        Buf out = {0};
-        buf_add(&out, "");
-        const char *e = split(m->lines[b], &t);
-        if (e)
-            error(a, &sub, nos[b], "%s", e);
-        for (int i = 0; !e && i < t.n; i++) {
-            const char *tok = t.t[i];
-            char joined[300], local[320];
-            if (strchr(tok, '#')) {
-                size_t at = 0;
-                const char *s = tok;
-                for (;;) {
-                    const char *h = strchr(s, '#');
-                    size_t len = h ? (size_t)(h - s) : strlen(s);
-                    char piece[300];
-                    snprintf(piece, sizeof piece, "%.*s", (int)len, s);
-                    int p = param(m, piece);
-                    at += (size_t)snprintf(joined + at, sizeof joined - at, "%s",
-                                           p >= 0 ? args[p] : piece);
-                    if (!h || at >= sizeof joined)
-                        break;
-                    s = h + 1;
-                }
-                tok = joined;
-            } else {
-                int p = param(m, tok);
-                if (p >= 0)
-                    tok = args[p];
-            }
-            if (tok[0] == '@' && tok[1] && !strchr(tok, ':')) {
-                if (!identifier(tok + 1)) {
-                    error(a, &sub, nos[b], "'%s' is not a valid local name", tok);
-                    break;
-                }
-                snprintf(local, sizeof local, "@%u:%s", id, tok + 1);
-                tok = local;
-            }
-            int quote = !*tok || strchr(tok, ' ');
+    unsigned call = ++a->calls;
+    const char *from = f->from;
+    if (!from) {
+        char site[512];
+        snprintf(site, sizeof site, "%s:%d", f->file, line);
+        from = keep(a, tc_xstrdup(site));
+    }
+    Frame body = {0};
+    body.file = m->file;
+    body.dir = m->dir;
+    body.from = from;
+    body.depth = f->depth + 1;
+    body.local_ok = 1;
+    body.n = m->nbody;
+    body.lines = tc_xmalloc((size_t)(m->nbody + 1) * sizeof *body.lines);
+    body.nos = tc_xmalloc((size_t)(m->nbody + 1) * sizeof *body.nos);
+    for (int b = 0; b < m->nbody; b++) {
+        Text out = {0};
+        text_put(&out, "", 0);
+        Line l;
+        const char *bad = lex(m->body[b], &l);
+        if (bad)
+            error(a, &body, m->body_no[b], "%s", bad);
+        for (int i = 0; !bad && i < l.n; i++) {
             if (i)
-                buf_add(&out, " ");
-            if (quote)
-                buf_add(&out, "\"");
-            buf_add(&out, tok);
-            if (quote)
-                buf_add(&out, "\"");
+                text_puts(&out, " ");
+            if (!rewrite_token(a, &body, m->body_no[b], m, args, call, l.tok[i], &out))
+                break;
         }
-        free(t.copy);
-        body[b] = out.s;
+        line_free(&l);
+        body.lines[b] = out.s;
+        body.nos[b] = m->body_no[b];
     }
-    if (!a->failed)
-        assemble_lines(a, &sub, body, nos, n);
-    for (int b = 0; b < n; b++)
-        free(body[b]);
-    free(body);
+    *push_frame(a) = body;  /* f may have moved */
 }
 
-/* ---- lines --------------------------------------------------------------------------------- */
+/* ---- the driver -------------------------------------------------------------------------------- */
 
-static void one_line(Asm *a, const Where *w, int line, const Toks *t)
+static void statement(Asm *a, Frame *f, int line, Line *l)
 {
-    const char *op = t->t[0];
+    const char *op = l->tok[0];
     if (op[0] == '.') {
-        if (tc_same_name(op, ".in"))
-            io_list(a, w, line, t, &a->in, &a->nin, &a->capin);
-        else if (tc_same_name(op, ".out"))
-            io_list(a, w, line, t, &a->out, &a->nout, &a->capout);
+        if (tc_same_name(op, ".in") || tc_same_name(op, ".out"))
+            declare_io(a, f, line, l, tc_same_name(op, ".out"));
         else if (tc_same_name(op, ".link"))
-            link_line(a, w, line, t);
-        else if (tc_same_name(op, ".include") && t->n == 2)
-            include(a, w, line, t->t[1]);
+            declare_link(a, f, line, l);
+        else if (tc_same_name(op, ".include") && l->n == 2)
+            include(a, f, line, l->tok[1]);
         else if (tc_same_name(op, ".include"))
-            error(a, w, line, ".include expects one file name");
+            error(a, f, line, ".include expects one file name");
         else if (tc_same_name(op, ".endm"))
-            error(a, w, line, ".endm without .macro");
+            error(a, f, line, ".endm without .macro");
         else
-            error(a, w, line, "unknown directive %s", op);
-        return;
+            error(a, f, line, "unknown directive %s", op);
+    } else if (is_opcode(op)) {
+        instruction(a, f, line, l);
+    } else {
+        long mi = find_macro(a, op);
+        if (mi < 0)
+            error(a, f, line, "unknown instruction or macro '%s'", op);
+        else if (l->n - 1 != a->macros[mi].nparams)
+            error(a, f, line, "macro %s expects %d argument%s, got %d", a->macros[mi].name,
+                  a->macros[mi].nparams, a->macros[mi].nparams == 1 ? "" : "s", l->n - 1);
+        else
+            call_macro(a, f, line, mi, l->tok + 1);
     }
-    if (instruction_name(op)) {
-        if (t->n != 2) {
-            error(a, w, line, "%s expects exactly one cell", op);
-            return;
-        }
-        if (!name_ok(a, w, line, t->t[1]))
-            return;
-        uint32_t c = cell(a, t->t[1]);
-        int sto = tc_same_name(op, "STO");
-        if (sto && readonly(a, c)) {
-            error(a, w, line, "cannot store to %s cell %s", kind_text(a, c), t->t[1]);
-            return;
-        }
-        if (a->len == a->cap) {
-            a->cap = a->cap ? 2 * a->cap : 256;
-            a->code = tc_xrealloc(a->code, a->cap * sizeof *a->code);
-        }
-        a->code[a->len].op = (uint8_t)(sto ? OP_STO : OP_NAND);
-        a->code[a->len].addr = c;
-        a->len++;
-        return;
-    }
-    const Macro *m = find_macro(a, op);
-    if (!m) {
-        error(a, w, line, "unknown instruction or macro '%s'", op);
-        return;
-    }
-    if (t->n - 1 != m->nparams) {
-        error(a, w, line, "macro %s expects %d argument%s, got %d", m->name, m->nparams,
-              m->nparams == 1 ? "" : "s", t->n - 1);
-        return;
-    }
-    call_macro(a, w, line, m, t->t + 1);
 }
 
-static void assemble_lines(Asm *a, const Where *w, char **lines, const int *nos, int n)
+/* Reads lines from the top frame until every frame is done or an error is recorded. */
+static void drive(Asm *a)
 {
-    for (int i = 0; i < n && !a->failed; i++) {
-        int line = nos ? nos[i] : i + 1;
-        Toks t;
-        const char *e = split(lines[i], &t);
-        if (e)
-            error(a, w, line, "%s", e);
-        else if (t.n > 0 && tc_same_name(t.t[0], ".macro"))
-            i = define_macro(a, w, &t, lines, nos, i, n);
-        else if (t.n > 0)
-            one_line(a, w, line, &t);
-        free(t.copy);
+    while (a->nframes && !a->failed) {
+        Frame *f = &a->frames[a->nframes - 1];
+        if (f->at == f->n) {
+            pop_frame(a);
+            continue;
+        }
+        int line = f->nos[f->at];
+        Line l;
+        const char *bad = lex(f->lines[f->at++], &l);
+        if (bad)
+            error(a, f, line, "%s", bad);
+        else if (l.n && tc_same_name(l.tok[0], ".macro"))
+            define_macro(a, f, &l);
+        else if (l.n)
+            statement(a, f, line, &l);
+        line_free(&l);
     }
+    while (a->nframes)
+        pop_frame(a);
 }
 
-/* ---- entry points -------------------------------------------------------------------------- */
+/* ---- entry points ------------------------------------------------------------------------------ */
 
-static void start(Asm *a, char *err, size_t errlen)
+static void begin(Asm *a, char *err, size_t errlen)
 {
     memset(a, 0, sizeof *a);
     a->err = err;
     a->errlen = errlen;
     if (errlen)
         err[0] = '\0';
-    grow_slots(a);
     cell(a, "ZERO");
     cell(a, "ONE");
 }
 
-static int finish(Asm *a, Program *out)
+static int end(Asm *a, Program *out)
 {
     for (int i = 0; i < a->nmacros; i++) {
         Macro *m = &a->macros[i];
         for (int k = 0; k < m->nparams; k++)
             free(m->params[k]);
-        for (int k = 0; k < m->nlines; k++)
-            free(m->lines[k]);
+        for (int k = 0; k < m->nbody; k++)
+            free(m->body[k]);
         free(m->name);
         free(m->params);
-        free(m->lines);
-        free(m->line_no);
-        free(m->file);
-        free(m->dir);
+        free(m->body);
+        free(m->body_no);
     }
     free(a->macros);
-    free(a->slots);
+    free(a->macro_names);
+    free(a->macro_table.slot);
+    free(a->cells.slot);
+    for (size_t i = 0; i < a->nstrings; i++)
+        free(a->strings[i]);
+    free(a->strings);
+    free(a->frames);
     Program p;
     memset(&p, 0, sizeof p);
     p.code = a->code;
@@ -701,11 +815,10 @@ static int finish(Asm *a, Program *out)
     p.ninputs = a->nin;
     p.outputs = a->out;
     p.noutputs = a->nout;
-    p.special = a->info;
-    if (!a->special) {
+    if (a->special)
+        p.special = a->info;
+    else
         free(a->info);
-        p.special = NULL;
-    }
     if (a->failed) {
         tc_program_free(&p);
         memset(out, 0, sizeof *out);
@@ -719,26 +832,27 @@ int tc_asm_string(const char *src, const char *name, const char *base_dir, Progr
                   char *err, size_t errlen)
 {
     Asm a;
-    start(&a, err, errlen);
-    char *text = tc_xstrdup(src);
-    assemble_text(&a, text, name ? name : "<string>", base_dir ? base_dir : ".", NULL, 0);
-    free(text);
-    return finish(&a, out);
+    begin(&a, err, errlen);
+    const char *file = keep(&a, tc_xstrdup(name));
+    const char *dir = keep(&a, tc_xstrdup(base_dir));
+    push_text(&a, tc_xstrdup(src), file, dir, NULL, 0);
+    drive(&a);
+    return end(&a, out);
 }
 
 int tc_asm_file(const char *path, Program *out, char *err, size_t errlen)
 {
-    char *text = slurp(path);
+    char *text = read_text(path);
     if (!text) {
         memset(out, 0, sizeof *out);
         snprintf(err, errlen, "%s: cannot open file", path);
         return 0;
     }
     Asm a;
-    start(&a, err, errlen);
-    char *dir = directory(path);
-    assemble_text(&a, text, path, dir, NULL, 0);
-    free(dir);
-    free(text);
-    return finish(&a, out);
+    begin(&a, err, errlen);
+    const char *file = keep(&a, tc_xstrdup(path));
+    const char *dir = keep(&a, parent_dir(path));
+    push_text(&a, text, file, dir, NULL, 0);
+    drive(&a);
+    return end(&a, out);
 }
