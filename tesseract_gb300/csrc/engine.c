@@ -246,21 +246,25 @@ functions:
 
 /* ---- verify / equiv / search ---------------------------------------------------------------- */
 
+/* Keeps hit[0..nhit) the EN_SHOW smallest hits seen, ascending (the contract of enum_add_hit,
+   src/enum.c:31-46): x goes after the hits not above it, and the largest falls off a full list. */
 void cuda_enum_add_hit(EnumResult *r, uint64_t x)
 {
-    int i;
-    if (r->nhit < EN_SHOW) {
-        i = r->nhit++;
-    } else {
-        if (x >= r->hit[EN_SHOW - 1])
-            return;
-        i = EN_SHOW - 1;
+    int n = r->nhit;
+    if (n == EN_SHOW && x >= r->hit[EN_SHOW - 1])
+        return;
+    int lo = 0, hi = n;  /* the first hit above x */
+    while (lo < hi) {
+        int mid = (lo + hi) / 2;
+        if (r->hit[mid] > x)
+            hi = mid;
+        else
+            lo = mid + 1;
     }
-    while (i > 0 && r->hit[i - 1] > x) {
-        r->hit[i] = r->hit[i - 1];
-        i--;
-    }
-    r->hit[i] = x;
+    int kept = n < EN_SHOW ? n : EN_SHOW - 1;
+    memmove(&r->hit[lo + 1], &r->hit[lo], (size_t)(kept - lo) * sizeof r->hit[0]);
+    r->hit[lo] = x;
+    r->nhit = kept + 1;
 }
 
 /* Adds one share's result into a total, as merge_raw does with --raw lines
@@ -278,6 +282,8 @@ void cuda_enum_merge(EnumResult *into, const EnumResult *part)
         cuda_enum_add_hit(into, part->hit[i]);
 }
 
+/* map[i] = the position in lb of the cell named like la[i] (names compare without case; the
+   last of equal names wins), for lists of equal length (enum_match, src/enum.c:48-78). */
 static int match_names(const Program *a, const uint32_t *la, size_t na, const Program *b,
                        const uint32_t *lb, size_t nb, int *map, const char *what, char *err,
                        size_t errlen)
@@ -285,13 +291,14 @@ static int match_names(const Program *a, const uint32_t *la, size_t na, const Pr
     if (na != nb)
         return tc_fail(err, errlen, "the programs have %zu and %zu %s", na, nb, what);
     for (size_t i = 0; i < na; i++) {
-        map[i] = -1;
-        for (size_t j = 0; j < nb; j++)
-            if (tc_same_name(a->cell_names[la[i]], b->cell_names[lb[j]]))
-                map[i] = (int)j;
-        if (map[i] < 0)
+        const char *name = a->cell_names[la[i]];
+        size_t j = nb;
+        while (j > 0 && !tc_same_name(b->cell_names[lb[j - 1]], name))
+            j--;
+        if (!j)
             return tc_fail(err, errlen, "the second program has no %s called %s",
-                           what[0] == 'i' ? "input" : "output", a->cell_names[la[i]]);
+                           what[0] == 'i' ? "input" : "output", name);
+        map[i] = (int)(j - 1);
     }
     return 1;
 }

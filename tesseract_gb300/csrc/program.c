@@ -5,6 +5,7 @@
 #include <stdarg.h>
 #include <stdlib.h>
 #include <string.h>
+#include <strings.h>
 
 #include "tc_host.h"
 
@@ -46,10 +47,7 @@ char *tc_xstrdup(const char *s)
 
 int tc_same_name(const char *a, const char *b)
 {
-    for (; *a && *b; a++, b++)
-        if (tolower((unsigned char)*a) != tolower((unsigned char)*b))
-            return 0;
-    return *a == *b;
+    return strcasecmp(a, b) == 0;
 }
 
 uint64_t tc_splitmix64(uint64_t *s)

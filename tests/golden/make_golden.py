@@ -3,6 +3,7 @@
     python tests/golden/make_golden.py [path/to/alpha]          # programs.json, enum.json
     python tests/golden/make_golden.py --cli [path/to/alpha]    # cli.json
     python tests/golden/make_golden.py --tester1 [path/to/alpha]  # tester1.json
+    python tests/golden/make_golden.py --cli-cpu [path/to/alpha]  # cli_cpu.json
 
 Needs the reference's `alpha` binary built from its sources (oracle/Makefile builds it into
 oracle/_ref/alpha on an x86 host that has the sources).  Programs come from the reference's own
@@ -16,6 +17,8 @@ Outputs:
     enum.json       enumeration cases and the reference's results
     cli.json        the reference's stdout and exit code for command lines of the hot path
     tester1.json    the reference's `tester1 --raw` histogram lines for a few configurations
+    cli_cpu.json    the reference's stdout, stderr and exit code for command lines that need no
+                    GPU: --merge of shares it wrote, option errors and refusals
 """
 from __future__ import annotations
 
@@ -191,7 +194,7 @@ def main():
         json.dump(results, f, indent=1)
 
 
-if __name__ == "__main__" and "--cli" not in sys.argv and "--tester1" not in sys.argv:
+if __name__ == "__main__" and not {"--cli", "--tester1", "--cli-cpu"} & set(sys.argv):
     main()
 
 
@@ -281,3 +284,84 @@ def t1_main():
 
 if __name__ == "__main__" and "--tester1" in sys.argv:
     t1_main()
+
+
+# ---- the command line without a GPU: merged shares, option errors, refusals -------------------
+
+# (args, shares): shares are command lines whose --raw output the reference writes into the files
+# {raw0}, {raw1}, ... named by args; every other case runs as given.
+CLI_CPU_CASES = [
+    (["verify", "{mul10}", "--spec", "p = a * b ^ (a & 1)", "--merge", "{raw0}", "{raw1}",
+      "{raw2}"],
+     [["verify", "{mul10}", "--spec", "p = a * b ^ (a & 1)", "--part", f"{i}/3", "--raw"]
+      for i in range(3)]),
+    (["verify", "{mul10}", "--spec", "p = a * b ^ (a & 1)", "--merge", "{raw0}", "{raw1}"],
+     [["verify", "{mul10}", "--spec", "p = a * b ^ (a & 1)", "--part", "0-1/4", "--raw"],
+      ["verify", "{mul10}", "--spec", "p = a * b ^ (a & 1)", "--part", "3/4", "--raw"]]),
+    (["verify", "{mul10}", "--spec", "p = a * b", "--merge", "{raw0}", "{raw1}"],
+     [["verify", "{mul10}", "--spec", "p = a * b", "--part", f"{i}/2", "--raw"]
+      for i in range(2)]),
+    (["equiv", "{ra}", "{rc}", "--merge", "{raw0}", "{raw1}"],
+     [["equiv", "{ra}", "{rc}", "--part", f"{i}/2", "--raw"] for i in range(2)]),
+    (["search", "{hash16}", "--want", "h = 34272", "--merge", "{raw0}", "{raw1}"],
+     [["search", "{hash16}", "--want", "h = 34272", "--part", f"{i}/2", "--raw"]
+      for i in range(2)]),
+    (["search", "{hash16}", "--want", "h = 1", "--merge", "{raw0}"],
+     [["search", "{hash16}", "--want", "h = 1", "--part", "0/1", "--raw"]]),
+    (["verify", "{mul10}", "--spec", "p = a * b", "--merge", "{raw0}", "missing.raw"],
+     [["verify", "{mul10}", "--spec", "p = a * b", "--part", "0/2", "--raw"]]),
+    (["verify"], []),
+    (["verify", "{mul4}"], []),
+    (["search", "{mul4}"], []),
+    (["verify", "{mul4}", "--spec"], []),
+    (["verify", "{mul4}", "--spec", "p = a * b", "--ticks", "0"], []),
+    (["verify", "{mul4}", "--spec", "p = a * b", "--ticks", "x"], []),
+    (["verify", "{mul4}", "--spec", "p = a * b", "--ticks"], []),
+    (["verify", "{mul4}", "--spec", "p = a * b", "--part", "1"], []),
+    (["verify", "{mul4}", "--spec", "p = a * b", "--part", "1-x/4"], []),
+    (["verify", "{mul4}", "--spec", "p = a * b", "--bogus"], []),
+    (["verify", "{mul4}", "--spec", "q = a"], []),
+    (["verify", "{mul4}", "--spec", "p = a +"], []),
+    (["search", "{hash16}", "--want", "h = x"], []),
+    (["verify", "missing.asm", "--spec", "p = a"], []),
+    (["equiv", "{ra}", "{mul4}"], []),
+    (["equiv", "{mul4}", "missing.asm"], []),
+    (["verify", "{links}", "--spec", "y = x"], []),
+    (["verify", "{mul4}", "--spec", "p = a * b", "--part", "3/2"], []),
+]
+
+
+def cli_cpu_main():
+    out = []
+    with tempfile.TemporaryDirectory() as tmp:
+        progs, paths = cli_programs(tmp)
+        extra = {"mul10": gen_text("mul", {"bits": 10}),
+                 "links": ".in x\n.out y\n.link l = x @ 3\nNAND l\nSTO y\n"}
+        for k, v in extra.items():
+            paths[k] = os.path.join(tmp, k + ".asm")
+            with open(paths[k], "w") as f:
+                f.write(v)
+        for args, shares in CLI_CPU_CASES:
+            raws = []
+            for i, sh in enumerate(shares):
+                rc, stdout, stderr = run([a.format(**paths) for a in sh])
+                assert rc == 0, (sh, stderr)
+                raws.append(stdout)
+                paths["raw%d" % i] = os.path.join(tmp, "raw%d" % i)
+                with open(paths["raw%d" % i], "w") as f:
+                    f.write(stdout)
+            cwd = os.getcwd()
+            os.chdir(tmp)
+            try:
+                rc, stdout, stderr = run([a.format(**paths) for a in args])
+            finally:
+                os.chdir(cwd)
+            out.append({"args": args, "raws": raws, "rc": rc,
+                        "stdout": stdout.replace(tmp + "/", ""),
+                        "stderr": stderr.replace(tmp + "/", "")})
+    with open(os.path.join(HERE, "cli_cpu.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__" and "--cli-cpu" in sys.argv:
+    cli_cpu_main()

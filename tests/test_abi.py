@@ -45,3 +45,20 @@ def test_no_gpu_calls_fail_cleanly_without_a_gpu():
     p = T.Program.gen_mul(4)
     with pytest.raises(T.EngineError, match="CUDA"):
         T.enum_run(T.EN_VERIFY, p, spec=T.Spec(p, "p = a * b"))
+
+
+def test_enum_add_hit_keeps_the_sixteen_smallest():
+    """cuda_enum_add_hit against a plain model of enum_add_hit (src/enum.c:31-46): hits in any
+    order, repeats included, leave the 16 smallest in ascending order."""
+    import ctypes as C
+    import random
+    L = T.lib()
+    L.cuda_enum_add_hit.argtypes = [C.POINTER(T.EnumResult), C.c_uint64]
+    rng = random.Random(8)
+    for trial in range(300):
+        r, model = T.EnumResult(), []
+        for _ in range(rng.randint(0, 60)):
+            x = rng.randrange(40 if trial % 3 == 0 else 2**64)
+            L.cuda_enum_add_hit(C.byref(r), x)
+            model = sorted(model + [x])[:16]
+        assert [r.hit[i] for i in range(r.nhit)] == model
