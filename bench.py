@@ -1,29 +1,46 @@
-"""Benchmark: exhaustive verify of the 16 x 16 array multiplier on the GPU.
+"""Benchmark: exhaustive verify of the 16 x 16 array multiplier on the GPU, and the other
+workloads beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config verify|life|batch|super|serve] [--replicas]
 
-Workload (one step): `alpha verify <gen mul --bits 16> --spec "p = a * b"` -- the 6,040-instruction
-NAND/STO multiplier run on all 2^32 (a, b) and compared with a * b, through the engine's C ABI
-(cuda_enum_run).  The metric is the reference's "1-bit operations" (program length x
-assignments x ticks, src/enum.c:164): 6,040 x 2^32 = 2.594e13 lane-ops per step.
+Headline workload (one step): `alpha verify <gen mul --bits 16> --spec "p = a * b"` -- the
+6,040-instruction NAND/STO multiplier run on all 2^32 (a, b) and compared with a * b, through the
+engine's C ABI (cuda_enum_run).  The metric is the reference's "1-bit operations" (program length
+x assignments x ticks, src/enum.c:164): 6,040 x 2^32 = 2.594e13 lane-ops per step.
 
-  value      lane-ops/s from the kernel's own CUDA-event time (device work only)
+  value      lane-ops/s from the kernel's own CUDA-event time (device work only); beside it
+             assignments/s
   e2e        lane-ops/s from the host clock around the C-ABI call: code generation and module
              cache lookup, launch, and the device-to-host read of the result
   roofline   the verify kernel against the measured LOP3 issue rate of the same GPU
-             (cuda_lop3_peak: 32-bit 3-input logic ops/s; x 32 one-bit lanes)
+             (cuda_lop3_peak, 32-bit 3-input logic ops/s): achieved = the logic operations the
+             generated kernel issues per 32-lane word (LUTs per step, hoisted LUTs over their
+             stretch, the compare's carry chain; counted by the code generator) x words / kernel
+             time.  frac_accounting is the reference's lane-op accounting over the same peak
+             x 32 lanes (above 1: the LUT network and the hoisting do less work than 6,040 NAND/STO
+             per lane).
+  sustained  the same launch back to back for at least 5 s, with the SM clock sampled
+  configs    the other four workloads (cube Life, the 4,096-pair batch, the superoptimizer, the
+             served streams), each with its own clocks, wall time and pass/fail
   cpu_baseline  the oracle's CPU port of the reference's enumerator (bit-sliced, all host
              threads, scalar per-lane spec compare as in src/enum.c:186-200) on a bounded sample
 
---impl reference times that CPU port on the same workload as the main line (the reference's own
-AVX2/x86 engines do not build on this aarch64 host).
+--impl reference times the reference's own enumerator where it was built from its sources on
+this host (x86), else the oracle's C port of it (the reference's AVX2/x86 engines do not build on
+the aarch64 GPU host).  Its inputs are the reference's own generator output
+(tests/golden/mul16.asm.gz, sha256-pinned) read by the oracle: nothing of this engine is loaded.
 
-With N > 1 (torchrun, one rank per GPU) every rank verifies the whole space on its own GPU
-(replicas: the enumeration needs no exchange), rank 0 prints the line; value is the sum.
+With N > 1 (torchrun, one rank per GPU) rank r verifies share r of N of the space (the
+reference's --part rule, no exchange on the data path) and the shares' results are gathered and
+merged once afterwards (scaling "strong"); --replicas runs the whole space on every rank
+instead (scaling "weak").
 """
 from __future__ import annotations
 
 import argparse
+import gzip
+import hashlib
 import json
 import os
 import statistics
@@ -33,20 +50,23 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 METRIC = "bit-exact 1-bit NAND lane-ops/s vs LOP3 peak; batched jobs/s, p50/p99 vs plain"
 WORKLOAD = ("verify gen mul --bits 16 (6040 NAND/STO instructions, 72 cells) over all 2^32 "
             "(a, b) against p = a * b")
 
-
-VERIFY_DRAM_BYTES = 32000  # dram__bytes_read.sum + dram__bytes_write.sum, one tc_enum launch
+# dram__bytes_read.sum + dram__bytes_write.sum of one full-space tc_enum launch, from the ncu
+# capture summarised in this file (the kernel's code and arguments; its state is in registers)
+VERIFY_DRAM_BYTES = 32000
+VERIFY_PROFILE = "profiles/tc_enum_verify_mul16.md"
+VERIFY_ALU_PIPE_NCU = 0.973
 
 
 def measured_peaks() -> dict:
     """MEASURED_PEAKS.json beside this file, when the run has one."""
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
     try:
-        with open(path) as f:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             return json.load(f)
     except (OSError, ValueError):
         return {}
@@ -64,9 +84,10 @@ class Clocks:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu: int):
+    def __init__(self, gpu: int = 0):
         self.gpu = gpu
         self.p = None
+        self.out = ""
 
     def __enter__(self):
         try:
@@ -79,7 +100,6 @@ class Clocks:
         return self
 
     def __exit__(self, *exc):
-        self.out = ""
         if self.p:
             self.p.terminate()
             try:
@@ -88,15 +108,16 @@ class Clocks:
                 self.p.kill()
 
     def summary(self):
-        sm, mx, reasons = [], [], set()
+        sm, mx, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in getattr(self, "out", "").splitlines():
+        for line in self.out.splitlines():
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
             try:
                 sm.append(float(f[1]))
                 mx.append(float(f[2]))
+                power.append(float(f[3]))
             except ValueError:
                 continue
             for n, v in zip(names, f[5:9]):
@@ -105,20 +126,36 @@ class Clocks:
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
-                "reasons": sorted(reasons)}
+                "power_w_max": max(power), "reasons": sorted(reasons)}
+
+
+# ---- the CPU side: the reference's inputs, read by the oracle --------------------------------
+
+def reference_inputs():
+    """The headline program and spec without this engine: the text the reference's `gen mul
+    --bits 16` printed (tests/golden/mul16.asm.gz, checked against the sha256 pinned in
+    tests/golden/programs.json), read by the oracle, and `p = a * b` laid out by the oracle."""
+    import oracle as O
+    with gzip.open(os.path.join(GOLDEN, "mul16.asm.gz"), "rt") as f:
+        text = f.read()
+    with open(os.path.join(GOLDEN, "programs.json")) as f:
+        pinned = json.load(f)['mul:{"bits": 16}']
+    if hashlib.sha256(text.encode()).hexdigest() != pinned:
+        raise RuntimeError("tests/golden/mul16.asm.gz is not the reference's gen mul output")
+    prog = O.PrintedProgram(text)
+    return prog, prog.product_spec()
 
 
 def cpu_sample(seconds_target=12.0):
-    """The oracle's CPU port on a bounded sample of the same workload: lane-ops/s."""
+    """The oracle's CPU port on a bounded sample of the headline workload: lane-ops/s."""
     import oracle as O
-    import tesseract_gb300 as T
-    p = T.Program.gen_mul(16)
-    s = T.Spec(p, "p = a * b")
+    prog, spec = reference_inputs()
+    e = O.verify_struct(prog, spec)
     threads = os.cpu_count() or 1
     chunks = threads
     while True:
         t0 = time.perf_counter()
-        r = O.enum_run(T.EN_VERIFY, p, spec=s, threads=threads, limit_chunks=chunks)
+        r = O.enum_run_struct(e, threads=threads, limit_chunks=chunks)
         dt = time.perf_counter() - t0
         if dt > seconds_target / 4 or chunks > 1 << 20:
             break
@@ -126,7 +163,7 @@ def cpu_sample(seconds_target=12.0):
     if dt < seconds_target * 0.8:
         chunks = max(chunks, int(chunks * seconds_target / dt))
         t0 = time.perf_counter()
-        r = O.enum_run(T.EN_VERIFY, p, spec=s, threads=threads, limit_chunks=chunks)
+        r = O.enum_run_struct(e, threads=threads, limit_chunks=chunks)
         dt = time.perf_counter() - t0
     assert r["hits"] == 0
     return {"value": r["ops"] / dt, "unit": "lane-ops/s", "cores": threads, "kind": "port",
@@ -142,9 +179,6 @@ def run_reference(args):
     if rank != 0:
         return 0
     import oracle as O
-    import tesseract_gb300 as T
-    from tesseract_gb300 import build
-    build.build(reference=False)
     threads = os.cpu_count() or 1
     if O.have_reference():
         import tempfile
@@ -153,6 +187,7 @@ def run_reference(args):
             with open(prog, "w") as f:
                 f.write(subprocess.run([O.REF_BIN, "gen", "mul", "--bits", "16"], check=True,
                                        capture_output=True, text=True).stdout)
+
             def step(i):
                 out = subprocess.run([O.REF_BIN, "verify", prog, "--spec", "p = a * b", "--part",
                                       "%d/64" % (i % 64), "--raw"], check=True,
@@ -169,16 +204,16 @@ def run_reference(args):
             dt = time.perf_counter() - t0
         kind, sample = "reference", "alpha verify --part i/64 (2^26 assignments) per step"
     else:
-        p = T.Program.gen_mul(16)
-        s = T.Spec(p, "p = a * b")
+        prog, spec = reference_inputs()
+        e = O.verify_struct(prog, spec)
         base, _, _ = cpu_sample(seconds_target=4.0)
         chunks = int(base["sample"].split()[0])
         for _ in range(args.warmup):
-            O.enum_run(T.EN_VERIFY, p, spec=s, threads=threads, limit_chunks=max(1, chunks // 8))
+            O.enum_run_struct(e, threads=threads, limit_chunks=max(1, chunks // 8))
         ops = 0
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            r = O.enum_run(T.EN_VERIFY, p, spec=s, threads=threads, limit_chunks=chunks)
+            r = O.enum_run_struct(e, threads=threads, limit_chunks=chunks)
             assert r["hits"] == 0
             ops += r["ops"]
         dt = time.perf_counter() - t0
@@ -195,21 +230,21 @@ def run_reference(args):
                     "d2h_bytes_per_step": 0}}
     if kind == "port":
         line["note"] = ("the reference's AVX2 lane engine and x86 JIT do not build on this host; "
-                        "this is the oracle's portable C port of its enumerator")
+                        "this is the oracle's portable C port of its enumerator, on the "
+                        "reference's own gen mul output")
     print(json.dumps(line), flush=True)
     return 0
 
 
-def bench_life(args):
+# ---- the other workloads ---------------------------------------------------------------------
+
+def config_life(gens=1000):
     """Config 2: one 8192 x 8192 B3/S23 board on 65,536 machines (gen_life_cube 32 x 32 tiles,
     2^8 x 2^8 machines), board from splitmix64(42), `gens` generations on the GPU cube engine,
     checked bit for bit against plain C Life (the oracle's word-parallel life_scalar)."""
-    import numpy as np
     import oracle as O
     import tesseract_gb300 as T
-    from tesseract_gb300 import build
     from tesseract_gb300.life import LifeCube, pack_rows, unpack_rows
-    build.build(reference=False)
     t0 = time.perf_counter()
     L = LifeCube(16)
     setup_s = time.perf_counter() - t0
@@ -217,66 +252,65 @@ def bench_life(args):
     start = L.board()
     L.run(16)                       # warm-up: graph capture, first launches
     L.seed(42)
-    with Clocks(0) as clk:
+    with Clocks() as clk:
         t0 = time.perf_counter()
-        ms = L.run(args.gens)
+        ms = L.run(gens)
         wall = time.perf_counter() - t0
     final = L.board()
     packed = pack_rows(start)
     tc = time.perf_counter()
-    O.life_words(packed, args.gens)
+    O.life_words(packed, gens)
     cpu_s = time.perf_counter() - tc
     ok = bool((unpack_rows(packed) == final).all())
     n = L.program
-    cells = 8192 * 8192
-    line = {"config": "life", "metric": "generations/s (cube Life, 65,536 machines)",
-            "value": args.gens / (ms / 1e3), "unit": "gen/s", "gens": args.gens,
-            "bit_exact_vs_plain_c": ok, "kernel_ms": ms, "wall_s": wall,
-            "cell_updates_per_s": args.gens * cells / (ms / 1e3),
-            "lane_ops_per_s": args.gens * len(n) * 65536 / (ms / 1e3),
-            "program": {"instructions": len(n), "cells": n.ncells,
-                        "segments": L.cube.segments, "kernels_per_pass": L.cube.kernels},
-            "setup_s_incl_nvrtc": setup_s,
-            "cpu_word_parallel_life_s": cpu_s, "cpu_threads": os.cpu_count()}
+    rec = {"metric": "generations/s (cube Life, 65,536 machines, 8192^2 board)",
+           "value": gens / (ms / 1e3), "unit": "gen/s", "gens": gens,
+           "bit_exact_vs_plain_c": ok, "kernel_ms": ms, "wall_s": wall,
+           "cell_updates_per_s": gens * 8192 * 8192 / (ms / 1e3),
+           "lane_ops_per_s": gens * len(n) * 65536 / (ms / 1e3),
+           "program": {"instructions": len(n), "cells": n.ncells,
+                       "segments": L.cube.segments, "kernels_per_pass": L.cube.kernels},
+           "setup_s_incl_nvrtc": setup_s, "cpu_word_parallel_life_s": cpu_s,
+           "cpu_threads": os.cpu_count(), "clocks": clk.summary()}
     # the exchange between machines: 1,056 link reads per machine per generation (4 gathers
     # of the tile edges), one bit each, 476 of them across 512-machine groups
     exchange = 65536 * 1056 / 8
     peaks = measured_peaks()
-    gbs = exchange * args.gens / (ms / 1e3) / 1e9
-    line["roofline"] = {"bound": "instruction fetch and latency (2,048 words of state; the "
-                                 "27.2 MB state stays in L2)",
-                        "exchange_bytes_per_gen": exchange, "achieved": gbs,
-                        "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                        "frac": gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None,
-                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth); the "
-                                       "exchange is served from L2, not HBM",
-                        "lane_ops_per_s": args.gens * len(n) * 65536 / (ms / 1e3),
-                        "traffic": None}
-    c = clk.summary()
-    if c:
-        line["clocks"] = c
-    print(json.dumps(line), flush=True)
-    return 0 if ok else 3
+    gbs = exchange * gens / (ms / 1e3) / 1e9
+    rec["roofline"] = {"bound": "instruction issue and latency (2,048 words of state per cell; "
+                                "the 27.2 MB state stays in L2)",
+                       "exchange_bytes_per_gen": exchange, "achieved": gbs,
+                       "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                       "frac": gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None,
+                       "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth); the "
+                                      "exchange is served from L2, not HBM",
+                       "traffic": None}
+    return rec, ok
 
 
-def bench_batch(args):
-    """Config 3: 4,096 random equivalence jobs (workloads.batch_equiv_jobs) in one persistent
-    launch, against the plain engine (one NVRTC-compiled kernel per job) on a sample."""
+def config_batch(njobs=4096):
+    """Config 3: the 4,096 random equivalence pairs (workloads.batch_equiv_jobs) in one call,
+    every verdict against the reference's own (tests/golden/batch_equiv.json.gz), and the plain
+    engine (one NVRTC-compiled kernel per job) on a sample, compiling and cached."""
     import tesseract_gb300 as T
-    from tesseract_gb300 import build
     from tesseract_gb300.workloads import batch_equiv_jobs
-    build.build(reference=False)
-    jobs = batch_equiv_jobs(args.jobs)
+    jobs = batch_equiv_jobs(njobs)
     T.batch_run(jobs[:64])          # warm-up
-    with Clocks(0) as clk:
+    with Clocks() as clk:
         t0 = time.perf_counter()
         res = T.batch_run(jobs)
         wall = time.perf_counter() - t0
     ms = T.last_launch()["kernel_ms"]
     ops = sum(r["ops"] for r in res)
-    bad_equal = [j["seed"] for j, r in zip(jobs, res) if not j["mutated"] and r["hits"]]
+    ref = None
+    golden = os.path.join(GOLDEN, "batch_equiv.json.gz")
+    if njobs == 4096 and os.path.exists(golden):
+        with gzip.open(golden, "rt") as f:
+            want = json.load(f)["results"]
+        got = [[r["space"], r["tried"], r["hits"], r["ops"],
+                ",".join("%x" % x for x in r["hit"])] for r in res]
+        ref = sum(w == g for w, g in zip(want, got)) == len(want)
     controls = [r["hits"] for j, r in zip(jobs, res) if j["mutated"]]
-    # the plain engine, one generated kernel per job, on a sample: compile + run, then cached
     sample = jobs[:: max(1, len(jobs) // 32)][:32]
     t0 = time.perf_counter()
     plain = [T.enum_run(j["mode"], j["a"], j["b"]) for j in sample]
@@ -287,62 +321,59 @@ def bench_batch(args):
     idx = {j["seed"]: i for i, j in enumerate(jobs)}
     same = all(p["hits"] == q["hits"] == res[idx[j["seed"]]]["hits"] and
                p["hit"] == res[idx[j["seed"]]]["hit"] for p, q, j in zip(plain, plain2, sample))
-    line = {"config": "batch", "metric": "batched equivalence jobs/s", "jobs": len(jobs),
-            "value": len(jobs) / wall, "unit": "jobs/s", "kernel_ms": ms, "wall_s": wall,
-            "lane_ops_per_s_kernel": ops / (ms / 1e3), "lane_ops": ops,
-            "equal_pairs_with_hits": bad_equal[:10], "negative_controls": len(controls),
-            "negative_controls_detected": sum(1 for h in controls if h),
-            "plain_sample_jobs": len(sample),
-            "plain_jobs_per_s_with_compile": len(sample) / plain_cold,
-            "plain_jobs_per_s_cached": len(sample) / plain_warm,
-            "speedup_vs_plain_cached": (len(jobs) / wall) / (len(sample) / plain_warm),
-            "sample_identical_to_plain": same}
-    peak = T.lop3_peak() * 32
-    line["roofline"] = {"bound": "interpreter dispatch and shared-memory latency (LUT ops "
-                                  "interpreted from shared-memory slots)",
-                        "achieved": ops / (ms / 1e3), "peak": peak, "unit": "lane-op/s",
-                        "frac": ops / (ms / 1e3) / peak,
-                        "peak_source": "measured: cuda_lop3_peak (32-bit LOP3/s x 32 lanes)",
-                        "traffic": None}
-    c = clk.summary()
-    if c:
-        line["clocks"] = c
-    print(json.dumps(line), flush=True)
-    return 0 if (same and not bad_equal) else 3
+    rate = len(jobs) / wall
+    rec = {"metric": "batched equivalence jobs/s", "jobs": len(jobs), "value": rate,
+           "unit": "jobs/s", "kernel_ms": ms, "wall_s": wall,
+           "lane_ops_per_s_kernel": ops / (ms / 1e3), "lane_ops": ops,
+           "bit_exact_vs_reference": ref, "negative_controls": len(controls),
+           "negative_controls_detected": sum(1 for h in controls if h),
+           "plain_sample_jobs": len(sample),
+           "plain_jobs_per_s_with_compile": len(sample) / plain_cold,
+           "plain_jobs_per_s_cached": len(sample) / plain_warm,
+           "speedup_vs_plain_with_compile": rate / (len(sample) / plain_cold),
+           "speedup_vs_plain_cached": rate / (len(sample) / plain_warm),
+           "sample_identical_to_plain": same, "clocks": clk.summary()}
+    return rec, bool(same and ref is not False)
 
 
-def bench_super(args):
+def config_super():
     """Config 4: the shortest NAND/STO full adder (19, nothing of 18 or fewer) and XOR (7)."""
     import tesseract_gb300 as T
-    from tesseract_gb300 import build
-    build.build(reference=False)
-    out = {"config": "super", "metric": "proven shortest programs", "results": []}
-    for text, want in (("RR = RR ^ x", 7), ("s{a,b} = a ^ b ^ c; c = a&b | a&c | b&c", 19)):
+    out = []
+    with Clocks() as clk:
         t0 = time.perf_counter()
-        r = T.super_search(text, max_cost=24, quiet=False)
-        out["results"].append({"spec": text, "cost": r["cost"], "below": r["below"],
-                               "expected": want, "nodes": r["nodes"],
-                               "seconds": time.perf_counter() - t0, "checked": r["checked"],
-                               "program": [" ".join(x) for x in r["program"]]})
-    ok = all(x["cost"] == x["expected"] == x["below"] and x["checked"] for x in out["results"])
-    out["reference_here"] = "alpha super FA: 19, nothing <= 18, 1.2e10 nodes, 87.2 s on 8 threads"
-    print(json.dumps(out), flush=True)
-    return 0 if ok else 3
+        for text, want in (("RR = RR ^ x", 7), ("s{a,b} = a ^ b ^ c; c = a&b | a&c | b&c", 19)):
+            t1 = time.perf_counter()
+            r = T.super_search(text, max_cost=24, quiet=True)
+            out.append({"spec": text, "cost": r["cost"], "below": r["below"], "expected": want,
+                        "nodes": r["nodes"], "seconds": time.perf_counter() - t1,
+                        "checked": r["checked"],
+                        "program": [" ".join(x) for x in r["program"]]})
+        wall = time.perf_counter() - t0
+    ok = all(x["cost"] == x["expected"] == x["below"] and x["checked"] for x in out)
+    rec = {"metric": "proven shortest programs", "value": out[-1]["seconds"], "unit": "s",
+           "higher_is_better": False, "results": out, "wall_s": wall, "clocks": clk.summary(),
+           "reference_here": "alpha super FA: 19, nothing <= 18, 1.2e10 nodes, 87.2 s on 8 x86 "
+                             "threads"}
+    return rec, ok
 
 
-def bench_serve(args):
+def config_serve(n=400):
     """Config 5: a Poisson stream (2,000 jobs/s, seed 1) of mixed verify / equiv / search jobs,
     served with continuous batching (interpreter waves and compiled kernels, routed per job);
-    p50/p99 latency and jobs/s, against the plain engine (one NVRTC-compiled kernel per job, in
-    arrival order) on the first jobs of the same stream, timed before serving so that their
-    compilation counts."""
+    p50/p99 latency and jobs/s, every result against the reference's own
+    (tests/golden/serve_stream.json.gz), and the plain engine (one NVRTC-compiled kernel per
+    job, in arrival order) on the first jobs of the same stream, timed before serving so that
+    their compilation counts."""
     import tesseract_gb300 as T
-    from tesseract_gb300 import build
     from tesseract_gb300.workloads import serve_stream
-    build.build(reference=False)
-    n = args.jobs if args.jobs != 4096 else 400
-    lines, same_all = [], True
-    for label, wmax in (("config", 34), ("light", 22)):
+    golden = os.path.join(GOLDEN, "serve_stream.json.gz")
+    want = None
+    if n == 400 and os.path.exists(golden):
+        with gzip.open(golden, "rt") as f:
+            want = json.load(f)["streams"]
+    lines, ok = [], True
+    for wmax in (34, 22):
         jobs, arrivals = serve_stream(n, rate=2000.0, seed=1, max_width=wmax)
         sample = jobs[:16]
         t0 = time.perf_counter()
@@ -350,30 +381,222 @@ def bench_serve(args):
         plain_s = time.perf_counter() - t0
         T.serve_run(sample[:4], [0.0] * 4)  # warm-up: streams, slots, threads
         engines = []
-        t0 = time.perf_counter()
-        res, start, finish = T.serve_run(jobs, arrivals, engines=engines)
-        wall = time.perf_counter() - t0
+        with Clocks() as clk:
+            t0 = time.perf_counter()
+            res, start, finish = T.serve_run(jobs, arrivals, engines=engines)
+            wall = time.perf_counter() - t0
         same = all(p[k] == r[k] for p, r in zip(plain, res)
                    for k in ("space", "tried", "hits", "hit", "ops"))
-        same_all = same_all and same
+        ref = None
+        if want:
+            got = [[r["space"], r["tried"], r["hits"], r["ops"],
+                    ",".join("%x" % x for x in r["hit"])] for r in res]
+            ref = got == want[str(wmax)]
+        ok = ok and same and ref is not False
         lat = sorted(f - a for f, a in zip(finish, arrivals))
         ops = sum(r["ops"] for r in res)
         q = lambda p: lat[min(len(lat) - 1, int(p * len(lat)))]
         span = max(finish) - min(arrivals)
         plain_rate = len(sample) / plain_s
-        lines.append({"stream": label, "jobs": n, "max_width": wmax,
-                      "offered_jobs_per_s": 2000.0, "served_jobs_per_s": n / span,
-                      "p50_s": q(0.50), "p99_s": q(0.99), "wall_s": wall,
-                      "jobs_on_generated_kernels": sum(engines),
+        lines.append({"jobs": n, "max_width": wmax, "offered_jobs_per_s": 2000.0,
+                      "value": n / span, "unit": "jobs/s", "p50_s": q(0.50), "p99_s": q(0.99),
+                      "wall_s": wall, "jobs_on_generated_kernels": sum(engines),
                       "lane_ops": ops, "lane_ops_per_s": ops / span,
                       "offered_lane_ops_per_s": ops / (arrivals[-1] - arrivals[0]),
-                      "plain_sample_jobs": len(sample), "plain_jobs_per_s_with_compile": plain_rate,
+                      "bit_exact_vs_reference": ref, "plain_sample_jobs": len(sample),
+                      "plain_jobs_per_s_with_compile": plain_rate,
                       "served_vs_plain": (n / span) / plain_rate,
-                      "sample_identical_to_plain": same})
-    out = {"config": "serve", "metric": "served jobs/s, p50/p99 latency", "streams": lines,
-           "sample_identical_to_plain": same_all}
-    print(json.dumps(out), flush=True)
-    return 0 if same_all else 3
+                      "sample_identical_to_plain": same, "clocks": clk.summary()})
+    return {"metric": "served jobs/s, p50/p99 latency", "streams": lines}, ok
+
+
+CONFIGS = {"life": config_life, "batch": config_batch, "super": config_super,
+           "serve": config_serve}
+
+
+def run_configs(names):
+    """Each named workload with its own pass/fail and wall time; an error is recorded, not
+    raised, so that the headline line is still printed."""
+    out = {}
+    for name in names:
+        t0 = time.perf_counter()
+        try:
+            rec, ok = CONFIGS[name]()
+        except Exception as e:  # noqa: BLE001 -- reported in the line
+            rec, ok = {"error": "%s: %s" % (type(e).__name__, e)}, False
+        rec["ok"] = ok
+        rec["total_s"] = time.perf_counter() - t0
+        out[name] = rec
+    return out
+
+
+# ---- the headline ---------------------------------------------------------------------------
+
+def sustained(T, p, s, seconds, share):
+    """The verify launch back to back for `seconds`, with the SM clock sampled meanwhile."""
+    n, kernel_s, ops = 0, 0.0, 0
+    with Clocks() as clk:
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            r = T.enum_run(T.EN_VERIFY, p, spec=s, **share)
+            assert r["hits"] == 0
+            kernel_s += r["seconds"]
+            ops += r["ops"]
+            n += 1
+        wall = time.perf_counter() - t0
+    c = clk.summary() or {}
+    rec = {"launches": n, "wall_s": wall, "kernel_s": kernel_s, "value": ops / kernel_s,
+           "unit": "lane-ops/s", "ms_per_launch": 1e3 * kernel_s / n, "clocks": c or None}
+    if c.get("sm_mhz"):
+        # time x clock: cycles per launch, comparable across clocks
+        rec["mcycles_per_launch"] = kernel_s / n * c["sm_mhz"]
+    return rec
+
+
+def headline(args):
+    world, rank, local = dist_env()
+    dist = None
+    device = 0
+    if world > 1:
+        import torch.distributed as dist  # barrier and the result gather; no torch in the engine
+        dist.init_process_group("gloo")
+        if "CUDA_VISIBLE_DEVICES" not in os.environ:
+            os.environ["CUDA_VISIBLE_DEVICES"] = str(local)  # this rank sees its GPU as 0
+        elif len(os.environ["CUDA_VISIBLE_DEVICES"].split(",")) > local:
+            device = local  # all GPUs visible: take this rank's
+
+    import tesseract_gb300 as T
+    from tesseract_gb300 import build, shard
+    if rank == 0:
+        build.build(reference=False)
+    if dist:
+        dist.barrier()
+    err = T._err()
+    if not T.lib().cuda_engine_init(device, err, len(err)):
+        raise T.EngineError(err.value.decode())
+    p = T.Program.gen_mul(16)
+    s = T.Spec(p, "p = a * b")
+    info = T.device_info()
+    lop3 = T.lop3_peak()  # 32-bit LOP3 ops/s
+
+    sharded = world > 1 and not args.replicas
+    if sharded:
+        part = dict(part=rank, part_end=rank, parts=world)
+    else:
+        part = dict(part=0, part_end=0, parts=args.share)
+    for _ in range(max(3, args.warmup)):
+        r = T.enum_run(T.EN_VERIFY, p, spec=s, **part)
+        assert r["hits"] == 0
+    stats = T.last_launch()
+
+    if dist:
+        dist.barrier()
+    kernel_s, ops, tried, results = 0.0, 0, 0, []
+    visible = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")
+    gpu = int(visible[min(device, len(visible) - 1)] or 0)
+    with Clocks(gpu) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r = T.enum_run(T.EN_VERIFY, p, spec=s, **part)
+            kernel_s += r["seconds"]
+            ops += r["ops"]
+            tried += r["tried"]
+            results.append(r)
+        wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    assert all(x["hits"] == 0 for x in results), "verify found mismatches"
+    merged = None
+    if dist:
+        import torch
+        t = torch.tensor([wall, kernel_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        wall, kernel_s = float(t[0]), float(t[1])
+        if sharded:  # the shares' records, gathered once and merged (src/work.c:341-371)
+            merged = shard.gather_merge(results[-1])
+        t = torch.tensor([ops, tried], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        ops, tried = int(t[0]), int(t[1])
+    if rank != 0:
+        return 0
+    # a negative control outside the timed region: a wrong spec of the same shape must fail on
+    # exactly the assignments where a != 0, so the kernel visibly checks every assignment
+    control = None
+    if args.share == 1:
+        cs = T.Spec(p, "p = a * b + a")
+        if sharded:
+            cr = shard.merge([T.enum_run(T.EN_VERIFY, p, spec=cs, part=k, part_end=k,
+                                         parts=world) for k in range(world)])
+        else:
+            cr = T.enum_run(T.EN_VERIFY, p, spec=cs)
+        want = (1 << 32) - (1 << 16)
+        control = {"spec": "p = a * b + a", "hits": cr["hits"], "expected": want,
+                   "first_hits": cr["hit"][:4], "ok": cr["hits"] == want}
+        assert control["ok"], control
+    steps = args.steps
+    value = ops / kernel_s          # kernel_s: the slowest rank's
+    e2e = ops / wall
+    launch_s = kernel_s / steps
+    words = results[-1]["tried"] // 32            # per launch on one rank
+    logic = stats["logic_ops_per_word"]
+    achieved = logic * words / launch_s if logic else None
+    lane_peak = lop3 * 32
+    per_launch = results[-1]["ops"] / launch_s
+    line = {
+        "metric": METRIC, "value": value, "unit": "lane-ops/s", "n_gpus": world,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * launch_s,
+        "higher_is_better": True, "scaling": "strong" if sharded else "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "assignments_per_s": tried / kernel_s,
+        "config": {"workload": WORKLOAD + ("" if args.share == 1 else
+                                           f" (share 0 of {args.share})"),
+                   "assignments_per_step": tried // steps,
+                   "lane_ops_per_step": ops // steps,
+                   "l2": "no DRAM inputs: cell state lives in registers and every input word is "
+                         "derived from the lane index, so there is nothing to flush",
+                   "device": info,
+                   "parallelism": (f"--part shares x{world}" if sharded else
+                                   f"replicas x{world}")},
+        "result": {"mismatches": 0, "tried_per_step": tried // steps,
+                   "negative_control": control,
+                   "merged_shares": ({k: merged[k] for k in ("space", "tried", "hits", "ops")}
+                                     if merged else None)},
+        "roofline": {
+            "bound": "alu-lop3", "achieved": achieved, "peak": lop3, "unit": "LOP3/s",
+            "frac": achieved / lop3 if achieved else None,
+            "peak_source": "measured: cuda_lop3_peak microbenchmark on this GPU (32-bit LOP3/s)",
+            "logic_ops_per_word": logic, "words_per_launch": words,
+            "work_per_word": {"luts_per_step": stats["luts_per_step"],
+                              "luts_per_stretch": stats["luts_per_stretch"],
+                              "stretch_steps": stats["stretch_steps"],
+                              "compare_ops": stats["compare_ops"]},
+            "frac_accounting": per_launch / lane_peak,
+            "accounting": {"achieved": per_launch, "peak": lane_peak, "unit": "lane-op/s",
+                           "note": "the reference's 6,040 NAND/STO lane-ops per assignment "
+                                   "over the LOP3 peak x 32 lanes"},
+            "traffic": VERIFY_DRAM_BYTES if args.share == 1 and not sharded else None,
+            "traffic_unit": "bytes per launch", "traffic_source": VERIFY_PROFILE,
+            "alu_pipe_busy_ncu": VERIFY_ALU_PIPE_NCU},
+        "kernel": {"regs": stats["regs"], "local_bytes": stats["local_bytes"],
+                   "grid": stats["grid"], "block": stats["block"],
+                   "compile_seconds": stats["compile_seconds"]},
+        "e2e": {"value": e2e, "unit": "lane-ops/s", "h2d_bytes_per_step": 72,
+                "d2h_bytes_per_step": 8 + 4 * stats["grid"] * stats["block"] // 32,
+                "path": "cuda_enum_run through the C ABI with host Program/Spec structs"},
+        "gpu_launches": steps,
+    }
+    clocks = clk.summary()
+    if clocks:
+        line["clocks"] = clocks
+    if args.sustained > 0:
+        line["sustained"] = sustained(T, p, s, args.sustained, part)
+    if args.configs and world == 1:
+        line["configs"] = run_configs(args.configs.split(","))
+    if not args.no_cpu:
+        base, _, _ = cpu_sample()
+        line["cpu_baseline"] = base
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def main():
@@ -385,132 +608,36 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--share", type=int, default=1,
                     help="verify only share 0 of this many (a small case for profiling)")
+    ap.add_argument("--replicas", action="store_true",
+                    help="N > 1: every rank verifies the whole space (default: --part shares)")
+    ap.add_argument("--sustained", type=float, default=5.0,
+                    help="seconds of back-to-back launches after the timed steps (0: none)")
+    ap.add_argument("--configs", default="life,batch,super,serve",
+                    help="the other workloads run after the headline, comma separated ('' "
+                         "for none)")
     ap.add_argument("--config", default="verify",
                     choices=["verify", "life", "batch", "super", "serve"],
-                    help="verify: the headline; life: cube Life 2^16 machines, 1000 "
-                         "generations; batch: 4,096 equivalence jobs in one launch")
+                    help="one workload alone: verify is the headline line")
     ap.add_argument("--jobs", type=int, default=4096, help="batch: number of jobs")
     ap.add_argument("--gens", type=int, default=1000, help="life: generations")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.config == "life":
-        return bench_life(args)
-    if args.config == "batch":
-        return bench_batch(args)
-    if args.config == "super":
-        return bench_super(args)
-    if args.config == "serve":
-        return bench_serve(args)
-
-    world, rank, local = dist_env()
-    dist = None
-    device = 0
-    if world > 1:
-        import torch.distributed as dist  # barrier only; the engine itself uses no torch
-        dist.init_process_group("gloo")
-        if "CUDA_VISIBLE_DEVICES" not in os.environ:
-            os.environ["CUDA_VISIBLE_DEVICES"] = str(local)  # this rank sees its GPU as 0
-        elif len(os.environ["CUDA_VISIBLE_DEVICES"].split(",")) > local:
-            device = local  # all GPUs visible: take this rank's
-
-    import tesseract_gb300 as T
-    from tesseract_gb300 import build
-    if rank == 0:
+    if args.config != "verify":
+        from tesseract_gb300 import build
         build.build(reference=False)
-    if dist:
-        dist.barrier()
-    err = T._err()
-    if not T.lib().cuda_engine_init(device, err, len(err)):
-        raise T.EngineError(err.value.decode())
-    p = T.Program.gen_mul(16)
-    s = T.Spec(p, "p = a * b")
-    info = T.device_info()
-
-    lop3 = T.lop3_peak()  # 32-bit LOP3 ops/s
-    peak_lane_ops = lop3 * 32
-
-    share = dict(part=0, part_end=0, parts=args.share)
-    for _ in range(max(3, args.warmup)):
-        r = T.enum_run(T.EN_VERIFY, p, spec=s, **share)
-        assert r["hits"] == 0
-    stats = T.last_launch()
-
-    if dist:
-        dist.barrier()
-    kernel_s, ops, results = 0.0, 0, []
-    visible = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")
-    with Clocks(int(visible[min(device, len(visible) - 1)] or 0)) as clk:
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            r = T.enum_run(T.EN_VERIFY, p, spec=s, **share)
-            kernel_s += r["seconds"]
-            ops += r["ops"]
-            results.append(r["hits"])
-        wall = time.perf_counter() - t0
-    if dist:
-        import torch
-        t = torch.tensor([wall, kernel_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        wall, kernel_s = float(t[0]), float(t[1])
-    assert all(h == 0 for h in results), "verify found mismatches"
-    if rank != 0:
-        return 0
-    # a negative control outside the timed region: a wrong spec of the same shape must fail on
-    # exactly the assignments where a != 0, so the kernel visibly checks every assignment
-    control = None
-    if args.share == 1:
-        cs = T.Spec(p, "p = a * b + a")
-        cr = T.enum_run(T.EN_VERIFY, p, spec=cs)
-        want = (1 << 32) - (1 << 16)
-        control = {"spec": "p = a * b + a", "hits": cr["hits"], "expected": want,
-                   "first_hits": cr["hit"][:4], "ok": cr["hits"] == want}
-        assert control["ok"], control
-    value = world * ops / kernel_s
-    e2e = world * ops / wall
-    per_launch = ops / args.steps / (kernel_s / args.steps)
-    line = {
-        "metric": METRIC, "value": value, "unit": "lane-ops/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * kernel_s / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-        "data": "synthetic",
-        "config": {"workload": WORKLOAD + ("" if args.share == 1 else
-                                           f" (share 0 of {args.share})"),
-                   "assignments_per_step": r["tried"],
-                   "lane_ops_per_step": ops // args.steps,
-                   "l2": "no DRAM inputs: cell state lives in registers and every input word is "
-                         "derived from the lane index, so there is nothing to flush",
-                   "device": info, "parallelism": f"replicas x{world}"},
-        "result": {"mismatches": 0, "tried_per_step": r["tried"], "negative_control": control},
-        "roofline": {"bound": "alu-lop3", "achieved": per_launch, "peak": peak_lane_ops,
-                     "unit": "lane-op/s", "frac": per_launch / peak_lane_ops,
-                     "peak_source": "measured: cuda_lop3_peak microbenchmark on this GPU "
-                                    "(32-bit LOP3/s x 32 lanes)",
-                     "lop3_per_s": lop3,
-                     # DRAM bytes (read + write) of one full-space launch, from the ncu capture
-                     # of the same kernel (ALU pipe 97.3 % busy in that capture)
-                     "traffic": VERIFY_DRAM_BYTES if args.share == 1 else None,
-                     "traffic_unit": "bytes per launch", "alu_pipe_busy_ncu": 0.973,
-                     "note": "achieved counts the reference's 6,040 NAND/STO lane-ops per "
-                             "assignment; the kernel issues 720 LOP3 for them, 532 of those once "
-                             "per 16 steps, so frac exceeds 1; the machine-level figure is "
-                             "alu_pipe_busy_ncu (integer ALU pipe, share of its sustained peak)"},
-        "kernel": {"regs": stats["regs"], "local_bytes": stats["local_bytes"],
-                   "grid": stats["grid"], "block": stats["block"],
-                   "compile_seconds": stats["compile_seconds"]},
-        "e2e": {"value": e2e, "unit": "lane-ops/s", "h2d_bytes_per_step": 72,
-                "d2h_bytes_per_step": 8 + 4 * stats["grid"] * stats["block"] // 32,
-                "path": "cuda_enum_run through the C ABI with host Program/Spec structs"},
-        "gpu_launches": args.steps,
-    }
-    clocks = clk.summary()
-    if clocks:
-        line["clocks"] = clocks
-    if not args.no_cpu:
-        base, _, _ = cpu_sample()
-        line["cpu_baseline"] = base
-    print(json.dumps(line), flush=True)
-    return 0
+        if args.config == "life":
+            rec, ok = config_life(args.gens)
+        elif args.config == "batch":
+            rec, ok = config_batch(args.jobs)
+        elif args.config == "serve":
+            rec, ok = config_serve(400 if args.jobs == 4096 else args.jobs)
+        else:
+            rec, ok = CONFIGS[args.config]()
+        rec = dict(config=args.config, ok=ok, **rec)
+        print(json.dumps(rec), flush=True)
+        return 0 if ok else 3
+    return headline(args)
 
 
 if __name__ == "__main__":

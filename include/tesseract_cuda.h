@@ -158,6 +158,11 @@ int  cuda_device_info(char *buf, size_t len);
    (spills), grid and block, and the NVRTC compile time of its module (cached = 1 when the module
    came from the cache).  cuda_lop3_peak measures the device's 3-input logic issue rate with a
    microbenchmark: 32-bit LOP3 operations per second (each is 32 one-bit lane operations).
+   For a generated enumeration kernel the launch stats also give its logic work per 32-lane word
+   as the code generator laid it out: LUTs run every step, LUTs run once per stretch of
+   stretch_steps steps, and the bit-sliced output compare (compare_ops, -1 when the spec is
+   evaluated per lane); logic_ops_per_word = luts_per_step + luts_per_stretch / stretch_steps +
+   compare_ops, or 0 when not counted.
    Neither has a counterpart in the reference, whose engines run on the CPU. */
 typedef struct {
     double   kernel_ms;
@@ -165,6 +170,8 @@ typedef struct {
     unsigned grid, block;
     double   compile_seconds;
     int      cached;
+    int      luts_per_step, luts_per_stretch, stretch_steps, compare_ops;
+    double   logic_ops_per_word;
 } CudaLaunchStats;
 int  cuda_last_launch(CudaLaunchStats *s);
 int  cuda_lop3_peak(double *ops_per_second, double *seconds, char *err, size_t errlen);

@@ -177,3 +177,96 @@ def ref_lib():
                                C.c_size_t]
         _ref = L
     return _ref
+
+
+# ---- inputs for the reference arm that need nothing of the product ------------------------
+
+class _RefItem(C.Structure):
+    _fields_ = [("op", C.c_int), ("v", C.c_uint64)]
+
+
+class RefSpec(C.Structure):
+    """The reference's private struct Spec (src/spec.c:20-29), filled in here for `p = a * b`
+    shaped specifications without its parser or this engine's."""
+    _fields_ = [("width", C.c_int), ("out", C.c_uint32 * 64), ("nvars", C.c_int),
+                ("var_name", (C.c_char * 64) * 32), ("var_bits", C.c_int * 32),
+                ("var_pos", (C.c_int * 64) * 32), ("rpn", _RefItem * 256), ("nrpn", C.c_int),
+                ("depth", C.c_int), ("max_depth", C.c_int)]
+
+
+_T_VAR, _T_MUL = 1, 4  # RPN items (src/spec.c:11)
+
+
+class PrintedProgram:
+    """A Program struct (the reference's layout) from the text its generators print (`alpha gen
+    ...`, src/build.c:417-444): .in/.out lines and one NAND or STO per line, cells numbered ZERO,
+    ONE, then by first appearance.  The printed form has no macros, includes or links."""
+
+    def __init__(self, text: str):
+        names, index, code, ins, outs = ["ZERO", "ONE"], {"zero": 0, "one": 1}, [], [], []
+
+        def cell(n):
+            if n.lower() not in index:
+                index[n.lower()] = len(names)
+                names.append(n)
+            return index[n.lower()]
+        for line in text.splitlines():
+            f = line.split(";")[0].split()
+            if not f:
+                continue
+            if f[0] in (".in", ".out"):
+                (ins if f[0] == ".in" else outs).extend(cell(n) for n in f[1:])
+            else:
+                code.append((0 if f[0].upper() == "NAND" else 1, cell(f[1])))
+        self.names, self.inputs, self.outputs = names, ins, outs
+        self._code = (T.Instr * len(code))(*[T.Instr(op, a) for op, a in code])
+        self._names = (C.c_char_p * len(names))(*[n.encode() for n in names])
+        self._in = (C.c_uint32 * len(ins))(*ins)
+        self._out = (C.c_uint32 * len(outs))(*outs)
+        self.s = T.ProgramStruct(self._code, len(code), len(names), self._names, self._in,
+                                 len(ins), self._out, len(outs), None)
+
+    def vector(self, cells, stem):
+        """Positions in `cells` of stem0, stem1, ... (bit order)."""
+        pos = {self.names[c].lower(): i for i, c in enumerate(cells)}
+        out = []
+        while f"{stem}{len(out)}" in pos:
+            out.append(pos[f"{stem}{len(out)}"])
+        return out
+
+    def product_spec(self, out="p", x="a", y="b") -> RefSpec:
+        """`out = x * y` over the input vectors x and y (input k of n is bit n-1-k)."""
+        s = RefSpec()
+        n = len(self.inputs)
+        for c in [self.outputs[i] for i in self.vector(self.outputs, out)]:
+            s.out[s.width] = c
+            s.width += 1
+        for k, stem in enumerate((x, y)):
+            bits = self.vector(self.inputs, stem)
+            s.var_name[k].value = stem.encode()
+            s.var_bits[k] = len(bits)
+            for b, i in enumerate(bits):
+                s.var_pos[k][b] = n - 1 - i
+        s.nvars = 2
+        for i, (op, v) in enumerate(((_T_VAR, 0), (_T_VAR, 1), (_T_MUL, 0))):
+            s.rpn[i].op, s.rpn[i].v = op, v
+        s.nrpn, s.depth, s.max_depth = 3, 1, 2
+        return s
+
+
+def verify_struct(prog: PrintedProgram, spec: RefSpec) -> "T.EnumStruct":
+    e = T.EnumStruct()
+    e.mode = T.EN_VERIFY
+    e.a = C.pointer(prog.s)
+    e.spec = C.cast(C.pointer(spec), C.c_void_p)
+    e.ticks, e.part, e.part_end, e.parts = 1, 0, 0, 1
+    return e
+
+
+def enum_run_struct(e, threads=None, limit_chunks=0) -> dict:
+    """orc_enum_run on a prepared Enum struct."""
+    r, err = T.EnumResult(), C.create_string_buffer(1024)
+    if not lib().orc_enum_run(C.byref(e), C.byref(r), threads or os.cpu_count() or 1,
+                              limit_chunks, err, len(err)):
+        raise T.EngineError(err.value.decode())
+    return r.as_dict()

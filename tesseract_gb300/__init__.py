@@ -102,7 +102,9 @@ class SuperResult(C.Structure):
 class LaunchStats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("regs", C.c_int), ("local_bytes", C.c_int),
                 ("grid", C.c_uint), ("block", C.c_uint), ("compile_seconds", C.c_double),
-                ("cached", C.c_int)]
+                ("cached", C.c_int), ("luts_per_step", C.c_int), ("luts_per_stretch", C.c_int),
+                ("stretch_steps", C.c_int), ("compare_ops", C.c_int),
+                ("logic_ops_per_word", C.c_double)]
 
 
 _lib = None

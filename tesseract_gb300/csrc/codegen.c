@@ -466,6 +466,7 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
     L.step_bits = 5;
     Src outer = {0}, inner = {0}, fields = {0}, stores = {0}, loads = {0};
     int step_tz = 0;
+    TcGenWork work = {0, 0, 1, -1};
     /* the cells compared, as (program, cell) pairs: a first */
     char (*val_a)[24] = tc_xcalloc(a->ncells + 1, sizeof *val_a);
     char (*val_b)[24] = tc_xcalloc((g->b ? g->b->ncells : 0) + 1, sizeof *val_b);
@@ -530,6 +531,8 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         const int hoisted = invariant_luts(sup, norder, L.inner);
         L.split = L.inner && hoisted > 0 && 5 * hoisted >= norder &&
                   nfields <= SPLIT_MAX_FIELDS;
+        work.luts_per_step = L.split ? norder - hoisted : norder;
+        work.luts_per_stretch = L.split ? hoisted : 0;
         if (!L.split) {
             memset(field, 0, (size_t)size + 1);
             L.permuted = 0;
@@ -582,6 +585,10 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         free(leaf);
         tc_net_free(net);
     } else {
+        for (size_t i = 0; i < a->len; i++)
+            work.luts_per_step += (a->code[i].op == OP_NAND) * (int)g->ticks;
+        for (size_t i = 0; g->mode == EN_EQUIV && i < g->b->len; i++)
+            work.luts_per_step += (g->b->code[i].op == OP_NAND) * (int)g->ticks;
         for (size_t k = 0; k < n; k++)
             emit_input(&inner, k, n, (int)(n - 1 - k), "wlo", "word");
         body(&inner, a, "a", a->inputs, n, g->ticks);
@@ -592,6 +599,8 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         for (uint32_t c = 0; g->mode == EN_EQUIV && c < g->b->ncells; c++)
             snprintf(val_b[c], sizeof val_b[c], c == 0 ? "0u" : c == 1 ? "TC_ONES" : "b%u", c);
     }
+    work.compare_ops = g->mode == EN_SEARCH ? s->width : g->mode == EN_EQUIV ? (int)a->noutputs
+                                                                            : -1;
     if (g->mode == EN_SEARCH) {
         emit(&inner, "    u32 m = TC_ONES;\n");
         for (int b = 0; b < s->width; b++) {
@@ -634,7 +643,11 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         emit(&inner, "    const u32 d = e[0] - sf0;\n");
         emit(&inner, "    u32 m = 0u, c = 0u;\n    (void)c;\n    (void)d;\n");
         /* below bit step_tz, d is known to be zero: no carry, the sum bit is the kept one */
+        work.compare_ops = 0;
         for (int b = 0; b < s->width; b++) {
+            /* below step_tz: one XOR-OR; above: the sign spread of d's bit (2 ops), a 4-input
+               XOR-OR (2) and, but for the top bit, the carry's majority (1) */
+            work.compare_ops += b < step_tz ? 1 : b + 1 < s->width ? 5 : 4;
             if (b < step_tz) {
                 emit(&inner, "    m |= %s ^ sp%d;\n", val_a[s->out[b]], b);
                 continue;
@@ -665,6 +678,11 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
     }
     free(val_a);
     free(val_b);
+    work.stretch_steps = 1 << L.step_bits;
+    if (!work.luts_per_stretch)
+        work.stretch_steps = 1;
+    if (g->work)
+        *g->work = work;
     /* what a chunk computes once (cword: the word with its step bits, 5..9, zero), what each step
        computes, and the two together for one word */
     emit(o, "typedef struct {%s } TcInv;\n", fields.len ? fields.s : " u32 unused_;");

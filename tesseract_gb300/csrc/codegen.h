@@ -8,6 +8,16 @@
 extern "C" {
 #endif
 
+/* The logic work of one 32-lane word in a generated enumeration kernel, as the code generator
+   lays it out: LUTs run at every step, LUTs run once per stretch of stretch_steps steps, and the
+   bit-sliced compare of the outputs (equiv: one XOR-OR per output; search: one op per output
+   bit; a separable spec: its carry chain, 4 or 5 ops per bit above the step part's trailing
+   zeros and 1 below; -1 when the spec is evaluated per lane, which is not counted).  With
+   ticks > 1 or the mapping off, luts_per_step counts the NAND instructions instead. */
+typedef struct {
+    int luts_per_step, luts_per_stretch, stretch_steps, compare_ops;
+} TcGenWork;
+
 typedef struct {
     int             mode;       /* EN_VERIFY, EN_EQUIV, EN_SEARCH */
     const Program  *a, *b;      /* b: equiv */
@@ -18,6 +28,7 @@ typedef struct {
     unsigned        ticks;
     int             block;      /* threads per block */
     int             no_map;     /* 1: keep the NAND/STO body as written (no LOP3 mapping) */
+    TcGenWork      *work;       /* out, when not NULL: the kernel's work per word */
 } TcGenEnum;
 
 /* The argument block of the generated kernel `tc_enum`, in one place: the host launchers declare

@@ -106,6 +106,15 @@ int cuda_last_launch(CudaLaunchStats *s)
     s->block = tc_engine.last_block;
     s->compile_seconds = tc_engine.last.cached ? 0 : tc_engine.last.compile_seconds;
     s->cached = tc_engine.last.cached;
+    const TcModInfo *m = &tc_engine.last;
+    s->luts_per_step = m->luts_per_step;
+    s->luts_per_stretch = m->luts_per_stretch;
+    s->stretch_steps = m->stretch_steps;
+    s->compare_ops = m->compare_ops;
+    s->logic_ops_per_word = m->stretch_steps && m->compare_ops >= 0
+                                ? m->luts_per_step + (double)m->luts_per_stretch /
+                                  m->stretch_steps + m->compare_ops
+                                : 0;
     return tc_engine.ready;
 }
 
@@ -567,9 +576,15 @@ int tc_enum_job_prepare(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
     enum_key(&pl.g, &k1, &k2);
     if (!lookup_enum(k1, k2, &j->m)) {
         size_t len;
+        TcGenWork work;
+        pl.g.work = &work;
         src = tc_codegen_enum(&pl.g, &len);
         if (!tc_module(src, len, names, 1, NULL, &j->m, err, errlen))
             goto done;
+        j->m.info.luts_per_step = work.luts_per_step;
+        j->m.info.luts_per_stretch = work.luts_per_stretch;
+        j->m.info.stretch_steps = work.stretch_steps;
+        j->m.info.compare_ops = work.compare_ops;
         remember_enum(k1, k2, &j->m);
     }
     uint64_t space = 1ull << e->a->ninputs, sel, tried, pruns;

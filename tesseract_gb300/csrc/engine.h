@@ -24,6 +24,9 @@ typedef struct {
     double   compile_seconds;
     size_t   cubin_bytes;
     int      regs, local_bytes, cached;
+    /* generated enumeration kernels: the code generator's count of their work per word
+       (TcGenWork); stretch_steps = 0 for other kernels */
+    int      luts_per_step, luts_per_stretch, stretch_steps, compare_ops;
     char     log[2048];
 } TcModInfo;
 

@@ -80,3 +80,14 @@ def random_spec(r, depth: int = 3) -> str:
             return "(" + expr(d - 1) + ") << " + str(r.randrange(0, 4))
         return "(" + expr(d - 1) + " " + op + " " + expr(d - 1) + ")"
     return "p = " + ("a * b + " if r.random() < 0.7 else "") + expr(depth)
+
+
+def load_gz(name):
+    import gzip
+    with gzip.open(os.path.join(GOLDEN, name), "rt") as f:
+        return json.load(f)
+
+
+def as_record(r):
+    """An EnumResult dict in the fixtures' per-job form: [space, tried, hits, ops, "hex,..."]."""
+    return [r["space"], r["tried"], r["hits"], r["ops"], ",".join("%x" % x for x in r["hit"])]
