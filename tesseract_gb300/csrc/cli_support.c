@@ -7,6 +7,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "cli_support.h"
 #include "engine.h"
 #include "ref_host.h"
 
@@ -103,22 +104,82 @@ static void plain_life(uint64_t *board, int w64, int h, unsigned long long gens)
     free(tmp);
 }
 
-int tc_life_cube_run(int dims, int rbits, int size, unsigned long long gens, uint64_t seed,
-                     double *gpu_ms, int check, int *ok, char *err, size_t errlen)
+/* ---- plain C Life, one byte a cell, for boards whose width is not a multiple of 64 ----------- */
+
+static void life_bytes(uint8_t *b, int w, int h, unsigned long long gens)
 {
-    int cbits = dims - rbits, w = size, h = size, cells = w * h;
+    uint8_t *next = tc_xmalloc((size_t)w * h);
+    for (unsigned long long g = 0; g < gens; g++) {
+        for (int r = 0; r < h; r++) {
+            const uint8_t *up = b + (size_t)((r + h - 1) % h) * w, *row = b + (size_t)r * w,
+                          *dn = b + (size_t)((r + 1) % h) * w;
+            for (int c = 0; c < w; c++) {
+                int l = (c + w - 1) % w, rt = (c + 1) % w;
+                int n = up[l] + up[c] + up[rt] + row[l] + row[rt] + dn[l] + dn[c] + dn[rt];
+                next[(size_t)r * w + c] = (uint8_t)(n == 3 || (n == 2 && row[c]));
+            }
+        }
+        memcpy(b, next, (size_t)w * h);
+    }
+    free(next);
+}
+
+typedef struct {
+    uint8_t           *boards;  /* boards[k * cells ...]: board k, row-major */
+    int                w, h, k0, k1;
+    unsigned long long gens;
+} BoardRange;
+
+static void *boards_step(void *arg)
+{
+    BoardRange *R = arg;
+    for (int k = R->k0; k < R->k1; k++)
+        life_bytes(R->boards + (size_t)k * R->w * R->h, R->w, R->h, R->gens);
+    return NULL;
+}
+
+/* n independent w x h boards, each `gens` generations, on up to 16 host threads */
+static void life_many(uint8_t *boards, int n, int w, int h, unsigned long long gens)
+{
+    enum { T = 16 };
+    pthread_t tid[T];
+    BoardRange r[T];
+    for (int t = 0; t < T; t++) {
+        r[t] = (BoardRange){boards, w, h, n * t / T, n * (t + 1) / T, gens};
+        pthread_create(&tid[t], NULL, boards_step, &r[t]);
+    }
+    for (int t = 0; t < T; t++)
+        pthread_join(tid[t], NULL);
+}
+
+/* `life` (src/work.c:490-701) on the GPU cube engine: 512 independent boards (gen_life, one lane
+   each) or one board over the cube (gen_life_cube), seeded from splitmix64 as the reference
+   seeds them, run `gens` generations, and checked against plain C Life: every board, or the whole
+   board row by row.  Fills what the command prints. */
+int tc_life_run(const TcLifeRun *a, TcLifeResult *r, char *err, size_t errlen)
+{
+    memset(r, 0, sizeof *r);
+    r->bad = -1;
+    int w = a->size, h = a->size, cells = w * h;
+    int dims = a->cube ? a->dims : CUBE_DIMS, rbits = a->cube ? a->rbits : 0;
+    int cbits = dims - rbits;
     uint32_t *board = tc_xmalloc((size_t)cells * sizeof *board);
     Program p;
-    tc_gen_life_cube(&p, w, h, rbits, cbits, board);
+    if (a->cube)
+        tc_gen_life_cube(&p, w, h, rbits, cbits, board);
+    else
+        tc_gen_life(&p, w, h, board);
+    r->len = p.len;
     CudaCube *c;
     if (!cuda_cube_new(&p, &c, err, errlen)) {
         free(board);
         tc_program_free(&p);
         return 0;
     }
+    r->segments = cuda_cube_segments(c);
     unsigned machines = 1u << dims, W = machines / 32;
     uint32_t *mem = tc_xcalloc((size_t)W * p.ncells, 4), *rr = tc_xcalloc(W, 4);
-    uint64_t s = seed;
+    uint64_t s = a->seed;  /* group by group, cell by cell, the line's eight 64-bit words */
     for (unsigned g = 0; g < machines / 512; g++)
         for (int i = 0; i < cells; i++)
             for (int k = 0; k < 8; k++) {
@@ -127,40 +188,77 @@ int tc_life_cube_run(int dims, int rbits, int size, unsigned long long gens, uin
                 mem[at] = (uint32_t)v;
                 mem[at + 1] = (uint32_t)(v >> 32);
             }
-    int gw = w << cbits, gh = h << rbits, w64 = (gw + 63) / 64;
+#define LANE(cell, m) ((mem[(size_t)(cell) * W + ((m) >> 5)] >> ((m) & 31)) & 1u)
+    int gw = w << cbits, gh = h << rbits, w64 = (gw + 63) / 64, packed = gw % 64 == 0;
+    uint8_t *start = NULL;
     uint64_t *big = NULL;
-    if (check) {
+    if (!a->cube) {
+        start = tc_xmalloc((size_t)machines * cells);
+        for (unsigned l = 0; l < machines; l++)
+            for (int i = 0; i < cells; i++)
+                start[(size_t)l * cells + i] = (uint8_t)LANE(board[i], l);
+    } else if (packed) {
         big = tc_xcalloc((size_t)w64 * gh, 8);
-        for (int R = 0; R < gh; R++)
-            for (int C = 0; C < gw; C++) {
-                unsigned m = tc_grid_machine((unsigned)(R / h), (unsigned)(C / w), cbits);
-                uint32_t cell = board[(R % h) * w + C % w];
-                if ((mem[(size_t)cell * W + (m >> 5)] >> (m & 31)) & 1)
-                    big[(size_t)R * w64 + C / 64] |= 1ull << (C % 64);
-            }
+    } else {
+        start = tc_xcalloc((size_t)gw * gh, 1);
     }
+    for (int R = 0; a->cube && R < gh; R++)
+        for (int C = 0; C < gw; C++) {
+            unsigned m = tc_grid_machine((unsigned)(R / h), (unsigned)(C / w), cbits);
+            unsigned v = LANE(board[(R % h) * w + C % w], m);
+            if (packed)
+                big[(size_t)R * w64 + C / 64] |= (uint64_t)v << (C % 64);
+            else
+                start[(size_t)R * gw + C] = (uint8_t)v;
+        }
     int okay = cuda_cube_write_words(c, mem, rr, err, errlen) &&
-               cuda_cube_run(c, gens, err, errlen) &&
+               cuda_cube_run(c, a->gens, err, errlen) &&
                cuda_cube_read_words(c, mem, rr, err, errlen);
     CudaLaunchStats st;
     cuda_last_launch(&st);
-    *gpu_ms = st.kernel_ms;
-    *ok = 1;
-    if (okay && check && gw % 64 == 0) {
-        plain_life(big, w64, gh, gens);
-        for (int R = 0; R < gh && *ok; R++)
+    r->gpu_ms = st.kernel_ms;
+    if (okay && !a->cube) {
+        life_many(start, (int)machines, w, h, a->gens);
+        for (unsigned l = 0; l < machines && r->bad < 0; l++)
+            for (int i = 0; i < cells; i++)
+                if (start[(size_t)l * cells + i] != LANE(board[i], l)) {
+                    r->bad = (int)l;
+                    break;
+                }
+        r->shown = tc_xmalloc((size_t)cells);  /* board 0 as the engine left it */
+        for (int i = 0; i < cells; i++) {
+            r->shown[i] = (uint8_t)LANE(board[i], 0);
+            r->alive += r->shown[i];
+        }
+    } else if (okay) {
+        if (packed)
+            plain_life(big, w64, gh, a->gens);
+        else
+            life_bytes(start, gw, gh, a->gens);
+#define PLAIN(R, C) (packed ? (unsigned)((big[(size_t)(R) * w64 + (C) / 64] >> ((C) % 64)) & 1) \
+                            : (unsigned)start[(size_t)(R) * gw + (C)])
+        for (int R = 0; R < gh && r->bad < 0; R++)
             for (int C = 0; C < gw; C++) {
                 unsigned m = tc_grid_machine((unsigned)(R / h), (unsigned)(C / w), cbits);
-                uint32_t cell = board[(R % h) * w + C % w];
-                unsigned got = (mem[(size_t)cell * W + (m >> 5)] >> (m & 31)) & 1;
-                unsigned want = (big[(size_t)R * w64 + C / 64] >> (C % 64)) & 1;
-                if (got != want) {
-                    *ok = 0;
+                if (PLAIN(R, C) != LANE(board[(R % h) * w + C % w], m)) {
+                    r->bad = R;
                     break;
                 }
             }
+        r->rows = gh < 48 ? gh : 48;  /* the top left corner of the plain C board */
+        r->cols = gw < 128 ? gw : 128;
+        r->shown = tc_xmalloc((size_t)r->rows * r->cols);
+        for (int R = 0; R < r->rows; R++)
+            for (int C = 0; C < r->cols; C++)
+                r->shown[(size_t)R * r->cols + C] = (uint8_t)PLAIN(R, C);
+#undef PLAIN
     }
+#undef LANE
+    r->board_w = gw;
+    r->board_h = gh;
+    r->machines = machines;
     free(big);
+    free(start);
     free(mem);
     free(rr);
     free(board);

@@ -215,6 +215,26 @@ CLI_CASES = [
     (["run", "{rt}", "--table"], None),
     (["run", "{rt}", "--table", "--ticks", "3"], None),
     (["run", "{rr}", "--table", "--ticks", "2"], None),
+    # check (src/main.c:503-567), life (src/work.c:490-701), cube (src/cubedemo.c:549-623),
+    # super (src/supercmd.c:81-180), tester1 --raw (src/main.c:1071-1160): the kind names how
+    # tests/test_cli_gpu.py compares them (timings, engine names and search traces aside)
+    (["check", "{mul4}"], "check"),
+    (["check", "{rt}", "--ticks", "3", "--seed", "7"], "check"),
+    (["check", "{links10}"], "check"),
+    (["life", "--gens", "5", "--size", "8", "--show", "--seconds", "0"], "life"),
+    (["life", "--gens", "7", "--seconds", "0"], "life"),
+    (["life", "--cube", "--size", "8", "--gens", "4", "--seconds", "0"], "life"),
+    (["life", "--dims", "10", "--size", "8", "--gens", "3", "--show", "--seconds", "0"], "life"),
+    (["life", "--dims", "11", "--rows", "3", "--size", "4", "--gens", "5", "--seconds", "0"],
+     "life"),
+    (["life", "--size", "2"], "life"),
+    (["cube", "any", "--dims", "10", "--seconds", "0.01"], "cube"),
+    (["cube", "rank", "--dims", "10", "--seconds", "0.01"], "cube"),
+    (["cube", "sort", "--dims", "10", "--seconds", "0.01"], "cube"),
+    (["super", "RR = RR ^ x"], "super"),
+    (["super", "o{{x,y}} = x ^ y"], "super"),
+    (["super", "r{{a,b}} = s ? a : b"], "super"),
+    (["tester1", "--programs", "8", "--raw", "--threads", "1"], "tester1"),
 ]
 
 RR_ONLY = ".in x y z\nNAND x\nNAND y\nSTO t\nNAND z\nNAND t\nSTO x\n"
@@ -235,6 +255,8 @@ def cli_programs(tmp):
     progs["mul3"] = gen_text("mul", {"bits": 3})
     progs["rt"] = T.Program.random_in(6, 5, 40, 7).text()
     progs["rr"] = RR_ONLY
+    progs["links10"] = (".in x\n.out y z\n.link l = x @ 9\n.link k = l @ 2\nNAND l\nSTO y\n"
+                        "NAND k\nNAND ID3\nSTO z\nNAND ID9\nSTO x\n")
     paths = {}
     for k, v in progs.items():
         paths[k] = os.path.join(tmp, k + ".asm")
@@ -244,14 +266,23 @@ def cli_programs(tmp):
 
 
 def cli_main():
+    global ALPHA
     out = []
     with tempfile.TemporaryDirectory() as tmp:
         progs, paths = cli_programs(tmp)
-        for args, _ in CLI_CASES:
+        # the cube demos read lib/std.inc beside the binary's directory: a copy of the binary
+        # in tmp/bin next to a link to the reference's lib
+        import shutil
+        os.makedirs(os.path.join(tmp, "bin"))
+        shutil.copy(ALPHA, os.path.join(tmp, "bin", "alpha"))
+        with open(os.path.join(ROOT, "oracle", "_ref", "SOURCE")) as f:
+            os.symlink(os.path.join(f.read().strip(), "lib"), os.path.join(tmp, "lib"))
+        ALPHA = os.path.join(tmp, "bin", "alpha")
+        for args, kind in CLI_CASES:
             real = [a.format(**paths) for a in args]
             rc, stdout, stderr = run(real)
             text = stdout.replace(tmp + "/", "")
-            out.append({"args": args, "rc": rc, "stdout": text})
+            out.append({"args": args, "rc": rc, "stdout": text, "kind": kind or "enum"})
     with open(os.path.join(HERE, "cli.json"), "w") as f:
         json.dump(out, f, indent=1)
 
