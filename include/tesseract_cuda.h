@@ -199,6 +199,23 @@ void cuda_free(CudaCode *c);
    the device work. */
 int  cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen);
 void cuda_enum_add_hit(EnumResult *r, uint64_t x);   /* enum_add_hit, src/enum.c:31-46 */
+
+/* The autotuner: kernels of job e for 128, 256 and 512 threads per block and, where the work
+   splits into stretches, stretches of 8, 16 and 32 steps (step_bits 3..5; 0: not split) are
+   compiled in parallel, checked to give the same result and timed on the job (or on the share of
+   its chunks that takes about 20 ms: probe_fraction); the fastest is kept as the job's kernel
+   for every later launch of it in this process (cuda_enum_run, batches, serving,
+   cuda_enum_run_static).  cand[i].ms is candidate i's best of three, -1 when it did not compile.
+   No counterpart in the reference. */
+typedef struct {
+    int    n, ncand, best;
+    struct {
+        int    block, step_bits;
+        double ms;
+    } cand[9];
+    double probe_fraction;
+} CudaTune;
+int  cuda_enum_tune(const Enum *e, CudaTune *t, char *err, size_t errlen);
 /* Adds the result of one share (--part) into a total, as merge_raw does (src/work.c:341-371):
    the host side of running shares on several GPUs or machines.  Needs no GPU. */
 void cuda_enum_merge(EnumResult *into, const EnumResult *part);
@@ -222,6 +239,13 @@ int  cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, size_t errlen
    runs one enumeration per command. */
 int  cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char *err,
                     size_t errlen);
+/* The last cuda_batch_run: jobs, how many ran as generated kernels and how many on the
+   interpreter, the compile threads it used and its wall time in seconds. */
+typedef struct {
+    int    jobs, compiled, interpreted, compile_threads;
+    double seconds;
+} CudaBatchStats;
+int  cuda_batch_stats(CudaBatchStats *s);
 
 /* The superoptimizer.  cuda_super_parse replaces super_parse (src/super.c:225-371): same
    language, same SuperSpec.  cuda_super_search replaces super_search (src/super.c:821-896):
@@ -323,6 +347,10 @@ typedef struct CudaCube CudaCube;
 int  cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen);
 void cuda_cube_free(CudaCube *c);
 unsigned cuda_cube_groups(const CudaCube *c);
+/* cuda_cube_segments: the segments the ISA's rule cuts a pass into (a cut wherever a cell written
+   in the segment is read across dimension 9 or up, docs/ISA.md step 7f), as the reference's
+   engines cut it; this engine itself cuts only from dimension 10 up (1,024 machines run in
+   lockstep inside one warp) and cuda_cube_kernels counts its launches per pass. */
 unsigned cuda_cube_segments(const CudaCube *c);
 int  cuda_cube_load(CudaCube *c, unsigned group, const uint64_t *mem_lines, const uint64_t *rr_line,
                     char *err, size_t errlen);

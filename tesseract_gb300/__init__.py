@@ -371,6 +371,32 @@ def enum_run(mode, a: Program, b: Program | None = None, spec: Spec | None = Non
     return r.as_dict()
 
 
+class _TuneCand(C.Structure):
+    _fields_ = [("block", C.c_int), ("step_bits", C.c_int), ("ms", C.c_double)]
+
+
+class CudaTune(C.Structure):
+    _fields_ = [("n", C.c_int), ("ncand", C.c_int), ("best", C.c_int),
+                ("cand", _TuneCand * 9), ("probe_fraction", C.c_double)]
+
+
+def enum_tune(mode, a: Program, b: Program | None = None, spec: Spec | None = None, ticks=1,
+              part=0, part_end=None, parts=1) -> dict:
+    """The autotuner (cuda_enum_tune): the job's kernel variants timed on the job; the fastest
+    becomes its kernel for every later launch in this process."""
+    e = make_enum(mode, a, b, spec, ticks, part, part_end, parts)
+    t, err = CudaTune(), _err()
+    L = lib()
+    L.cuda_enum_tune.restype = C.c_int
+    L.cuda_enum_tune.argtypes = [C.POINTER(EnumStruct), C.POINTER(CudaTune), C.c_char_p,
+                                 C.c_size_t]
+    if not L.cuda_enum_tune(C.byref(e), C.byref(t), err, len(err)):
+        raise EngineError(err.value.decode())
+    cands = [{"block": t.cand[i].block, "step_bits": t.cand[i].step_bits,
+              "ms": t.cand[i].ms if t.cand[i].ms >= 0 else None} for i in range(t.n)]
+    return {"candidates": cands, "best": cands[t.best], "probe_fraction": t.probe_fraction}
+
+
 def table(p: Program, ticks: int = 1):
     """`run --table --engine cuda` (cuda_table): every row's output columns (.out cells, or RR
     when there are none) as a list of rows of 0/1."""
@@ -416,6 +442,19 @@ def batch_run(jobs) -> list:
     if not L.cuda_batch_run(C.cast(arr, C.c_void_p), n, C.cast(res, C.c_void_p), err, len(err)):
         raise EngineError(err.value.decode())
     return [res[i].as_dict() for i in range(n)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("jobs", C.c_int), ("compiled", C.c_int), ("interpreted", C.c_int),
+                ("compile_threads", C.c_int), ("seconds", C.c_double)]
+
+
+def batch_stats() -> dict:
+    """The last batch_run: jobs on generated kernels and on the interpreter, compile threads,
+    wall seconds (cuda_batch_stats)."""
+    s = BatchStats()
+    lib().cuda_batch_stats(C.byref(s))
+    return {f: getattr(s, f) for f, _ in BatchStats._fields_}
 
 
 SERVE_AUTO, SERVE_INTERPRETER, SERVE_COMPILED = 0, 1, 2

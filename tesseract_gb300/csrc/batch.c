@@ -7,6 +7,7 @@
    launch.  Jobs whose cells do not fit the interpreter's slot space (255 slots per job) or that
    ask for --part shares are refused with an error; cuda_enum_run handles those. */
 #include <stdlib.h>
+#include <unistd.h>
 #include <string.h>
 
 #include <pthread.h>
@@ -813,30 +814,126 @@ void tc_wave_free(TcWave *w)
     free(w);
 }
 
-/* Runs every job in one persistent launch.  results[i] is job i's EnumResult; seconds is the
-   device time of the whole batch. */
+/* ---- a batch: every job at once ---------------------------------------------------------------
+
+   cuda_batch_run hands the jobs to the serving loop as if they all arrived at the start, the
+   heaviest first: the jobs the interpreter keeps run in one persistent launch (one wave, one
+   launch per slot class) with 90 % of the GPU's blocks, while the host's cores compile the jobs
+   whose GPU time saved pays for their compile (heaviest first) and the remaining blocks run them
+   as they come; a job whose kernel is already cached goes to compiled code whenever its work is
+   worth a launch.  Results do not depend on the route: both engines enumerate the whole job. */
+
+int    tc_serve_batch(const Enum *const *jobs, int njobs, const CudaServeOpts *opts,
+                      const signed char *route, double *finish, EnumResult *results,
+                      int *engine_used, char *err, size_t errlen);
+double tc_route_compile_s(const Enum *e, double instrs);
+double tc_route_compiled_s(double work);
+
+/* The interpreter's rate on a batch with most of the GPU (1.39e14 NAND/STO lane-ops/s measured
+   on the 4,096-job batch alone; host packing and a 90 % share of the blocks beside compiled
+   jobs bring it to about this). */
+#define BATCH_RATE_INTERP 1.1e14
+#define BATCH_SHARE 0.9
+
+static CudaBatchStats last_batch;
+
+typedef struct {
+    double work, instrs, compile_s, gain;
+    int    i;
+} Planned;
+
+static int by_gain(const void *x, const void *y)
+{
+    const Planned *a = x, *b = y;
+    return a->gain < b->gain ? 1 : a->gain > b->gain ? -1 : a->i - b->i;
+}
+
+/* The batch's plan: jobs by the interpreter time they would save per second of compiling (a
+   cached kernel costs none), taken for generated code while the compiling of those taken, spread
+   over the compile threads, ends before the interpreter is through with the jobs it keeps; cached
+   jobs whenever their work is worth a launch.  The compiles then cost no time of the batch. */
+static void plan(Planned *p, int n, int threads, signed char *route)
+{
+    double interp = 0, compile = 0;
+    for (int k = 0; k < n; k++)
+        interp += p[k].work / BATCH_RATE_INTERP;
+    for (int k = 0; k < n; k++) {
+        double saved = p[k].work / BATCH_RATE_INTERP - tc_route_compiled_s(p[k].work);
+        double c = p[k].compile_s / threads;
+        route[k] = saved > 0 && (c == 0 || compile + c <= interp - p[k].work / BATCH_RATE_INTERP);
+        if (route[k]) {
+            compile += c;
+            interp -= p[k].work / BATCH_RATE_INTERP;
+        }
+    }
+}
+
 int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char *err,
                    size_t errlen)
 {
+    memset(&last_batch, 0, sizeof last_batch);
     if (njobs <= 0)
         return 1;
     if (!cuda_engine_init(0, err, errlen))
         return 0;
-    TcWave *w;
-    if (!tc_wave_prepare(&w, jobs, njobs, err, errlen))
-        return 0;
-    int ok = tc_wave_launch(w, tc_engine.stream, 1.0, err, errlen) &&
-             tc_cu_check(cudaEventSynchronize(w->ev1), "batch", err, errlen);
-    if (ok) {
-        float ms = tc_wave_ms(w);
-        for (int i = 0; i < njobs; i++) {
-            tc_wave_result(w, i, &results[i]);
-            results[i].seconds = ms / 1e3;
-        }
-        tc_engine.last_kernel_ms = ms;
-        tc_engine.last_grid = (unsigned)w->grid;
-        tc_engine.last_block = TC_BATCH_BLOCK;
+    double t0 = tc_now();
+    long cores = sysconf(_SC_NPROCESSORS_ONLN);
+    int threads = cores > 2 ? (int)cores - 1 : 1;
+    Planned *p = tc_xmalloc((size_t)njobs * sizeof *p);
+    for (int i = 0; i < njobs; i++) {
+        const Enum *e = jobs[i];
+        p[i].i = i;
+        p[i].instrs = (double)e->a->len + (e->mode == EN_EQUIV && e->b ? (double)e->b->len : 0);
+        p[i].work = (e->a->ninputs < 64 ? (double)(1ull << e->a->ninputs) : 0) * e->ticks *
+                    p[i].instrs;
+        p[i].compile_s = e->parts == 1 ? tc_route_compile_s(e, p[i].instrs) : 1e30;
+        p[i].gain = p[i].work / (p[i].compile_s > 0 ? p[i].compile_s : 1e-9);
     }
-    tc_wave_free(w);
+    qsort(p, (size_t)njobs, sizeof *p, by_gain);
+    signed char *route = tc_xcalloc((size_t)njobs, 1);
+    plan(p, njobs, threads, route);
+    const Enum **order = tc_xmalloc((size_t)njobs * sizeof *order);
+    for (int k = 0; k < njobs; k++)
+        order[k] = jobs[p[k].i];
+    double *finish = tc_xcalloc((size_t)njobs, sizeof *finish);
+    EnumResult *res = tc_xcalloc((size_t)njobs, sizeof *res);
+    int *engine = tc_xcalloc((size_t)njobs, sizeof *engine), any = 0;
+    for (int k = 0; k < njobs; k++)
+        any |= route[k];
+    CudaServeOpts o;
+    memset(&o, 0, sizeof o);
+    o.streams = 1;
+    o.max_inflight_jobs = njobs;
+    o.max_wave_jobs = njobs;
+    o.max_device_bytes = (size_t)64 << 30;
+    o.share = any ? BATCH_SHARE : 1.0;
+    o.compile_threads = any ? threads : -1;
+    o.compiled_slots = 8;
+    o.route = any ? CUDA_SERVE_AUTO : CUDA_SERVE_INTERPRETER;
+    int ok = tc_serve_batch(order, njobs, &o, route, finish, res, engine, err, errlen);
+    double wall = tc_now() - t0;
+    if (ok) {
+        for (int k = 0; k < njobs; k++) {
+            results[p[k].i] = res[k];
+            results[p[k].i].seconds = wall;
+            last_batch.compiled += engine[k];
+        }
+        last_batch.jobs = njobs;
+        last_batch.interpreted = njobs - last_batch.compiled;
+        last_batch.compile_threads = any ? threads : 0;
+        last_batch.seconds = wall;
+    }
+    free(p);
+    free(route);
+    free(order);
+    free(finish);
+    free(res);
+    free(engine);
     return ok;
+}
+
+int cuda_batch_stats(CudaBatchStats *s)
+{
+    *s = last_batch;
+    return last_batch.jobs > 0;
 }

@@ -322,8 +322,10 @@ static uint64_t input_bit(size_t n, int j)  /* the input on x bit j */
    LUTs invariant (or the identity's, x bits 10..9+sb, if that is as good), then the sb whose
    estimated work per word is least: the LUTs that change per step, plus the invariant ones and
    `outer_extra` (what else runs once per stretch) spread over its 2^sb steps.  Measured on mul16
-   with the spec hoisted: 2.64 ms per 2^32 at sb = 4, 2.67 at 3, 2.77 at 5; the estimate picks 4. */
-static void choose_layout(Layout *L, size_t n, const uint64_t *sup, int norder, int outer_extra)
+   with the spec hoisted: 2.64 ms per 2^32 at sb = 4, 2.67 at 3, 2.77 at 5; the estimate picks 4.
+   force_sb (3..5) leaves the estimate out and takes that sb (the autotuner's candidates). */
+static void choose_layout(Layout *L, size_t n, const uint64_t *sup, int norder, int outer_extra,
+                          int force_sb)
 {
     memset(L, 0, sizeof *L);
     for (int j = 0; j < 64; j++)
@@ -336,7 +338,7 @@ static void choose_layout(Layout *L, size_t n, const uint64_t *sup, int norder, 
     int best_sb = 0, best_perm = 0;
     for (int sb = 5; sb >= 3; sb--) {
         const int top = 10 + sb;  /* x bits 0..top-1 may move */
-        if ((int)n < top)
+        if ((int)n < top || (force_sb && sb != force_sb))
             continue;
         uint64_t id = 0, set = 0;
         for (int j = 10; j < top; j++)
@@ -509,7 +511,7 @@ static void emit_word_function(Src *o, const TcGenEnum *g)
         }
         /* once per stretch besides the LUTs: a verify's per-lane spec and transpose */
         const int outer_extra = g->mode == EN_VERIFY ? 64 * s->nrpn + 256 : 0;
-        choose_layout(&L, n, sup, norder, outer_extra);
+        choose_layout(&L, n, sup, norder, outer_extra, g->step_bits);
         /* values of the chunk read by the steps: kept in TcInv */
         char *field = tc_xcalloc((size_t)size + 1, 1);
         int nfields = 0;

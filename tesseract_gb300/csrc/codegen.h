@@ -28,6 +28,7 @@ typedef struct {
     unsigned        ticks;
     int             block;      /* threads per block */
     int             no_map;     /* 1: keep the NAND/STO body as written (no LOP3 mapping) */
+    int             step_bits;  /* 3..5: the stretch length to use; 0: the cost model's choice */
     TcGenWork      *work;       /* out, when not NULL: the kernel's work per word */
 } TcGenEnum;
 

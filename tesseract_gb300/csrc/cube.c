@@ -54,7 +54,7 @@ struct CudaCube {
     unsigned    dims, groups, W, machines;
     uint32_t   *mem, *rr;   /* device */
     size_t     *first;      /* kernel k runs instructions first[k] .. first[k + 1] - 1 */
-    unsigned    nk, nseg;
+    unsigned    nk, nseg, isa_seg;
     int         loop;       /* one kernel, passes loop inside it */
     cudaKernel_t *fn;
     unsigned    *warps;     /* warp groups of kernel k */
@@ -69,9 +69,12 @@ struct CudaCode {
 
 /* ---- the plan --------------------------------------------------------------------------------- */
 
-/* Segment starts: a cut wherever a segment would both write a cell and read it across a far
-   dimension (either order), as late as possible.  Returns the number of segments; first[n] = len. */
-static unsigned find_cuts(const Program *p, size_t *first)
+/* The cuts of a pass into segments, as late as possible: a new segment starts wherever a cell the
+   segment has written is read across dimension far_dim or up, or a cell it has read that way is
+   written.  The ISA's rule (docs/ISA.md, step 7f) uses far_dim = 9; this engine needs far_dim =
+   FAR_DIM only, since dimensions 0..9 stay inside one warp's 1,024 machines, which run in
+   lockstep.  Returns the number of segments; first[n] = len. */
+static unsigned find_cuts(const Program *p, size_t *first, unsigned far_dim)
 {
     uint32_t *stored = tc_xcalloc(p->ncells + 1, sizeof *stored);
     uint32_t *read = tc_xcalloc(p->ncells + 1, sizeof *read);
@@ -83,7 +86,7 @@ static unsigned find_cuts(const Program *p, size_t *first)
         if (in.op == OP_NAND) {
             unsigned mask;
             uint32_t a = tc_program_resolve(p, in.addr, &mask);
-            if ((mask >> FAR_DIM) && !tc_program_readonly(p, a)) {
+            if ((mask >> far_dim) && !tc_program_readonly(p, a)) {
                 if (stored[a] == seg) {
                     seg++;
                     first[n++] = i;
@@ -856,7 +859,7 @@ static void *compile_job(void *arg)
 /* ---- the cube -------------------------------------------------------------------------------- */
 
 unsigned cuda_cube_groups(const CudaCube *c) { return c->groups; }
-unsigned cuda_cube_segments(const CudaCube *c) { return c->nseg; }
+unsigned cuda_cube_segments(const CudaCube *c) { return c->isa_seg; }
 unsigned cuda_cube_kernels(const CudaCube *c) { return c->nk; }
 
 void cuda_cube_free(CudaCube *c)
@@ -887,7 +890,12 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
     c->groups = c->machines / 512;
     c->W = c->machines / 32;
     size_t *cuts = tc_xmalloc((p->len + 2) * sizeof *cuts);
-    c->nseg = find_cuts(p, cuts);
+    c->nseg = find_cuts(p, cuts, FAR_DIM);
+    {
+        size_t *isa = tc_xmalloc((p->len + 2) * sizeof *isa);
+        c->isa_seg = find_cuts(p, isa, CUBE_DIMS);
+        free(isa);
+    }
     /* split long segments into kernels of at most tc_cube_chunk instructions */
     size_t chunk = tc_cube_chunk > 0 ? (size_t)tc_cube_chunk : 12000;
     c->first = tc_xmalloc((p->len / chunk + c->nseg + 2) * sizeof *c->first);

@@ -449,7 +449,7 @@ static void mix_program(Key *k, const Program *p)
 static void enum_key(const TcGenEnum *g, uint64_t *k1, uint64_t *k2)
 {
     Key k = {0xcbf29ce484222325ull, 0x6a09e667f3bcc909ull};
-    int head[4] = {g->mode, (int)g->ticks, g->block, g->no_map};
+    int head[5] = {g->mode, (int)g->ticks, g->block, g->no_map, g->step_bits};
     mix_bytes(&k, head, sizeof head);
     mix_program(&k, g->a);
     if (g->b) {
@@ -523,6 +523,49 @@ char *tc_codegen_enum_for(const Enum *e, size_t *len, char *err, size_t errlen)
     return src;
 }
 
+/* ---- the autotuner's choices ---------------------------------------------------------------
+
+   cuda_enum_tune measures kernels of one job that differ in threads per block and stretch length
+   and keeps the fastest here, keyed by the job's default plan; every later launch of the same job
+   (cuda_enum_run, the serving and batch paths, cuda_enum_run_static) takes the kernel of the
+   choice. */
+typedef struct {
+    uint64_t k1, k2;
+    int      block, step_bits;
+} Tuned;
+
+static Tuned tuned[256];
+static size_t ntuned;
+
+/* The tuned block and stretch for the job planned in g (default block, stretch of the cost
+   model), when the autotuner has chosen them. */
+static void apply_tuning(TcGenEnum *g)
+{
+    uint64_t k1, k2;
+    enum_key(g, &k1, &k2);
+    pthread_mutex_lock(&engine_lock);
+    for (size_t i = 0; i < ntuned; i++)
+        if (tuned[i].k1 == k1 && tuned[i].k2 == k2) {
+            g->block = tuned[i].block;
+            g->step_bits = tuned[i].step_bits;
+            break;
+        }
+    pthread_mutex_unlock(&engine_lock);
+}
+
+static void remember_tuning(uint64_t k1, uint64_t k2, int block, int step_bits)
+{
+    pthread_mutex_lock(&engine_lock);
+    size_t i = 0;
+    while (i < ntuned && !(tuned[i].k1 == k1 && tuned[i].k2 == k2))
+        i++;
+    if (i == ntuned && ntuned < sizeof tuned / sizeof tuned[0])
+        ntuned++;
+    if (i < ntuned)
+        tuned[i] = (Tuned){k1, k2, block, step_bits};
+    pthread_mutex_unlock(&engine_lock);
+}
+
 /* The loaded kernel of an enumeration, only when an earlier cuda_enum_run of the same job compiled
    and loaded it: no code generation, no compilation, no module load.  For cuda_enum_run_static,
    whose callers cannot allocate. */
@@ -543,6 +586,7 @@ int tc_enum_cached(const Enum *e, TcModule *m, char *err, size_t errlen)
     pl.b_in = b_in;
     if (!plan_fill(e, &pl, err, errlen))
         return 0;
+    apply_tuning(&pl.g);
     uint64_t k1, k2;
     enum_key(&pl.g, &k1, &k2);
     if (!lookup_enum(k1, k2, m))
@@ -561,32 +605,37 @@ void tc_free(void *p)
 /* Workspace of a launch: the hit counter, then 16 hits per warp, then a count per warp. */
 #define WS_LIST 256u
 
-int tc_enum_job_prepare(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
+/* The kernel for the plan in g: from the cache, else generated, compiled and cached. */
+static int enum_module(TcGenEnum *g, TcModule *m, char *err, size_t errlen)
 {
-    memset(j, 0, sizeof *j);
-    EnumPlan pl;
-    if (!plan_enum(e, &pl, err, errlen))
-        return 0;
-    int ok = 0;
-    char *src = NULL;
-    if (!cuda_engine_init(0, err, errlen))
-        goto done;
     static const char *const names[] = {"tc_enum"};
     uint64_t k1, k2;
-    enum_key(&pl.g, &k1, &k2);
-    if (!lookup_enum(k1, k2, &j->m)) {
-        size_t len;
-        TcGenWork work;
-        pl.g.work = &work;
-        src = tc_codegen_enum(&pl.g, &len);
-        if (!tc_module(src, len, names, 1, NULL, &j->m, err, errlen))
-            goto done;
-        j->m.info.luts_per_step = work.luts_per_step;
-        j->m.info.luts_per_stretch = work.luts_per_stretch;
-        j->m.info.stretch_steps = work.stretch_steps;
-        j->m.info.compare_ops = work.compare_ops;
-        remember_enum(k1, k2, &j->m);
-    }
+    enum_key(g, &k1, &k2);
+    if (lookup_enum(k1, k2, m))
+        return 1;
+    size_t len;
+    TcGenWork work;
+    g->work = &work;
+    char *src = tc_codegen_enum(g, &len);
+    g->work = NULL;
+    int ok = tc_module(src, len, names, 1, NULL, m, err, errlen);
+    free(src);
+    if (!ok)
+        return 0;
+    m->info.luts_per_step = work.luts_per_step;
+    m->info.luts_per_stretch = work.luts_per_stretch;
+    m->info.stretch_steps = work.stretch_steps;
+    m->info.compare_ops = work.compare_ops;
+    m->info.block = g->block;
+    remember_enum(k1, k2, m);
+    return 1;
+}
+
+/* The launch shape of job e on module m: as many blocks as are resident on the device at once
+   (at most one warp per 32 words), each warp a contiguous run of the selected words. */
+static int enum_shape(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
+{
+    const int block = j->m.info.block;
     uint64_t space = 1ull << e->a->ninputs, sel, tried, pruns;
     tc_enum_shares(e, space, &sel, &tried, &pruns);
     j->base.space = space;
@@ -594,18 +643,18 @@ int tc_enum_job_prepare(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
     j->base.ops = pruns * 512 * e->ticks * (e->a->len + (e->mode == EN_EQUIV ? e->b->len : 0));
     int per_sm = 0;
     if (!tc_cu_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                         &per_sm, (const void *)j->m.fn[0], TC_ENUM_BLOCK, 0),
+                         &per_sm, (const void *)j->m.fn[0], block, 0),
                      "occupancy", err, errlen))
-        goto done;
+        return 0;
     if (per_sm < 1)
         per_sm = 1;
     uint64_t words = sel * 1024;
     uint64_t blocks = (uint64_t)tc_engine.sms * (uint64_t)per_sm;
     uint64_t warps_needed = (words + 31) / 32;
-    uint64_t max_blocks = (warps_needed + TC_ENUM_BLOCK / 32 - 1) / (TC_ENUM_BLOCK / 32);
+    uint64_t max_blocks = (warps_needed + block / 32 - 1) / (block / 32);
     if (blocks > max_blocks)
         blocks = max_blocks ? max_blocks : 1;
-    uint64_t warps = blocks * (TC_ENUM_BLOCK / 32);
+    uint64_t warps = blocks * (uint64_t)(block / 32);
     uint64_t per_warp = (words + warps - 1) / warps;
     per_warp = (per_warp + 31) / 32 * 32;
     if (!per_warp)
@@ -618,9 +667,20 @@ int tc_enum_job_prepare(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
     j->parts = (uint32_t)e->parts;
     j->part = (uint32_t)e->part;
     j->nsel = (uint32_t)(e->part_end - e->part + 1);
-    ok = 1;
-done:
-    free(src);
+    return 1;
+}
+
+int tc_enum_job_prepare(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
+{
+    memset(j, 0, sizeof *j);
+    EnumPlan pl;
+    if (!plan_enum(e, &pl, err, errlen))
+        return 0;
+    int ok = cuda_engine_init(0, err, errlen);
+    if (ok) {
+        apply_tuning(&pl.g);
+        ok = enum_module(&pl.g, &j->m, err, errlen) && enum_shape(e, j, err, errlen);
+    }
     plan_free(&pl);
     return ok;
 }
@@ -653,7 +713,7 @@ static int launch_enum(const TcEnumJob *j, void *hits, void *list, void *count, 
     void *params[] = {&args};
     return tc_cu_check(cudaMemsetAsync(hits, 0, 8, st), "memset", err, errlen) &&
            tc_cu_check(cudaLaunchKernel((const void *)j->m.fn[0], dim3u((unsigned)j->blocks),
-                                        dim3u(TC_ENUM_BLOCK), params, 0, st),
+                                        dim3u((unsigned)j->m.info.block), params, 0, st),
                        "launch tc_enum", err, errlen);
 }
 
@@ -675,7 +735,7 @@ void tc_enum_job_result(const TcEnumJob *j, const void *host_ws, EnumResult *r)
     const uint32_t *count = (const uint32_t *)(h + WS_LIST + (size_t)j->warps * 16 * 8);
     *r = j->base;
     memcpy(&r->hits, h, 8);
-    r->threads = (int)(j->blocks * TC_ENUM_BLOCK);
+    r->threads = (int)(j->blocks * (uint64_t)j->m.info.block);
     /* every warp's list: a kernel whose enumeration order is permuted does not find the
        smallest hits in the first warps */
     for (uint64_t w = 0; w < j->warps && r->hits; w++)
@@ -683,12 +743,10 @@ void tc_enum_job_result(const TcEnumJob *j, const void *host_ws, EnumResult *r)
             cuda_enum_add_hit(r, list[w * 16 + i]);
 }
 
-int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
+/* Runs a prepared job on the engine's stream into the engine's workspace; r gets its result. */
+static int run_prepared(const TcEnumJob *jp, EnumResult *r, char *err, size_t errlen)
 {
-    memset(r, 0, sizeof *r);
-    TcEnumJob j;
-    if (!tc_enum_job_prepare(e, &j, err, errlen))
-        return 0;
+    const TcEnumJob j = *jp;
     uint64_t warps = j.warps;
     if (!tc_scratch(&tc_engine.ws_hits, 8, err, errlen) ||
         !tc_scratch(&tc_engine.ws_list, warps * 16 * 8, err, errlen) ||
@@ -732,12 +790,126 @@ int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
     cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
     r->seconds = ms / 1e3;
     r->hits = hits;
-    r->threads = (int)(j.blocks * TC_ENUM_BLOCK);
+    r->threads = (int)(j.blocks * (uint64_t)j.m.info.block);
     tc_engine.last = j.m.info;
     tc_engine.last_kernel_ms = ms;
     tc_engine.last_grid = (unsigned)j.blocks;
-    tc_engine.last_block = TC_ENUM_BLOCK;
+    tc_engine.last_block = (unsigned)j.m.info.block;
     return 1;
+}
+
+int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
+{
+    memset(r, 0, sizeof *r);
+    TcEnumJob j;
+    return tc_enum_job_prepare(e, &j, err, errlen) && run_prepared(&j, r, err, errlen);
+}
+
+/* ---- the autotuner --------------------------------------------------------------------------- */
+
+typedef struct {
+    const Enum *e;
+    TcGenEnum   g;
+    TcEnumJob   j;
+    int         ok;
+    char        err[256];
+} Candidate;
+
+static void *compile_candidate(void *arg)
+{
+    Candidate *c = arg;
+    memset(&c->j, 0, sizeof c->j);
+    c->ok = enum_module(&c->g, &c->j.m, c->err, sizeof c->err) &&
+            enum_shape(c->e, &c->j, c->err, sizeof c->err);
+    return NULL;
+}
+
+/* Kernels of job e for threads per block 128, 256 and 512 and, where the work splits into
+   stretches, stretches of 8, 16 and 32 steps: compiled in parallel host threads, each run once on
+   a probe -- the whole job, or the share of its chunks that takes about 20 ms -- with every
+   result compared, then timed three times; the fastest becomes the job's kernel for every later
+   launch.  t gets each candidate's best time. */
+int cuda_enum_tune(const Enum *e, CudaTune *t, char *err, size_t errlen)
+{
+    memset(t, 0, sizeof *t);
+    EnumPlan pl;
+    if (!cuda_engine_init(0, err, errlen) || !plan_enum(e, &pl, err, errlen))
+        return 0;
+    uint64_t k1, k2;
+    enum_key(&pl.g, &k1, &k2);  /* the default plan's key: the tuning table's */
+    /* the probe: a share of about 20 ms at the generated code's rate (2e15 lane-ops/s) */
+    double work = (double)(1ull << e->a->ninputs) * e->ticks *
+                  (double)(e->a->len + (e->mode == EN_EQUIV ? e->b->len : 0)) *
+                  (e->part_end - e->part + 1) / e->parts;
+    uint64_t chunks = ((1ull << e->a->ninputs) + 32767) / 32768, parts = 1;
+    while (work / parts > 2e15 * 0.02 && parts * 2 <= chunks)
+        parts *= 2;
+    Enum probe = *e;
+    if (parts > 1) {
+        probe.part = probe.part_end = 0;
+        probe.parts = (int)parts;
+    }
+    t->probe_fraction = parts > 1 ? 1.0 / (double)parts : 1.0;
+    static const int blocks[3] = {128, 256, 512};
+    int splits = pl.g.ticks == 1 && !pl.g.no_map && e->a->ninputs >= 13;
+    Candidate c[9];
+    pthread_t tid[9];
+    int n = 0;
+    for (int b = 0; b < 3; b++)
+        for (int sb = splits ? 3 : 0; sb <= (splits ? 5 : 0); sb++) {
+            c[n].e = parts > 1 ? &probe : e;
+            c[n].g = pl.g;
+            c[n].g.block = blocks[b];
+            c[n].g.step_bits = sb;
+            c[n].ok = 0;
+            n++;
+        }
+    int started = 0;
+    for (; started < n; started++)
+        if (pthread_create(&tid[started], NULL, compile_candidate, &c[started]) != 0)
+            break;
+    for (int i = 0; i < started; i++)
+        pthread_join(tid[i], NULL);
+    int ok = 1, best = -1;
+    EnumResult want;
+    memset(&want, 0, sizeof want);
+    for (int i = 0; i < n && ok; i++) {
+        t->cand[i].block = c[i].g.block;
+        t->cand[i].step_bits = c[i].g.step_bits;
+        t->cand[i].ms = -1;
+        if (i >= started || !c[i].ok)
+            continue;  /* e.g. too many registers for 512 threads: not a candidate */
+        EnumResult r;
+        if (!run_prepared(&c[i].j, &r, err, errlen)) {
+            ok = 0;
+            break;
+        }
+        if (best < 0 && t->ncand == 0)
+            want = r;
+        if (r.hits != want.hits || r.nhit != want.nhit ||
+            memcmp(r.hit, want.hit, sizeof r.hit) != 0) {
+            ok = tc_fail(err, errlen, "autotune: candidate %d gives a different result", i);
+            break;
+        }
+        double ms = 1e30;
+        for (int rep = 0; rep < 3 && ok; rep++) {
+            ok = run_prepared(&c[i].j, &r, err, errlen);
+            if (ok && r.seconds * 1e3 < ms)
+                ms = r.seconds * 1e3;
+        }
+        t->cand[i].ms = ms;
+        t->ncand++;
+        if (best < 0 || ms < t->cand[best].ms)
+            best = i;
+    }
+    t->n = n;
+    t->best = best;
+    if (ok && best < 0)
+        ok = tc_fail(err, errlen, "autotune: no candidate compiled: %s", c[0].err);
+    if (ok)
+        remember_tuning(k1, k2, c[best].g.block, c[best].g.step_bits);
+    plan_free(&pl);
+    return ok;
 }
 
 /* ---- truth tables --------------------------------------------------------------------------- */

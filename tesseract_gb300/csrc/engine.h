@@ -27,6 +27,7 @@ typedef struct {
     /* generated enumeration kernels: the code generator's count of their work per word
        (TcGenWork); stretch_steps = 0 for other kernels */
     int      luts_per_step, luts_per_stretch, stretch_steps, compare_ops;
+    int      block;  /* generated enumeration kernels: the threads per block they were made for */
     char     log[2048];
 } TcModInfo;
 

@@ -84,8 +84,9 @@ extern "C" int cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, siz
     r->ops = pruns * 512 * e->ticks * (e->a->len + (e->mode == EN_EQUIV ? e->b->len : 0));
 
     int per_sm = 0;
+    const int block = m.info.block;  // the kernel's own block size (the autotuner may change it)
     if (!tc_cu_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)m.fn[0],
-                                                                     TC_ENUM_BLOCK, 0),
+                                                                     block, 0),
                      "occupancy", err, errlen))
         return 0;
     if (per_sm < 1)
@@ -93,10 +94,10 @@ extern "C" int cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, siz
     uint64_t words = sel * 1024;
     uint64_t blocks = (uint64_t)tc_engine.sms * (uint64_t)per_sm;
     uint64_t warps_needed = (words + 31) / 32;
-    uint64_t max_blocks = (warps_needed + TC_ENUM_BLOCK / 32 - 1) / (TC_ENUM_BLOCK / 32);
+    uint64_t max_blocks = (warps_needed + block / 32 - 1) / (block / 32);
     if (blocks > max_blocks)
         blocks = max_blocks ? max_blocks : 1;
-    uint64_t warps = blocks * (TC_ENUM_BLOCK / 32);
+    uint64_t warps = blocks * (uint64_t)(block / 32);
     if (warps > TC_STATIC_WARPS)
         return tc_fail(err, errlen, "cuda_enum_run_static: the launch needs %llu warps of hit "
                        "lists; the static workspace holds %u", (unsigned long long)warps,
@@ -123,7 +124,7 @@ extern "C" int cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, siz
         !tc_cu_check(cudaMemsetAsync(args.count, 0, warps * 4, st), "memset", err, errlen) ||
         !tc_cu_check(cudaEventRecord(tc_engine.ev0, st), "event", err, errlen) ||
         !tc_cu_check(cudaLaunchKernel((const void *)m.fn[0], dim3u((unsigned)blocks),
-                                      dim3u(TC_ENUM_BLOCK), params, 0, st),
+                                      dim3u((unsigned)block), params, 0, st),
                      "launch tc_enum", err, errlen) ||
         !tc_cu_check(cudaEventRecord(tc_engine.ev1, st), "event", err, errlen))
         return 0;
@@ -155,10 +156,10 @@ extern "C" int cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, siz
     cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
     r->seconds = ms / 1e3;
     r->hits = hits;
-    r->threads = (int)(blocks * TC_ENUM_BLOCK);
+    r->threads = (int)(blocks * (uint64_t)block);
     tc_engine.last = m.info;
     tc_engine.last_kernel_ms = ms;
     tc_engine.last_grid = (unsigned)blocks;
-    tc_engine.last_block = TC_ENUM_BLOCK;
+    tc_engine.last_block = (unsigned)block;
     return 1;
 }

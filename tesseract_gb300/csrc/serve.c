@@ -45,6 +45,9 @@ void   tc_wave_free(TcWave *w);
 #define RATE_COMPILED 2.0e15
 #define COMPILE_S0 0.1
 #define COMPILE_S_PER_INSTR 4.0e-5  /* ptxas -O2: 0.15 s at 5,000 instructions, 0.77 s at 20,000 */
+/* A job whose kernel is already compiled (the cache is keyed by what the code generator reads)
+   costs only its launch and the polling of its event: about this many seconds. */
+#define LAUNCH_S 3.0e-5
 
 typedef struct {
     TcWave *w;
@@ -99,9 +102,10 @@ typedef struct {
     void        *dev, *host;  /* workspace and its pinned host copy */
 } Slot;
 
-/* Compiled code for job e when the GPU time it saves over the interpreter is worth more than its
-   compile time spread over the compile threads. */
-static int route_compiled(const Enum *e, const CudaServeOpts *o, int threads)
+/* Compiled code for job e when the GPU time it saves over the interpreter (running at
+   rate_interp) is worth more than its compile time spread over the compile threads -- or, when
+   its kernel is in the cache already, more than a launch. */
+static int route_compiled(const Enum *e, const CudaServeOpts *o, int threads, double rate_interp)
 {
     if (o->route == CUDA_SERVE_INTERPRETER || threads < 1)
         return 0;
@@ -109,8 +113,27 @@ static int route_compiled(const Enum *e, const CudaServeOpts *o, int threads)
         return 1;
     double instrs = (double)e->a->len + (e->mode == EN_EQUIV ? (double)e->b->len : 0.0);
     double work = (double)(1ull << e->a->ninputs) * (double)e->ticks * instrs;
-    double saved = work / RATE_INTERP - work / RATE_COMPILED;
+    double saved = work / rate_interp - work / RATE_COMPILED;
+    TcModule m;
+    char why[8];
+    if (tc_enum_cached(e, &m, why, sizeof why))
+        return saved > LAUNCH_S;
     return saved > (COMPILE_S0 + COMPILE_S_PER_INSTR * instrs) / threads;
+}
+
+/* The routing model's figures for a batch planner: seconds to compile a job of `instrs`
+   NAND/STO instructions (0 when its kernel is cached), the GPU seconds of `work` lane-ops on
+   generated code, and a launch's cost. */
+double tc_route_compile_s(const Enum *e, double instrs)
+{
+    TcModule m;
+    char why[8];
+    return tc_enum_cached(e, &m, why, sizeof why) ? 0.0 : COMPILE_S0 + COMPILE_S_PER_INSTR * instrs;
+}
+
+double tc_route_compiled_s(double work)
+{
+    return work / RATE_COMPILED + LAUNCH_S;
 }
 
 static void nap(void)
@@ -119,9 +142,41 @@ static void nap(void)
     nanosleep(&t, NULL);
 }
 
+/* The loop of cuda_serve_run, with the interpreter's routing rate as a parameter: in the served
+   mix its waves share the GPU with compiled jobs and run at about RATE_INTERP; a batch's single
+   wave (tc_serve_batch) has the GPU nearly to itself. */
+static int serve(const Enum *const *jobs, const double *arrival, int njobs,
+                 const CudaServeOpts *opts, double rate_interp, const signed char *route,
+                 double *start, double *finish, EnumResult *results, int *engine_used, char *err,
+                 size_t errlen);
+
 int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
                    const CudaServeOpts *opts, double *start, double *finish, EnumResult *results,
                    int *engine_used, char *err, size_t errlen)
+{
+    return serve(jobs, arrival, njobs, opts, RATE_INTERP, NULL, start, finish, results,
+                 engine_used, err, errlen);
+}
+
+/* Every job arriving at once with its engine chosen by the caller (route[i]: 1 generated code,
+   0 the interpreter). */
+int tc_serve_batch(const Enum *const *jobs, int njobs, const CudaServeOpts *opts,
+                   const signed char *route, double *finish, EnumResult *results,
+                   int *engine_used, char *err, size_t errlen)
+{
+    double *zero = tc_xcalloc((size_t)njobs, sizeof *zero);
+    double *start = tc_xcalloc((size_t)njobs, sizeof *start);
+    int ok = serve(jobs, zero, njobs, opts, RATE_INTERP, route, start, finish, results,
+                   engine_used, err, errlen);
+    free(zero);
+    free(start);
+    return ok;
+}
+
+static int serve(const Enum *const *jobs, const double *arrival, int njobs,
+                 const CudaServeOpts *opts, double rate_interp, const signed char *route,
+                 double *start, double *finish, EnumResult *results, int *engine_used, char *err,
+                 size_t errlen)
 {
     if (njobs <= 0)
         return 1;
@@ -207,7 +262,8 @@ int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
         int progress = 0;
         /* arrivals: to the interpreter's queue or the compile threads */
         while (next < njobs && arrival[next] <= now) {
-            int compiled = route_compiled(jobs[next], &o, nthreads);
+            int compiled = route ? route[next] && nthreads > 0
+                                 : route_compiled(jobs[next], &o, nthreads, rate_interp);
             if (engine_used)
                 engine_used[next] = compiled;
             if (compiled) {

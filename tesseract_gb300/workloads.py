@@ -40,9 +40,11 @@ def job_shape(seed: int):
     return cells, width, max(16, min(4096, length))
 
 
-def batch_equiv_jobs(n: int = 4096, mutate_every: int = 8, width_cap: int | None = None):
+def batch_equiv_jobs(n: int = 4096, mutate_every: int = 8, width_cap: int | None = None,
+                     seeds=None):
+    """The batch's jobs for seeds 0..n-1, or for the given seeds (same generator and shapes)."""
     jobs = []
-    for seed in range(n):
+    for seed in (range(n) if seeds is None else seeds):
         cells, width, length = job_shape(seed)
         if width_cap:
             width = min(width, width_cap)
