@@ -311,6 +311,9 @@ def config_batch(njobs=4096):
                            "jobs_on_generated_kernels": st["compiled"],
                            "jobs_on_interpreter": st["interpreted"],
                            "compile_threads": st["compile_threads"],
+                           "interpreter_start_s": st["interpreter_start"],
+                           "interpreter_end_s": st["interpreter_end"],
+                           "compiled_end_s": st["compiled_end"],
                            "lane_ops_per_s": sum(r["ops"] for r in res) / wall,
                            "results": res}
     ref = None

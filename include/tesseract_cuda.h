@@ -240,10 +240,12 @@ int  cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, size_t errlen
 int  cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char *err,
                     size_t errlen);
 /* The last cuda_batch_run: jobs, how many ran as generated kernels and how many on the
-   interpreter, the compile threads it used and its wall time in seconds. */
+   interpreter, the compile threads it used, its wall time, and in seconds from its start when the
+   interpreter's first launch went out (after packing) and when the last interpreted and the last
+   compiled job finished. */
 typedef struct {
     int    jobs, compiled, interpreted, compile_threads;
-    double seconds;
+    double seconds, interpreter_start, interpreter_end, compiled_end;
 } CudaBatchStats;
 int  cuda_batch_stats(CudaBatchStats *s);
 

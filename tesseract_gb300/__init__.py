@@ -446,7 +446,9 @@ def batch_run(jobs) -> list:
 
 class BatchStats(C.Structure):
     _fields_ = [("jobs", C.c_int), ("compiled", C.c_int), ("interpreted", C.c_int),
-                ("compile_threads", C.c_int), ("seconds", C.c_double)]
+                ("compile_threads", C.c_int), ("seconds", C.c_double),
+                ("interpreter_start", C.c_double), ("interpreter_end", C.c_double),
+                ("compiled_end", C.c_double)]
 
 
 def batch_stats() -> dict:

@@ -3,9 +3,9 @@
    (batch_kernels.cu) and turns its counters back into one EnumResult per job, with the same
    fields, hits, 16 smallest hits and ops accounting as enum_run (src/enum.c:244-332).
 
-   Nothing here is compiled per program, so a batch of thousands of different programs costs one
-   launch.  Jobs whose cells do not fit the interpreter's slot space (255 slots per job) or that
-   ask for --part shares are refused with an error; cuda_enum_run handles those. */
+   Nothing here is compiled per program, so thousands of different programs cost a few persistent
+   launches.  Jobs routed to the interpreter whose cells do not fit its slot space (255 slots per
+   job), or that ask for --part shares, are refused with an error; cuda_enum_run handles those. */
 #include <stdlib.h>
 #include <unistd.h>
 #include <string.h>
@@ -816,17 +816,22 @@ void tc_wave_free(TcWave *w)
 
 /* ---- a batch: every job at once ---------------------------------------------------------------
 
-   cuda_batch_run hands the jobs to the serving loop as if they all arrived at the start, the
-   heaviest first: the jobs the interpreter keeps run in one persistent launch (one wave, one
-   launch per slot class) with 90 % of the GPU's blocks, while the host's cores compile the jobs
-   whose GPU time saved pays for their compile (heaviest first) and the remaining blocks run them
-   as they come; a job whose kernel is already cached goes to compiled code whenever its work is
-   worth a launch.  Results do not depend on the route: both engines enumerate the whole job. */
+   cuda_batch_run hands the jobs to the serving loop as if they all arrived at the start.  A plan
+   (plan() below) sends to generated code the jobs that save the most interpreter time per second
+   of compiling, as long as their compiles, spread over the host's cores, end well before the
+   interpreter is through with the rest; a job whose kernel is cached already goes there whenever
+   its work is worth a launch.  The interpreter's jobs run as persistent launches from a device
+   work queue, in waves of a quarter of the batch on two streams (the GPU starts once the first
+   quarter is packed) with 90 % of the blocks; the compiles start once the first wave is out and
+   the remaining blocks run the compiled jobs as they come; jobs still waiting for a compile
+   thread when the interpreter runs out of work go back to it.  Results do not depend on the
+   route: both engines enumerate the whole job. */
 
 int    tc_serve_batch(const Enum *const *jobs, int njobs, const CudaServeOpts *opts,
                       const signed char *route, double *finish, EnumResult *results,
                       int *engine_used, char *err, size_t errlen);
 double tc_route_compile_s(const Enum *e, double instrs);
+extern double tc_serve_last_wave_at;
 double tc_route_compiled_s(double work);
 
 /* The interpreter's rate on a batch with most of the GPU (1.39e14 NAND/STO lane-ops/s measured
@@ -860,7 +865,11 @@ static void plan(Planned *p, int n, int threads, signed char *route)
     for (int k = 0; k < n; k++) {
         double saved = p[k].work / BATCH_RATE_INTERP - tc_route_compiled_s(p[k].work);
         double c = p[k].compile_s / threads;
-        route[k] = saved > 0 && (c == 0 || compile + c <= interp - p[k].work / BATCH_RATE_INTERP);
+        /* half the interpreter's time: compiles start once its first wave is packed and run
+           slower than modelled when every core compiles; jobs still queued when the
+           interpreter runs out go back to it */
+        route[k] = saved > 0 &&
+                   (c == 0 || compile + c <= 0.5 * (interp - p[k].work / BATCH_RATE_INTERP));
         if (route[k]) {
             compile += c;
             interp -= p[k].work / BATCH_RATE_INTERP;
@@ -878,7 +887,7 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
         return 0;
     double t0 = tc_now();
     long cores = sysconf(_SC_NPROCESSORS_ONLN);
-    int threads = cores > 2 ? (int)cores - 1 : 1;
+    int threads = cores > 3 ? (int)cores - 2 : 1;  /* the host loop and the driver keep a core */
     Planned *p = tc_xmalloc((size_t)njobs * sizeof *p);
     for (int i = 0; i < njobs; i++) {
         const Enum *e = jobs[i];
@@ -902,9 +911,10 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
         any |= route[k];
     CudaServeOpts o;
     memset(&o, 0, sizeof o);
-    o.streams = 1;
+    /* waves of a quarter on two streams: the GPU starts once the first quarter is packed */
+    o.streams = 2;
     o.max_inflight_jobs = njobs;
-    o.max_wave_jobs = njobs;
+    o.max_wave_jobs = njobs >= 256 ? (njobs + 3) / 4 : njobs;
     o.max_device_bytes = (size_t)64 << 30;
     o.share = any ? BATCH_SHARE : 1.0;
     o.compile_threads = any ? threads : -1;
@@ -922,6 +932,15 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
         last_batch.interpreted = njobs - last_batch.compiled;
         last_batch.compile_threads = any ? threads : 0;
         last_batch.seconds = wall;
+        last_batch.interpreter_start = tc_serve_last_wave_at;
+        double last_interp = 0, last_compiled = 0;
+        for (int k = 0; k < njobs; k++) {
+            double *at = engine[k] ? &last_compiled : &last_interp;
+            if (finish[k] > *at)
+                *at = finish[k];
+        }
+        last_batch.interpreter_end = last_interp;
+        last_batch.compiled_end = last_compiled;
     }
     free(p);
     free(route);

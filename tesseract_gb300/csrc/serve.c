@@ -95,6 +95,16 @@ static void *compile_worker(void *arg)
     }
 }
 
+/* Hands held jobs to the compile threads. */
+static void release_held(Compiler *c, const int *ids, int n)
+{
+    pthread_mutex_lock(&c->mu);
+    for (int i = 0; i < n; i++)
+        c->queue[c->qtail++] = ids[i];
+    pthread_cond_broadcast(&c->cv);
+    pthread_mutex_unlock(&c->mu);
+}
+
 typedef struct {
     int          id;          /* -1: free */
     cudaStream_t st;
@@ -149,6 +159,9 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
                  const CudaServeOpts *opts, double rate_interp, const signed char *route,
                  double *start, double *finish, EnumResult *results, int *engine_used, char *err,
                  size_t errlen);
+
+/* when the last call's first interpreter wave went out, in seconds from its start (-1: none) */
+double tc_serve_last_wave_at = -1;
 
 int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
                    const CudaServeOpts *opts, double *start, double *finish, EnumResult *results,
@@ -253,10 +266,14 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
     size_t bytes = 0;
     int *ready = tc_xmalloc((size_t)njobs * sizeof *ready), nready = 0, rhead = 0;
     const Enum **wj = tc_xmalloc((size_t)njobs * sizeof *wj);
+    /* a batch holds its compiles until its first interpreter wave is out: packing the wave
+       needs the host's cores first */
+    int held = route != NULL, nheld = 0;
+    int *held_ids = tc_xmalloc((size_t)njobs * sizeof *held_ids);
     TcWave *pending = NULL;  /* a wave prepared but not yet admitted */
     int pending_n = 0;
     size_t pending_need = 0;
-    double t0 = tc_now();
+    double t0 = tc_now(), wave_launched_at = -1;
     while (ok && finished < njobs) {
         double now = tc_now() - t0;
         int progress = 0;
@@ -266,7 +283,9 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
                                  : route_compiled(jobs[next], &o, nthreads, rate_interp);
             if (engine_used)
                 engine_used[next] = compiled;
-            if (compiled) {
+            if (compiled && held) {
+                held_ids[nheld++] = next;
+            } else if (compiled) {
                 pthread_mutex_lock(&cc.mu);
                 cc.queue[cc.qtail++] = next;
                 pthread_cond_signal(&cc.cv);
@@ -275,6 +294,10 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
                 ready[nready++] = next;
             }
             next++;
+        }
+        if (held && next == njobs && nready == 0) {  /* a batch with no interpreter jobs */
+            held = 0;
+            release_held(&cc, held_ids, nheld);
         }
         /* compiled jobs: launch into free slots, collect finished ones */
         if (nsl) {
@@ -327,6 +350,18 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
                 s = i;
                 break;
             }
+        /* a batch whose interpreter has run out of work takes back the jobs still waiting for a
+           compile thread: the GPU is free now, the compile threads are not */
+        if (route && !held && s >= 0 && !pending && rhead == nready && next == njobs) {
+            pthread_mutex_lock(&cc.mu);
+            while (cc.qhead < cc.qtail) {
+                int id = cc.queue[--cc.qtail];
+                ready[nready++] = id;
+                if (engine_used)
+                    engine_used[id] = 0;
+            }
+            pthread_mutex_unlock(&cc.mu);
+        }
         if (s >= 0 && !pending && rhead < nready && inflight < o.max_inflight_jobs) {
             int n = 0;
             while (rhead + n < nready && n < o.max_wave_jobs && inflight + n < o.max_inflight_jobs)
@@ -357,6 +392,11 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
             fl[s].bytes = pending_need;
             for (int i = 0; i < n; i++)
                 start[ready[rhead + i]] = at;
+            if (held) {
+                held = 0;
+                release_held(&cc, held_ids, nheld);
+                wave_launched_at = at;
+            }
             busy[s] = 1;
             rhead += n;
             inflight += n;
@@ -435,5 +475,7 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
     free(cc.ready);
     free(ready);
     free(wj);
+    free(held_ids);
+    tc_serve_last_wave_at = wave_launched_at;
     return ok;
 }

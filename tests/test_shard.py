@@ -66,3 +66,32 @@ def test_share_rule():
     assert shard.share(1, 4) == dict(part=1, part_end=1, parts=4)
     with pytest.raises(ValueError):
         shard.share(4, 4)
+
+
+def gpu_rank_main(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        out[rank] = [shard.gather_merge(shard.run_share(mode, a, b, spec, rank=rank, world=world))
+                     for mode, a, b, spec in jobs()]
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("world", [2, 3])
+def test_gpu_shares_over_gloo_merge_to_the_whole(world):
+    """The same over the real path: each gloo rank runs its share on the GPU (cuda_enum_run with
+    --part rank/world; the ranks share this host's one GPU, and no rank's kernel waits on
+    another's), gathers the records and merges them; every rank's total equals the oracle's
+    whole run."""
+    port = free_port()
+    with mp.get_context("spawn").Manager() as mgr:
+        out = mgr.dict()
+        mp.spawn(gpu_rank_main, args=(world, port, out), nprocs=world, join=True)
+        results = dict(out)
+    for i, (mode, a, b, spec) in enumerate(jobs()):
+        whole = O.enum_run(mode, a, b, spec)
+        for r in range(world):
+            for k in KEYS:
+                assert results[r][i][k] == whole[k], (i, r, k)
