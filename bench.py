@@ -249,6 +249,9 @@ def config_life(gens=1000):
     L = LifeCube(16)
     setup_s = time.perf_counter() - t0
     L.seed(42)
+    t0 = time.perf_counter()
+    tune = L.cube.tune(32)  # runs of words per group-major block, measured on this board
+    tune["seconds"] = time.perf_counter() - t0
     start = L.board()
     L.run(16)                       # warm-up: graph capture, first launches
     L.seed(42)
@@ -270,7 +273,7 @@ def config_life(gens=1000):
            "lane_ops_per_s": gens * len(n) * 65536 / (ms / 1e3),
            "program": {"instructions": len(n), "cells": n.ncells,
                        "segments": L.cube.segments, "kernels_per_pass": L.cube.kernels},
-           "setup_s_incl_nvrtc": setup_s, "cpu_word_parallel_life_s": cpu_s,
+           "setup_s_incl_nvrtc": setup_s, "autotune": tune, "cpu_word_parallel_life_s": cpu_s,
            "cpu_threads": os.cpu_count(), "clocks": clk.summary()}
     # the exchange between machines: 1,056 link reads per machine per generation (4 gathers
     # of the tile edges), one bit each, 476 of them across 512-machine groups

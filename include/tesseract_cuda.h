@@ -359,6 +359,21 @@ int  cuda_cube_load(CudaCube *c, unsigned group, const uint64_t *mem_lines, cons
 int  cuda_cube_store(const CudaCube *c, unsigned group, uint64_t *mem_lines, uint64_t *rr_line,
                      char *err, size_t errlen);
 int  cuda_cube_run(CudaCube *c, uint64_t passes, char *err, size_t errlen);
+/* The cube's autotuner: the kernels whose blocks each run one warp group's code are compiled for
+   1, 2, 4 and 8 runs of words per block (as the cube's size allows), each variant is run for
+   probe_passes passes from the cube's present state (saved before, restored after: the state is
+   unchanged), and the fastest is kept for every later pass.  cand[i].ms is variant i's time.
+   No counterpart in the reference. */
+typedef struct {
+    int      n, best;
+    struct {
+        unsigned iters;
+        double   ms;
+    } cand[4];
+    unsigned probe_passes;
+} CudaCubeTune;
+int  cuda_cube_tune(CudaCube *c, unsigned probe_passes, CudaCubeTune *t, char *err,
+                    size_t errlen);
 /* The whole cube at once, cell-major: cell c of machine m is bit m % 32 of word c * W + m / 32,
    W = machines / 32 (ncells x W words), and RR as W words; ZERO and ONE keep their values.
    cuda_cube_kernels: kernel launches per pass (segments, long ones split). */

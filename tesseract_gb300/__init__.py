@@ -569,6 +569,15 @@ def cube_demo(name: str, dims: int, checks: int = 3, seconds: float = 0.2) -> di
             for f, _ in DemoResult._fields_}
 
 
+class _CubeCand(C.Structure):
+    _fields_ = [("iters", C.c_uint), ("ms", C.c_double)]
+
+
+class CudaCubeTune(C.Structure):
+    _fields_ = [("n", C.c_int), ("best", C.c_int), ("cand", _CubeCand * 4),
+                ("probe_passes", C.c_uint)]
+
+
 class Cube:
     """A program's cube of machines on the device (LaneCube + jit_cube_run).
 
@@ -600,6 +609,20 @@ class Cube:
         if not lib().cuda_cube_run(self.h, passes, e, len(e)):
             raise EngineError(e.value.decode())
         return last_launch()["kernel_ms"]
+
+    def tune(self, probe_passes: int = 16) -> dict:
+        """The cube's autotuner (cuda_cube_tune): word runs per group-major block, measured on
+        this cube from its present state, which it leaves unchanged."""
+        t, e = CudaCubeTune(), _err()
+        L = lib()
+        L.cuda_cube_tune.restype = C.c_int
+        L.cuda_cube_tune.argtypes = [C.c_void_p, C.c_uint, C.POINTER(CudaCubeTune), C.c_char_p,
+                                     C.c_size_t]
+        if not L.cuda_cube_tune(self.h, probe_passes, C.byref(t), e, len(e)):
+            raise EngineError(e.value.decode())
+        cands = [{"iters": t.cand[i].iters, "ms": t.cand[i].ms if t.cand[i].ms >= 0 else None}
+                 for i in range(t.n)]
+        return {"candidates": cands, "best": cands[t.best], "probe_passes": probe_passes}
 
     def read(self):
         np = self.np

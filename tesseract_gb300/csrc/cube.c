@@ -61,6 +61,7 @@ struct CudaCube {
     int         *gmajor;    /* kernel k is group-major (one group per block) */
     cudaGraphExec_t graph;
     unsigned    graph_passes;
+    unsigned    iters;      /* runs of words each group-major block walks (cuda_cube_tune) */
 };
 
 struct CudaCode {
@@ -701,8 +702,18 @@ static unsigned gm_warps(unsigned W)
     return wpb;
 }
 
+/* The runs of 32 * gm_warps(W) words a group-major block walks: `iters` (a power of two), as
+   far as the word blocks of a group divide evenly. */
+static unsigned gm_iters(unsigned W, unsigned iters)
+{
+    unsigned nwb = (W + 32 * gm_warps(W) - 1) / (32 * gm_warps(W)), it = 1;
+    while (2 * it <= iters && nwb % (2 * it) == 0)
+        it *= 2;
+    return it;
+}
+
 static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size_t from, size_t to,
-                        int loop, int *group_major)
+                        int loop, int *group_major, unsigned iters)
 {
     Chunk k = {p, W, tc_xcalloc(p->ncells + 1, 1), tc_xcalloc(p->ncells + 1, 1)};
     unsigned groups = chunk_groups(p, from, to, loop);
@@ -732,20 +743,25 @@ static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size
         Src body = {0};
         split_body(&body, &k, from, to, groups, 0, &gm);
         unsigned wpb = gm_warps(W), nwb = (W + 32 * wpb - 1) / (32 * wpb);
+        unsigned it = gm ? gm_iters(W, iters) : 1;
         emit(o, "extern \"C\" __global__ void __launch_bounds__(%u) tc_cube_%u(u32 *__restrict__ "
                 "mem, u32 *__restrict__ rr, const u32 passes)\n{\n",
              gm ? 32 * wpb : TC_CUBE_BLOCK * groups, idx);
         if (gm) {
-            emit(o, "    const u32 group = blockIdx.x / %uu;\n", nwb);
-            emit(o, "    const u32 t = (blockIdx.x %% %uu) * %uu + threadIdx.y * 32u + threadIdx.x;\n",
-                 nwb, 32 * wpb);
+            /* a block is one group over `it` runs of 32 * wpb words, one after the other: the
+               group's straight-line code is fetched for the first run and found in the
+               instruction cache for the others */
+            emit(o, "    const u32 group = blockIdx.x / %uu;\n", nwb / it);
+            emit(o, "#pragma unroll 1\n    for (u32 it = 0; it < %uu; it++) {\n", it);
+            emit(o, "    const u32 t = ((blockIdx.x %% %uu) * %uu + it) * %uu + threadIdx.y * 32u + "
+                    "threadIdx.x;\n", nwb / it, it, 32 * wpb);
         } else {
-            emit(o, "    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;\n");
+            emit(o, "    {\n    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;\n");
         }
         emit(o, "    const u32 w = t & (W - 1u);\n");
         emit(o, "    u32 *const m = mem + w;\n");
         emit(o, "    u32 r = rr[w];\n");
-        emit(o, "%.*s}\n", (int)body.len, body.s ? body.s : "");
+        emit(o, "%.*s    }\n}\n", (int)body.len, body.s ? body.s : "");
         free(body.s);
         free(k.loaded);
         free(k.written);
@@ -799,7 +815,7 @@ char *tc_codegen_cube(const Program *p, const size_t *first, unsigned nk, int bl
     emit(&o, "#define W %uu\n", W);
     emit(&o, "%s", CUBE_PRELUDE);
     for (unsigned k = 0; k < nk; k++)
-        emit_kernel(&o, p, W, k, first[k], first[k + 1], loop, NULL);
+        emit_kernel(&o, p, W, k, first[k], first[k + 1], loop, NULL, 1);
     if (len)
         *len = o.len;
     return o.s;
@@ -808,10 +824,13 @@ char *tc_codegen_cube(const Program *p, const size_t *first, unsigned nk, int bl
 /* ---- compilation: kernels in parallel NVRTC programs ---------------------------------------- */
 
 typedef struct {
-    CudaCube *c;
-    unsigned  k0, k1;  /* kernels of this module */
-    int       ok;
-    char      err[512];
+    CudaCube     *c;
+    unsigned      k0, k1;  /* kernels of this module */
+    unsigned      iters;   /* group-major runs per block */
+    cudaKernel_t *fn;      /* where the kernels go */
+    int          *gm;      /* where each kernel's group-major choice goes */
+    int           ok;
+    char          err[512];
 } CompileJob;
 
 static void *compile_job(void *arg)
@@ -826,13 +845,13 @@ static void *compile_job(void *arg)
         first[k] = c->first[j->k0 + k];
     int loop = c->nk == 1 && c->dims <= FAR_DIM;
     Src o = {0};
-    emit(&o, "// generated by the tesseract GB300 engine: cube of 2^%u machines, kernels %u..%u\n",
-         c->dims, j->k0, j->k1 - 1);
+    emit(&o, "// generated by the tesseract GB300 engine: cube of 2^%u machines, kernels %u..%u, "
+            "%u run(s) per group-major block\n", c->dims, j->k0, j->k1 - 1, j->iters);
     emit(&o, "#define W %uu\n", c->W);
     emit(&o, "%s", CUBE_PRELUDE);
     for (unsigned k = 0; k < nk; k++)
         emit_kernel(&o, &c->p, c->W, j->k0 + k, first[k], first[k + 1], loop,
-                    &c->gmajor[j->k0 + k]);
+                    &j->gm[j->k0 + k], j->iters);
     len = o.len;
     char **names = tc_xmalloc(nk * sizeof *names);
     for (unsigned k = 0; k < nk; k++) {
@@ -846,7 +865,7 @@ static void *compile_job(void *arg)
         j->ok = tc_module(o.s, len, (const char *const *)names + k0, (int)n, NULL, &m, j->err,
                           sizeof j->err);
         for (unsigned k = 0; j->ok && k < n; k++)
-            c->fn[j->k0 + k0 + k] = m.fn[k];
+            j->fn[j->k0 + k0 + k] = m.fn[k];
     }
     for (unsigned k = 0; k < nk; k++)
         free(names[k]);
@@ -929,10 +948,14 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
     unsigned per = 1, nj = (c->nk + per - 1) / per;
     CompileJob *jobs = tc_xcalloc(nj, sizeof *jobs);
     pthread_t *tid = tc_xcalloc(nj, sizeof *tid);
+    c->iters = 1;
     for (unsigned j = 0; j < nj; j++) {
         jobs[j].c = c;
         jobs[j].k0 = j * per;
         jobs[j].k1 = (j + 1) * per < c->nk ? (j + 1) * per : c->nk;
+        jobs[j].iters = c->iters;
+        jobs[j].fn = c->fn;
+        jobs[j].gm = c->gmajor;
         pthread_create(&tid[j], NULL, compile_job, &jobs[j]);
     }
     int ok = 1;
@@ -1026,10 +1049,10 @@ static int launch_pass(CudaCube *c, cudaStream_t s, unsigned passes)
         uint32_t *mem = c->mem, *rr = c->rr;
         void *args[] = {&mem, &rr, &passes};
         dim3 b = dim3u(block), g = dim3u(grid);
-        if (c->gmajor[k]) {  /* blocks of one group: gm_warps warps of 32 words */
+        if (c->gmajor[k]) {  /* blocks of one group: gm_warps warps over gm_iters runs */
             unsigned wpb = gm_warps(c->W);
             b.y = wpb;
-            g.x = ((c->W + 32 * wpb - 1) / (32 * wpb)) * c->warps[k];
+            g.x = ((c->W + 32 * wpb - 1) / (32 * wpb)) / gm_iters(c->W, c->iters) * c->warps[k];
         } else {
             b.y = c->warps[k];
         }
@@ -1092,6 +1115,122 @@ int cuda_cube_run(CudaCube *c, uint64_t passes, char *err, size_t errlen)
     cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
     tc_engine.last_kernel_ms = ms;
     return 1;
+}
+
+/* ---- the autotuner for cube kernels ------------------------------------------------------------
+
+   A group-major kernel's block runs one group's straight-line code, once per warp; with the code
+   fetched cold every time, instruction fetch, not the ALU, sets the pace (Life on 65,536
+   machines: no_instruction the first stall).  Blocks that walk 2, 4 or 8 runs of words in a loop
+   find the code cached after the first run, at the price of fewer blocks in flight.  Which is
+   fastest depends on the program and the cube's size, so it is measured: every variant is
+   compiled (in parallel), run for probe_passes passes from the cube's present state, which is
+   saved before and restored after, and the fastest kept. */
+int cuda_cube_tune(CudaCube *c, unsigned probe_passes, CudaCubeTune *t, char *err, size_t errlen)
+{
+    memset(t, 0, sizeof *t);
+    int any_gm = 0;
+    for (unsigned k = 0; k < c->nk; k++)
+        any_gm |= c->gmajor[k];
+    static const unsigned wanted[4] = {1, 2, 4, 8};
+    unsigned its[4];
+    int n = 0;
+    for (int i = 0; i < 4; i++) {
+        unsigned e = any_gm && !c->loop ? gm_iters(c->W, wanted[i]) : 1;
+        int seen = 0;
+        for (int j = 0; j < n; j++)
+            seen |= its[j] == e;
+        if (!seen)
+            its[n++] = e;
+    }
+    t->n = n;
+    t->probe_passes = probe_passes;
+    for (int i = 0; i < n; i++) {
+        t->cand[i].iters = its[i];
+        t->cand[i].ms = -1;
+    }
+    if (n == 1 || probe_passes == 0) {
+        t->best = 0;
+        return 1;
+    }
+    cudaKernel_t *fns[4];
+    int *gms = tc_xcalloc(c->nk, sizeof *gms);
+    CompileJob *jobs = tc_xcalloc((size_t)n * c->nk, sizeof *jobs);
+    pthread_t *tid = tc_xcalloc((size_t)n * c->nk, sizeof *tid);
+    unsigned nj = 0;
+    for (int i = 0; i < n; i++) {
+        fns[i] = its[i] == c->iters ? c->fn : tc_xcalloc(c->nk, sizeof *fns[i]);
+        for (unsigned k = 0; its[i] != c->iters && k < c->nk; k++) {
+            jobs[nj] = (CompileJob){c, k, k + 1, its[i], fns[i], gms, 0, ""};
+            if (pthread_create(&tid[nj], NULL, compile_job, &jobs[nj]) == 0)
+                nj++;
+        }
+    }
+    int ok = 1;
+    for (unsigned j = 0; j < nj; j++) {
+        pthread_join(tid[j], NULL);
+        if (!jobs[j].ok && ok)
+            ok = tc_fail(err, errlen, "%s", jobs[j].err);
+    }
+    free(jobs);
+    free(tid);
+    free(gms);
+    size_t words = (size_t)c->W * (c->p.ncells + 1);
+    uint32_t *save_mem = NULL, *save_rr = NULL;
+    cudaStream_t s = tc_engine.stream;
+    ok = ok &&
+         tc_cu_check(cudaMalloc((void **)&save_mem, words * 4), "cudaMalloc", err, errlen) &&
+         tc_cu_check(cudaMalloc((void **)&save_rr, (size_t)c->W * 4), "cudaMalloc", err, errlen) &&
+         tc_cu_check(cudaMemcpyAsync(save_mem, c->mem, words * 4, cudaMemcpyDeviceToDevice, s),
+                     "save", err, errlen) &&
+         tc_cu_check(cudaMemcpyAsync(save_rr, c->rr, (size_t)c->W * 4, cudaMemcpyDeviceToDevice,
+                                     s), "save", err, errlen);
+    cudaKernel_t *keep_fn = c->fn;
+    unsigned keep_iters = c->iters;
+    int best = -1;
+    for (int i = 0; ok && i < n; i++) {
+        c->fn = fns[i];
+        c->iters = its[i];
+        for (int rep = 0; ok && rep < 2; rep++) {  /* a warm-up run, then the timed one */
+            ok = tc_cu_check(cudaMemcpyAsync(c->mem, save_mem, words * 4,
+                                             cudaMemcpyDeviceToDevice, s), "restore", err,
+                             errlen) &&
+                 tc_cu_check(cudaMemcpyAsync(c->rr, save_rr, (size_t)c->W * 4,
+                                             cudaMemcpyDeviceToDevice, s), "restore", err,
+                             errlen) &&
+                 tc_cu_check(cudaEventRecord(tc_engine.ev0, s), "event", err, errlen);
+            for (unsigned q = 0; ok && q < probe_passes; q++)
+                ok = launch_pass(c, s, 1) ||
+                     tc_cu_check(cudaGetLastError(), "cube launch", err, errlen);
+            ok = ok && tc_cu_check(cudaEventRecord(tc_engine.ev1, s), "event", err, errlen) &&
+                 tc_cu_check(cudaEventSynchronize(tc_engine.ev1), "tune", err, errlen);
+        }
+        float ms = 0;
+        if (ok)
+            cudaEventElapsedTime(&ms, tc_engine.ev0, tc_engine.ev1);
+        t->cand[i].ms = ms;
+        if (ok && (best < 0 || ms < t->cand[best].ms))
+            best = i;
+    }
+    if (ok)
+        ok = tc_cu_check(cudaMemcpyAsync(c->mem, save_mem, words * 4, cudaMemcpyDeviceToDevice,
+                                         s), "restore", err, errlen) &&
+             tc_cu_check(cudaMemcpyAsync(c->rr, save_rr, (size_t)c->W * 4,
+                                         cudaMemcpyDeviceToDevice, s), "restore", err, errlen) &&
+             tc_cu_check(cudaStreamSynchronize(s), "restore", err, errlen);
+    c->fn = ok ? fns[best] : keep_fn;
+    c->iters = ok ? its[best] : keep_iters;
+    for (int i = 0; i < n; i++)
+        if (fns[i] != c->fn)
+            free(fns[i]);
+    cudaFree(save_mem);
+    cudaFree(save_rr);
+    if (ok && c->graph) {  /* the captured passes hold the old kernels */
+        cudaGraphExecDestroy(c->graph);
+        c->graph = NULL;
+    }
+    t->best = ok ? best : 0;
+    return ok;
 }
 
 /* ---- compiled code handles (jit_compile / jit_free) ----------------------------------------- */

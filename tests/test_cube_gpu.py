@@ -129,3 +129,35 @@ def test_life_dims16_full_board():
     start = L.board()
     L.run(10)
     assert (L.board() == life_reference(start, 10)).all()
+
+
+def test_cube_tune_keeps_state_and_results():
+    """cuda_cube_tune: every variant (word runs per group-major block) is timed from the cube's
+    present state, the state is the same afterwards, the fastest is kept, and generations after
+    tuning still equal plain C Life."""
+    L = LifeCube(14, w=8, h=8)  # 512 words: up to 4 runs of 128 words per block
+    L.seed(7)
+    start = L.board()
+    t = L.cube.tune(8)
+    assert [c["iters"] for c in t["candidates"]] == [1, 2, 4]
+    assert (L.board() == start).all()
+    timed = [c["ms"] for c in t["candidates"] if c["ms"] is not None]
+    assert t["best"]["ms"] == min(timed)
+    L.run(9)
+    assert (L.board() == life_reference(start, 9)).all()
+
+
+def test_life_dims16_tuned_1000_generations():
+    """The benchmark's configuration in full: 65,536 machines, 8192 x 8192, seed 42, the tuned
+    kernels, 1,000 generations, against the oracle's word-parallel plain C Life."""
+    import oracle as O
+    from tesseract_gb300.life import pack_rows, unpack_rows
+    L = LifeCube(16)
+    L.seed(42)
+    t = L.cube.tune(16)
+    assert len(t["candidates"]) >= 2
+    start = L.board()
+    L.run(1000)
+    packed = pack_rows(start)
+    O.life_words(packed, 1000)
+    assert (unpack_rows(packed) == L.board()).all()
