@@ -272,7 +272,9 @@ def config_life(gens=1000):
            "cell_updates_per_s": gens * 8192 * 8192 / (ms / 1e3),
            "lane_ops_per_s": gens * len(n) * 65536 / (ms / 1e3),
            "program": {"instructions": len(n), "cells": n.ncells,
-                       "segments": L.cube.segments, "kernels_per_pass": L.cube.kernels},
+                       "segments": L.cube.segments, "kernels_per_pass": L.cube.kernels,
+                       "closing_copy_kernels": L.cube.closing_copies,
+                       "kernels_per_generation": L.cube.kernels - L.cube.closing_copies},
            "setup_s_incl_nvrtc": setup_s, "autotune": tune, "cpu_word_parallel_life_s": cpu_s,
            "cpu_threads": os.cpu_count(), "clocks": clk.summary()}
     # the exchange between machines: 1,056 link reads per machine per generation (4 gathers

@@ -376,12 +376,17 @@ int  cuda_cube_tune(CudaCube *c, unsigned probe_passes, CudaCubeTune *t, char *e
                     size_t errlen);
 /* The whole cube at once, cell-major: cell c of machine m is bit m % 32 of word c * W + m / 32,
    W = machines / 32 (ncells x W words), and RR as W words; ZERO and ONE keep their values.
-   cuda_cube_kernels: kernel launches per pass (segments, long ones split). */
+   cuda_cube_kernels: kernel launches per pass (segments, long ones split).
+   cuda_cube_closing_copies: how many of them are the pass's closing copies (A <- B: a Life
+   board taking its next generation), which a run leaves out of every pass but its last by
+   exchanging A's and B's memory in alternate passes (0: the program has none, or they do not
+   qualify). */
 int  cuda_cube_read_words(const CudaCube *c, uint32_t *mem, uint32_t *rr, char *err,
                           size_t errlen);
 int  cuda_cube_write_words(CudaCube *c, const uint32_t *mem, const uint32_t *rr, char *err,
                            size_t errlen);
 unsigned cuda_cube_kernels(const CudaCube *c);
+unsigned cuda_cube_closing_copies(const CudaCube *c);
 
 /* `alpha cube DEMO --dims D` (src/cubedemo.c:549-623) on the GPU cube: builds demo any, rank,
    sort or life for 2^dims machines (dims 9..16), runs `checks` rounds of random inputs one pass

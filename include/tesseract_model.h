@@ -54,6 +54,12 @@ void     tc_gen_cube_max(Program *p, int dims);
 void     tc_gen_cube_anf(Program *p, int dims);
 void     tc_gen_cube_walsh(Program *p, int dims);
 void     tc_gen_cube_ring(Program *p, int dims);
+/* pack (.in/.out v0..v7 h: the bytes of the machines with h = 1 gathered, in order, into the
+   first machines, which end with h = 1, src/cubedemo.c:134-151), xorconv (.in f g, .out h0..:
+   h(k) = how many j have f(j) = g(j ^ k) = 1, dims + 1 bits, by Walsh-Hadamard spectra,
+   src/cubedemo.c:231-251). */
+void     tc_gen_cube_pack(Program *p, int dims);
+void     tc_gen_cube_xorconv(Program *p, int dims);
 /* polymul (dims 9..11): .in a0.. b0.. zf<d>_0.. zi<d>_0.., .out c0..: c = a b in
    Z_12289[x]/(x^(2^dims) + 1), one coefficient per machine, by the number-theoretic transform
    (the reference's demo, src/gen.c:456-669, src/cubedemo.c:253-284); zf and zi are the forward

@@ -158,6 +158,7 @@ def lib():
             "cuda_cube_groups": (C.c_uint, [C.c_void_p]),
             "cuda_cube_segments": (C.c_uint, [C.c_void_p]),
             "cuda_cube_kernels": (C.c_uint, [C.c_void_p]),
+            "cuda_cube_closing_copies": (C.c_uint, [C.c_void_p]),
             "cuda_cube_load": (C.c_int, [C.c_void_p, C.c_uint, C.c_void_p, C.c_void_p,
                                          C.c_char_p, C.c_size_t]),
             "cuda_cube_store": (C.c_int, [C.c_void_p, C.c_uint, C.c_void_p, C.c_void_p,
@@ -257,9 +258,11 @@ class Program:
 
     @classmethod
     def gen_cube_demo(cls, name: str, dims: int):
-        """The cube demo `name` (any, rank, sort, max, anf, walsh, ring) for 2^dims machines."""
+        """The cube demo `name` (any, rank, sort, max, pack, anf, walsh, xorconv, ring, polymul)
+        for 2^dims machines."""
         fn = {"any": "tc_gen_cube_any", "rank": "tc_gen_cube_rank", "sort": "tc_gen_cube_sort",
-              "max": "tc_gen_cube_max", "anf": "tc_gen_cube_anf", "walsh": "tc_gen_cube_walsh",
+              "max": "tc_gen_cube_max", "pack": "tc_gen_cube_pack", "anf": "tc_gen_cube_anf",
+              "walsh": "tc_gen_cube_walsh", "xorconv": "tc_gen_cube_xorconv",
               "ring": "tc_gen_cube_ring", "polymul": "tc_gen_cube_polymul"}
         p = cls()
         f = getattr(lib(), fn[name])
@@ -598,6 +601,7 @@ class Cube:
         self.W = self.machines // 32
         self.segments = lib().cuda_cube_segments(self.h)
         self.kernels = lib().cuda_cube_kernels(self.h)
+        self.closing_copies = lib().cuda_cube_closing_copies(self.h)
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:

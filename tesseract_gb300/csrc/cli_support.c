@@ -371,6 +371,48 @@ static void polymul_inputs(const Program *p, int dims, uint32_t *mem, unsigned W
     free(y);
 }
 
+/* h(k) = how many j have f(j) = g(j ^ k) = 1, f in bit 0 and g in bit 1 of fg[j]: the sum
+   itself up to 2^12 machines, beyond that through the integer Walsh-Hadamard transform
+   (exact: the transform of h is the product of those of f and g). */
+static uint64_t *xor_convolution(const uint64_t *fg, int dims)
+{
+    unsigned n = 1u << dims;
+    uint64_t *h = tc_xcalloc(n, sizeof *h);
+    if (dims <= 12) {
+        for (unsigned k = 0; k < n; k++)
+            for (unsigned j = 0; j < n; j++)
+                h[k] += fg[j] & fg[j ^ k] >> 1 & 1;
+        return h;
+    }
+    int64_t *a = tc_xmalloc((size_t)n * sizeof *a), *b = tc_xmalloc((size_t)n * sizeof *b);
+    for (unsigned k = 0; k < n; k++) {
+        a[k] = (int64_t)(fg[k] & 1);
+        b[k] = (int64_t)(fg[k] >> 1);
+    }
+    for (int pass = 0; pass < 2; pass++) {
+        for (unsigned d = 1; d < n; d <<= 1)
+            for (unsigned k = 0; k < n; k++)
+                if (!(k & d)) {
+                    int64_t u = a[k], v = a[k | d];
+                    a[k] = u + v;
+                    a[k | d] = u - v;
+                    if (!pass) {
+                        u = b[k], v = b[k | d];
+                        b[k] = u + v;
+                        b[k | d] = u - v;
+                    }
+                }
+        if (!pass)
+            for (unsigned k = 0; k < n; k++)
+                a[k] *= b[k];
+    }
+    for (unsigned k = 0; k < n; k++)
+        h[k] = (uint64_t)(a[k] >> dims);
+    free(a);
+    free(b);
+    return h;
+}
+
 int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaDemoResult *r,
                    char *err, size_t errlen)
 {
@@ -394,6 +436,12 @@ int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaD
     } else if (!strcmp(name, "max")) {
         snprintf(r->what, sizeof r->what, "largest of %u bytes", n);
         tc_gen_cube_max(&p, dims);
+    } else if (!strcmp(name, "pack")) {
+        snprintf(r->what, sizeof r->what, "gather the bytes of the machines with a hit");
+        tc_gen_cube_pack(&p, dims);
+    } else if (!strcmp(name, "xorconv")) {
+        snprintf(r->what, sizeof r->what, "h(k) = #x: f(x) = g(x^k) = 1, by spectra");
+        tc_gen_cube_xorconv(&p, dims);
     } else if (!strcmp(name, "anf")) {
         snprintf(r->what, sizeof r->what, "truth table of %d inputs -> normal form (Mobius)", dims);
         tc_gen_cube_anf(&p, dims);
@@ -414,8 +462,8 @@ int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaD
         board = tc_xmalloc((size_t)T * T * sizeof *board);
         tc_gen_life_cube(&p, T, T, rbits, cbits, board);
     } else {
-        return tc_fail(err, errlen, "unknown demo '%s' (any, rank, max, sort, anf, walsh, ring, "
-                       "polymul, life)", name);
+        return tc_fail(err, errlen, "unknown demo '%s' (any, rank, max, sort, pack, anf, walsh, "
+                       "xorconv, ring, polymul, life)", name);
     }
     r->instr = p.len;
     CudaCube *c;
@@ -466,6 +514,24 @@ int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaD
                 vput(mem, W, x, 8, k, v);
                 count = v > count ? v : count;
             }
+        } else if (!strcmp(name, "pack")) {
+            find_cells(&p, "v", 8, x);
+            tc_program_find_cell(&p, "h", &x[8]);
+            for (unsigned k = 0; k < n; k++) {  /* want: the bytes of the hits, in order */
+                uint64_t v = tc_splitmix64(&s) & 255, hit = tc_splitmix64(&s) % 10 == 0;
+                vput(mem, W, x, 8, k, v);
+                mset(mem, W, x[8], k, (unsigned)hit);
+                if (hit)
+                    want[count++] = v;
+            }
+        } else if (!strcmp(name, "xorconv")) {
+            tc_program_find_cell(&p, "f", &x[0]);
+            tc_program_find_cell(&p, "g", &x[1]);
+            for (unsigned k = 0; k < n; k++) {  /* want: f in bit 0, g in bit 1 */
+                want[k] = tc_splitmix64(&s) & 3;
+                mset(mem, W, x[0], k, (unsigned)(want[k] & 1));
+                mset(mem, W, x[1], k, (unsigned)(want[k] >> 1));
+            }
         } else if (!strcmp(name, "anf") || !strcmp(name, "walsh")) {
             tc_program_find_cell(&p, "f", &x[0]);
             for (unsigned k = 0; k < n; k++)
@@ -510,6 +576,16 @@ int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaD
             find_cells(&p, "m", 8, pv);
             for (unsigned k = 0; k < n && ok; k++)
                 ok = vget(mem, W, pv, 8, k) == count;
+        } else if (!strcmp(name, "pack")) {
+            for (unsigned k = 0; k < n && ok; k++)
+                ok = mget(mem, W, x[8], k) == (k < count) &&
+                     (k >= count || vget(mem, W, x, 8, k) == want[k]);
+        } else if (!strcmp(name, "xorconv")) {
+            uint64_t *h = xor_convolution(want, dims);
+            find_cells(&p, "h", dims + 1, pv);
+            for (unsigned k = 0; k < n && ok; k++)
+                ok = vget(mem, W, pv, dims + 1, k) == h[k];
+            free(h);
         } else if (!strcmp(name, "anf")) {
             for (unsigned d = 1; d < n; d <<= 1)  /* the Mobius transform in plain C */
                 for (unsigned k = 0; k < n; k++)

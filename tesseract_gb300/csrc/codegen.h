@@ -60,6 +60,9 @@ char *tc_codegen_enum(const TcGenEnum *g, size_t *len);
 char *tc_codegen_table(const Program *p, unsigned ticks, int block, size_t *len);
 
 /* CUDA C for the cube kernels of a program with id/link cells (cube.c). */
+/* A program's closing copies as the cube plans them (cube.c): 1 with the copy segment's first
+   instruction in *from and the second memory variant's cell map in slot1. */
+int   tc_cube_copy_plan(const Program *p, size_t *from, uint32_t *slot1);
 char *tc_codegen_cube(const Program *p, const size_t *seg_first, unsigned nseg, int block,
                       size_t *len);
 

@@ -21,7 +21,15 @@
    cell had when the segment started, which is what lockstep shows it.  Long segments are split
    into kernels of at most tc_cube_chunk instructions that hand their cells over through memory,
    so no single kernel is too large for the compiler.  When the whole pass is one kernel and no
-   read crosses warps (at most 1024 machines), the passes loop inside the kernel. */
+   read crosses warps (at most 1024 machines), the passes loop inside the kernel.
+
+   A pass that ends in a segment of plain copies A <- B (a Life board taking its next generation
+   from the cells it was computed into) runs without that segment: every kernel is compiled twice,
+   the second time with the memory of each A and its B exchanged, and the passes alternate between
+   the two.  After a pass without the copies A's value is in B's memory, which is where the other
+   variant reads A; B's own memory is free because every pass writes B before reading it.  The
+   last pass of a run includes the copy kernels (in its variant), so the state is as the program
+   leaves it whenever the host looks. */
 #include <pthread.h>
 #include <stdarg.h>
 #include <stdlib.h>
@@ -43,6 +51,8 @@ int tc_cube_groups = 32;
 int tc_cube_min_cells = 16;
 /* warps per block of a group-major kernel (0: never group-major) */
 int tc_cube_gm_warps = 4;
+/* 1: a pass's closing copies are left out of all but a run's last pass (two memory variants) */
+int tc_cube_copy_swap = 1;
 /* the most instructions in one kernel: longer segments are split.  Fewer, longer kernels win
    once they are split over warps (Life on 65,536 machines: 3 kernels of up to 125,722
    instructions run 36-38k generations/s, 13 kernels of 12,000 run 29k), at the price of a longer
@@ -56,7 +66,10 @@ struct CudaCube {
     size_t     *first;      /* kernel k runs instructions first[k] .. first[k + 1] - 1 */
     unsigned    nk, nseg, isa_seg;
     int         loop;       /* one kernel, passes loop inside it */
-    cudaKernel_t *fn;
+    unsigned    copy_k0;    /* kernels copy_k0.. are the pass's closing copies (nk: none) */
+    uint32_t   *slot1;      /* with copies: cell -> memory of the second variant (A <-> B) */
+    unsigned    variants;   /* 2 with copies, else 1 */
+    cudaKernel_t *fn;       /* variant v's kernel k at fn[v * nk + k] */
     unsigned    *warps;     /* warp groups of kernel k */
     int         *gmajor;    /* kernel k is group-major (one group per block) */
     cudaGraphExec_t graph;
@@ -106,6 +119,92 @@ static unsigned find_cuts(const Program *p, size_t *first, unsigned far_dim)
     free(stored);
     free(read);
     return n;
+}
+
+/* The closing copies of a pass, if the last segment (from `cut`, moved back over the NANDs that
+   compute RR for its first store) is only that: loads of plain cells (NAND ZERO, NAND B,
+   NAND ONE: RR = B) each stored into a cell A (A <- B), no B written and no A read in it, every B
+   copied to one A.  And for the memory exchange to be sound, before it: the pass starts by
+   setting RR (NAND ZERO), and every B is written before anything reads it, so what a pass finds
+   in B's memory (A's value of the pass before, in the other variant) is never seen.  On success *from is where the copies start
+   and slot1 the second variant's memory map (A and B exchanged, the rest in place). */
+static int copy_tail(const Program *p, size_t cut, uint32_t *slot1, size_t *from_out)
+{
+    size_t from = cut;
+    while (from > 0 && from <= p->len && p->code[from - 1].op == OP_NAND)
+        from--;
+    if (from == 0 || from >= p->len || p->code[0].op != OP_NAND)
+        return 0;
+    unsigned mask;
+    if (tc_program_resolve(p, p->code[0].addr, &mask) != CELL_ZERO)
+        return 0;
+    uint32_t n = p->ncells;
+    uint32_t *src = tc_xcalloc(n + 1, sizeof *src);     /* A -> B + 1 */
+    uint32_t *dst = tc_xcalloc(n + 1, sizeof *dst);     /* B -> A + 1 */
+    unsigned char *touch = tc_xcalloc(n + 1, 1);        /* 1 read, 2 written (in the tail) */
+    int ok = 1, copies = 0;
+    enum { RR_OTHER, RR_ONE, RR_CELL, RR_NOT_CELL } rr = RR_OTHER;
+    uint32_t rc = 0;
+    for (size_t i = from; i < p->len && ok; i++) {
+        Instr in = p->code[i];
+        if (in.op == OP_NAND) {
+            uint32_t c = tc_program_resolve(p, in.addr, &mask);
+            if (c == CELL_ZERO) {
+                rr = RR_ONE;
+            } else if (c == CELL_ONE) {
+                rr = rr == RR_CELL ? RR_NOT_CELL : rr == RR_NOT_CELL ? RR_CELL : RR_OTHER;
+            } else if (rr == RR_ONE && mask == 0 && !tc_program_readonly(p, c) &&
+                       !(p->special && p->special[c].kind != CK_PLAIN) && touch[c] != 2) {
+                rr = RR_NOT_CELL;
+                rc = c;
+                touch[c] = 1;
+            } else {
+                ok = 0;
+            }
+        } else if (!tc_program_readonly(p, in.addr)) {
+            uint32_t a = in.addr;
+            if (rr != RR_CELL || touch[a] || (p->special && p->special[a].kind != CK_PLAIN) ||
+                (dst[rc] && dst[rc] != a + 1)) {
+                ok = 0;
+            } else {
+                src[a] = rc + 1;
+                dst[rc] = a + 1;
+                touch[a] = 2;
+                copies++;
+            }
+        }
+    }
+    /* the rest of the pass: every B written before it is read */
+    unsigned char *first = tc_xcalloc(n + 1, 1);  /* 1 read first, 2 written first */
+    for (size_t i = 0; i < from && ok; i++) {
+        Instr in = p->code[i];
+        if (in.op == OP_NAND) {
+            uint32_t c = tc_program_resolve(p, in.addr, &mask);
+            if (!first[c])
+                first[c] = 1;
+        } else if (!tc_program_readonly(p, in.addr) && !first[in.addr]) {
+            first[in.addr] = 2;
+        }
+    }
+    for (uint32_t b = 0; b < n && ok; b++)
+        if (dst[b] && first[b] != 2)
+            ok = 0;
+    ok = ok && copies > 0;
+    *from_out = from;
+    if (ok) {
+        for (uint32_t c = 0; c < n; c++)
+            slot1[c] = c;
+        for (uint32_t a = 0; a < n; a++)
+            if (src[a]) {
+                slot1[a] = src[a] - 1;
+                slot1[src[a] - 1] = a;
+            }
+    }
+    free(src);
+    free(dst);
+    free(touch);
+    free(first);
+    return ok;
 }
 
 /* ---- code generation ------------------------------------------------------------------------ */
@@ -162,12 +261,18 @@ typedef struct {
     const Program *p;
     unsigned       W;
     unsigned char *loaded, *written;
+    const uint32_t *slot;  /* cell -> where its words are in memory (NULL: the cell itself) */
 } Chunk;
+
+static unsigned slot_of(const Chunk *k, uint32_t c)
+{
+    return (unsigned)(k->slot ? k->slot[c] : c);
+}
 
 static void use_cell(Src *o, Chunk *k, uint32_t c)
 {
     if (!k->loaded[c]) {
-        emit(o, "    u32 c%u = m[%uu * W];\n", (unsigned)c, (unsigned)c);
+        emit(o, "    u32 c%u = m[%uu * W];\n", (unsigned)c, slot_of(k, c));
         k->loaded[c] = 1;
     }
 }
@@ -199,7 +304,7 @@ static void operand(Src *o, Chunk *k, uint32_t a, char *expr, size_t len)
         use_cell(o, k, c);
         snprintf(v, sizeof v, "__shfl_xor_sync(TC_FULL, c%u, %uu)", (unsigned)c, hi);
     } else {
-        snprintf(v, sizeof v, "mem[%uu * W + (w ^ %uu)]", (unsigned)c, hi);
+        snprintf(v, sizeof v, "mem[%uu * W + (w ^ %uu)]", slot_of(k, c), hi);
     }
     if (lo)
         snprintf(expr, len, "tc_perm(%s, %uu)", v, lo);
@@ -337,7 +442,7 @@ static void chunk_net(Chunk *k, size_t from, size_t to, ChunkNet *cn)
                 char src[96];
                 int from_node = -1;
                 if (hi >= 32) {
-                    snprintf(src, sizeof src, "mem[%uu * W + (w ^ %uu)]", (unsigned)c, hi);
+                    snprintf(src, sizeof src, "mem[%uu * W + (w ^ %uu)]", slot_of(k, c), hi);
                 } else {
                     from_node = cur[c];
                     need[nneed++] = cur[c];  /* the source value must exist as a register */
@@ -453,7 +558,8 @@ static void emit_group(Src *o, Chunk *k, const ChunkNet *cn, const uint32_t *out
     char nm[32];
     for (int v = 2; v < n; v++)
         if (in_cone[v] && is_leaf(&cn->L, v) && cn->L.cell[v] >= 0)
-            emit(o, "        const u32 c%d = m[%du * W];\n", cn->L.cell[v], cn->L.cell[v]);
+            emit(o, "        const u32 c%d = m[%uu * W];\n", cn->L.cell[v],
+                 slot_of(k, (uint32_t)cn->L.cell[v]));
     for (int v = 2; v < n; v++)
         if (in_cone[v] && is_leaf(&cn->L, v) && cn->L.far[v])
             emit(o, "        const u32 n%d = %s;\n", v, cn->L.expr[v]);
@@ -473,7 +579,7 @@ static void emit_group(Src *o, Chunk *k, const ChunkNet *cn, const uint32_t *out
         }
         for (int c = store_at[v]; c >= 0; c = store_next[c]) {
             name_of(nm, sizeof nm, cn->cur[c]);
-            emit(o, "        if (t < W) m[%uu * W] = %s;\n", (unsigned)c, nm);
+            emit(o, "        if (t < W) m[%uu * W] = %s;\n", slot_of(k, (uint32_t)c), nm);
             k->written[c] = 2;
         }
     }
@@ -713,9 +819,9 @@ static unsigned gm_iters(unsigned W, unsigned iters)
 }
 
 static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size_t from, size_t to,
-                        int loop, int *group_major, unsigned iters)
+                        int loop, int *group_major, unsigned iters, const uint32_t *slot)
 {
-    Chunk k = {p, W, tc_xcalloc(p->ncells + 1, 1), tc_xcalloc(p->ncells + 1, 1)};
+    Chunk k = {p, W, tc_xcalloc(p->ncells + 1, 1), tc_xcalloc(p->ncells + 1, 1), slot};
     unsigned groups = chunk_groups(p, from, to, loop);
     int gm = 0;
     if (tc_cube_map && loop && groups > 1) {
@@ -797,7 +903,7 @@ static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size
     emit(o, "    if (t < W) {\n");
     for (uint32_t c = CELL_FIRST_FREE; c < p->ncells; c++)
         if (k.written[c] == 1)
-            emit(o, "        m[%uu * W] = c%u;\n", (unsigned)c, (unsigned)c);
+            emit(o, "        m[%uu * W] = c%u;\n", slot_of(&k, c), (unsigned)c);
     emit(o, "        rr[w] = r;\n    }\n}\n");
     free(k.loaded);
     free(k.written);
@@ -815,7 +921,7 @@ char *tc_codegen_cube(const Program *p, const size_t *first, unsigned nk, int bl
     emit(&o, "#define W %uu\n", W);
     emit(&o, "%s", CUBE_PRELUDE);
     for (unsigned k = 0; k < nk; k++)
-        emit_kernel(&o, p, W, k, first[k], first[k + 1], loop, NULL, 1);
+        emit_kernel(&o, p, W, k, first[k], first[k + 1], loop, NULL, 1, NULL);
     if (len)
         *len = o.len;
     return o.s;
@@ -827,7 +933,8 @@ typedef struct {
     CudaCube     *c;
     unsigned      k0, k1;  /* kernels of this module */
     unsigned      iters;   /* group-major runs per block */
-    cudaKernel_t *fn;      /* where the kernels go */
+    unsigned      variant; /* 1: the second variant's memory (A and B exchanged) */
+    cudaKernel_t *fn;      /* where the kernels go (variant v's kernel k at fn[v * nk + k]) */
     int          *gm;      /* where each kernel's group-major choice goes */
     int           ok;
     char          err[512];
@@ -846,12 +953,17 @@ static void *compile_job(void *arg)
     int loop = c->nk == 1 && c->dims <= FAR_DIM;
     Src o = {0};
     emit(&o, "// generated by the tesseract GB300 engine: cube of 2^%u machines, kernels %u..%u, "
-            "%u run(s) per group-major block\n", c->dims, j->k0, j->k1 - 1, j->iters);
+            "%u run(s) per group-major block, memory variant %u\n", c->dims, j->k0, j->k1 - 1,
+         j->iters, j->variant);
     emit(&o, "#define W %uu\n", c->W);
     emit(&o, "%s", CUBE_PRELUDE);
-    for (unsigned k = 0; k < nk; k++)
-        emit_kernel(&o, &c->p, c->W, j->k0 + k, first[k], first[k + 1], loop,
-                    &j->gm[j->k0 + k], j->iters);
+    for (unsigned k = 0; k < nk; k++) {
+        int gm;  /* the same in both variants: variant 0's job reports it */
+        emit_kernel(&o, &c->p, c->W, j->k0 + k, first[k], first[k + 1], loop, &gm, j->iters,
+                    j->variant ? c->slot1 : NULL);
+        if (!j->variant)
+            j->gm[j->k0 + k] = gm;
+    }
     len = o.len;
     char **names = tc_xmalloc(nk * sizeof *names);
     for (unsigned k = 0; k < nk; k++) {
@@ -865,7 +977,7 @@ static void *compile_job(void *arg)
         j->ok = tc_module(o.s, len, (const char *const *)names + k0, (int)n, NULL, &m, j->err,
                           sizeof j->err);
         for (unsigned k = 0; j->ok && k < n; k++)
-            j->fn[j->k0 + k0 + k] = m.fn[k];
+            j->fn[j->variant * c->nk + j->k0 + k0 + k] = m.fn[k];
     }
     for (unsigned k = 0; k < nk; k++)
         free(names[k]);
@@ -878,6 +990,21 @@ static void *compile_job(void *arg)
 /* ---- the cube -------------------------------------------------------------------------------- */
 
 unsigned cuda_cube_groups(const CudaCube *c) { return c->groups; }
+unsigned cuda_cube_closing_copies(const CudaCube *c) { return c->nk - c->copy_k0; }
+
+/* The plan cuda_cube_new makes for a program's closing copies: 1 with the first instruction of
+   the copy segment in *from and the second variant's memory map in slot1 (ncells entries). */
+int tc_cube_copy_plan(const Program *p, size_t *from, uint32_t *slot1)
+{
+    size_t *cuts = tc_xmalloc((p->len + 2) * sizeof *cuts);
+    unsigned n = find_cuts(p, cuts, FAR_DIM);
+    int ok = n >= 2 && tc_program_dims(p) > FAR_DIM && copy_tail(p, cuts[n - 1], slot1, from) &&
+             *from > cuts[n - 2];
+    if (!ok)
+        *from = p->len;
+    free(cuts);
+    return ok;
+}
 unsigned cuda_cube_segments(const CudaCube *c) { return c->isa_seg; }
 unsigned cuda_cube_kernels(const CudaCube *c) { return c->nk; }
 
@@ -891,6 +1018,7 @@ void cuda_cube_free(CudaCube *c)
     cudaFree(c->rr);
     free(c->first);
     free(c->fn);
+    free(c->slot1);
     free(c->warps);
     free(c->gmajor);
     tc_program_free(&c->p);
@@ -915,6 +1043,20 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
         c->isa_seg = find_cuts(p, isa, CUBE_DIMS);
         free(isa);
     }
+    /* closing copies: their segment starts where they do (cuts[nseg - 1] moves back over the
+       loads of the first copy) */
+    int copies = 0;
+    if (tc_cube_copy_swap && c->nseg >= 2 && c->dims > FAR_DIM) {
+        size_t from;
+        c->slot1 = tc_xmalloc((p->ncells + 1) * sizeof *c->slot1);
+        copies = copy_tail(p, cuts[c->nseg - 1], c->slot1, &from) && from > cuts[c->nseg - 2];
+        if (copies) {
+            cuts[c->nseg - 1] = from;
+        } else {
+            free(c->slot1);
+            c->slot1 = NULL;
+        }
+    }
     /* split long segments into kernels of at most tc_cube_chunk instructions */
     size_t chunk = tc_cube_chunk > 0 ? (size_t)tc_cube_chunk : 12000;
     c->first = tc_xmalloc((p->len / chunk + c->nseg + 2) * sizeof *c->first);
@@ -927,9 +1069,17 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
                 break;
         }
     c->first[c->nk] = p->len;
-    free(cuts);
     c->loop = c->nk == 1 && c->dims <= FAR_DIM;
-    c->fn = tc_xcalloc(c->nk, sizeof *c->fn);
+    c->copy_k0 = c->nk;
+    c->variants = 1;
+    if (copies) {
+        for (unsigned k = c->nk; k-- > 0;)
+            if (c->first[k] == cuts[c->nseg - 1])
+                c->copy_k0 = k;
+        c->variants = 2;
+    }
+    free(cuts);
+    c->fn = tc_xcalloc((size_t)c->nk * c->variants, sizeof *c->fn);
     c->warps = tc_xcalloc(c->nk, sizeof *c->warps);
     c->gmajor = tc_xcalloc(c->nk, sizeof *c->gmajor);
     for (unsigned k = 0; k < c->nk; k++)
@@ -944,15 +1094,16 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
                      "cudaMemset", err, errlen) ||
         !tc_cu_check(cudaMemset(c->rr, 0, (size_t)c->W * 4), "cudaMemset", err, errlen))
         goto fail;
-    /* compile: one module per kernel, all in parallel */
-    unsigned per = 1, nj = (c->nk + per - 1) / per;
+    /* compile: one module per kernel and memory variant, all in parallel */
+    unsigned nj = c->nk * c->variants;
     CompileJob *jobs = tc_xcalloc(nj, sizeof *jobs);
     pthread_t *tid = tc_xcalloc(nj, sizeof *tid);
     c->iters = 1;
     for (unsigned j = 0; j < nj; j++) {
         jobs[j].c = c;
-        jobs[j].k0 = j * per;
-        jobs[j].k1 = (j + 1) * per < c->nk ? (j + 1) * per : c->nk;
+        jobs[j].k0 = j % c->nk;
+        jobs[j].k1 = j % c->nk + 1;
+        jobs[j].variant = j / c->nk;
         jobs[j].iters = c->iters;
         jobs[j].fn = c->fn;
         jobs[j].gm = c->gmajor;
@@ -1040,12 +1191,15 @@ int cuda_cube_write_words(CudaCube *c, const uint32_t *mem, const uint32_t *rr, 
     return 1;
 }
 
-static int launch_pass(CudaCube *c, cudaStream_t s, unsigned passes)
+/* One pass (or `passes` for a looping cube) in memory variant `variant`; the closing copies only
+   with `copies`. */
+static int launch_pass(CudaCube *c, cudaStream_t s, unsigned passes, unsigned variant, int copies)
 {
     unsigned threads = c->W < 32 ? 32 : c->W;
     unsigned block = threads < TC_CUBE_BLOCK ? threads : TC_CUBE_BLOCK;
     unsigned grid = (threads + block - 1) / block;
-    for (unsigned k = 0; k < c->nk; k++) {
+    unsigned nk = copies ? c->nk : c->copy_k0;
+    for (unsigned k = 0; k < nk; k++) {
         uint32_t *mem = c->mem, *rr = c->rr;
         void *args[] = {&mem, &rr, &passes};
         dim3 b = dim3u(block), g = dim3u(grid);
@@ -1056,7 +1210,8 @@ static int launch_pass(CudaCube *c, cudaStream_t s, unsigned passes)
         } else {
             b.y = c->warps[k];
         }
-        if (cudaLaunchKernel((const void *)c->fn[k], g, b, args, 0, s) != cudaSuccess)
+        if (cudaLaunchKernel((const void *)c->fn[variant * c->nk + k], g, b, args, 0, s) !=
+            cudaSuccess)
             return 0;
     }
     return 1;
@@ -1070,14 +1225,18 @@ int cuda_cube_run(CudaCube *c, uint64_t passes, char *err, size_t errlen)
     if (c->loop) {
         while (passes) {
             unsigned n = passes > (1u << 30) ? 1u << 30 : (unsigned)passes;
-            if (!launch_pass(c, s, n))
+            if (!launch_pass(c, s, n, 0, 1))
                 return tc_cu_check(cudaGetLastError(), "cube launch", err, errlen);
             passes -= n;
         }
-    } else {
-        /* many passes of several kernels: replay a captured graph of up to 16 passes */
+    } else if (passes) {
+        /* many passes of several kernels: replay a captured graph of 16 passes.  With two memory
+           variants pass i runs in variant i % 2 without the closing copies, except the last,
+           which has them (and stays out of the graph) */
         const unsigned G = 16;
-        if (passes >= G && !c->graph) {
+        int swap = c->variants == 2;
+        uint64_t open = swap ? passes - 1 : passes, done = 0;
+        if (open >= G && !c->graph) {
             cudaGraph_t g;
             cudaStream_t cs;
             if (!tc_cu_check(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "stream", err,
@@ -1086,7 +1245,7 @@ int cuda_cube_run(CudaCube *c, uint64_t passes, char *err, size_t errlen)
             int ok = tc_cu_check(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal),
                                  "capture", err, errlen);
             for (unsigned i = 0; ok && i < G; i++)
-                ok = launch_pass(c, cs, 1);
+                ok = launch_pass(c, cs, 1, swap ? i % 2 : 0, !swap);
             cudaError_t e = cudaStreamEndCapture(cs, &g);
             if (ok)
                 ok = tc_cu_check(e, "capture", err, errlen);
@@ -1099,14 +1258,16 @@ int cuda_cube_run(CudaCube *c, uint64_t passes, char *err, size_t errlen)
                 return 0;
             c->graph_passes = G;
         }
-        while (c->graph && passes >= c->graph_passes) {
+        while (c->graph && open - done >= c->graph_passes) {
             if (!tc_cu_check(cudaGraphLaunch(c->graph, s), "graph launch", err, errlen))
                 return 0;
-            passes -= c->graph_passes;
+            done += c->graph_passes;
         }
-        for (; passes; passes--)
-            if (!launch_pass(c, s, 1))
+        for (; done < open; done++)
+            if (!launch_pass(c, s, 1, swap ? (unsigned)(done % 2) : 0, !swap))
                 return tc_cu_check(cudaGetLastError(), "cube launch", err, errlen);
+        if (swap && !launch_pass(c, s, 1, (unsigned)(done % 2), 1))
+            return tc_cu_check(cudaGetLastError(), "cube launch", err, errlen);
     }
     if (!tc_cu_check(cudaEventRecord(tc_engine.ev1, s), "event", err, errlen) ||
         !tc_cu_check(cudaEventSynchronize(tc_engine.ev1), "cube run", err, errlen))
@@ -1154,14 +1315,16 @@ int cuda_cube_tune(CudaCube *c, unsigned probe_passes, CudaCubeTune *t, char *er
         return 1;
     }
     cudaKernel_t *fns[4];
+    unsigned nkv = c->nk * c->variants;
     int *gms = tc_xcalloc(c->nk, sizeof *gms);
-    CompileJob *jobs = tc_xcalloc((size_t)n * c->nk, sizeof *jobs);
-    pthread_t *tid = tc_xcalloc((size_t)n * c->nk, sizeof *tid);
+    CompileJob *jobs = tc_xcalloc((size_t)n * nkv, sizeof *jobs);
+    pthread_t *tid = tc_xcalloc((size_t)n * nkv, sizeof *tid);
     unsigned nj = 0;
     for (int i = 0; i < n; i++) {
-        fns[i] = its[i] == c->iters ? c->fn : tc_xcalloc(c->nk, sizeof *fns[i]);
-        for (unsigned k = 0; its[i] != c->iters && k < c->nk; k++) {
-            jobs[nj] = (CompileJob){c, k, k + 1, its[i], fns[i], gms, 0, ""};
+        fns[i] = its[i] == c->iters ? c->fn : tc_xcalloc(nkv, sizeof *fns[i]);
+        for (unsigned kv = 0; its[i] != c->iters && kv < nkv; kv++) {
+            jobs[nj] = (CompileJob){c, kv % c->nk, kv % c->nk + 1, its[i], kv / c->nk, fns[i],
+                                    gms, 0, ""};
             if (pthread_create(&tid[nj], NULL, compile_job, &jobs[nj]) == 0)
                 nj++;
         }
@@ -1199,8 +1362,9 @@ int cuda_cube_tune(CudaCube *c, unsigned probe_passes, CudaCubeTune *t, char *er
                                              cudaMemcpyDeviceToDevice, s), "restore", err,
                              errlen) &&
                  tc_cu_check(cudaEventRecord(tc_engine.ev0, s), "event", err, errlen);
-            for (unsigned q = 0; ok && q < probe_passes; q++)
-                ok = launch_pass(c, s, 1) ||
+            for (unsigned q = 0; ok && q < probe_passes; q++)  /* as cuda_cube_run runs them */
+                ok = launch_pass(c, s, 1, c->variants == 2 ? q % 2 : 0,
+                                 c->variants == 1 || q + 1 == probe_passes) ||
                      tc_cu_check(cudaGetLastError(), "cube launch", err, errlen);
             ok = ok && tc_cu_check(cudaEventRecord(tc_engine.ev1, s), "event", err, errlen) &&
                  tc_cu_check(cudaEventSynchronize(tc_engine.ev1), "tune", err, errlen);

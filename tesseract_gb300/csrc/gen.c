@@ -657,22 +657,10 @@ static void add_into(Bld *b, const uint32_t *s, const uint32_t *a, int n, uint32
    bit 0 first): the hypercube prefix sum.  Each machine keeps t, the count of its subcube so
    far; across dimension d it reads the neighbour's t, adds it to t, and to p when bit d of the
    machine number is 1 (the neighbour holds the lower half). */
-void tc_gen_cube_rank(Program *p, int dims)
+static void prefix_count(Bld *b, uint32_t x, const uint32_t *pv, const uint32_t *tv, int dims)
 {
-    Bld *b = bnew();
     int n = dims + 1;
-    uint32_t x = bcell(b, "x"), carry = bcell(b, "cy");
-    uint32_t pv[CUBE_MAX_DIMS + 1], tv[CUBE_MAX_DIMS + 1], nb[CUBE_MAX_DIMS + 1],
-        ad[CUBE_MAX_DIMS + 1];
-    binput(b, x);
-    for (int i = 0; i < n; i++)
-        pv[i] = bcell(b, bname(b, "p%d", i));
-    for (int i = 0; i < n; i++)
-        tv[i] = bcell(b, bname(b, "t%d", i));
-    for (int i = 0; i < n; i++)
-        boutput(b, pv[i]);
-    for (int i = 0; i < n; i++)
-        boutput(b, tv[i]);
+    uint32_t carry = bcell(b, "cy"), nb[CUBE_MAX_DIMS + 1], ad[CUBE_MAX_DIMS + 1];
     for (int i = 0; i < n; i++) {
         nb[i] = bcell(b, bname(b, "n%d", i));
         ad[i] = bcell(b, bname(b, "m%d", i));
@@ -693,6 +681,90 @@ void tc_gen_cube_rank(Program *p, int dims)
             gate2(b, G_AND, ad[i], nb[i], id);
         add_into(b, pv, ad, n, carry);
         add_into(b, tv, nb, n, carry);
+    }
+}
+
+void tc_gen_cube_rank(Program *p, int dims)
+{
+    Bld *b = bnew();
+    int n = dims + 1;
+    uint32_t x = bcell(b, "x"), pv[CUBE_MAX_DIMS + 1], tv[CUBE_MAX_DIMS + 1];
+    binput(b, x);
+    for (int i = 0; i < n; i++)
+        pv[i] = bcell(b, bname(b, "p%d", i));
+    for (int i = 0; i < n; i++)
+        tv[i] = bcell(b, bname(b, "t%d", i));
+    for (int i = 0; i < n; i++)
+        boutput(b, pv[i]);
+    for (int i = 0; i < n; i++)
+        boutput(b, tv[i]);
+    prefix_count(b, x, pv, tv, dims);
+    bfinish(b, p);
+}
+
+/* x = sel ? y : x, one bit (x ^= (x ^ y) & sel); t is a scratch cell */
+static void take_if(Bld *b, uint32_t x, uint32_t y, uint32_t sel, uint32_t t)
+{
+    gate2(b, G_XOR, t, x, y);
+    gate2(b, G_AND, t, t, sel);
+    gate2(b, G_XOR, x, x, t);
+}
+
+/* The machines with h = 1 hand their bytes v0..v7 to the first machines, in machine order:
+   afterwards machine k holds h = 1 and the byte of the k-th such machine when k is below their
+   number, h = 0 otherwise.  A byte's destination is its machine's prefix count p.  Bytes move
+   across dimension 0, 1, .., dims - 1 in turn, crossing d when bit d of where they are differs
+   from bit d of p, and two never meet: after dimension d a byte sits at p's bits 0..d and its
+   start's bits above d; two starts that agree above bit d are less than 2^(d+1) apart, so are
+   their prefix counts, which then differ in bits 0..d. */
+void tc_gen_cube_pack(Program *p, int dims)
+{
+    Bld *b = bnew();
+    int n = dims + 1;
+    uint32_t v[8], nv[8], pv[CUBE_MAX_DIMS + 1], tv[CUBE_MAX_DIMS + 1], np[CUBE_MAX_DIMS + 1];
+    for (int i = 0; i < 8; i++)
+        v[i] = bcell(b, bname(b, "v%d", i));
+    uint32_t h = bcell(b, "h");
+    for (int i = 0; i < 8; i++)
+        binput(b, v[i]);
+    binput(b, h);
+    for (int i = 0; i < 8; i++)
+        boutput(b, v[i]);
+    boutput(b, h);
+    for (int i = 0; i < n; i++)
+        pv[i] = bcell(b, bname(b, "p%d", i));
+    for (int i = 0; i < n; i++)
+        tv[i] = bcell(b, bname(b, "t%d", i));
+    prefix_count(b, h, pv, tv, dims);
+    for (int i = 0; i < 8; i++)
+        nv[i] = bcell(b, bname(b, "u%d", i));
+    for (int i = 0; i < n; i++)
+        np[i] = bcell(b, bname(b, "q%d", i));
+    uint32_t go = bcell(b, "go"), ngo = bcell(b, "ngo"), stay = bcell(b, "stay"),
+             t = bcell(b, "tk");
+    for (int d = 0; d < dims; d++) {
+        /* this machine's byte leaves across d */
+        gate2(b, G_XOR, go, pv[d], bcell(b, bname(b, "ID%d", d)));
+        gate2(b, G_AND, go, go, h);
+        /* every read of the neighbour before anything it reads is changed */
+        gate1(b, G_BUF, ngo, blink(b, bname(b, "lg%d", d), go, d));
+        for (int i = 0; i < 8; i++) {
+            char ln[32];
+            snprintf(ln, sizeof ln, "lv%d_%d", i, d);
+            gate1(b, G_BUF, nv[i], blink(b, ln, v[i], d));
+        }
+        for (int j = d + 1; j < dims; j++) {
+            char ln[32];
+            snprintf(ln, sizeof ln, "lp%d_%d", j, d);
+            gate1(b, G_BUF, np[j], blink(b, ln, pv[j], d));
+        }
+        /* a byte that stays keeps its place; otherwise the neighbour's, if it crosses, arrives */
+        gate2(b, G_XOR, stay, h, go);  /* go implies h: h and not go */
+        for (int i = 0; i < 8; i++)
+            take_if(b, v[i], nv[i], ngo, t);
+        for (int j = d + 1; j < dims; j++)
+            take_if(b, pv[j], np[j], ngo, t);
+        gate2(b, G_OR, h, stay, ngo);
     }
     bfinish(b, p);
 }
@@ -798,31 +870,27 @@ void tc_gen_cube_anf(Program *p, int dims)
     bfinish(b, p);
 }
 
-/* w = the Walsh-Hadamard spectrum of f: w(k) = sum over j of (-1)^(f(j) + j.k), dims + 3 bits in
-   two's complement (bit 0 first).  Start from 1 - 2 f(k), then across each dimension the
-   machine below takes a + a', the one above a' - a (its value subtracted from the one below). */
-void tc_gen_cube_walsh(Program *p, int dims)
+/* The Walsh-Hadamard transform of the n-bit two's complement numbers w (bit 0 first, arithmetic
+   mod 2^n) over all dims dimensions: across each dimension the machine below takes a + a', the one
+   above a' - a (its own value subtracted from the one below).  Scratch and link cells are named
+   after `tag`. */
+static void spectrum(Bld *b, const uint32_t *w, int n, int dims, const char *tag)
 {
-    Bld *b = bnew();
-    int n = dims + 3;
-    uint32_t f = bcell(b, "f"), w[CUBE_MAX_DIMS + 3], o[CUBE_MAX_DIMS + 3], y[CUBE_MAX_DIMS + 3];
-    binput(b, f);
-    for (int i = 0; i < n; i++)
-        boutput(b, w[i] = bcell(b, bname(b, "w%d", i)));
+    uint32_t o[2 * CUBE_MAX_DIMS + 4], y[2 * CUBE_MAX_DIMS + 4];
+    char fo[16], fy[16], fl[16];
+    snprintf(fo, sizeof fo, "%so%%d", tag);
+    snprintf(fy, sizeof fy, "%sy%%d", tag);
+    snprintf(fl, sizeof fl, "l%s%%d_%%d", tag[0] ? tag : "w");
     for (int i = 0; i < n; i++) {
-        o[i] = bcell(b, bname(b, "o%d", i));
-        y[i] = bcell(b, bname(b, "y%d", i));
+        o[i] = bcell(b, bname(b, fo, i));
+        y[i] = bcell(b, bname(b, fy, i));
     }
-    /* 1 - 2f: f = 0 gives 1 (bit 0 set), f = 1 gives -1 (all bits set) */
-    gate1(b, G_BUF, w[0], CELL_ONE);
-    for (int i = 1; i < n; i++)
-        gate1(b, G_BUF, w[i], f);
     uint32_t carry = bcell(b, "cy");
     for (int d = 0; d < dims; d++) {
         uint32_t id = bcell(b, bname(b, "ID%d", d));
         for (int i = 0; i < n; i++) {
             char ln[32];
-            snprintf(ln, sizeof ln, "lw%d_%d", i, d);
+            snprintf(ln, sizeof ln, fl, i, d);
             gate1(b, G_BUF, o[i], blink(b, ln, w[i], d));
         }
         /* below (id 0): w + o; above (id 1): o - w = o + ~w + 1 */
@@ -832,6 +900,62 @@ void tc_gen_cube_walsh(Program *p, int dims)
         for (int i = 0; i < n; i++)
             full_add(b, w[i], carry, o[i], y[i], carry);
     }
+}
+
+/* w = the Walsh-Hadamard spectrum of f: w(k) = sum over j of (-1)^(f(j) + j.k), dims + 3 bits in
+   two's complement (bit 0 first), starting from 1 - 2 f(k). */
+void tc_gen_cube_walsh(Program *p, int dims)
+{
+    Bld *b = bnew();
+    int n = dims + 3;
+    uint32_t f = bcell(b, "f"), w[CUBE_MAX_DIMS + 3];
+    binput(b, f);
+    for (int i = 0; i < n; i++)
+        boutput(b, w[i] = bcell(b, bname(b, "w%d", i)));
+    /* 1 - 2f: f = 0 gives 1 (bit 0 set), f = 1 gives -1 (all bits set) */
+    gate1(b, G_BUF, w[0], CELL_ONE);
+    for (int i = 1; i < n; i++)
+        gate1(b, G_BUF, w[i], f);
+    spectrum(b, w, n, dims, "");
+    bfinish(b, p);
+}
+
+/* h(k) = how many j have f(j) = g(j ^ k) = 1, the XOR convolution of f and g, by spectra: the
+   transform of the convolution is the product of the transforms F and G, and transforming it
+   again gives 2^dims h.  The arithmetic is mod 2^(2 dims + 2), which holds 2^dims h <= 2^(2 dims)
+   exactly; h has dims + 1 bits. */
+void tc_gen_cube_xorconv(Program *p, int dims)
+{
+    Bld *b = bnew();
+    int n = 2 * dims + 2;
+    uint32_t f = bcell(b, "f"), g = bcell(b, "g"), fw[2 * CUBE_MAX_DIMS + 2],
+             gw[2 * CUBE_MAX_DIMS + 2], pw[2 * CUBE_MAX_DIMS + 2];
+    binput(b, f);
+    binput(b, g);
+    for (int i = 0; i <= dims; i++)
+        boutput(b, bcell(b, bname(b, "h%d", i)));
+    for (int i = 0; i < n; i++) {
+        gate1(b, G_BUF, fw[i] = bcell(b, bname(b, "F%d", i)), i == 0 ? f : CELL_ZERO);
+        gate1(b, G_BUF, gw[i] = bcell(b, bname(b, "G%d", i)), i == 0 ? g : CELL_ZERO);
+        pw[i] = bcell(b, bname(b, "P%d", i));
+    }
+    spectrum(b, fw, n, dims, "F");
+    spectrum(b, gw, n, dims, "G");
+    /* pw = fw gw mod 2^n: row j of the schoolbook product added into bits j.. */
+    uint32_t pp = bcell(b, "pp"), carry = bcell(b, "mc");
+    for (int k = 0; k < n; k++)
+        gate2(b, G_AND, pw[k], fw[k], gw[0]);
+    for (int j = 1; j < n; j++)
+        for (int k = j; k < n; k++) {
+            gate2(b, G_AND, pp, fw[k - j], gw[j]);
+            if (k == j)
+                half_add(b, pw[k], carry, pw[k], pp);
+            else
+                full_add(b, pw[k], carry, pw[k], pp, carry);
+        }
+    spectrum(b, pw, n, dims, "P");
+    for (int i = 0; i <= dims; i++)  /* divided by 2^dims */
+        gate1(b, G_BUF, bcell(b, bname(b, "h%d", i)), pw[dims + i]);
     bfinish(b, p);
 }
 

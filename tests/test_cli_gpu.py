@@ -43,7 +43,8 @@ def programs(tmp):
     return paths
 
 
-DEMOS = ("any", "rank", "max", "sort", "anf", "walsh", "ring", "polymul", "life")
+DEMOS = ("any", "rank", "max", "sort", "pack", "anf", "walsh", "xorconv", "ring", "polymul",
+         "life")
 WHAT = 5 + 1 + 44  # the demo and what one pass does; then instr, segs, check, timings
 
 

@@ -1,0 +1,124 @@
+"""A pass's closing copies (A <- B: a Life board taking its next generation from the cells it was
+computed into) are left out of every pass of a cube run but the last: the engine compiles its
+kernels twice, the second time with A's and B's memory exchanged, and alternates.  That is sound
+when the copies are plain (every B copied to one A, no B written and no A read among them), the
+pass begins by setting RR, and every B is written before it is read, so that what a pass finds in
+B's memory is never seen (tesseract_gb300/csrc/cube.c, copy_tail).
+
+No GPU: the plan the engine makes (tc_cube_copy_plan) is applied on the oracle's reference
+machine, where running a pass in the other memory variant is the same as exchanging A's and B's
+values before it, and the state after several passes must equal the plain run's, cell by cell and
+RR, in every machine.  Programs that break a condition get no plan."""
+import ctypes as C
+import random
+
+import pytest
+
+import oracle as O
+import tesseract_gb300 as T
+
+
+def plan(p):
+    L = T.lib()
+    L.tc_cube_copy_plan.restype = C.c_int
+    L.tc_cube_copy_plan.argtypes = [C.c_void_p, C.POINTER(C.c_size_t), C.POINTER(C.c_uint32)]
+    slot = (C.c_uint32 * (p.s.ncells + 1))()
+    start = C.c_size_t()
+    if not L.tc_cube_copy_plan(p.ptr, C.byref(start), slot):
+        return None
+    pairs = [(a, slot[a]) for a in range(p.s.ncells) if slot[a] > a]
+    return start.value, pairs
+
+
+def plain_cells(p):
+    """Cells a random state may fill: not ZERO/ONE, not id or link cells."""
+    out = []
+    for c in range(2, p.s.ncells):
+        if p.s.special and p.s.special[c].kind != 0:
+            continue
+        out.append(c)
+    return out
+
+
+def random_cube(p, machines, seed):
+    cube = O.RefCube(p, machines)
+    rnd = random.Random(seed)
+    for k in range(machines):
+        for c in plain_cells(p):
+            cube.set(k, c, rnd.randrange(2))
+        cube.set_rr(k, rnd.randrange(2))
+    return cube
+
+
+def state(cube, p, machines):
+    cells = plain_cells(p)
+    return [[cube.get(k, c) for c in cells] + [cube.rr(k)] for k in range(machines)]
+
+
+def run_exchanged(p, cube, machines, passes, start, pairs):
+    """Every pass but the last without its closing copies (their effect on A and RR undone), A's
+    and B's values exchanged after it, as the other memory variant sees them."""
+    for i in range(passes):
+        if i + 1 == passes:
+            cube.tick()
+            break
+        for _ in range(start):
+            cube.step()
+        keep = [([cube.get(k, a) for a, _ in pairs], cube.rr(k)) for k in range(machines)]
+        for _ in range(len(p) - start):
+            cube.step()
+        for k in range(machines):
+            vals, rr = keep[k]
+            cube.set_rr(k, rr)
+            for (a, b), v in zip(pairs, vals):
+                cube.set(k, a, v)                # the pass without its copies ...
+            for a, b in pairs:                   # ... and the other variant's view of it
+                va, vb = cube.get(k, a), cube.get(k, b)
+                cube.set(k, a, vb)
+                cube.set(k, b, va)
+
+
+@pytest.mark.parametrize("passes", [1, 2, 3, 4])
+def test_life_board_copies_exchanged_match_the_plain_run(passes):
+    p = T.Program.gen_life_cube(4, 4, 5, 6)  # 2,048 machines: far reads, three segments
+    machines = 1 << p.dims()
+    got = plan(p)
+    assert got is not None
+    start, pairs = got
+    assert len(pairs) == 16 and start < len(p)
+    plain = random_cube(p, machines, 7)
+    for _ in range(passes):
+        plain.tick()
+    other = random_cube(p, machines, 7)
+    run_exchanged(p, other, machines, passes, start, pairs)
+    assert state(other, p, machines) == state(plain, p, machines)
+
+
+def test_plan_of_the_full_life_board():
+    """gen_life_cube(32, 32, 8, 8): 1,024 board cells take their next generation in the last
+    segment (4,096 instructions)."""
+    p = T.Program.gen_life_cube(32, 32, 8, 8)
+    start, pairs = plan(p)
+    assert len(pairs) == 1024 and len(p) - start == 4096
+
+
+BASE = (".in x\n.out x\n.link lx = x @ 10\n"
+        "NAND ZERO\nNAND lx\nSTO y\n")          # y from x across dimension 10
+COPY = "NAND ZERO\nNAND y\nNAND ONE\nSTO x\n"  # x <- y after x was read far: a new segment
+
+
+def test_small_program_gets_a_plan():
+    p = T.Program.from_asm(BASE + COPY)
+    assert plan(p) is not None
+
+
+@pytest.mark.parametrize("text", [
+    ".in x\n.out x\n.link lx = x @ 10\nNAND ZERO\nNAND y\nSTO z\nNAND lx\nSTO y\n" + COPY,  # y read first
+    ".in x\n.out x\n.link lx = x @ 10\nNAND ONE\nNAND lx\nSTO y\n" + COPY,  # RR live at the start
+    BASE + "NAND ZERO\nNAND y\nSTO x\n",                                    # a NOT, not a copy
+    BASE + "NAND ZERO\nNAND y\nNAND ONE\nSTO x\nSTO w\n",                    # one B, two As
+    BASE + "NAND ZERO\nNAND y\nNAND ONE\nSTO x\nNAND ZERO\nNAND x\nNAND ONE\nSTO w\n",  # A read
+])
+def test_unsound_programs_get_no_plan(text):
+    p = T.Program.from_asm(text)
+    assert plan(p) is None

@@ -161,3 +161,41 @@ def test_life_dims16_tuned_1000_generations():
     packed = pack_rows(start)
     O.life_words(packed, 1000)
     assert (unpack_rows(packed) == L.board()).all()
+
+
+@pytest.mark.parametrize("dims,w", [(11, 4), (13, 8), (16, 32)])
+def test_life_closing_copies_in_two_memory_variants(dims, w):
+    """The board's closing copies run only in each run's last pass; the others alternate between
+    the kernels of two memory variants (A's and B's memory exchanged).  Runs of 1, 2, 3, 16, 17
+    and 33 generations, one after the other on the same cube (graph replays, single passes, even
+    and odd endings), against plain C Life after each."""
+    L = LifeCube(dims, w=w, h=w)
+    assert L.cube.closing_copies >= 1
+    L.seed(dims)
+    board = L.board()
+    for gens in (1, 2, 3, 16, 17, 33):
+        L.run(gens)
+        board = life_reference(board, gens)
+        assert (L.board() == board).all(), gens
+
+
+def test_closing_copies_off_gives_the_same_cube():
+    """With the exchange switched off (tc_cube_copy_swap = 0) every pass runs its copies: the same
+    boards, from one kernel set."""
+    import ctypes as C
+    flag = C.c_int.in_dll(T.lib(), "tc_cube_copy_swap")
+    flag.value = 0
+    try:
+        L = LifeCube(12, w=8, h=8)
+        assert L.cube.closing_copies == 0
+    finally:
+        flag.value = 1
+    L.seed(3)
+    start = L.board()
+    L.run(18)
+    M = LifeCube(12, w=8, h=8)
+    assert M.cube.closing_copies >= 1
+    M.seed(3)
+    M.run(18)
+    assert (L.board() == M.board()).all()
+    assert (M.board() == life_reference(start, 18)).all()

@@ -179,3 +179,54 @@ def test_polymul_ntt():
             want[(i + j) % n] = (want[(i + j) % n] + (t if i + j < n else q - t)) % q
     got = [sum(cube.get(k, cl) << i for i, cl in enumerate(c)) for k in range(n)]
     assert got == want
+
+
+@pytest.mark.parametrize("dims,seed,rate", [(9, 12, 0.1), (10, 13, 0.5), (9, 14, 0.0),
+                                            (9, 15, 1.0)])
+def test_pack(dims, seed, rate):
+    """The bytes of the machines with a hit end, in machine order, in the first machines, which
+    alone keep h = 1 (src/cubedemo.c:134-151); no hit and every machine a hit included."""
+    p = T.Program.gen_cube_demo("pack", dims)
+    rnd = random.Random(seed)
+    n = 1 << dims
+    vs = [rnd.randrange(256) for _ in range(n)]
+    hs = [int(rnd.random() < rate) for _ in range(n)]
+    v, h = cells(p, "v", 8), cell(p, "h")
+
+    def setup(c):
+        for k in range(n):
+            c.set(k, h, hs[k])
+            for b in range(8):
+                c.set(k, v[b], (vs[k] >> b) & 1)
+
+    cube = run(p, dims, setup)
+    hits = [x for x, hit in zip(vs, hs) if hit]
+    for k in range(n):
+        assert cube.get(k, h) == int(k < len(hits))
+        if k < len(hits):
+            assert sum(cube.get(k, v[b]) << b for b in range(8)) == hits[k]
+
+
+@pytest.mark.parametrize("dims,seed", [(9, 16), (10, 17)])
+def test_xorconv(dims, seed):
+    """h(k) = #j with f(j) = g(j ^ k) = 1 (src/cubedemo.c:231-251), against the sum itself."""
+    p = T.Program.gen_cube_demo("xorconv", dims)
+    rnd = random.Random(seed)
+    n = 1 << dims
+    fs = [rnd.randrange(2) for _ in range(n)]
+    gs = [int(rnd.random() < 0.7) for _ in range(n)]
+    f, g, h = cell(p, "f"), cell(p, "g"), cells(p, "h", dims + 1)
+    cube = run(p, dims, lambda c: [(c.set(k, f, fs[k]), c.set(k, g, gs[k])) for k in range(n)])
+    for k in range(n):
+        want = sum(fs[j] & gs[j ^ k] for j in range(n))
+        assert sum(cube.get(k, h[b]) << b for b in range(dims + 1)) == want
+
+
+def test_xorconv_largest_value():
+    """f = g = 1 everywhere: h = 2^dims in every machine, the top bit of the dims + 1."""
+    dims = 9
+    p = T.Program.gen_cube_demo("xorconv", dims)
+    f, g, h = cell(p, "f"), cell(p, "g"), cells(p, "h", dims + 1)
+    cube = run(p, dims, lambda c: [(c.set(k, f, 1), c.set(k, g, 1)) for k in range(1 << dims)])
+    assert all(sum(cube.get(k, h[b]) << b for b in range(dims + 1)) == 1 << dims
+               for k in range(1 << dims))

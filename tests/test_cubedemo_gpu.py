@@ -12,7 +12,8 @@ import tesseract_gb300 as T
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", ["any", "rank", "max", "sort", "anf", "walsh", "ring", "life"])
+@pytest.mark.parametrize("name", ["any", "rank", "max", "sort", "pack", "anf", "walsh", "xorconv",
+                                  "ring", "life"])
 @pytest.mark.parametrize("dims", [9, 11, 16])
 def test_demo_checks(name, dims):
     r = T.cube_demo(name, dims, checks=3, seconds=0.05)
@@ -54,7 +55,7 @@ def test_sort_through_the_cube_api(dims):
 
 @pytest.mark.parametrize("name,dims", [("any", 10), ("rank", 9), ("rank", 11), ("sort", 9),
                                        ("sort", 10), ("max", 11), ("anf", 12), ("walsh", 10),
-                                       ("ring", 11)])
+                                       ("ring", 11), ("pack", 10), ("xorconv", 9)])
 def test_check_demo_programs(name, dims):
     p = T.Program.gen_cube_demo(name, dims)
     r = T.check(p, seed=dims, ticks=2)
