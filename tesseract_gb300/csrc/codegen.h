@@ -63,6 +63,9 @@ char *tc_codegen_table(const Program *p, unsigned ticks, int block, size_t *len)
 /* A program's closing copies as the cube plans them (cube.c): 1 with the copy segment's first
    instruction in *from and the second memory variant's cell map in slot1. */
 int   tc_cube_copy_plan(const Program *p, size_t *from, uint32_t *slot1);
+/* The source of every kernel of a cube's pass in memory variant 0 or 1, as the cube compiles them
+   (NULL when the program has no variant 1); *nk gets the kernel count. */
+char *tc_cube_source(const Program *p, unsigned variant, unsigned *nk, size_t *len);
 char *tc_codegen_cube(const Program *p, const size_t *seg_first, unsigned nseg, int block,
                       size_t *len);
 

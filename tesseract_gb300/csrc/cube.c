@@ -17,8 +17,10 @@
      M bits 10..15 another warp: a load of that word from the cell's memory
    Warps do not run in lockstep, so the pass is cut into segments as src/jit.c:526-560 cuts it
    for groups: wherever a segment would both write a cell and read it across a dimension of 10 or
-   more.  Each segment is its own kernel launch; inside a segment every far read sees the value the
-   cell had when the segment started, which is what lockstep shows it.  Long segments are split
+   more, unless the value read can be computed again by the reading warp from cells the segment
+   does not write (then it is: a Life board's halo corners).  Each segment is its own kernel
+   launch; inside a segment every far load sees the value the cell had when the segment started,
+   which is what lockstep shows it.  Long segments are split
    into kernels of at most tc_cube_chunk instructions that hand their cells over through memory,
    so no single kernel is too large for the compiler.  When the whole pass is one kernel and no
    read crosses warps (at most 1024 machines), the passes loop inside the kernel.
@@ -53,6 +55,8 @@ int tc_cube_min_cells = 16;
 int tc_cube_gm_warps = 4;
 /* 1: a pass's closing copies are left out of all but a run's last pass (two memory variants) */
 int tc_cube_copy_swap = 1;
+/* 1: far reads of computed cells are recomputed where they can be, instead of cutting */
+int tc_cube_recompute = 1;
 /* the most instructions in one kernel: longer segments are split.  Fewer, longer kernels win
    once they are split over warps (Life on 65,536 machines: 3 kernels of up to 125,722
    instructions run 36-38k generations/s, 13 kernels of 12,000 run 29k), at the price of a longer
@@ -118,6 +122,199 @@ static unsigned find_cuts(const Program *p, size_t *first, unsigned far_dim)
     first[n] = p->len;
     free(stored);
     free(read);
+    return n;
+}
+
+/* Cuts with far reads of computed cells recomputed.  find_cuts ends a segment where a cell it has
+   written is read across a far dimension, because another warp's copy of that cell may not be
+   written yet.  But when the value read is a function of cells the segment never writes (and of
+   id cells and constants), the reading warp can compute it itself from the other machine's cells:
+   their memory holds the same values all through the segment.  So such a read does not cut; the
+   cells the recomputation reads count as read across a far dimension (a later write to one cuts).
+
+   The values of a segment form a DAG: start values of cells, id patterns, RR's start value,
+   NANDs, and reads of a value in another machine (a link: that node at machine ^ mask).  A far
+   read of a computed cell is recomputable when its node, evaluated at machine ^ mask, reaches
+   only start values of cells not written so far in the segment, ids and constants (not RR's
+   start value), in at most RECOMPUTE_LIMIT
+   (node, mask) visits.  flags[s] is set for segments that recompute; their code must be
+   generated as one kernel (the recomputation starts from the segment's start values). */
+enum { V_CONST, V_START, V_ID, V_RR0, V_NAND, V_LINK };
+#define RECOMPUTE_LIMIT 4096
+
+typedef struct {
+    uint8_t  *kind;
+    int32_t  *a, *b;      /* NAND: fanins; LINK: a = node, b = mask; START: a = cell; CONST: a */
+    size_t    n, cap;
+    /* the visit of one recomputability check */
+    uint64_t *seen;       /* (node, mask) pairs, open addressing; 0 = empty */
+    size_t    nseen, capseen;
+    uint32_t *reads;      /* cells whose start values the recomputation reads */
+    size_t    nreads, capreads;
+    const uint32_t *stored;  /* per cell: the last segment that wrote it */
+    uint32_t  seg;
+} Dag;
+
+static int32_t dag_add(Dag *g, uint8_t kind, int32_t a, int32_t b)
+{
+    if (g->n == g->cap) {
+        g->cap = g->cap ? 2 * g->cap : 4096;
+        g->kind = tc_xrealloc(g->kind, g->cap);
+        g->a = tc_xrealloc(g->a, g->cap * sizeof *g->a);
+        g->b = tc_xrealloc(g->b, g->cap * sizeof *g->b);
+    }
+    g->kind[g->n] = kind;
+    g->a[g->n] = a;
+    g->b[g->n] = b;
+    return (int32_t)g->n++;
+}
+
+/* 1: a new (node, mask) pair; 0: seen before; -1: over the limit */
+static int dag_visit(Dag *g, int32_t v, unsigned mask)
+{
+    uint64_t key = ((uint64_t)(uint32_t)v << 20 | mask) + 1;
+    if (g->nseen >= RECOMPUTE_LIMIT)
+        return -1;
+    if (2 * (g->nseen + 1) > g->capseen) {
+        size_t cap = g->capseen ? 2 * g->capseen : 1024;
+        uint64_t *t = tc_xcalloc(cap, sizeof *t);
+        for (size_t i = 0; i < g->capseen; i++)
+            if (g->seen[i]) {
+                size_t h = (size_t)(g->seen[i] * 0x9E3779B97F4A7C15ull) & (cap - 1);
+                while (t[h])
+                    h = (h + 1) & (cap - 1);
+                t[h] = g->seen[i];
+            }
+        free(g->seen);
+        g->seen = t;
+        g->capseen = cap;
+    }
+    size_t h = (size_t)(key * 0x9E3779B97F4A7C15ull) & (g->capseen - 1);
+    while (g->seen[h]) {
+        if (g->seen[h] == key)
+            return 0;
+        h = (h + 1) & (g->capseen - 1);
+    }
+    g->seen[h] = key;
+    g->nseen++;
+    return 1;
+}
+
+static int dag_recomputable(Dag *g, int32_t v, unsigned mask)
+{
+    int fresh = dag_visit(g, v, mask);
+    if (fresh <= 0)
+        return fresh == 0;
+    switch (g->kind[v]) {
+    case V_CONST:
+    case V_ID:
+        return 1;
+    case V_RR0:
+        return 0;
+    case V_START:
+        if (g->stored[g->a[v]] == g->seg)  /* written since: its memory has moved on */
+            return 0;
+        if (g->nreads == g->capreads) {
+            g->capreads = g->capreads ? 2 * g->capreads : 64;
+            g->reads = tc_xrealloc(g->reads, g->capreads * sizeof *g->reads);
+        }
+        g->reads[g->nreads++] = (uint32_t)g->a[v];
+        return 1;
+    case V_LINK:
+        return dag_recomputable(g, g->a[v], mask ^ (unsigned)g->b[v]);
+    default:
+        return dag_recomputable(g, g->a[v], mask) && dag_recomputable(g, g->b[v], mask);
+    }
+}
+
+static unsigned find_cuts_recompute(const Program *p, size_t *first, unsigned char *flags)
+{
+    uint32_t *stored = tc_xcalloc(p->ncells + 1, sizeof *stored);
+    uint32_t *read = tc_xcalloc(p->ncells + 1, sizeof *read);
+    int32_t *cur = tc_xmalloc((p->ncells + 1) * sizeof *cur);
+    uint32_t *cur_seg = tc_xcalloc(p->ncells + 1, sizeof *cur_seg);  /* cur[c] valid in seg */
+    Dag g = {0};
+    int32_t zero = dag_add(&g, V_CONST, 0, 0), one = dag_add(&g, V_CONST, 1, 0);
+    uint32_t seg = 1;
+    unsigned n = 0;
+    int32_t rr = dag_add(&g, V_RR0, 0, 0);
+    first[n] = 0;
+    flags[n++] = 0;
+#define CELL_NODE(c)                                                                               (cur_seg[c] == seg ? cur[c] : (cur_seg[c] = seg, cur[c] = dag_add(&g, V_START, (int32_t)(c), 0)))
+    for (size_t i = 0; i < p->len; i++) {
+        Instr in = p->code[i];
+        if (in.op == OP_NAND) {
+            unsigned mask;
+            uint32_t a = tc_program_resolve(p, in.addr, &mask);
+            int32_t v;
+            if (a == CELL_ZERO || a == CELL_ONE) {
+                v = a == CELL_ONE ? one : zero;
+            } else if (p->special && p->special[a].kind == CK_ID) {
+                v = dag_add(&g, V_ID, 0, 0);
+            } else if (mask >> FAR_DIM && stored[a] == seg) {
+                g.nseen = 0;
+                g.nreads = 0;
+                g.stored = stored;
+                g.seg = seg;
+                if (g.seen)
+                    memset(g.seen, 0, g.capseen * sizeof *g.seen);
+                if (dag_recomputable(&g, cur[a], mask)) {
+                    for (size_t k = 0; k < g.nreads; k++)
+                        read[g.reads[k]] = seg;
+                    flags[n - 1] = 1;
+                    v = dag_add(&g, V_LINK, cur[a], (int32_t)mask);
+                } else {  /* a new segment: the value is read from memory there */
+                    seg++;
+                    rr = dag_add(&g, V_RR0, 0, 0);
+                    first[n] = i;
+                    flags[n++] = 0;
+                    read[a] = seg;
+                    v = dag_add(&g, V_LINK, CELL_NODE(a), (int32_t)mask);
+                }
+            } else {
+                if (mask >> FAR_DIM && !tc_program_readonly(p, a))
+                    read[a] = seg;
+                int32_t src = CELL_NODE(a);
+                v = mask ? dag_add(&g, V_LINK, src, (int32_t)mask) : src;
+            }
+            /* NAND with 0 is 1 whatever RR was (the usual start of a gate) */
+            rr = v == zero || rr == zero ? one
+                 : v == one && rr == one ? zero
+                                         : dag_add(&g, V_NAND, rr, v);
+        } else if (!tc_program_readonly(p, in.addr)) {
+            if (read[in.addr] == seg) {
+                seg++;
+                rr = dag_add(&g, V_RR0, 0, 0);
+                first[n] = i;
+                flags[n++] = 0;
+            }
+            stored[in.addr] = seg;
+            cur_seg[in.addr] = seg;
+            cur[in.addr] = rr;
+        }
+    }
+#undef CELL_NODE
+    first[n] = p->len;
+    free(stored);
+    free(read);
+    free(cur);
+    free(cur_seg);
+    free(g.kind);
+    free(g.a);
+    free(g.b);
+    free(g.seen);
+    free(g.reads);
+    return n;
+}
+
+/* The segments the engine runs: with mapped kernels, far reads of computed cells are recomputed
+   where they can be (flags[s] set for those segments); else the plain rule. */
+static unsigned plan_cuts(const Program *p, size_t *cuts, unsigned char *flags)
+{
+    if (tc_cube_map && tc_cube_recompute)
+        return find_cuts_recompute(p, cuts, flags);
+    unsigned n = find_cuts(p, cuts, FAR_DIM);
+    memset(flags, 0, n);
     return n;
 }
 
@@ -262,6 +459,7 @@ typedef struct {
     unsigned       W;
     unsigned char *loaded, *written;
     const uint32_t *slot;  /* cell -> where its words are in memory (NULL: the cell itself) */
+    int            bad;    /* a far read of a computed cell that cannot be recomputed */
 } Chunk;
 
 static unsigned slot_of(const Chunk *k, uint32_t c)
@@ -342,6 +540,10 @@ typedef struct {
     int           *cell;  /* per node: the cell whose start value the leaf is, else -1 */
     int           *src;   /* per node: the node a near link read takes its value from, else -1 */
     unsigned char *far;   /* per node: a far load */
+    int           *fcell; /* per node: a far load's cell, else -1 */
+    int           *mask;  /* per node: a link read's mask (near or far) */
+    int           *idd;   /* per node: an id pattern's dimension, else -1 */
+    unsigned char *flip;  /* per node: an id pattern complemented */
     size_t         n, cap;
 } Leaves;
 
@@ -357,10 +559,15 @@ static int leaf(TcNet *net, Leaves *L, const char *expr)
         L->cell = tc_xrealloc(L->cell, cap * sizeof *L->cell);
         L->src = tc_xrealloc(L->src, cap * sizeof *L->src);
         L->far = tc_xrealloc(L->far, cap);
+        L->fcell = tc_xrealloc(L->fcell, cap * sizeof *L->fcell);
+        L->mask = tc_xrealloc(L->mask, cap * sizeof *L->mask);
+        L->idd = tc_xrealloc(L->idd, cap * sizeof *L->idd);
+        L->flip = tc_xrealloc(L->flip, cap);
         for (size_t i = L->cap; i < cap; i++) {
             L->expr[i] = NULL;
-            L->cell[i] = L->src[i] = -1;
-            L->far[i] = 0;
+            L->cell[i] = L->src[i] = L->fcell[i] = L->idd[i] = -1;
+            L->mask[i] = 0;
+            L->far[i] = L->flip[i] = 0;
         }
         L->cap = cap;
     }
@@ -393,6 +600,131 @@ typedef struct {
     unsigned char *mapped;       /* per node: a chosen LUT */
 } ChunkNet;
 
+/* A far read of a cell the kernel has computed, recomputed from the other machine's start values
+   (find_cuts_recompute allows it only where that works: start values of cells the segment does
+   not write, ids, constants).  rc_node(v, M) is node v evaluated at machine ^ M, built into the
+   network; memo holds the (node, mask) pairs done. */
+typedef struct {
+    Chunk    *k;
+    TcNet    *net;
+    Leaves   *L;
+    int      *cur, *start;
+    uint64_t *key;
+    int      *val;
+    size_t    n, cap;
+} Recompute;
+
+static int *rc_find(Recompute *r, uint64_t key, int add)
+{
+    if (add && 2 * (r->n + 1) > r->cap) {
+        size_t cap = r->cap ? 2 * r->cap : 1024;
+        uint64_t *k2 = tc_xcalloc(cap, sizeof *k2);
+        int *v2 = tc_xmalloc(cap * sizeof *v2);
+        for (size_t i = 0; i < r->cap; i++)
+            if (r->key[i]) {
+                size_t h = (size_t)(r->key[i] * 0x9E3779B97F4A7C15ull) & (cap - 1);
+                while (k2[h])
+                    h = (h + 1) & (cap - 1);
+                k2[h] = r->key[i];
+                v2[h] = r->val[i];
+            }
+        free(r->key);
+        free(r->val);
+        r->key = k2;
+        r->val = v2;
+        r->cap = cap;
+    }
+    if (!r->cap)
+        return NULL;
+    size_t h = (size_t)(key * 0x9E3779B97F4A7C15ull) & (r->cap - 1);
+    while (r->key[h]) {
+        if (r->key[h] == key)
+            return &r->val[h];
+        h = (h + 1) & (r->cap - 1);
+    }
+    if (!add)
+        return NULL;
+    r->key[h] = key;
+    r->n++;
+    return &r->val[h];
+}
+
+/* cell c's start value at machine ^ M */
+static int rc_start(Recompute *r, uint32_t c, unsigned M)
+{
+    Leaves *L = r->L;
+    char buf[160], src[96], nm[32];
+    if (r->start[c] < 0) {
+        snprintf(buf, sizeof buf, "c%u", (unsigned)c);
+        r->start[c] = leaf(r->net, L, buf);
+        L->cell[r->start[c]] = (int)c;
+        if (r->cur[c] < 0)
+            r->cur[c] = r->start[c];
+    }
+    int sl = r->start[c];
+    unsigned hi = M >> 5, lo = M & 31;
+    if (M == 0)
+        return sl;
+    int from = -1;
+    if (hi >= 32) {
+        snprintf(src, sizeof src, "mem[%uu * W + (w ^ %uu)]", slot_of(r->k, c), hi);
+    } else {
+        from = sl;
+        name_of(nm, sizeof nm, sl);
+        if (hi)
+            snprintf(src, sizeof src, "__shfl_xor_sync(TC_FULL, %s, %uu)", nm, hi);
+        else
+            snprintf(src, sizeof src, "%s", nm);
+    }
+    if (lo)
+        snprintf(buf, sizeof buf, "tc_perm(%s, %uu)", src, lo);
+    else
+        snprintf(buf, sizeof buf, "%s", src);
+    int v = leaf(r->net, L, buf);
+    L->src[v] = from;
+    L->far[v] = hi >= 32;
+    L->fcell[v] = hi >= 32 ? (int)c : -1;
+    L->mask[v] = (int)M;
+    return v;
+}
+
+static int rc_node(Recompute *r, int v, unsigned M)
+{
+    uint64_t key = ((uint64_t)(unsigned)v << 16 | M) + 1;
+    int *hit = rc_find(r, key, 0);
+    if (hit)
+        return *hit;
+    const TcNode nd = *tc_net_node(r->net, v);
+    Leaves *L = r->L;
+    int out = -1;
+    if (nd.kind == TN_CONST) {
+        out = v;
+    } else if (nd.kind == TN_NAND) {
+        int a = rc_node(r, nd.a, M), b = rc_node(r, nd.b, M);
+        out = a < 0 || b < 0 ? -1 : tc_net_nand(r->net, a, b);
+    } else if (nd.kind == TN_NOT) {
+        int a = rc_node(r, nd.a, M);
+        out = a < 0 ? -1 : tc_net_not(r->net, a);
+    } else if (L->cell[v] >= 0) {
+        out = rc_start(r, (uint32_t)L->cell[v], M);
+    } else if (L->idd[v] >= 0) {
+        unsigned d = (unsigned)L->idd[v], flip = L->flip[v] ^ ((M >> d) & 1);
+        Src t = {0};
+        id_word(&t, d, flip);
+        out = leaf(r->net, L, t.s);
+        L->idd[out] = (int)d;
+        L->flip[out] = (unsigned char)flip;
+        free(t.s);
+    } else if (L->far[v]) {
+        out = rc_start(r, (uint32_t)L->fcell[v], M ^ (unsigned)L->mask[v]);
+    } else if (L->src[v] >= 0) {
+        out = rc_node(r, L->src[v], M ^ (unsigned)L->mask[v]);
+    }
+    if (out >= 0)
+        *rc_find(r, key, 1) = out;
+    return out;
+}
+
 /* Builds and maps the network of instructions from .. to-1 (marks the cells written). */
 static void chunk_net(Chunk *k, size_t from, size_t to, ChunkNet *cn)
 {
@@ -409,6 +741,7 @@ static void chunk_net(Chunk *k, size_t from, size_t to, ChunkNet *cn)
     cur[CELL_ZERO] = 0;
     cur[CELL_ONE] = 1;
     int rr = leaf(net, L, "r");
+    Recompute rc = {k, net, L, cur, start, NULL, NULL, 0, 0};
     for (size_t i = from; i < to; i++) {
         Instr in = p->code[i];
         if (in.op != OP_NAND) {
@@ -428,7 +761,16 @@ static void chunk_net(Chunk *k, size_t from, size_t to, ChunkNet *cn)
             unsigned d = p->special[c].dim;
             id_word(&t, d, (mask >> d) & 1);
             v = leaf(net, L, t.s);
+            L->idd[v] = (int)d;
+            L->flip[v] = (unsigned char)((mask >> d) & 1);
             free(t.s);
+        } else if ((mask >> 5) >= 32 && k->written[c]) {
+            /* a far read of a value this kernel computed: computed again for the other machine */
+            v = rc_node(&rc, cur[c], mask);
+            if (v < 0) {  /* cannot happen after find_cuts_recompute: fail the compile */
+                k->bad = 1;
+                v = 0;
+            }
         } else {
             unsigned hi = mask >> 5, lo = mask & 31;
             if (hi < 32 && cur[c] < 0) {  /* first use: the value loaded at the chunk start */
@@ -460,10 +802,14 @@ static void chunk_net(Chunk *k, size_t from, size_t to, ChunkNet *cn)
                 v = leaf(net, L, buf);
                 L->src[v] = from_node;
                 L->far[v] = hi >= 32;
+                L->fcell[v] = hi >= 32 ? (int)c : -1;
+                L->mask[v] = (int)mask;
             }
         }
         rr = tc_net_nand(net, rr, v);
     }
+    free(rc.key);
+    free(rc.val);
     cn->rr = rr;
     for (uint32_t c = CELL_FIRST_FREE; c < p->ncells; c++)
         if (k->written[c])
@@ -486,6 +832,10 @@ static void chunk_net_free(ChunkNet *cn)
     free(cn->L.cell);
     free(cn->L.src);
     free(cn->L.far);
+    free(cn->L.fcell);
+    free(cn->L.mask);
+    free(cn->L.idd);
+    free(cn->L.flip);
     free(cn->order);
     free(cn->mapped);
     free(cn->cur);
@@ -821,7 +1171,7 @@ static unsigned gm_iters(unsigned W, unsigned iters)
 static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size_t from, size_t to,
                         int loop, int *group_major, unsigned iters, const uint32_t *slot)
 {
-    Chunk k = {p, W, tc_xcalloc(p->ncells + 1, 1), tc_xcalloc(p->ncells + 1, 1), slot};
+    Chunk k = {p, W, tc_xcalloc(p->ncells + 1, 1), tc_xcalloc(p->ncells + 1, 1), slot, 0};
     unsigned groups = chunk_groups(p, from, to, loop);
     int gm = 0;
     if (tc_cube_map && loop && groups > 1) {
@@ -839,6 +1189,8 @@ static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size
         emit(o, "%.*s", (int)body.len, body.s ? body.s : "");
         emit(o, "    __syncthreads();\n    }\n}\n");
         free(body.s);
+        if (k.bad)
+            emit(o, "#error \"a far read of a computed cell that cannot be recomputed\"\n");
         free(k.loaded);
         free(k.written);
         if (group_major)
@@ -869,6 +1221,8 @@ static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size
         emit(o, "    u32 r = rr[w];\n");
         emit(o, "%.*s    }\n}\n", (int)body.len, body.s ? body.s : "");
         free(body.s);
+        if (k.bad)
+            emit(o, "#error \"a far read of a computed cell that cannot be recomputed\"\n");
         free(k.loaded);
         free(k.written);
         if (group_major)
@@ -905,6 +1259,8 @@ static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size
         if (k.written[c] == 1)
             emit(o, "        m[%uu * W] = c%u;\n", slot_of(&k, c), (unsigned)c);
     emit(o, "        rr[w] = r;\n    }\n}\n");
+    if (k.bad)
+        emit(o, "#error \"a far read of a computed cell that cannot be recomputed\"\n");
     free(k.loaded);
     free(k.written);
 }
@@ -994,16 +1350,57 @@ unsigned cuda_cube_closing_copies(const CudaCube *c) { return c->nk - c->copy_k0
 
 /* The plan cuda_cube_new makes for a program's closing copies: 1 with the first instruction of
    the copy segment in *from and the second variant's memory map in slot1 (ncells entries). */
+static void plan_cube(CudaCube *c, const Program *p);
+
+/* A plan made on the host alone (no device memory, no kernels) */
+static void plan_free(CudaCube *c)
+{
+    free(c->first);
+    free(c->slot1);
+    free(c->warps);
+    free(c->gmajor);
+    tc_program_free(&c->p);
+    free(c);
+}
+
 int tc_cube_copy_plan(const Program *p, size_t *from, uint32_t *slot1)
 {
-    size_t *cuts = tc_xmalloc((p->len + 2) * sizeof *cuts);
-    unsigned n = find_cuts(p, cuts, FAR_DIM);
-    int ok = n >= 2 && tc_program_dims(p) > FAR_DIM && copy_tail(p, cuts[n - 1], slot1, from) &&
-             *from > cuts[n - 2];
-    if (!ok)
-        *from = p->len;
-    free(cuts);
+    CudaCube *c = tc_xcalloc(1, sizeof *c);
+    tc_program_copy(p, &c->p);
+    plan_cube(c, &c->p);
+    int ok = c->variants == 2;
+    *from = ok ? c->first[c->copy_k0] : p->len;
+    if (ok)
+        memcpy(slot1, c->slot1, p->ncells * sizeof *slot1);
+    plan_free(c);
     return ok;
+}
+
+/* The source of every kernel of the cube's pass in memory variant `variant` (0, or 1 for the
+   exchanged memory of a program with closing copies), as the cube compiles them, in one text;
+   *nk gets the kernel count.  NULL when there is no such variant.  For tests: the text compiles
+   for sm_103a. */
+char *tc_cube_source(const Program *p, unsigned variant, unsigned *nk, size_t *len)
+{
+    CudaCube *c = tc_xcalloc(1, sizeof *c);
+    tc_program_copy(p, &c->p);
+    plan_cube(c, &c->p);
+    char *out = NULL;
+    *nk = c->nk;
+    if (variant < c->variants) {
+        Src o = {0};
+        emit(&o, "#define W %uu\n", c->W);
+        emit(&o, "%s", CUBE_PRELUDE);
+        for (unsigned k = 0; k < c->nk; k++) {
+            int gm;
+            emit_kernel(&o, &c->p, c->W, k, c->first[k], c->first[k + 1], c->loop, &gm, 1,
+                        variant ? c->slot1 : NULL);
+        }
+        out = o.s;
+        *len = o.len;
+    }
+    plan_free(c);
+    return out;
 }
 unsigned cuda_cube_segments(const CudaCube *c) { return c->isa_seg; }
 unsigned cuda_cube_kernels(const CudaCube *c) { return c->nk; }
@@ -1025,19 +1422,17 @@ void cuda_cube_free(CudaCube *c)
     free(c);
 }
 
-int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
+/* The cube's plan: segments (far reads of computed cells recomputed where they can be), the
+   closing copies and their memory variant, kernels (long segments split), warp groups. */
+static void plan_cube(CudaCube *c, const Program *p)
 {
-    *out = NULL;
-    if (!cuda_engine_init(0, err, errlen))
-        return 0;
-    CudaCube *c = tc_xcalloc(1, sizeof *c);
-    tc_program_copy(p, &c->p);
     c->dims = tc_program_dims(p);
     c->machines = 1u << c->dims;
     c->groups = c->machines / 512;
     c->W = c->machines / 32;
     size_t *cuts = tc_xmalloc((p->len + 2) * sizeof *cuts);
-    c->nseg = find_cuts(p, cuts, FAR_DIM);
+    unsigned char *recomputes = tc_xmalloc(p->len + 2);
+    c->nseg = plan_cuts(p, cuts, recomputes);
     {
         size_t *isa = tc_xmalloc((p->len + 2) * sizeof *isa);
         c->isa_seg = find_cuts(p, isa, CUBE_DIMS);
@@ -1057,17 +1452,19 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
             c->slot1 = NULL;
         }
     }
-    /* split long segments into kernels of at most tc_cube_chunk instructions */
+    /* split long segments into kernels of at most tc_cube_chunk instructions (not those that
+       recompute: the recomputation starts from the segment's start values) */
     size_t chunk = tc_cube_chunk > 0 ? (size_t)tc_cube_chunk : 12000;
     c->first = tc_xmalloc((p->len / chunk + c->nseg + 2) * sizeof *c->first);
     c->nk = 0;
     for (unsigned s = 0; s < c->nseg; s++)
         for (size_t i = cuts[s]; i < cuts[s + 1] || (i == cuts[s] && cuts[s] == cuts[s + 1]);
-             i += chunk) {
+             i += recomputes[s] ? cuts[s + 1] - cuts[s] : chunk) {
             c->first[c->nk++] = i;
             if (cuts[s] == cuts[s + 1])
                 break;
         }
+    free(recomputes);
     c->first[c->nk] = p->len;
     c->loop = c->nk == 1 && c->dims <= FAR_DIM;
     c->copy_k0 = c->nk;
@@ -1079,11 +1476,21 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
         c->variants = 2;
     }
     free(cuts);
-    c->fn = tc_xcalloc((size_t)c->nk * c->variants, sizeof *c->fn);
     c->warps = tc_xcalloc(c->nk, sizeof *c->warps);
     c->gmajor = tc_xcalloc(c->nk, sizeof *c->gmajor);
     for (unsigned k = 0; k < c->nk; k++)
         c->warps[k] = chunk_groups(p, c->first[k], c->first[k + 1], c->loop);
+}
+
+int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
+{
+    *out = NULL;
+    if (!cuda_engine_init(0, err, errlen))
+        return 0;
+    CudaCube *c = tc_xcalloc(1, sizeof *c);
+    tc_program_copy(p, &c->p);
+    plan_cube(c, &c->p);
+    c->fn = tc_xcalloc((size_t)c->nk * c->variants, sizeof *c->fn);
     size_t words = (size_t)c->W * (p->ncells + 1);
     if (!tc_cu_check(cudaMalloc((void **)&c->mem, words * 4), "cudaMalloc", err, errlen) ||
         !tc_cu_check(cudaMalloc((void **)&c->rr, (size_t)c->W * 4), "cudaMalloc", err, errlen))

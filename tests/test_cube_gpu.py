@@ -9,31 +9,10 @@ import pytest
 
 import oracle as O
 import tesseract_gb300 as T
+from cube_cases import random_link_program
 from tesseract_gb300.life import LifeCube, pack_rows, unpack_rows
 
 pytestmark = pytest.mark.gpu
-
-
-def random_link_program(seed: int, dims: int, cells: int, links: int, length: int) -> str:
-    """A random program over plain, id and link cells reaching dimensions below `dims`
-    (the shape of tests/test_cube.c:198-241, from Python's own generator)."""
-    rnd = random.Random(seed)
-    names = ["c%d" % i for i in range(cells)]
-    lines = [".out " + " ".join(names[: min(cells, 16)])]
-    readable = list(names) + ["ZERO", "ONE"] + ["ID%d" % d for d in range(dims)]
-    for i in range(links):
-        src = rnd.choice(readable)
-        d = rnd.randrange(dims)
-        if i == 0:
-            d = dims - 1  # the cube spans exactly `dims` dimensions
-        lines.append(".link l%d = %s @ %d" % (i, src, d))
-        readable.append("l%d" % i)
-    for _ in range(length):
-        if rnd.random() < 0.6:
-            lines.append("NAND " + rnd.choice(readable))
-        else:
-            lines.append("STO " + rnd.choice(names))
-    return "\n".join(lines) + "\n"
 
 
 @pytest.mark.parametrize("seed", range(12))
@@ -199,3 +178,14 @@ def test_closing_copies_off_gives_the_same_cube():
     M.run(18)
     assert (L.board() == M.board()).all()
     assert (M.board() == life_reference(start, 18)).all()
+
+
+def test_check_programs_that_recompute_far_reads():
+    """Random programs whose plan recomputes far reads of computed cells (fewer kernels than
+    with the plain cut rule): every machine's full state against the reference machine after
+    every tick."""
+    from test_cube_plan import recomputing_programs
+    for seed, text in recomputing_programs(4, 13) + recomputing_programs(2, 12):
+        p = T.Program.from_asm(text)
+        r = T.check(p, seed=seed, ticks=3)
+        assert r["ok"], (seed, r)

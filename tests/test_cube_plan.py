@@ -1,5 +1,12 @@
-"""A pass's closing copies (A <- B: a Life board taking its next generation from the cells it was
-computed into) are left out of every pass of a cube run but the last: the engine compiles its
+"""The cube's plan, on the CPU.
+
+Far reads of computed cells: where the value read is a function of cells the segment never
+writes, the reading warp computes it again for the other machine instead of cutting the pass
+(tesseract_gb300/csrc/cube.c, find_cuts_recompute); the generated kernels of such plans compile
+for sm_103a (nvcc), and the GPU tests check them against the reference machine.
+
+Closing copies: a pass's closing copies (A <- B: a Life board taking its next generation from the
+cells it was computed into) are left out of every pass of a cube run but the last: the engine compiles its
 kernels twice, the second time with A's and B's memory exchanged, and alternates.  That is sound
 when the copies are plain (every B copied to one A, no B written and no A read among them), the
 pass begins by setting RR, and every B is written before it is read, so that what a pass finds in
@@ -10,12 +17,52 @@ machine, where running a pass in the other memory variant is the same as exchang
 values before it, and the state after several passes must equal the plain run's, cell by cell and
 RR, in every machine.  Programs that break a condition get no plan."""
 import ctypes as C
+import os
 import random
+import shutil
+import subprocess
+import tempfile
 
 import pytest
 
 import oracle as O
 import tesseract_gb300 as T
+from cube_cases import random_link_program
+
+NVCC = shutil.which("nvcc") or ("/usr/local/cuda/bin/nvcc"
+                                if os.path.exists("/usr/local/cuda/bin/nvcc") else None)
+
+
+def cube_source(p, variant=0, recompute=True):
+    """(kernels per pass, the source of the pass's kernels in memory variant `variant`)."""
+    L = T.lib()
+    L.tc_cube_source.restype = C.c_void_p
+    L.tc_cube_source.argtypes = [C.c_void_p, C.c_uint, C.POINTER(C.c_uint),
+                                 C.POINTER(C.c_size_t)]
+    flag = C.c_int.in_dll(L, "tc_cube_recompute")
+    old, flag.value = flag.value, int(recompute)
+    try:
+        nk, n = C.c_uint(), C.c_size_t()
+        ptr = L.tc_cube_source(p.ptr, variant, C.byref(nk), C.byref(n))
+    finally:
+        flag.value = old
+    if not ptr:
+        return nk.value, None
+    text = C.string_at(ptr, n.value).decode()
+    C.CDLL(None).free(C.c_void_p(ptr))
+    return nk.value, text
+
+
+def recomputing_programs(count, dims):
+    """Seeded random link programs whose plan recomputes at least one far read."""
+    out, seed = [], 0
+    while len(out) < count:
+        text = random_link_program(seed, dims, 24, 24, 400)
+        p = T.Program.from_asm(text)
+        if cube_source(p, recompute=True)[0] < cube_source(p, recompute=False)[0]:
+            out.append((seed, text))
+        seed += 1
+    return out
 
 
 def plan(p):
@@ -122,3 +169,36 @@ def test_small_program_gets_a_plan():
 def test_unsound_programs_get_no_plan(text):
     p = T.Program.from_asm(text)
     assert plan(p) is None
+
+
+def test_life_is_one_kernel_per_generation():
+    """gen_life_cube(32, 32, 8, 8): the west and east halo cells the north and south halos read
+    across far dimensions are recomputed, so the masks, the halos and the rule are one kernel;
+    the closing copies are the other (run only at the end of a run).  Without recomputation:
+    three."""
+    p = T.Program.gen_life_cube(32, 32, 8, 8)
+    assert cube_source(p, recompute=True)[0] == 2
+    assert cube_source(p, recompute=False)[0] == 3
+
+
+@pytest.mark.skipif(NVCC is None, reason="nvcc not installed")
+@pytest.mark.parametrize("which", ["life", "random"])
+def test_recomputing_kernels_compile(which):
+    if which == "life":
+        progs = [T.Program.gen_life_cube(4, 4, 5, 6)]
+    else:
+        progs = [T.Program.from_asm(t) for _, t in recomputing_programs(3, 13)]
+    d = tempfile.mkdtemp()
+    for i, p in enumerate(progs):
+        for variant in (0, 1):
+            nk, src = cube_source(p, variant)
+            if src is None:
+                continue
+            assert "#error" not in src
+            path = os.path.join(d, "cube%d_%d.cu" % (i, variant))
+            with open(path, "w") as f:
+                f.write(src)
+            r = subprocess.run([NVCC, "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17",
+                                "-Xptxas", "-O2", "-c", path, "-o", path + ".o"],
+                               capture_output=True, text=True, timeout=600)
+            assert r.returncode == 0, r.stderr[-2000:]
