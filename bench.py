@@ -316,6 +316,10 @@ def config_batch(njobs=4096):
                            "jobs_on_generated_kernels": st["compiled"],
                            "jobs_on_interpreter": st["interpreted"],
                            "compile_threads": st["compile_threads"],
+                           "planned_for_generated_kernels": st["planned"],
+                           "taken_back_by_interpreter": st["taken_back"],
+                           "compile_busy_s": st["compile_busy"],
+                           "module_load_s": st["compile_load"],
                            "interpreter_start_s": st["interpreter_start"],
                            "interpreter_end_s": st["interpreter_end"],
                            "compiled_end_s": st["compiled_end"],

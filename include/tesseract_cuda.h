@@ -240,12 +240,17 @@ int  cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, size_t errlen
 int  cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char *err,
                     size_t errlen);
 /* The last cuda_batch_run: jobs, how many ran as generated kernels and how many on the
-   interpreter, the compile threads it used, its wall time, and in seconds from its start when the
-   interpreter's first launch went out (after packing) and when the last interpreted and the last
-   compiled job finished. */
+   interpreter, the compile threads it used, how many jobs its plan sent to generated code and how
+   many of those the interpreter took back (still waiting for a compile thread when it ran out of
+   work), its wall time, in seconds from its start when the interpreter's first launch went out
+   (after packing) and when the last interpreted and the last compiled job finished, the compile
+   threads' busy seconds summed (code generation and NVRTC), the seconds the host loop spent
+   loading the compiled modules (a load waits for the device's running work), and when the host
+   loop had every result. */
 typedef struct {
-    int    jobs, compiled, interpreted, compile_threads;
-    double seconds, interpreter_start, interpreter_end, compiled_end;
+    int    jobs, compiled, interpreted, compile_threads, planned, taken_back;
+    double seconds, interpreter_start, interpreter_end, compiled_end, compile_busy, compile_load,
+        loop_end;
 } CudaBatchStats;
 int  cuda_batch_stats(CudaBatchStats *s);
 

@@ -449,9 +449,11 @@ def batch_run(jobs) -> list:
 
 class BatchStats(C.Structure):
     _fields_ = [("jobs", C.c_int), ("compiled", C.c_int), ("interpreted", C.c_int),
-                ("compile_threads", C.c_int), ("seconds", C.c_double),
-                ("interpreter_start", C.c_double), ("interpreter_end", C.c_double),
-                ("compiled_end", C.c_double)]
+                ("compile_threads", C.c_int), ("planned", C.c_int), ("taken_back", C.c_int),
+                ("seconds", C.c_double), ("interpreter_start", C.c_double),
+                ("interpreter_end", C.c_double), ("compiled_end", C.c_double),
+                ("compile_busy", C.c_double), ("compile_load", C.c_double),
+                ("loop_end", C.c_double)]
 
 
 def batch_stats() -> dict:

@@ -831,7 +831,9 @@ int    tc_serve_batch(const Enum *const *jobs, int njobs, const CudaServeOpts *o
                       const signed char *route, double *finish, EnumResult *results,
                       int *engine_used, char *err, size_t errlen);
 double tc_route_compile_s(const Enum *e, double instrs);
-extern double tc_serve_last_wave_at;
+extern double tc_serve_last_wave_at, tc_serve_last_compile_busy, tc_serve_last_compile_load,
+    tc_serve_last_loop_end;
+extern int    tc_serve_last_routed, tc_serve_last_taken_back;
 double tc_route_compiled_s(double work);
 
 /* The interpreter's rate on a batch with most of the GPU (1.39e14 NAND/STO lane-ops/s measured
@@ -841,6 +843,11 @@ double tc_route_compiled_s(double work);
 #define BATCH_SHARE 0.9
 
 static CudaBatchStats last_batch;
+
+/* compile threads of a batch (0: the host's cores less two) */
+int tc_batch_threads = 0;
+/* the share of the interpreter's time the plan fills with compiling (see plan()) */
+double tc_batch_plan_share = 0.5;
 
 typedef struct {
     double work, instrs, compile_s, gain;
@@ -868,8 +875,8 @@ static void plan(Planned *p, int n, int threads, signed char *route)
         /* half the interpreter's time: compiles start once its first wave is packed and run
            slower than modelled when every core compiles; jobs still queued when the
            interpreter runs out go back to it */
-        route[k] = saved > 0 &&
-                   (c == 0 || compile + c <= 0.5 * (interp - p[k].work / BATCH_RATE_INTERP));
+        route[k] = saved > 0 && (c == 0 || compile + c <= tc_batch_plan_share *
+                                                              (interp - p[k].work / BATCH_RATE_INTERP));
         if (route[k]) {
             compile += c;
             interp -= p[k].work / BATCH_RATE_INTERP;
@@ -887,7 +894,8 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
         return 0;
     double t0 = tc_now();
     long cores = sysconf(_SC_NPROCESSORS_ONLN);
-    int threads = cores > 3 ? (int)cores - 2 : 1;  /* the host loop and the driver keep a core */
+    int threads = tc_batch_threads > 0 ? tc_batch_threads
+                  : cores > 3 ? (int)cores - 2 : 1;  /* the host loop and the driver keep a core */
     Planned *p = tc_xmalloc((size_t)njobs * sizeof *p);
     for (int i = 0; i < njobs; i++) {
         const Enum *e = jobs[i];
@@ -895,7 +903,10 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
         p[i].instrs = (double)e->a->len + (e->mode == EN_EQUIV && e->b ? (double)e->b->len : 0);
         p[i].work = (e->a->ninputs < 64 ? (double)(1ull << e->a->ninputs) : 0) * e->ticks *
                     p[i].instrs;
-        p[i].compile_s = e->parts == 1 ? tc_route_compile_s(e, p[i].instrs) : 1e30;
+        /* a job whose GPU time saved would not pay for a launch stays on the interpreter
+           whatever the cache holds: no need to look (the look hashes both programs) */
+        int worth = p[i].work / BATCH_RATE_INTERP - tc_route_compiled_s(p[i].work) > 0;
+        p[i].compile_s = e->parts == 1 && worth ? tc_route_compile_s(e, p[i].instrs) : 1e30;
         p[i].gain = p[i].work / (p[i].compile_s > 0 ? p[i].compile_s : 1e-9);
     }
     qsort(p, (size_t)njobs, sizeof *p, by_gain);
@@ -933,6 +944,11 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
         last_batch.compile_threads = any ? threads : 0;
         last_batch.seconds = wall;
         last_batch.interpreter_start = tc_serve_last_wave_at;
+        last_batch.planned = tc_serve_last_routed;
+        last_batch.taken_back = tc_serve_last_taken_back;
+        last_batch.compile_busy = tc_serve_last_compile_busy;
+        last_batch.compile_load = tc_serve_last_compile_load;
+        last_batch.loop_end = tc_serve_last_loop_end;
         double last_interp = 0, last_compiled = 0;
         for (int k = 0; k < njobs; k++) {
             double *at = engine[k] ? &last_compiled : &last_interp;

@@ -154,75 +154,103 @@ static uint64_t text_hash(const char *s, size_t n)
     return h;
 }
 
-int tc_module(const char *src, size_t len, const char *const *kernels, int nkernels,
-              const char *extra_opt, TcModule *out, char *err, size_t errlen)
+/* Finds src in the module cache (1: *out filled). */
+static int cache_find(const char *src, size_t len, uint64_t h, TcModule *out)
 {
-    uint64_t h = text_hash(src, len);
+    int found = 0;
     pthread_mutex_lock(&engine_lock);
-    for (size_t i = 0; i < ncache; i++)
+    for (size_t i = 0; i < ncache && !found; i++)
         if (cache[i].info.hash == h && cache[i].len == len && !memcmp(cache[i].src, src, len)) {
             out->lib = cache[i].lib;
             out->info = cache[i].info;
             out->info.cached = 1;
-            pthread_mutex_unlock(&engine_lock);
-            goto functions;
+            found = 1;
         }
     pthread_mutex_unlock(&engine_lock);
+    return found;
+}
 
-    {
-        double t0 = tc_now();
-        nvrtcProgram prog;
-        nvrtcResult nr = nvrtcCreateProgram(&prog, src, "tesseract_gen.cu", 0, NULL, NULL);
-        if (nr != NVRTC_SUCCESS)
-            return tc_fail(err, errlen, "NVRTC: %s", nvrtcGetErrorString(nr));
-        char arch[64];
-        snprintf(arch, sizeof arch, "--gpu-architecture=sm_%d%da", tc_engine.cc_major,
-                 tc_engine.cc_minor);
-        const char *opts[8];
-        int nopt = 0;
-        opts[nopt++] = arch;
-        opts[nopt++] = "--std=c++17";
-        opts[nopt++] = "-lineinfo";
-        opts[nopt++] = "--ptxas-options=-v";
-        /* ptxas -O2 rather than its default -O3: measured on the GB300, the kernels run the
-           same (mul16's verify 7.89 ms either way in alternating runs, cube Life 71,900 gen/s
-           either way) and compiling takes ~35 % less (0.77 against 1.18 s for a
-           20,000-instruction program); -O1 compiles faster still but runs Life 11 % slower */
+void tc_built_free(TcBuilt *b)
+{
+    free(b->cubin);
+    memset(b, 0, sizeof *b);
+}
+
+/* NVRTC on src, with no CUDA call: b gets the cubin (or cached = 1 when the module cache holds
+   this source already). */
+int tc_module_build(const char *src, size_t len, const char *extra_opt, TcBuilt *b, char *err,
+                    size_t errlen)
+{
+    memset(b, 0, sizeof *b);
+    b->info.hash = text_hash(src, len);
+    TcModule m;
+    if (cache_find(src, len, b->info.hash, &m)) {
+        b->cached = 1;
+        return 1;
+    }
+    double t0 = tc_now();
+    nvrtcProgram prog;
+    nvrtcResult nr = nvrtcCreateProgram(&prog, src, "tesseract_gen.cu", 0, NULL, NULL);
+    if (nr != NVRTC_SUCCESS)
+        return tc_fail(err, errlen, "NVRTC: %s", nvrtcGetErrorString(nr));
+    char arch[64];
+    snprintf(arch, sizeof arch, "--gpu-architecture=sm_%d%da", tc_engine.cc_major,
+             tc_engine.cc_minor);
+    const char *opts[8];
+    int nopt = 0;
+    opts[nopt++] = arch;
+    opts[nopt++] = "--std=c++17";
+    opts[nopt++] = "-lineinfo";
+    opts[nopt++] = "--ptxas-options=-v";
+    /* ptxas -O2 rather than its default -O3: measured on the GB300, the kernels run the
+       same (mul16's verify 7.89 ms either way in alternating runs, cube Life 71,900 gen/s
+       either way) and compiling takes ~35 % less (0.77 against 1.18 s for a
+       20,000-instruction program); -O1 compiles faster still but runs Life 11 % slower */
+    if (!(extra_opt && strstr(extra_opt, "--ptxas-options=-O")))
         opts[nopt++] = "--ptxas-options=-O2";
-        if (extra_opt && *extra_opt)
-            opts[nopt++] = extra_opt;
-        nr = nvrtcCompileProgram(prog, nopt, opts);
-        size_t loglen = 0;
-        nvrtcGetProgramLogSize(prog, &loglen);
-        char *log = tc_xmalloc(loglen + 1);
-        log[0] = '\0';
-        if (loglen)
-            nvrtcGetProgramLog(prog, log);
-        if (nr != NVRTC_SUCCESS) {
-            tc_fail(err, errlen, "NVRTC compile failed: %s: %.400s", nvrtcGetErrorString(nr), log);
-            free(log);
-            nvrtcDestroyProgram(&prog);
-            return 0;
-        }
-        size_t cubin_len = 0;
-        nvrtcGetCUBINSize(prog, &cubin_len);
-        char *cubin = tc_xmalloc(cubin_len + 1);
-        nvrtcGetCUBIN(prog, cubin);
-        nvrtcDestroyProgram(&prog);
-        cudaLibrary_t lib;
-        cudaError_t rc = cudaLibraryLoadData(&lib, cubin, NULL, NULL, 0, NULL, NULL, 0);
-        free(cubin);
-        if (!tc_cu_check(rc, "cudaLibraryLoadData", err, errlen)) {
-            free(log);
-            return 0;
-        }
-        TcModInfo info;
-        memset(&info, 0, sizeof info);
-        info.hash = h;
-        info.compile_seconds = tc_now() - t0;
-        info.cubin_bytes = cubin_len;
-        snprintf(info.log, sizeof info.log, "%s", log);
+    if (extra_opt && *extra_opt)
+        opts[nopt++] = extra_opt;
+    nr = nvrtcCompileProgram(prog, nopt, opts);
+    size_t loglen = 0;
+    nvrtcGetProgramLogSize(prog, &loglen);
+    char *log = tc_xmalloc(loglen + 1);
+    log[0] = '\0';
+    if (loglen)
+        nvrtcGetProgramLog(prog, log);
+    if (nr != NVRTC_SUCCESS) {
+        tc_fail(err, errlen, "NVRTC compile failed: %s: %.400s", nvrtcGetErrorString(nr), log);
         free(log);
+        nvrtcDestroyProgram(&prog);
+        return 0;
+    }
+    nvrtcGetCUBINSize(prog, &b->cubin_len);
+    b->cubin = tc_xmalloc(b->cubin_len + 1);
+    nvrtcGetCUBIN(prog, b->cubin);
+    nvrtcDestroyProgram(&prog);
+    b->info.compile_seconds = tc_now() - t0;
+    b->info.cubin_bytes = b->cubin_len;
+    snprintf(b->info.log, sizeof b->info.log, "%s", log);
+    free(log);
+    return 1;
+}
+
+/* Loads a built module (into the module cache) and finds its kernels; frees b's cubin.  With lazy
+   loading the module reaches the device at the first query of a kernel, here.  Loading waits for
+   the device's running work (it synchronises the context). */
+int tc_module_load(const char *src, size_t len, TcBuilt *b, const char *const *kernels,
+                   int nkernels, TcModule *out, char *err, size_t errlen)
+{
+    double tf = tc_now();
+    if (!cache_find(src, len, b->info.hash, out)) {
+        if (b->cached)
+            return tc_fail(err, errlen, "module cache: a built module went missing");
+        cudaLibrary_t lib;
+        cudaError_t rc = cudaLibraryLoadData(&lib, b->cubin, NULL, NULL, 0, NULL, NULL, 0);
+        if (!tc_cu_check(rc, "cudaLibraryLoadData", err, errlen)) {
+            tc_built_free(b);
+            return 0;
+        }
+        TcModInfo info = b->info;
         pthread_mutex_lock(&engine_lock);
         if (ncache == capcache) {
             capcache = capcache ? 2 * capcache : 16;
@@ -239,7 +267,7 @@ int tc_module(const char *src, size_t len, const char *const *kernels, int nkern
         out->lib = lib;
         out->info = info;
     }
-functions:
+    tc_built_free(b);
     for (int k = 0; k < nkernels && k < TC_MAX_KERNELS; k++) {
         if (!tc_cu_check(cudaLibraryGetKernel(&out->fn[k], out->lib, kernels[k]),
                          "cudaLibraryGetKernel", err, errlen))
@@ -250,7 +278,18 @@ functions:
             out->info.local_bytes = (int)fa.localSizeBytes;
         }
     }
+    out->info.load_seconds = tc_now() - tf;
+    if (!out->info.cached)
+        out->info.compile_seconds += out->info.load_seconds;
     return 1;
+}
+
+int tc_module(const char *src, size_t len, const char *const *kernels, int nkernels,
+              const char *extra_opt, TcModule *out, char *err, size_t errlen)
+{
+    TcBuilt b;
+    return tc_module_build(src, len, extra_opt, &b, err, errlen) &&
+           tc_module_load(src, len, &b, kernels, nkernels, out, err, errlen);
 }
 
 /* ---- verify / equiv / search ---------------------------------------------------------------- */
@@ -434,9 +473,12 @@ static void mix_bytes(Key *k, const void *p, size_t n)
 
 static void mix_program(Key *k, const Program *p)
 {
+    /* an instruction as one word: two multiplies each (a batch keys thousands of programs) */
     for (size_t i = 0; i < p->len; i++) {
-        uint32_t w = p->code[i].addr << 1 | p->code[i].op;
-        mix_bytes(k, &w, 4);
+        uint64_t w = p->code[i].addr << 1 | p->code[i].op;
+        k->h1 = (k->h1 ^ w) * 0x100000001b3ull;
+        k->h2 = (k->h2 + w + 0x9E3779B97F4A7C15ull) * 0xff51afd7ed558ccdull;
+        k->h2 ^= k->h2 >> 29;
     }
     mix_bytes(k, &p->len, sizeof p->len);
     mix_bytes(k, &p->ncells, sizeof p->ncells);
@@ -566,10 +608,25 @@ static void remember_tuning(uint64_t k1, uint64_t k2, int block, int step_bits)
     pthread_mutex_unlock(&engine_lock);
 }
 
-/* The loaded kernel of an enumeration, only when an earlier cuda_enum_run of the same job compiled
-   and loaded it: no code generation, no compilation, no module load.  For cuda_enum_run_static,
-   whose callers cannot allocate. */
-int tc_enum_cached(const Enum *e, TcModule *m, char *err, size_t errlen)
+/* Kernels compiled for a quick start (the serving loop's and a batch's compiled jobs): ptxas
+   without optimisation.  Measured on GB300 over 90 batch and served jobs: NVRTC 0.053 s +
+   8.3 us per NAND/STO instruction against 0.054 s + 13.9 us at -O2 (0.06 against 0.17 s for the
+   heaviest batch jobs), the kernels running at about half the speed (1.7e15 against 3.5e15
+   lane-ops/s), which a job that replaces interpreter time barely notices.  The source records
+   the option, so the two builds are cached apart. */
+#define FAST_NVRTC_OPT "--ptxas-options=-O0"
+
+/* The quick-start build's key from the optimised build's */
+static void fast_key(uint64_t *k2)
+{
+    *k2 ^= 0x9E3779B97F4A7C15ull;
+}
+
+/* The loaded kernel of an enumeration, only when an earlier run of the same job compiled and
+   loaded it (the optimised build; with `fast`, the quick-start build too): no code generation, no
+   compilation, no module load.  For cuda_enum_run_static, whose callers cannot allocate, and the
+   serving loop's routing. */
+int tc_enum_cached(const Enum *e, int fast, TcModule *m, char *err, size_t errlen)
 {
     /* the maps in fixed buffers: this lookup allocates nothing */
     int in_map[EN_MAX_IN + 1], out_map[TC_CACHED_MAX_OUTPUTS + 1];
@@ -589,10 +646,13 @@ int tc_enum_cached(const Enum *e, TcModule *m, char *err, size_t errlen)
     apply_tuning(&pl.g);
     uint64_t k1, k2;
     enum_key(&pl.g, &k1, &k2);
-    if (!lookup_enum(k1, k2, m))
-        return tc_fail(err, errlen, "cuda_enum_run_static: this job's kernel is not loaded; run the "
-                       "same job once through cuda_enum_run first");
-    return 1;
+    if (lookup_enum(k1, k2, m))
+        return 1;
+    fast_key(&k2);
+    if (fast && lookup_enum(k1, k2, m))
+        return 1;
+    return tc_fail(err, errlen, "cuda_enum_run_static: this job's kernel is not loaded; run the "
+                   "same job once through cuda_enum_run first");
 }
 
 void tc_free(void *p)
@@ -605,30 +665,87 @@ void tc_free(void *p)
 /* Workspace of a launch: the hit counter, then 16 hits per warp, then a count per warp. */
 #define WS_LIST 256u
 
-/* The kernel for the plan in g: from the cache, else generated, compiled and cached. */
-static int enum_module(TcGenEnum *g, TcModule *m, char *err, size_t errlen)
+/* A generated kernel compiled but not yet loaded */
+struct TcEnumPending {
+    char     *src;
+    size_t    len;
+    TcBuilt   b;
+    TcGenWork work;
+    uint64_t  k1, k2;
+    int       block;
+};
+
+/* The kernel for the plan in g: from the cache (m filled, *pend NULL), else generated and
+   compiled (*pend: the build, for enum_module_load); `fast` compiles it for a quick start
+   (FAST_NVRTC_OPT), unless the optimised build is cached. */
+static int enum_module_build(TcGenEnum *g, int fast, TcModule *m, TcEnumPending **pend, char *err,
+                             size_t errlen)
 {
-    static const char *const names[] = {"tc_enum"};
+    *pend = NULL;
     uint64_t k1, k2;
     enum_key(g, &k1, &k2);
     if (lookup_enum(k1, k2, m))
         return 1;
-    size_t len;
-    TcGenWork work;
-    g->work = &work;
-    char *src = tc_codegen_enum(g, &len);
+    if (fast)
+        fast_key(&k2);
+    if (fast && lookup_enum(k1, k2, m))
+        return 1;
+    TcEnumPending *p = tc_xcalloc(1, sizeof *p);
+    g->work = &p->work;
+    p->src = tc_codegen_enum(g, &p->len);
     g->work = NULL;
-    int ok = tc_module(src, len, names, 1, NULL, m, err, errlen);
-    free(src);
-    if (!ok)
+    if (fast) {
+        static const char mark[] = "// built with " FAST_NVRTC_OPT "\n";
+        char *s2 = tc_xmalloc(p->len + sizeof mark);
+        memcpy(s2, mark, sizeof mark - 1);
+        memcpy(s2 + sizeof mark - 1, p->src, p->len + 1);
+        free(p->src);
+        p->src = s2;
+        p->len += sizeof mark - 1;
+    }
+    p->k1 = k1;
+    p->k2 = k2;
+    p->block = g->block;
+    if (!tc_module_build(p->src, p->len, fast ? FAST_NVRTC_OPT : NULL, &p->b, err, errlen)) {
+        free(p->src);
+        free(p);
         return 0;
-    m->info.luts_per_step = work.luts_per_step;
-    m->info.luts_per_stretch = work.luts_per_stretch;
-    m->info.stretch_steps = work.stretch_steps;
-    m->info.compare_ops = work.compare_ops;
-    m->info.block = g->block;
-    remember_enum(k1, k2, m);
+    }
+    *pend = p;
     return 1;
+}
+
+static void enum_pending_free(TcEnumPending *p)
+{
+    if (!p)
+        return;
+    tc_built_free(&p->b);
+    free(p->src);
+    free(p);
+}
+
+/* Loads a built kernel (waits for the device's running work) and caches it; frees p. */
+static int enum_module_load(TcEnumPending *p, TcModule *m, char *err, size_t errlen)
+{
+    static const char *const names[] = {"tc_enum"};
+    int ok = tc_module_load(p->src, p->len, &p->b, names, 1, m, err, errlen);
+    if (ok) {
+        m->info.luts_per_step = p->work.luts_per_step;
+        m->info.luts_per_stretch = p->work.luts_per_stretch;
+        m->info.stretch_steps = p->work.stretch_steps;
+        m->info.compare_ops = p->work.compare_ops;
+        m->info.block = p->block;
+        remember_enum(p->k1, p->k2, m);
+    }
+    enum_pending_free(p);
+    return ok;
+}
+
+static int enum_module(TcGenEnum *g, int fast, TcModule *m, char *err, size_t errlen)
+{
+    TcEnumPending *p;
+    return enum_module_build(g, fast, m, &p, err, errlen) &&
+           (!p || enum_module_load(p, m, err, errlen));
 }
 
 /* The launch shape of job e on module m: as many blocks as are resident on the device at once
@@ -670,7 +787,7 @@ static int enum_shape(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
     return 1;
 }
 
-int tc_enum_job_prepare(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
+int tc_enum_job_build(const Enum *e, TcEnumJob *j, int fast, char *err, size_t errlen)
 {
     memset(j, 0, sizeof *j);
     EnumPlan pl;
@@ -679,10 +796,38 @@ int tc_enum_job_prepare(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
     int ok = cuda_engine_init(0, err, errlen);
     if (ok) {
         apply_tuning(&pl.g);
-        ok = enum_module(&pl.g, &j->m, err, errlen) && enum_shape(e, j, err, errlen);
+        ok = enum_module_build(&pl.g, fast, &j->m, &j->pending, err, errlen);
     }
     plan_free(&pl);
     return ok;
+}
+
+int tc_enum_job_load(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
+{
+    if (j->pending) {
+        TcEnumPending *p = j->pending;
+        j->pending = NULL;
+        if (!enum_module_load(p, &j->m, err, errlen))
+            return 0;
+    }
+    return enum_shape(e, j, err, errlen);
+}
+
+void tc_enum_job_drop(TcEnumJob *j)
+{
+    enum_pending_free(j->pending);
+    j->pending = NULL;
+}
+
+int tc_enum_job_prepare(const Enum *e, TcEnumJob *j, int fast, char *err, size_t errlen)
+{
+    if (!tc_enum_job_build(e, j, fast, err, errlen))
+        return 0;
+    if (!tc_enum_job_load(e, j, err, errlen)) {
+        tc_enum_job_drop(j);
+        return 0;
+    }
+    return 1;
 }
 
 size_t tc_enum_job_ws_bytes(const TcEnumJob *j)
@@ -802,7 +947,7 @@ int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
 {
     memset(r, 0, sizeof *r);
     TcEnumJob j;
-    return tc_enum_job_prepare(e, &j, err, errlen) && run_prepared(&j, r, err, errlen);
+    return tc_enum_job_prepare(e, &j, 0, err, errlen) && run_prepared(&j, r, err, errlen);
 }
 
 /* ---- the autotuner --------------------------------------------------------------------------- */
@@ -819,7 +964,7 @@ static void *compile_candidate(void *arg)
 {
     Candidate *c = arg;
     memset(&c->j, 0, sizeof c->j);
-    c->ok = enum_module(&c->g, &c->j.m, c->err, sizeof c->err) &&
+    c->ok = enum_module(&c->g, 0, &c->j.m, c->err, sizeof c->err) &&
             enum_shape(c->e, &c->j, c->err, sizeof c->err);
     return NULL;
 }

@@ -21,7 +21,8 @@ typedef struct {
 
 typedef struct {
     uint64_t hash;
-    double   compile_seconds;
+    double   compile_seconds;  /* NVRTC and the module load */
+    double   load_seconds;     /* the module load alone */
     size_t   cubin_bytes;
     int      regs, local_bytes, cached;
     /* generated enumeration kernels: the code generator's count of their work per word
@@ -36,6 +37,14 @@ typedef struct {
     cudaKernel_t  fn[TC_MAX_KERNELS];
     TcModInfo     info;
 } TcModule;
+
+/* A module compiled but not loaded (tc_module_build: NVRTC only, no CUDA call) */
+typedef struct {
+    char     *cubin;
+    size_t    cubin_len;
+    int       cached;  /* the module cache holds it already: nothing was compiled */
+    TcModInfo info;
+} TcBuilt;
 
 typedef struct {
     int          ready;
@@ -68,12 +77,18 @@ int    tc_cu_check(cudaError_t rc, const char *what, char *err, size_t errlen);
 int    tc_scratch(TcBuf *b, size_t bytes, char *err, size_t errlen);
 int    tc_module(const char *src, size_t len, const char *const *kernels, int nkernels,
                  const char *extra_opt, TcModule *out, char *err, size_t errlen);
+/* tc_module in two steps: NVRTC (safe from any host thread, no CUDA call), then the load */
+int    tc_module_build(const char *src, size_t len, const char *extra_opt, TcBuilt *b, char *err,
+                       size_t errlen);
+int    tc_module_load(const char *src, size_t len, TcBuilt *b, const char *const *kernels,
+                      int nkernels, TcModule *out, char *err, size_t errlen);
+void   tc_built_free(TcBuilt *b);
 int    tc_enum_prepare(const Enum *e, int *in_map, int *out_map, char *err, size_t errlen);
-/* The loaded kernel of a job that an earlier enumeration compiled, else an error; allocates
-   nothing (its maps are fixed buffers, so programs of more than TC_CACHED_MAX_OUTPUTS outputs
-   are refused). */
+/* The loaded kernel of a job that an earlier enumeration compiled (with `fast`, its quick-start
+   build counts too), else an error; allocates nothing (its maps are fixed buffers, so programs of
+   more than TC_CACHED_MAX_OUTPUTS outputs are refused). */
 #define TC_CACHED_MAX_OUTPUTS 4096
-int    tc_enum_cached(const Enum *e, TcModule *m, char *err, size_t errlen);
+int    tc_enum_cached(const Enum *e, int fast, TcModule *m, char *err, size_t errlen);
 
 /* One enumeration on the generated-kernel engine in steps, for callers that overlap many
    (serving): prepare (refusals, code generation, NVRTC and module load through the cache, the
@@ -81,13 +96,22 @@ int    tc_enum_cached(const Enum *e, TcModule *m, char *err, size_t errlen);
    a caller's device workspace of tc_enum_job_ws_bytes (at most tc_enum_job_ws_max) with the
    workspace copied behind it into the caller's pinned host memory, and the result from that copy
    once the stream has passed it. */
+typedef struct TcEnumPending TcEnumPending;
 typedef struct {
     TcModule   m;
     uint64_t   words, space, per_warp, blocks, warps;
     uint32_t   parts, part, nsel;
-    EnumResult base;  /* space, tried, ops */
+    EnumResult base;     /* space, tried, ops */
+    TcEnumPending *pending;  /* built by tc_enum_job_build, not yet loaded */
 } TcEnumJob;
-int    tc_enum_job_prepare(const Enum *e, TcEnumJob *j, char *err, size_t errlen);
+/* fast: compiled for a quick start (ptxas without optimisation) unless the optimised kernel is
+   cached already.  prepare = build (code generation and NVRTC: no CUDA call) + load (the module
+   load, which waits for the device's running work, and the launch shape); drop frees a build
+   that will not be loaded. */
+int    tc_enum_job_prepare(const Enum *e, TcEnumJob *j, int fast, char *err, size_t errlen);
+int    tc_enum_job_build(const Enum *e, TcEnumJob *j, int fast, char *err, size_t errlen);
+int    tc_enum_job_load(const Enum *e, TcEnumJob *j, char *err, size_t errlen);
+void   tc_enum_job_drop(TcEnumJob *j);
 size_t tc_enum_job_ws_bytes(const TcEnumJob *j);
 size_t tc_enum_job_ws_max(void);
 int    tc_enum_job_launch(const TcEnumJob *j, void *dev_ws, void *host_ws, cudaStream_t st,

@@ -40,11 +40,22 @@ void   tc_wave_free(TcWave *w);
    cost per NAND/STO instruction.  The interpreter reaches ~1.4e14 on the 4,096-job batch alone;
    in the served mix, in waves beside compiled jobs, half of 9e13 routes better (Poisson 2,000
    jobs/s, widths to 34: 114.9 against 111.5 jobs/s, p50 0.31 against 1.49 s, p99 2.47 against
-   2.73 s; widths to 22 unchanged). */
+   2.73 s; widths to 22 unchanged).  A served stream keeps the GPU busy, so its compiled jobs get
+   the optimised build; NVRTC alone takes 0.054 s + 13.9 us per NAND/STO instruction on one host
+   thread and the code runs at 3.5e15 (median, fitted over 90 batch and served jobs), but in the
+   serving loop a compile thread also waits for its module load (a load synchronises the
+   context, so it waits for the waves in flight), and the figures below, which include that
+   wait, route better (widths to 34: 121 against 114 jobs/s).  A batch waits on its compiles,
+   so its compiled jobs get the quick-start build (ptxas without optimisation): 0.053 s + 8.3 us
+   per instruction, running at 1.7e15, and their loads wait until the interpreter has every
+   job. */
 #define RATE_INTERP 4.5e13
 #define RATE_COMPILED 2.0e15
 #define COMPILE_S0 0.1
-#define COMPILE_S_PER_INSTR 4.0e-5  /* ptxas -O2: 0.15 s at 5,000 instructions, 0.77 s at 20,000 */
+#define COMPILE_S_PER_INSTR 4.0e-5
+#define RATE_COMPILED_FAST 1.7e15
+#define COMPILE_S0_FAST 0.053
+#define COMPILE_S_PER_INSTR_FAST 8.3e-6
 /* A job whose kernel is already compiled (the cache is keyed by what the code generator reads)
    costs only its launch and the polling of its event: about this many seconds. */
 #define LAUNCH_S 3.0e-5
@@ -67,6 +78,8 @@ typedef struct {
     int                *ready, rhead, rtail;
     int                 stop, failed;
     char                err[512];
+    int                 defer;            /* build only: the host loop loads (a batch) */
+    double              busy;             /* host seconds spent building or preparing */
 } Compiler;
 
 static void *compile_worker(void *arg)
@@ -83,8 +96,12 @@ static void *compile_worker(void *arg)
         int id = c->queue[c->qhead++];
         pthread_mutex_unlock(&c->mu);
         char e2[512];
-        int ok = tc_enum_job_prepare(c->jobs[id], &c->prep[id], e2, sizeof e2);
+        double t0 = tc_now();
+        int ok = c->defer ? tc_enum_job_build(c->jobs[id], &c->prep[id], 1, e2, sizeof e2)
+                          : tc_enum_job_prepare(c->jobs[id], &c->prep[id], 0, e2, sizeof e2);
+        double dt = tc_now() - t0;
         pthread_mutex_lock(&c->mu);
+        c->busy += dt;
         if (ok) {
             c->ready[c->rtail++] = id;
         } else if (!c->failed) {
@@ -126,24 +143,26 @@ static int route_compiled(const Enum *e, const CudaServeOpts *o, int threads, do
     double saved = work / rate_interp - work / RATE_COMPILED;
     TcModule m;
     char why[8];
-    if (tc_enum_cached(e, &m, why, sizeof why))
+    if (tc_enum_cached(e, 0, &m, why, sizeof why))
         return saved > LAUNCH_S;
     return saved > (COMPILE_S0 + COMPILE_S_PER_INSTR * instrs) / threads;
 }
 
-/* The routing model's figures for a batch planner: seconds to compile a job of `instrs`
-   NAND/STO instructions (0 when its kernel is cached), the GPU seconds of `work` lane-ops on
-   generated code, and a launch's cost. */
+/* The routing model's figures for a batch planner (quick-start builds): seconds to compile a job
+   of `instrs` NAND/STO instructions (0 when its kernel is cached), the GPU seconds of `work`
+   lane-ops on generated code, and a launch's cost. */
 double tc_route_compile_s(const Enum *e, double instrs)
 {
     TcModule m;
     char why[8];
-    return tc_enum_cached(e, &m, why, sizeof why) ? 0.0 : COMPILE_S0 + COMPILE_S_PER_INSTR * instrs;
+    return tc_enum_cached(e, 1, &m, why, sizeof why)
+               ? 0.0
+               : COMPILE_S0_FAST + COMPILE_S_PER_INSTR_FAST * instrs;
 }
 
 double tc_route_compiled_s(double work)
 {
-    return work / RATE_COMPILED + LAUNCH_S;
+    return work / RATE_COMPILED_FAST + LAUNCH_S;
 }
 
 static void nap(void)
@@ -162,6 +181,10 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
 
 /* when the last call's first interpreter wave went out, in seconds from its start (-1: none) */
 double tc_serve_last_wave_at = -1;
+/* the last run's jobs routed to generated code on arrival, those a batch's interpreter took
+   back from the compile queue, and the compile threads' busy seconds */
+int    tc_serve_last_routed, tc_serve_last_taken_back;
+double tc_serve_last_compile_busy, tc_serve_last_compile_load, tc_serve_last_loop_end;
 
 int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
                    const CudaServeOpts *opts, double *start, double *finish, EnumResult *results,
@@ -251,6 +274,11 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
     pthread_mutex_init(&cc.mu, NULL);
     pthread_cond_init(&cc.cv, NULL);
     cc.jobs = jobs;
+    /* a batch's compile threads only build, for a quick start: loading a module waits for the
+       device's running work (it synchronises the context), which would hold each compile thread
+       for most of an interpreter wave; the host loop loads the builds once the interpreter has
+       everything */
+    cc.defer = route != NULL;
     cc.prep = tc_xcalloc((size_t)njobs, sizeof *cc.prep);
     cc.queue = tc_xmalloc((size_t)njobs * sizeof *cc.queue);
     cc.ready = tc_xmalloc((size_t)njobs * sizeof *cc.ready);
@@ -273,7 +301,8 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
     TcWave *pending = NULL;  /* a wave prepared but not yet admitted */
     int pending_n = 0;
     size_t pending_need = 0;
-    double t0 = tc_now(), wave_launched_at = -1;
+    double t0 = tc_now(), wave_launched_at = -1, load_s = 0;
+    int routed = 0, taken_back = 0, loads_open = !cc.defer;
     while (ok && finished < njobs) {
         double now = tc_now() - t0;
         int progress = 0;
@@ -283,6 +312,7 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
                                  : route_compiled(jobs[next], &o, nthreads, rate_interp);
             if (engine_used)
                 engine_used[next] = compiled;
+            routed += compiled;
             if (compiled && held) {
                 held_ids[nheld++] = next;
             } else if (compiled) {
@@ -307,17 +337,24 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
                 pthread_mutex_unlock(&cc.mu);
                 break;
             }
-            for (int s = 0; s < nsl && cc.rhead < cc.rtail; s++) {
+            if (!loads_open && !held && next == njobs && rhead == nready && !pending)
+                loads_open = 1;  /* a batch's interpreter has every job it will get */
+            for (int s = 0; loads_open && s < nsl && cc.rhead < cc.rtail; s++) {
                 if (slot[s].id >= 0)
                     continue;
                 int id = cc.ready[cc.rhead++];
-                if (!tc_enum_job_launch(&cc.prep[id], slot[s].dev, slot[s].host, slot[s].st,
-                                        err, errlen) ||
-                    !tc_cu_check(cudaEventRecord(slot[s].done, slot[s].st), "event", err,
-                                 errlen)) {
-                    ok = 0;
+                pthread_mutex_unlock(&cc.mu);  /* the compile threads go on while this loads */
+                double tl = tc_now();
+                ok = tc_enum_job_load(jobs[id], &cc.prep[id], err, errlen);
+                load_s += tc_now() - tl;
+                if (ok)
+                    ok = tc_enum_job_launch(&cc.prep[id], slot[s].dev, slot[s].host, slot[s].st,
+                                            err, errlen) &&
+                         tc_cu_check(cudaEventRecord(slot[s].done, slot[s].st), "event", err,
+                                     errlen);
+                pthread_mutex_lock(&cc.mu);
+                if (!ok)
                     break;
-                }
                 slot[s].id = id;
                 start[id] = tc_now() - t0;
                 progress = 1;
@@ -359,6 +396,7 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
                 ready[nready++] = id;
                 if (engine_used)
                     engine_used[id] = 0;
+                taken_back++;
             }
             pthread_mutex_unlock(&cc.mu);
         }
@@ -440,6 +478,7 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
         if (!progress)
             nap();
     }
+    double loop_end = tc_now() - t0;
     pthread_mutex_lock(&cc.mu);
     cc.stop = 1;
     cc.qhead = cc.qtail;  /* nothing more to compile */
@@ -447,6 +486,8 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
     pthread_mutex_unlock(&cc.mu);
     for (int i = 0; i < nthreads; i++)
         pthread_join(tid[i], NULL);
+    for (int i = cc.rhead; i < cc.rtail; i++)  /* builds never loaded (after an error) */
+        tc_enum_job_drop(&cc.prep[cc.ready[i]]);
     tc_wave_free(pending);
     for (int i = 0; i < nst; i++) {
         if (busy[i]) {
@@ -477,5 +518,10 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
     free(wj);
     free(held_ids);
     tc_serve_last_wave_at = wave_launched_at;
+    tc_serve_last_routed = routed;
+    tc_serve_last_taken_back = taken_back;
+    tc_serve_last_compile_busy = cc.busy;
+    tc_serve_last_compile_load = load_s;
+    tc_serve_last_loop_end = loop_end;
     return ok;
 }
