@@ -517,13 +517,86 @@ done:
 
 /* ---- waves: a set of jobs packed, launched on a stream, finished job by job ----------------- */
 
+/* Mapped host buffers for waves, kept for reuse.  cudaFreeHost waits until every kernel on the
+   device has finished (measured on GB300: 305 ms while a 305 ms kernel ran on another stream,
+   where cudaHostAlloc took 1 ms), so freeing a finished wave's buffer would hold the serving loop
+   until the other waves in flight are done, and no new wave would start meanwhile.  A finished
+   wave's buffer goes back to the pool instead; tc_wave_pool_trim frees the pool once the device
+   is idle. */
+#define HOST_POOL 32
+static struct {
+    void  *p;
+    size_t bytes;
+    int    busy;
+} host_pool[HOST_POOL];
+static pthread_mutex_t host_pool_lock = PTHREAD_MUTEX_INITIALIZER;
+
+/* A mapped buffer of at least `bytes`; *pooled = 0 when the pool is full (freed directly) */
+static int host_get(void **p, size_t bytes, int *pooled, char *err, size_t errlen)
+{
+    pthread_mutex_lock(&host_pool_lock);
+    int best = -1;
+    for (int i = 0; i < HOST_POOL; i++)
+        if (host_pool[i].p && !host_pool[i].busy && host_pool[i].bytes >= bytes &&
+            (best < 0 || host_pool[i].bytes < host_pool[best].bytes))
+            best = i;
+    if (best >= 0) {
+        host_pool[best].busy = 1;
+        *p = host_pool[best].p;
+        *pooled = 1;
+        pthread_mutex_unlock(&host_pool_lock);
+        return 1;
+    }
+    int empty = -1;
+    for (int i = 0; i < HOST_POOL && empty < 0; i++)
+        if (!host_pool[i].p)
+            empty = i;
+    size_t cap = bytes + bytes / 4 + ((size_t)1 << 20);  /* room for a somewhat larger wave */
+    int ok = tc_cu_check(cudaHostAlloc(p, cap, cudaHostAllocMapped), "cudaHostAlloc", err, errlen);
+    *pooled = ok && empty >= 0;
+    if (*pooled) {
+        host_pool[empty].p = *p;
+        host_pool[empty].bytes = cap;
+        host_pool[empty].busy = 1;
+    }
+    pthread_mutex_unlock(&host_pool_lock);
+    return ok;
+}
+
+static void host_put(void *p, int pooled)
+{
+    if (!pooled) {
+        cudaFreeHost(p);
+        return;
+    }
+    pthread_mutex_lock(&host_pool_lock);
+    for (int i = 0; i < HOST_POOL; i++)
+        if (host_pool[i].p == p)
+            host_pool[i].busy = 0;
+    pthread_mutex_unlock(&host_pool_lock);
+}
+
+/* Frees the pool's idle buffers (each cudaFreeHost waits for the device to be idle). */
+void tc_wave_pool_trim(void)
+{
+    pthread_mutex_lock(&host_pool_lock);
+    for (int i = 0; i < HOST_POOL; i++)
+        if (host_pool[i].p && !host_pool[i].busy) {
+            cudaFreeHost(host_pool[i].p);
+            host_pool[i].p = NULL;
+            host_pool[i].bytes = 0;
+        }
+    pthread_mutex_unlock(&host_pool_lock);
+}
+
 struct TcWave {
     int                 njobs;
     const Enum        **jobs;       /* the wave's own copy: a caller may reuse its array */
     Pack                pk;
     uint32_t           *unit_job;
     void               *dev;        /* one device allocation for everything */
-    void               *host;       /* one mapped host allocation: unit lists, results, flags */
+    void               *host;       /* one mapped host buffer: unit lists, results, flags */
+    int                 host_pooled;
     unsigned long long *h_uhits, *h_hits;
     uint32_t           *h_ucount;
     volatile uint32_t  *h_done;
@@ -666,8 +739,7 @@ int tc_wave_launch(TcWave *w, cudaStream_t stream, double share, char *err, size
     }
     w->stream = stream;
     if (!tc_cu_check(cudaMallocAsync(&w->dev, at, stream), "cudaMallocAsync", err, errlen) ||
-        !tc_cu_check(cudaHostAlloc(&w->host, hat, cudaHostAllocMapped), "cudaHostAlloc", err,
-                     errlen))
+        !host_get(&w->host, hat, &w->host_pooled, err, errlen))
         return 0;
     memset(w->host, 0, hat);
     char *h = w->host;
@@ -797,7 +869,7 @@ void tc_wave_free(TcWave *w)
     if (w->host) {
         if (w->launched)
             cudaEventSynchronize(w->ev1);
-        cudaFreeHost(w->host);
+        host_put(w->host, w->host_pooled);
     }
     if (w->ev0)
         cudaEventDestroy(w->ev0);

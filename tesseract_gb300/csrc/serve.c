@@ -30,6 +30,7 @@ int    tc_wave_finished(const TcWave *w);
 void   tc_wave_result(const TcWave *w, int i, EnumResult *r);
 size_t tc_wave_bytes(const TcWave *w);
 void   tc_wave_free(TcWave *w);
+void   tc_wave_pool_trim(void);
 
 #define MAX_STREAMS 8
 #define MAX_COMPILED 8       /* compiled jobs on the device at once, one stream each */
@@ -497,6 +498,7 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
         cudaStreamSynchronize(st[i]);
         cudaStreamDestroy(st[i]);
     }
+    tc_wave_pool_trim();  /* every wave is done: the device is idle */
     for (int i = 0; i < MAX_COMPILED; i++) {
         if (slot[i].st) {
             cudaStreamSynchronize(slot[i].st);
