@@ -250,7 +250,7 @@ def config_life(gens=1000):
     setup_s = time.perf_counter() - t0
     L.seed(42)
     t0 = time.perf_counter()
-    tune = L.cube.tune(32)  # runs of words per group-major block, measured on this board
+    tune = L.cube.tune(32)  # warps and word runs per group-major block, measured on this board
     tune["seconds"] = time.perf_counter() - t0
     start = L.board()
     L.run(16)                       # warm-up: graph capture, first launches

@@ -365,16 +365,17 @@ int  cuda_cube_store(const CudaCube *c, unsigned group, uint64_t *mem_lines, uin
                      char *err, size_t errlen);
 int  cuda_cube_run(CudaCube *c, uint64_t passes, char *err, size_t errlen);
 /* The cube's autotuner: the kernels whose blocks each run one warp group's code are compiled for
-   1, 2, 4 and 8 runs of words per block (as the cube's size allows), each variant is run for
-   probe_passes passes from the cube's present state (saved before, restored after: the state is
-   unchanged), and the fastest is kept for every later pass.  cand[i].ms is variant i's time.
-   No counterpart in the reference. */
+   4 and 8 warps per block and 1, 2 and 4 runs of words per block (as the cube's size allows; the
+   present shape first), each variant is run for probe_passes passes from the cube's present
+   state (saved before, restored after: the state is unchanged), and the fastest is kept for every
+   later pass.  cand[i].ms is variant i's time.  No counterpart in the reference. */
+#define CUBE_TUNE_MAX 8
 typedef struct {
     int      n, best;
     struct {
-        unsigned iters;
+        unsigned warps, iters;
         double   ms;
-    } cand[4];
+    } cand[CUBE_TUNE_MAX];
     unsigned probe_passes;
 } CudaCubeTune;
 int  cuda_cube_tune(CudaCube *c, unsigned probe_passes, CudaCubeTune *t, char *err,

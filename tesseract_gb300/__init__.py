@@ -575,11 +575,11 @@ def cube_demo(name: str, dims: int, checks: int = 3, seconds: float = 0.2) -> di
 
 
 class _CubeCand(C.Structure):
-    _fields_ = [("iters", C.c_uint), ("ms", C.c_double)]
+    _fields_ = [("warps", C.c_uint), ("iters", C.c_uint), ("ms", C.c_double)]
 
 
 class CudaCubeTune(C.Structure):
-    _fields_ = [("n", C.c_int), ("best", C.c_int), ("cand", _CubeCand * 4),
+    _fields_ = [("n", C.c_int), ("best", C.c_int), ("cand", _CubeCand * 8),
                 ("probe_passes", C.c_uint)]
 
 
@@ -617,8 +617,8 @@ class Cube:
         return last_launch()["kernel_ms"]
 
     def tune(self, probe_passes: int = 16) -> dict:
-        """The cube's autotuner (cuda_cube_tune): word runs per group-major block, measured on
-        this cube from its present state, which it leaves unchanged."""
+        """The cube's autotuner (cuda_cube_tune): warps and word runs per group-major block,
+        measured on this cube from its present state, which it leaves unchanged."""
         t, e = CudaCubeTune(), _err()
         L = lib()
         L.cuda_cube_tune.restype = C.c_int
@@ -626,8 +626,8 @@ class Cube:
                                      C.c_size_t]
         if not L.cuda_cube_tune(self.h, probe_passes, C.byref(t), e, len(e)):
             raise EngineError(e.value.decode())
-        cands = [{"iters": t.cand[i].iters, "ms": t.cand[i].ms if t.cand[i].ms >= 0 else None}
-                 for i in range(t.n)]
+        cands = [{"warps": t.cand[i].warps, "iters": t.cand[i].iters,
+                  "ms": t.cand[i].ms if t.cand[i].ms >= 0 else None} for i in range(t.n)]
         return {"candidates": cands, "best": cands[t.best], "probe_passes": probe_passes}
 
     def read(self):

@@ -79,6 +79,7 @@ struct CudaCube {
     cudaGraphExec_t graph;
     unsigned    graph_passes;
     unsigned    iters;      /* runs of words each group-major block walks (cuda_cube_tune) */
+    unsigned    gmw;        /* warps per group-major block (cuda_cube_tune) */
 };
 
 struct CudaCode {
@@ -1149,27 +1150,28 @@ static void loop_body(Src *o, Chunk *k, size_t from, size_t to)
 }
 
 /* One kernel for instructions from .. to-1; with loop != 0 the whole pass, `passes` times. */
-/* Blocks of a group-major kernel over W words: tc_cube_gm_warps warps (at most enough for W). */
-static unsigned gm_warps(unsigned W)
+/* Blocks of a group-major kernel over W words: `want` warps (at most enough for W). */
+static unsigned gm_warps(unsigned W, unsigned want)
 {
-    unsigned wpb = (unsigned)(tc_cube_gm_warps > 0 ? tc_cube_gm_warps : 1);
+    unsigned wpb = want > 0 ? want : 1;
     while (wpb > 1 && 32 * wpb > W)
         wpb /= 2;
     return wpb;
 }
 
-/* The runs of 32 * gm_warps(W) words a group-major block walks: `iters` (a power of two), as
-   far as the word blocks of a group divide evenly. */
-static unsigned gm_iters(unsigned W, unsigned iters)
+/* The runs of 32 * gm_warps(W, gmw) words a group-major block walks: `iters` (a power of two),
+   as far as the word blocks of a group divide evenly. */
+static unsigned gm_iters(unsigned W, unsigned gmw, unsigned iters)
 {
-    unsigned nwb = (W + 32 * gm_warps(W) - 1) / (32 * gm_warps(W)), it = 1;
+    unsigned wpb = gm_warps(W, gmw), nwb = (W + 32 * wpb - 1) / (32 * wpb), it = 1;
     while (2 * it <= iters && nwb % (2 * it) == 0)
         it *= 2;
     return it;
 }
 
 static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size_t from, size_t to,
-                        int loop, int *group_major, unsigned iters, const uint32_t *slot)
+                        int loop, int *group_major, unsigned iters, const uint32_t *slot,
+                        unsigned gmw)
 {
     Chunk k = {p, W, tc_xcalloc(p->ncells + 1, 1), tc_xcalloc(p->ncells + 1, 1), slot, 0};
     unsigned groups = chunk_groups(p, from, to, loop);
@@ -1200,8 +1202,8 @@ static void emit_kernel(Src *o, const Program *p, unsigned W, unsigned idx, size
     if (tc_cube_map && !loop) {
         Src body = {0};
         split_body(&body, &k, from, to, groups, 0, &gm);
-        unsigned wpb = gm_warps(W), nwb = (W + 32 * wpb - 1) / (32 * wpb);
-        unsigned it = gm ? gm_iters(W, iters) : 1;
+        unsigned wpb = gm_warps(W, gmw), nwb = (W + 32 * wpb - 1) / (32 * wpb);
+        unsigned it = gm ? gm_iters(W, gmw, iters) : 1;
         emit(o, "extern \"C\" __global__ void __launch_bounds__(%u) tc_cube_%u(u32 *__restrict__ "
                 "mem, u32 *__restrict__ rr, const u32 passes)\n{\n",
              gm ? 32 * wpb : TC_CUBE_BLOCK * groups, idx);
@@ -1277,7 +1279,8 @@ char *tc_codegen_cube(const Program *p, const size_t *first, unsigned nk, int bl
     emit(&o, "#define W %uu\n", W);
     emit(&o, "%s", CUBE_PRELUDE);
     for (unsigned k = 0; k < nk; k++)
-        emit_kernel(&o, p, W, k, first[k], first[k + 1], loop, NULL, 1, NULL);
+        emit_kernel(&o, p, W, k, first[k], first[k + 1], loop, NULL, 1, NULL,
+                    (unsigned)(tc_cube_gm_warps > 0 ? tc_cube_gm_warps : 1));
     if (len)
         *len = o.len;
     return o.s;
@@ -1290,6 +1293,7 @@ typedef struct {
     unsigned      k0, k1;  /* kernels of this module */
     unsigned      iters;   /* group-major runs per block */
     unsigned      variant; /* 1: the second variant's memory (A and B exchanged) */
+    unsigned      gmw;     /* warps per group-major block */
     cudaKernel_t *fn;      /* where the kernels go (variant v's kernel k at fn[v * nk + k]) */
     int          *gm;      /* where each kernel's group-major choice goes */
     int           ok;
@@ -1316,7 +1320,7 @@ static void *compile_job(void *arg)
     for (unsigned k = 0; k < nk; k++) {
         int gm;  /* the same in both variants: variant 0's job reports it */
         emit_kernel(&o, &c->p, c->W, j->k0 + k, first[k], first[k + 1], loop, &gm, j->iters,
-                    j->variant ? c->slot1 : NULL);
+                    j->variant ? c->slot1 : NULL, j->gmw);
         if (!j->variant)
             j->gm[j->k0 + k] = gm;
     }
@@ -1394,7 +1398,7 @@ char *tc_cube_source(const Program *p, unsigned variant, unsigned *nk, size_t *l
         for (unsigned k = 0; k < c->nk; k++) {
             int gm;
             emit_kernel(&o, &c->p, c->W, k, c->first[k], c->first[k + 1], c->loop, &gm, 1,
-                        variant ? c->slot1 : NULL);
+                        variant ? c->slot1 : NULL, c->gmw);
         }
         out = o.s;
         *len = o.len;
@@ -1426,6 +1430,7 @@ void cuda_cube_free(CudaCube *c)
    closing copies and their memory variant, kernels (long segments split), warp groups. */
 static void plan_cube(CudaCube *c, const Program *p)
 {
+    c->gmw = (unsigned)(tc_cube_gm_warps > 0 ? tc_cube_gm_warps : 1);
     c->dims = tc_program_dims(p);
     c->machines = 1u << c->dims;
     c->groups = c->machines / 512;
@@ -1512,6 +1517,7 @@ int cuda_cube_new(const Program *p, CudaCube **out, char *err, size_t errlen)
         jobs[j].k1 = j % c->nk + 1;
         jobs[j].variant = j / c->nk;
         jobs[j].iters = c->iters;
+        jobs[j].gmw = c->gmw;
         jobs[j].fn = c->fn;
         jobs[j].gm = c->gmajor;
         pthread_create(&tid[j], NULL, compile_job, &jobs[j]);
@@ -1611,9 +1617,10 @@ static int launch_pass(CudaCube *c, cudaStream_t s, unsigned passes, unsigned va
         void *args[] = {&mem, &rr, &passes};
         dim3 b = dim3u(block), g = dim3u(grid);
         if (c->gmajor[k]) {  /* blocks of one group: gm_warps warps over gm_iters runs */
-            unsigned wpb = gm_warps(c->W);
+            unsigned wpb = gm_warps(c->W, c->gmw);
             b.y = wpb;
-            g.x = ((c->W + 32 * wpb - 1) / (32 * wpb)) / gm_iters(c->W, c->iters) * c->warps[k];
+            g.x = ((c->W + 32 * wpb - 1) / (32 * wpb)) / gm_iters(c->W, c->gmw, c->iters) *
+                  c->warps[k];
         } else {
             b.y = c->warps[k];
         }
@@ -1700,20 +1707,27 @@ int cuda_cube_tune(CudaCube *c, unsigned probe_passes, CudaCubeTune *t, char *er
     int any_gm = 0;
     for (unsigned k = 0; k < c->nk; k++)
         any_gm |= c->gmajor[k];
-    static const unsigned wanted[4] = {1, 2, 4, 8};
-    unsigned its[4];
+    /* (warps per block, runs per block) as the cube's size allows them, the present one first */
+    static const unsigned want_w[2] = {4, 8}, want_it[3] = {1, 2, 4};
+    unsigned ws[CUBE_TUNE_MAX], its[CUBE_TUNE_MAX];
     int n = 0;
-    for (int i = 0; i < 4; i++) {
-        unsigned e = any_gm && !c->loop ? gm_iters(c->W, wanted[i]) : 1;
-        int seen = 0;
-        for (int j = 0; j < n; j++)
-            seen |= its[j] == e;
-        if (!seen)
-            its[n++] = e;
-    }
+    ws[n] = c->gmw;
+    its[n++] = c->iters;
+    for (int a = 0; any_gm && !c->loop && a < 2; a++)
+        for (int i = 0; i < 3 && n < CUBE_TUNE_MAX; i++) {
+            unsigned w = gm_warps(c->W, want_w[a]), it = gm_iters(c->W, w, want_it[i]);
+            int seen = 0;
+            for (int j = 0; j < n; j++)
+                seen |= gm_warps(c->W, ws[j]) == w && its[j] == it;
+            if (!seen) {
+                ws[n] = w;
+                its[n++] = it;
+            }
+        }
     t->n = n;
     t->probe_passes = probe_passes;
     for (int i = 0; i < n; i++) {
+        t->cand[i].warps = gm_warps(c->W, ws[i]);
         t->cand[i].iters = its[i];
         t->cand[i].ms = -1;
     }
@@ -1721,17 +1735,17 @@ int cuda_cube_tune(CudaCube *c, unsigned probe_passes, CudaCubeTune *t, char *er
         t->best = 0;
         return 1;
     }
-    cudaKernel_t *fns[4];
+    cudaKernel_t *fns[CUBE_TUNE_MAX];
     unsigned nkv = c->nk * c->variants;
     int *gms = tc_xcalloc(c->nk, sizeof *gms);
     CompileJob *jobs = tc_xcalloc((size_t)n * nkv, sizeof *jobs);
     pthread_t *tid = tc_xcalloc((size_t)n * nkv, sizeof *tid);
     unsigned nj = 0;
     for (int i = 0; i < n; i++) {
-        fns[i] = its[i] == c->iters ? c->fn : tc_xcalloc(nkv, sizeof *fns[i]);
-        for (unsigned kv = 0; its[i] != c->iters && kv < nkv; kv++) {
-            jobs[nj] = (CompileJob){c, kv % c->nk, kv % c->nk + 1, its[i], kv / c->nk, fns[i],
-                                    gms, 0, ""};
+        fns[i] = i == 0 ? c->fn : tc_xcalloc(nkv, sizeof *fns[i]);
+        for (unsigned kv = 0; i > 0 && kv < nkv; kv++) {
+            jobs[nj] = (CompileJob){c, kv % c->nk, kv % c->nk + 1, its[i], kv / c->nk, ws[i],
+                                    fns[i], gms, 0, ""};
             if (pthread_create(&tid[nj], NULL, compile_job, &jobs[nj]) == 0)
                 nj++;
         }
@@ -1756,11 +1770,12 @@ int cuda_cube_tune(CudaCube *c, unsigned probe_passes, CudaCubeTune *t, char *er
          tc_cu_check(cudaMemcpyAsync(save_rr, c->rr, (size_t)c->W * 4, cudaMemcpyDeviceToDevice,
                                      s), "save", err, errlen);
     cudaKernel_t *keep_fn = c->fn;
-    unsigned keep_iters = c->iters;
+    unsigned keep_iters = c->iters, keep_gmw = c->gmw;
     int best = -1;
     for (int i = 0; ok && i < n; i++) {
         c->fn = fns[i];
         c->iters = its[i];
+        c->gmw = ws[i];
         for (int rep = 0; ok && rep < 2; rep++) {  /* a warm-up run, then the timed one */
             ok = tc_cu_check(cudaMemcpyAsync(c->mem, save_mem, words * 4,
                                              cudaMemcpyDeviceToDevice, s), "restore", err,
@@ -1791,6 +1806,7 @@ int cuda_cube_tune(CudaCube *c, unsigned probe_passes, CudaCubeTune *t, char *er
              tc_cu_check(cudaStreamSynchronize(s), "restore", err, errlen);
     c->fn = ok ? fns[best] : keep_fn;
     c->iters = ok ? its[best] : keep_iters;
+    c->gmw = ok ? ws[best] : keep_gmw;
     for (int i = 0; i < n; i++)
         if (fns[i] != c->fn)
             free(fns[i]);

@@ -111,14 +111,15 @@ def test_life_dims16_full_board():
 
 
 def test_cube_tune_keeps_state_and_results():
-    """cuda_cube_tune: every variant (word runs per group-major block) is timed from the cube's
-    present state, the state is the same afterwards, the fastest is kept, and generations after
-    tuning still equal plain C Life."""
-    L = LifeCube(14, w=8, h=8)  # 512 words: up to 4 runs of 128 words per block
+    """cuda_cube_tune: every variant (warps and word runs per group-major block) is timed from
+    the cube's present state, the state is the same afterwards, the fastest is kept, and
+    generations after tuning still equal plain C Life."""
+    L = LifeCube(14, w=8, h=8)  # 512 words: up to 4 runs of 4 warps' 128 words, 2 of 8 warps'
     L.seed(7)
     start = L.board()
     t = L.cube.tune(8)
-    assert [c["iters"] for c in t["candidates"]] == [1, 2, 4]
+    assert [(c["warps"], c["iters"]) for c in t["candidates"]] == [(4, 1), (4, 2), (4, 4), (8, 1),
+                                                                    (8, 2)]
     assert (L.board() == start).all()
     timed = [c["ms"] for c in t["candidates"] if c["ms"] is not None]
     assert t["best"]["ms"] == min(timed)
