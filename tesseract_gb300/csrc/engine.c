@@ -565,6 +565,7 @@ char *tc_codegen_enum_for(const Enum *e, size_t *len, char *err, size_t errlen)
     return src;
 }
 
+
 /* ---- the autotuner's choices ---------------------------------------------------------------
 
    cuda_enum_tune measures kernels of one job that differ in threads per block and stretch length
@@ -665,87 +666,192 @@ void tc_free(void *p)
 /* Workspace of a launch: the hit counter, then 16 hits per warp, then a count per warp. */
 #define WS_LIST 256u
 
-/* A generated kernel compiled but not yet loaded */
+/* Generated kernels compiled together into one module and not yet loaded: one kernel per job of
+   a group (up to TC_MAX_KERNELS), so the group pays NVRTC's fixed cost once and loads once (a
+   load waits for the device's running work).  Shared by the group's jobs until the last is
+   loaded or dropped. */
 struct TcEnumPending {
     char     *src;
     size_t    len;
     TcBuilt   b;
-    TcGenWork work;
-    uint64_t  k1, k2;
-    int       block;
+    int       n, refs, loaded;
+    TcModule  m;  /* once loaded: kernel k in fn[k] */
+    struct {
+        uint64_t  k1, k2;
+        TcGenWork work;
+        int       block;
+    } k[TC_MAX_KERNELS];
 };
 
-/* The kernel for the plan in g: from the cache (m filled, *pend NULL), else generated and
-   compiled (*pend: the build, for enum_module_load); `fast` compiles it for a quick start
-   (FAST_NVRTC_OPT), unless the optimised build is cached. */
-static int enum_module_build(TcGenEnum *g, int fast, TcModule *m, TcEnumPending **pend, char *err,
-                             size_t errlen)
+static void enum_pending_release(TcEnumPending *p)
 {
-    *pend = NULL;
-    uint64_t k1, k2;
-    enum_key(g, &k1, &k2);
-    if (lookup_enum(k1, k2, m))
-        return 1;
-    if (fast)
-        fast_key(&k2);
-    if (fast && lookup_enum(k1, k2, m))
-        return 1;
-    TcEnumPending *p = tc_xcalloc(1, sizeof *p);
-    g->work = &p->work;
-    p->src = tc_codegen_enum(g, &p->len);
-    g->work = NULL;
-    if (fast) {
-        static const char mark[] = "// built with " FAST_NVRTC_OPT "\n";
-        char *s2 = tc_xmalloc(p->len + sizeof mark);
-        memcpy(s2, mark, sizeof mark - 1);
-        memcpy(s2 + sizeof mark - 1, p->src, p->len + 1);
+    if (p && --p->refs == 0) {
+        tc_built_free(&p->b);
         free(p->src);
-        p->src = s2;
-        p->len += sizeof mark - 1;
+        free(p);
     }
-    p->k1 = k1;
-    p->k2 = k2;
-    p->block = g->block;
+}
+
+/* The module source of n jobs' kernels: one job's source as it is (kernel tc_enum); several,
+   each in a namespace of its own with its kernel renamed tc_enum_<k> and its macros undefined
+   after it (the common ones are defined alike by every job). */
+static char *group_source(char **srcs, const size_t *lens, int n, size_t *len)
+{
+    if (n == 1) {
+        char *s = tc_xmalloc(lens[0] + 1);
+        memcpy(s, srcs[0], lens[0] + 1);
+        *len = lens[0];
+        return s;
+    }
+    static const char sig[] = ") tc_enum(const TcEnumArgs";
+    size_t cap = 256, at = 0;
+    for (int k = 0; k < n; k++)
+        cap += lens[k] + 1024;
+    char *o = tc_xmalloc(cap);
+    for (int k = 0; k < n; k++) {
+        at += (size_t)snprintf(o + at, cap - at, "namespace tcj%d {\n", k);
+        const char *s = srcs[k], *hit = strstr(s, sig);
+        size_t pre = hit ? (size_t)(hit - s) : lens[k];
+        memcpy(o + at, s, pre);
+        at += pre;
+        if (hit) {
+            at += (size_t)snprintf(o + at, cap - at, ") tc_enum_%d(const TcEnumArgs", k);
+            size_t rest = lens[k] - pre - (sizeof sig - 1);
+            memcpy(o + at, hit + sizeof sig - 1, rest);
+            at += rest;
+        }
+        at += (size_t)snprintf(o + at, cap - at, "\n}\n");
+        /* #undef every macro the job defined */
+        for (const char *d = strstr(s, "#define "); d; d = strstr(d + 8, "#define ")) {
+            const char *nm = d + 8, *e = nm;
+            while ((*e >= 'A' && *e <= 'Z') || (*e >= 'a' && *e <= 'z') || (*e >= '0' && *e <= '9') ||
+                   *e == '_')
+                e++;
+            if (at + (size_t)(e - nm) + 16 > cap) {
+                cap = 2 * cap + (size_t)(e - nm) + 16;
+                o = tc_xrealloc(o, cap);
+            }
+            at += (size_t)snprintf(o + at, cap - at, "#undef %.*s\n", (int)(e - nm), nm);
+        }
+    }
+    o[at] = '\0';
+    *len = at;
+    return o;
+}
+
+/* The kernels for the plans in g[0..n): from the cache (m[i] filled, pend[i] NULL), else
+   generated and compiled together (pend[i]: the group's build, for enum_module_load); `fast`
+   compiles them for a quick start (FAST_NVRTC_OPT), unless the optimised build is cached. */
+static int enum_modules_build(TcGenEnum *const *g, int n, int fast, TcModule *m,
+                              TcEnumPending **pend, int *kidx, char *err, size_t errlen)
+{
+    TcEnumPending *p = NULL;
+    char *srcs[TC_MAX_KERNELS];
+    size_t lens[TC_MAX_KERNELS];
+    int who[TC_MAX_KERNELS], nb = 0;
+    for (int i = 0; i < n; i++) {
+        pend[i] = NULL;
+        kidx[i] = 0;
+        uint64_t k1, k2;
+        enum_key(g[i], &k1, &k2);
+        if (lookup_enum(k1, k2, &m[i]))
+            continue;
+        if (fast)
+            fast_key(&k2);
+        if (fast && lookup_enum(k1, k2, &m[i]))
+            continue;
+        if (!p)
+            p = tc_xcalloc(1, sizeof *p);
+        int k = nb++;
+        g[i]->work = &p->k[k].work;
+        srcs[k] = tc_codegen_enum(g[i], &lens[k]);
+        g[i]->work = NULL;
+        if (fast) {
+            static const char mark[] = "// built with " FAST_NVRTC_OPT "\n";
+            char *s2 = tc_xmalloc(lens[k] + sizeof mark);
+            memcpy(s2, mark, sizeof mark - 1);
+            memcpy(s2 + sizeof mark - 1, srcs[k], lens[k] + 1);
+            free(srcs[k]);
+            srcs[k] = s2;
+            lens[k] += sizeof mark - 1;
+        }
+        p->k[k].k1 = k1;
+        p->k[k].k2 = k2;
+        p->k[k].block = g[i]->block;
+        who[k] = i;
+        kidx[i] = k;
+    }
+    if (!p)
+        return 1;
+    p->n = nb;
+    p->src = group_source(srcs, lens, nb, &p->len);
+    for (int k = 0; k < nb; k++)
+        free(srcs[k]);
     if (!tc_module_build(p->src, p->len, fast ? FAST_NVRTC_OPT : NULL, &p->b, err, errlen)) {
         free(p->src);
         free(p);
         return 0;
     }
-    *pend = p;
+    p->refs = nb;
+    for (int k = 0; k < nb; k++)
+        pend[who[k]] = p;
     return 1;
 }
 
-static void enum_pending_free(TcEnumPending *p)
+/* Job i's kernel of a built group, loading the group's module first if no job of it has (the
+   load waits for the device's running work); releases the job's share of the group. */
+static int enum_module_load(TcEnumPending *p, int i, TcModule *m, char *err, size_t errlen)
 {
-    if (!p)
-        return;
-    tc_built_free(&p->b);
-    free(p->src);
-    free(p);
-}
-
-/* Loads a built kernel (waits for the device's running work) and caches it; frees p. */
-static int enum_module_load(TcEnumPending *p, TcModule *m, char *err, size_t errlen)
-{
-    static const char *const names[] = {"tc_enum"};
-    int ok = tc_module_load(p->src, p->len, &p->b, names, 1, m, err, errlen);
-    if (ok) {
-        m->info.luts_per_step = p->work.luts_per_step;
-        m->info.luts_per_stretch = p->work.luts_per_stretch;
-        m->info.stretch_steps = p->work.stretch_steps;
-        m->info.compare_ops = p->work.compare_ops;
-        m->info.block = p->block;
-        remember_enum(p->k1, p->k2, m);
+    int ok = 1;
+    if (!p->loaded) {
+        char names[TC_MAX_KERNELS][24];
+        const char *ptrs[TC_MAX_KERNELS];
+        for (int k = 0; k < p->n; k++) {
+            if (p->n == 1)
+                snprintf(names[k], sizeof names[k], "tc_enum");
+            else
+                snprintf(names[k], sizeof names[k], "tc_enum_%d", k);
+            ptrs[k] = names[k];
+        }
+        ok = tc_module_load(p->src, p->len, &p->b, ptrs, p->n, &p->m, err, errlen);
+        if (ok) {
+            p->loaded = 1;
+            for (int k = 0; k < p->n; k++) {
+                TcModule mk = p->m;
+                mk.fn[0] = p->m.fn[k];
+                mk.info.luts_per_step = p->k[k].work.luts_per_step;
+                mk.info.luts_per_stretch = p->k[k].work.luts_per_stretch;
+                mk.info.stretch_steps = p->k[k].work.stretch_steps;
+                mk.info.compare_ops = p->k[k].work.compare_ops;
+                mk.info.block = p->k[k].block;
+                remember_enum(p->k[k].k1, p->k[k].k2, &mk);
+            }
+        }
     }
-    enum_pending_free(p);
+    if (ok) {
+        *m = p->m;
+        m->fn[0] = p->m.fn[i];
+        struct cudaFuncAttributes fa;
+        if (i > 0 && cudaFuncGetAttributes(&fa, (const void *)m->fn[0]) == cudaSuccess) {
+            m->info.regs = fa.numRegs;
+            m->info.local_bytes = (int)fa.localSizeBytes;
+        }
+        m->info.luts_per_step = p->k[i].work.luts_per_step;
+        m->info.luts_per_stretch = p->k[i].work.luts_per_stretch;
+        m->info.stretch_steps = p->k[i].work.stretch_steps;
+        m->info.compare_ops = p->k[i].work.compare_ops;
+        m->info.block = p->k[i].block;
+    }
+    enum_pending_release(p);
     return ok;
 }
 
 static int enum_module(TcGenEnum *g, int fast, TcModule *m, char *err, size_t errlen)
 {
     TcEnumPending *p;
-    return enum_module_build(g, fast, m, &p, err, errlen) &&
-           (!p || enum_module_load(p, m, err, errlen));
+    int k;
+    return enum_modules_build(&g, 1, fast, m, &p, &k, err, errlen) &&
+           (!p || enum_module_load(p, 0, m, err, errlen));
 }
 
 /* The launch shape of job e on module m: as many blocks as are resident on the device at once
@@ -787,19 +893,45 @@ static int enum_shape(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
     return 1;
 }
 
+int tc_enum_jobs_build(const Enum *const *e, TcEnumJob *const *j, int n, int fast, char *err,
+                       size_t errlen)
+{
+    if (n < 1 || n > TC_MAX_KERNELS)
+        return tc_fail(err, errlen, "a build of %d jobs: 1 to %d", n, TC_MAX_KERNELS);
+    EnumPlan pl[TC_MAX_KERNELS];
+    TcGenEnum *g[TC_MAX_KERNELS];
+    TcModule m[TC_MAX_KERNELS];
+    TcEnumPending *pend[TC_MAX_KERNELS];
+    int kidx[TC_MAX_KERNELS];
+    int np = 0, ok = 1;
+    /* the refusals first (no device needed for them), then the device */
+    for (int i = 0; ok && i < n; i++) {
+        memset(j[i], 0, sizeof *j[i]);
+        ok = plan_enum(e[i], &pl[i], err, errlen);
+        if (ok) {
+            np++;
+            g[i] = &pl[i].g;
+        }
+    }
+    if (ok)
+        ok = cuda_engine_init(0, err, errlen);
+    for (int i = 0; ok && i < n; i++)
+        apply_tuning(&pl[i].g);
+    if (ok)
+        ok = enum_modules_build(g, n, fast, m, pend, kidx, err, errlen);
+    for (int i = 0; ok && i < n; i++) {
+        j[i]->m = m[i];
+        j[i]->pending = pend[i];
+        j[i]->pidx = kidx[i];
+    }
+    for (int i = 0; i < np; i++)
+        plan_free(&pl[i]);
+    return ok;
+}
+
 int tc_enum_job_build(const Enum *e, TcEnumJob *j, int fast, char *err, size_t errlen)
 {
-    memset(j, 0, sizeof *j);
-    EnumPlan pl;
-    if (!plan_enum(e, &pl, err, errlen))
-        return 0;
-    int ok = cuda_engine_init(0, err, errlen);
-    if (ok) {
-        apply_tuning(&pl.g);
-        ok = enum_module_build(&pl.g, fast, &j->m, &j->pending, err, errlen);
-    }
-    plan_free(&pl);
-    return ok;
+    return tc_enum_jobs_build(&e, &j, 1, fast, err, errlen);
 }
 
 int tc_enum_job_load(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
@@ -807,7 +939,7 @@ int tc_enum_job_load(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
     if (j->pending) {
         TcEnumPending *p = j->pending;
         j->pending = NULL;
-        if (!enum_module_load(p, &j->m, err, errlen))
+        if (!enum_module_load(p, j->pidx, &j->m, err, errlen))
             return 0;
     }
     return enum_shape(e, j, err, errlen);
@@ -815,7 +947,7 @@ int tc_enum_job_load(const Enum *e, TcEnumJob *j, char *err, size_t errlen)
 
 void tc_enum_job_drop(TcEnumJob *j)
 {
-    enum_pending_free(j->pending);
+    enum_pending_release(j->pending);
     j->pending = NULL;
 }
 
@@ -1104,4 +1236,28 @@ int cuda_table(const Program *p, unsigned ticks, uint8_t *vals, char *err, size_
     free(h);
     tc_engine.last = m.info;
     return ok;
+}
+
+/* The module source of n jobs built together (kernels tc_enum_0 ..), as the compile threads
+   make it; for tests. */
+char *tc_codegen_enum_group(const Enum *const *e, int n, size_t *len, char *err, size_t errlen)
+{
+    if (n < 1 || n > TC_MAX_KERNELS) {
+        tc_fail(err, errlen, "a group of %d jobs: 1 to %d", n, TC_MAX_KERNELS);
+        return NULL;
+    }
+    char *srcs[TC_MAX_KERNELS];
+    size_t lens[TC_MAX_KERNELS];
+    for (int i = 0; i < n; i++) {
+        srcs[i] = tc_codegen_enum_for(e[i], &lens[i], err, errlen);
+        if (!srcs[i]) {
+            for (int k = 0; k < i; k++)
+                free(srcs[k]);
+            return NULL;
+        }
+    }
+    char *out = group_source(srcs, lens, n, len);
+    for (int i = 0; i < n; i++)
+        free(srcs[i]);
+    return out;
 }

@@ -103,6 +103,7 @@ typedef struct {
     uint32_t   parts, part, nsel;
     EnumResult base;     /* space, tried, ops */
     TcEnumPending *pending;  /* built by tc_enum_job_build, not yet loaded */
+    int            pidx;     /* its kernel in the pending group */
 } TcEnumJob;
 /* fast: compiled for a quick start (ptxas without optimisation) unless the optimised kernel is
    cached already.  prepare = build (code generation and NVRTC: no CUDA call) + load (the module
@@ -110,6 +111,10 @@ typedef struct {
    that will not be loaded. */
 int    tc_enum_job_prepare(const Enum *e, TcEnumJob *j, int fast, char *err, size_t errlen);
 int    tc_enum_job_build(const Enum *e, TcEnumJob *j, int fast, char *err, size_t errlen);
+/* n (1..TC_MAX_KERNELS) jobs built together: their uncached kernels in one NVRTC program and,
+   later, one module load */
+int    tc_enum_jobs_build(const Enum *const *e, TcEnumJob *const *j, int n, int fast, char *err,
+                          size_t errlen);
 int    tc_enum_job_load(const Enum *e, TcEnumJob *j, char *err, size_t errlen);
 void   tc_enum_job_drop(TcEnumJob *j);
 size_t tc_enum_job_ws_bytes(const TcEnumJob *j);

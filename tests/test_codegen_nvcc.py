@@ -54,3 +54,33 @@ def test_generated_kernel_compiles(name, args):
         assert "0 bytes spill stores" in log and "0 bytes spill loads" in log, log
         regs = int(re.search(r"Used (\d+) registers", log).group(1))
         assert regs <= 128, log  # two blocks of 256 threads per SM
+
+
+def test_grouped_kernels_compile():
+    """Jobs that a compile thread builds together: one source, each job in a namespace of its own
+    with its kernel renamed tc_enum_<k> and its macros undefined after it; every kernel compiles
+    (ptxas -v names each entry) and the group holds the jobs' different shapes (hoisted,
+    permuted, spec and equiv kernels, block sizes)."""
+    import ctypes as C
+    from tesseract_gb300.workloads import batch_equiv_jobs
+    mul10 = T.Program.gen_mul(10)
+    specs = [T.Spec(mul10, "p = a * b"), T.Spec(mul10, "p = 561", False)]
+    pairs = batch_equiv_jobs(2)  # the structs point into these objects: keep them alive
+    jobs = [T.make_enum(T.EN_VERIFY, mul10, None, specs[0], 1),
+            T.make_enum(T.EN_SEARCH, mul10, None, specs[1], 1)]
+    for j in pairs:
+        jobs.append(T.make_enum(T.EN_EQUIV, j["a"], j["b"], None, 1))
+    L = T.lib()
+    L.tc_codegen_enum_group.restype = C.c_void_p
+    L.tc_codegen_enum_group.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_size_t), C.c_char_p,
+                                        C.c_size_t]
+    arr = (C.POINTER(T.EnumStruct) * len(jobs))(*[C.pointer(e) for e in jobs])
+    n, err = C.c_size_t(), C.create_string_buffer(256)
+    ptr = L.tc_codegen_enum_group(C.cast(arr, C.c_void_p), len(jobs), C.byref(n), err, len(err))
+    assert ptr, err.value
+    src = C.string_at(ptr, n.value).decode()
+    C.CDLL(None).free(C.c_void_p(ptr))
+    assert src.count("namespace tcj") == len(jobs)
+    log = compile_source(src)
+    entries = set(re.findall(r"Compiling entry function '(tc_enum_\d+)'", log))
+    assert entries == {"tc_enum_%d" % k for k in range(len(jobs))}, log[-2000:]
