@@ -91,3 +91,25 @@ def load_gz(name):
 def as_record(r):
     """An EnumResult dict in the fixtures' per-job form: [space, tried, hits, ops, "hex,..."]."""
     return [r["space"], r["tried"], r["hits"], r["ops"], ",".join("%x" % x for x in r["hit"])]
+
+
+def program_digest(s, rename=None) -> str:
+    """sha256 of a Program struct's structure by cell names, so that it does not depend on the
+    order cells were numbered in: its instructions, id and link cells, inputs and outputs.
+    rename maps each cell name first (a listing's spelling of macro-local names)."""
+    import hashlib
+    names = [s.cell_names[c].decode() for c in range(s.ncells)]
+    if rename:
+        names = [rename(n) for n in names]
+    h = hashlib.sha256()
+    h.update(b"%d %d;" % (s.len, s.ncells))
+    h.update("".join("%d,%s;" % (s.code[i].op, names[s.code[i].addr])
+                     for i in range(s.len)).encode())
+    h.update(("in" + ",".join(names[s.inputs[i]] for i in range(s.ninputs))).encode())
+    h.update(("out" + ",".join(names[s.outputs[i]] for i in range(s.noutputs))).encode())
+    if s.special:
+        h.update(("sp" + ";".join(sorted("%s,%d,%d,%s" % (names[c], s.special[c].kind,
+                                                        s.special[c].dim,
+                                                        names[s.special[c].src])
+                                         for c in range(s.ncells)))).encode())
+    return h.hexdigest()
