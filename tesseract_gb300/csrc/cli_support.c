@@ -443,7 +443,7 @@ int cuda_cube_demo(const char *name, int dims, int checks, double seconds, CudaD
         snprintf(r->what, sizeof r->what, "h(k) = #x: f(x) = g(x^k) = 1, by spectra");
         tc_gen_cube_xorconv(&p, dims);
     } else if (!strcmp(name, "anf")) {
-        snprintf(r->what, sizeof r->what, "truth table of %d inputs -> normal form (Mobius)", dims);
+        snprintf(r->what, sizeof r->what, "truth table of %d inputs -> normal form (M\xc3\xb6" "bius)", dims);
         tc_gen_cube_anf(&p, dims);
     } else if (!strcmp(name, "walsh")) {
         snprintf(r->what, sizeof r->what, "Walsh-Hadamard spectrum of f, %d-bit results", dims + 3);

@@ -228,6 +228,7 @@ CLI_CASES = [
     (["life", "--dims", "11", "--rows", "3", "--size", "4", "--gens", "5", "--seconds", "0"],
      "life"),
     (["life", "--size", "2"], "life"),
+    (["cube", "--checks", "3", "--seconds", "0.01"], "cube"),
     (["cube", "any", "--dims", "10", "--seconds", "0.01"], "cube"),
     (["cube", "rank", "--dims", "10", "--seconds", "0.01"], "cube"),
     (["cube", "sort", "--dims", "10", "--seconds", "0.01"], "cube"),
