@@ -53,6 +53,18 @@ class LifeCube:
             mem[c] = words[:, i, :].reshape(-1)
         self.cube.write(mem, rr)
 
+    def set_board(self, board: np.ndarray):
+        """The whole torus from 0/1 bytes, (2^rbits h) x (2^cbits w), the layout board() reads."""
+        nr, nc = 1 << self.rbits, 1 << self.cbits
+        t = np.asarray(board, dtype=np.uint8).reshape(nr, self.h, nc, self.w).transpose(1, 3, 0, 2)
+        bits = np.zeros((self.h * self.w, self.machines), dtype=np.uint8)
+        bits[:, self.grid] = t.reshape(self.h * self.w, nr, nc)
+        words = np.packbits(bits, axis=1, bitorder="little").view(np.uint32)
+        mem, rr = self.cube.read()
+        for i, c in enumerate(self.cells):
+            mem[c] = words[i]
+        self.cube.write(mem, rr)
+
     def tile_bits(self):
         """bits[i, m]: tile cell i of machine m."""
         mem, _ = self.cube.read()

@@ -1,5 +1,6 @@
 """Writes tests/golden/cube512.json.gz: the reference's own 512-machine cube demo programs, the
-ones `alpha cube` runs (src/cubedemo.c:344-378), as the reference assembles them.
+ones `alpha cube` runs (src/cubedemo.c:344-378), as the reference assembles them, and its
+collectives across groups (a bitonic sort of lib/cube.inc's macros, gen_rank).
 
     python tests/golden/make_cube_golden.py
 
@@ -80,6 +81,14 @@ def print_program(p) -> str:
     return buf.value.decode()
 
 
+def add(out, name, what, p, R):
+    listing = re.sub(LOCAL, r"mac\1_\2", print_program(p))
+    digest = program_digest(p, lambda n: re.sub(LOCAL, r"mac\1_\2", n))
+    R.program_free(C.byref(p))
+    out[name] = {"what": what, "program": listing, "structure": digest}
+    print(name, len(listing.splitlines()), "lines")
+
+
 def demos(src: str):
     block = src[src.index("static const Demo demos[] = {"):]
     block = block[:block.index("};")]
@@ -101,11 +110,28 @@ def main():
         text = '.include "%s/std.inc"\n.include "%s/cube.inc"\n%s\n' % (lib, lib, body)
         p, err = T.ProgramStruct(), C.create_string_buffer(512)
         assert R.asm_string(text.encode(), name.encode(), b".", C.byref(p), err, len(err)), err.value
-        listing = re.sub(LOCAL, r"mac\1_\2", print_program(p))
-        digest = program_digest(p, lambda n: re.sub(LOCAL, r"mac\1_\2", n))
-        R.program_free(C.byref(p))
-        out[name] = {"what": what, "program": listing, "structure": digest}
-        print(name, len(listing.splitlines()), "lines")
+        add(out, name, what, p, R)
+    # across groups: the bitonic sort from lib/cube.inc's compare-exchange macros (CMPX8 inside a
+    # group, CMPX8_FAR across groups; stage st sorts blocks of 2^st machines up or down by bit st,
+    # the last merge all up) at 1,024 and 2,048 machines, and the reference's gen_rank at 1,024
+    # and 4,096 (the collectives of tests/test_cube.c:1130-1170)
+    for dims in (10, 11):
+        lines = ['.include "%s/std.inc"' % lib, '.include "%s/cube.inc"' % lib,
+                 ".in v0 v1 v2 v3 v4 v5 v6 v7", ".out v0 v1 v2 v3 v4 v5 v6 v7"]
+        for st in range(1, dims + 1):
+            for j in range(st - 1, -1, -1):
+                lines.append("%s v %d %s" % ("CMPX8" if j < 9 else "CMPX8_FAR", j,
+                                             "ID%d" % st if st < dims else "ZERO"))
+        p, err = T.ProgramStruct(), C.create_string_buffer(512)
+        name = "sort%d" % dims
+        assert R.asm_string(("\n".join(lines) + "\n").encode(), name.encode(), b".", C.byref(p),
+                            err, len(err)), err.value
+        add(out, name, "sort %d bytes across groups" % (1 << dims), p, R)
+    R.gen_rank.argtypes = [C.POINTER(T.ProgramStruct), C.c_int]
+    for dims in (10, 12):
+        p = T.ProgramStruct()
+        R.gen_rank(C.byref(p), dims)
+        add(out, "rank%d" % dims, "gen_rank on %d machines" % (1 << dims), p, R)
     with gzip.open(os.path.join(HERE, "cube512.json.gz"), "wt") as f:
         json.dump(out, f, separators=(",", ":"))
 

@@ -38,11 +38,29 @@ def vec(cube, cs):
     return np.array([sum(cube.get(k, c) << i for i, c in enumerate(cs)) for k in range(N)])
 
 
+DIMS = {"sort10": 10, "sort11": 11, "rank10": 10, "rank12": 12}
+
+
 def test_every_listing_round_trips():
     for name, d in DEMOS.items():
         p = T.Program.from_asm(d["program"], name)
         assert program_digest(p.s) == d["structure"], name
-        assert p.dims() == 9, name
+        assert p.dims() == DIMS.get(name, 9), name
+
+
+def test_sort_across_groups_on_the_reference_machine():
+    """lib/cube.inc's bitonic sort at 1,024 machines: CMPX8_FAR across the two groups."""
+    n = 1024
+    p = T.Program.from_asm(DEMOS["sort10"]["program"], "sort10")
+    vc = cells(p, "v", 8)
+    v = np.random.default_rng(5).integers(0, 256, n)
+    cube = O.RefCube(p, n)
+    for k in range(n):
+        for i, c in enumerate(vc):
+            cube.set(k, c, int((v[k] >> i) & 1))
+    cube.tick()
+    got = [sum(cube.get(k, c) << i for i, c in enumerate(vc)) for k in range(n)]
+    assert got == sorted(v.tolist())
 
 
 def test_sort_pack_perm():

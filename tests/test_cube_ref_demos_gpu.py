@@ -1,7 +1,8 @@
 """The reference's own 512-machine cube demos (`alpha cube`, src/cubedemo.c:344-378; programs
 from its lib/cube.inc, assembled by the reference itself: tests/golden/cube512.json.gz, written
 by tests/golden/make_cube_golden.py) run on the GPU cube, every machine's result against plain
-Python, with the checks of src/cubedemo.c:62-306.  Each listing reassembles here to the
+Python, with the checks of src/cubedemo.c:62-306; and its collectives across groups and Life on
+one board across groups (tests/test_cube.c:1130-1215).  Each listing reassembles here to the
 reference's program (the digest of its structure)."""
 import random
 
@@ -27,11 +28,11 @@ def cells(p, stem, n=None):
 class Run:
     """A cube of the demo's program: values in per machine, one pass, values out."""
 
-    def __init__(self, name):
+    def __init__(self, name, machines=N):
         self.p = T.Program.from_asm(DEMOS[name]["program"], name)
         assert program_digest(self.p.s) == DEMOS[name]["structure"]
         self.cube = T.Cube(self.p)
-        assert self.cube.machines == N
+        assert self.cube.machines == machines
         mem, rr = self.cube.read()
         self.mem = mem.reshape(self.p.s.ncells, -1)
         self.mem[:] = 0
@@ -147,3 +148,53 @@ def test_anf_and_ring(seed):
         le, c, ri = gray((i - 1) % N), gray(i), gray((i + 1) % N)
         want[c] = (110 >> ((x[le] << 2) | (x[c] << 1) | x[ri])) & 1
     assert (r.get(cells(r.p, "x")) == want).all()
+
+
+@pytest.mark.parametrize("dims", [10, 11])
+def test_sort_across_groups(dims):
+    """lib/cube.inc's bitonic sort, CMPX8_FAR across groups: random bytes and a descending run
+    (the two kinds of tests/test_cube.c:1150-1170)."""
+    n = 1 << dims
+    for kind in (0, 1):
+        r = Run("sort%d" % dims, n)
+        v = (255 - np.arange(n) % 256) if kind else np.random.default_rng(dims).integers(0, 256, n)
+        r.put_vec(cells(r.p, "v", 8), v)
+        r.run()
+        assert (r.get_vec(cells(r.p, "v", 8)) == np.sort(v)).all(), kind
+
+
+@pytest.mark.parametrize("dims", [10, 12])
+def test_rank_across_groups(dims):
+    """The reference's gen_rank: p = how many machines below have x = 1, t = how many in all."""
+    n = 1 << dims
+    r = Run("rank%d" % dims, n)
+    x = (np.random.default_rng(dims).integers(0, 3, n) == 0).astype(int)
+    r.put(cells(r.p, "x"), x)
+    r.run()
+    bits = dims + 1
+    assert (r.get_vec(cells(r.p, "p", bits)) == np.concatenate([[0], np.cumsum(x)[:-1]])).all()
+    assert (r.get_vec(cells(r.p, "t", bits)) == x.sum()).all()
+
+
+@pytest.mark.parametrize("w,h,rb,cb,gens", [(1, 1, 5, 5, 4), (2, 3, 2, 9, 3), (4, 4, 6, 5, 3),
+                                            (3, 2, 10, 0, 3)])
+def test_life_shapes_across_groups(w, h, rb, cb, gens):
+    """Life on one board across groups in the reference's own shapes (tests/test_cube.c:1173-1215:
+    w x h tiles, 2^rbits x 2^cbits machines, a column of machines included), against plain C
+    Life."""
+    import oracle as O
+    from tesseract_gb300.life import LifeCube, pack_rows, unpack_rows
+    L = LifeCube(rb + cb, rb, w=w, h=h)
+    board = (np.random.default_rng(w * 100 + h).integers(0, 3, (h << rb, w << cb)) == 0)
+    L.set_board(board.astype(np.uint8))
+    L.run(gens)
+    if (w << cb) % 64 == 0:
+        packed = pack_rows(board.astype(np.uint8))
+        O.life_words(packed, gens)
+        want = unpack_rows(packed)
+    else:
+        want = bytearray(board.astype(np.uint8).tobytes())
+        for _ in range(gens):
+            O.life_scalar(want, w << cb, h << rb)
+        want = np.frombuffer(bytes(want), dtype=np.uint8).reshape(h << rb, w << cb)
+    assert (L.board() == want).all()
