@@ -190,3 +190,27 @@ def test_check_programs_that_recompute_far_reads():
         p = T.Program.from_asm(text)
         r = T.check(p, seed=seed, ticks=3)
         assert r["ok"], (seed, r)
+
+
+@pytest.mark.parametrize("w,h", [(8, 8), (10, 7), (3, 3)])
+def test_life_512_boards_20_generations(w, h):
+    """The reference's own Life test (tests/test_work.c:378-416): gen_life's w x h torus in each
+    of 512 machines, every board random, 20 passes, every board against plain C Life."""
+    p = T.Program.gen_life(w, h)
+    cube = T.Cube(p)
+    assert cube.machines == 512
+    rng = np.random.default_rng(w * 10 + h)
+    boards = rng.integers(0, 2, size=(512, h, w), dtype=np.uint8)
+    mem, rr = cube.read()
+    for i, c in enumerate(p.board):
+        bits = boards[:, i // w, i % w].astype(np.uint64).reshape(-1, 32)
+        mem[c] = (bits << np.arange(32, dtype=np.uint64)).sum(axis=1).astype(np.uint32)
+    cube.write(mem, rr)
+    cube.run(20)
+    mem, _ = cube.read()
+    for k in range(512):
+        want = bytearray(boards[k].tobytes())
+        for _ in range(20):
+            O.life_scalar(want, w, h)
+        got = [(int(mem[c][k // 32]) >> (k % 32)) & 1 for c in p.board]
+        assert got == list(want), k
