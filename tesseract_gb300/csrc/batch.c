@@ -967,7 +967,7 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
     double t0 = tc_now();
     long cores = sysconf(_SC_NPROCESSORS_ONLN);
     int threads = tc_batch_threads > 0 ? tc_batch_threads
-                  : cores > 3 ? (int)cores - 2 : 1;  /* the host loop and the driver keep a core */
+                  : cores > 3 ? (int)cores - 2 : 1;  /* the host loop and the CUDA runtime keep a core */
     Planned *p = tc_xmalloc((size_t)njobs * sizeof *p);
     for (int i = 0; i < njobs; i++) {
         const Enum *e = jobs[i];
