@@ -10,6 +10,7 @@
 #include <unistd.h>
 #include <string.h>
 
+#include <math.h>
 #include <pthread.h>
 
 #include "batch.h"
@@ -95,7 +96,7 @@ static void clear_list(Vec *lists, const Program *p, unsigned base, const unsign
 
 typedef struct {
     Vec jobs, code, luts, lists, rpn, vars;
-    uint32_t units;
+    uint32_t units, unit_words;
     int      slots;
     /* units in launch order: class by class (jobs needing few shared-memory slots first), each
        class one launch with its own slot count, so light jobs run with more blocks per SM */
@@ -424,7 +425,8 @@ static int pack_job(Pack *pk, const Enum *e, const LutJob *lj, char *err, size_t
             }
         }
         J.first_unit = pk->units;
-        J.units = (uint32_t)((J.words + TC_BATCH_UNIT_WORDS - 1) / TC_BATCH_UNIT_WORDS);
+        J.unit_words = pk->unit_words;
+        J.units = (uint32_t)((J.words + J.unit_words - 1) / J.unit_words);
         pk->units += J.units;
         if ((int)J.slots > pk->slots)
             pk->slots = (int)J.slots;
@@ -503,7 +505,8 @@ static int pack_job(Pack *pk, const Enum *e, const LutJob *lj, char *err, size_t
         }
     }
     J.first_unit = pk->units;
-    J.units = (uint32_t)((J.words + TC_BATCH_UNIT_WORDS - 1) / TC_BATCH_UNIT_WORDS);
+    J.unit_words = pk->unit_words;
+    J.units = (uint32_t)((J.words + J.unit_words - 1) / J.unit_words);
     pk->units += J.units;
     if ((int)slots > pk->slots)
         pk->slots = (int)slots;
@@ -676,6 +679,16 @@ int tc_wave_prepare(TcWave **out, const Enum *const *jobs, int njobs, char *err,
     w->pk.lists.elem = 2;
     w->pk.rpn.elem = sizeof(TcBatchRpn);
     w->pk.vars.elem = 1;
+    /* units of TC_BATCH_UNIT_WORDS, or smaller for a wave too small to give every resident block
+       of the GPU a few units (a served wave of light jobs): its units would run one after another
+       in a few blocks while the rest of the GPU waits */
+    double words = 0;
+    for (int i = 0; i < njobs; i++)
+        words += jobs[i]->a->ninputs < 64 ? ldexp(1.0, (int)jobs[i]->a->ninputs) / 32 : 1e30;
+    double want = 4.0 * (tc_engine.sms > 0 ? tc_engine.sms : 152) * 8;  /* units */
+    w->pk.unit_words = TC_BATCH_UNIT_WORDS;
+    while (w->pk.unit_words > TC_BATCH_UNIT_WORDS_MIN && words / w->pk.unit_words < want)
+        w->pk.unit_words /= 2;
     LutJob *lj = tc_xcalloc((size_t)njobs + 1, sizeof *lj);
     map_jobs(jobs, njobs, lj);
     int ok = 1;

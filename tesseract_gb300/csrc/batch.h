@@ -16,6 +16,7 @@
 
 #define TC_BATCH_BLOCK 128         /* threads per block; one 32-lane word per thread */
 #define TC_BATCH_UNIT_WORDS 4096   /* words per work unit: 131,072 assignments */
+#define TC_BATCH_UNIT_WORDS_MIN 256 /* the smallest unit a small wave is cut into */
 #define TC_BATCH_MAX_SLOTS 255
 #define TC_BATCH_SHOW 16
 
@@ -40,6 +41,8 @@ typedef struct {
     uint32_t vars;           /* verify: first entry (per var: bits, then positions) */
     uint32_t first_unit;     /* its first work unit */
     uint32_t units;
+    uint32_t unit_words;     /* words per work unit (the last may have fewer) */
+    uint32_t pad2;
 } TcBatchJob;
 
 typedef struct {

@@ -1,7 +1,8 @@
 // The batched engine's device side: one persistent kernel runs thousands of enumeration jobs of
 // uneven length, cell count and input width from a device work queue.
 //
-// A work unit is TC_BATCH_UNIT_WORDS consecutive 32-lane words of one job.  Each block takes
+// A work unit is J.unit_words consecutive 32-lane words of one job (TC_BATCH_UNIT_WORDS, or fewer
+// in a wave too small to fill the GPU with units of that size).  Each block takes
 // units from a global counter until none are left; each thread runs one word at a time.  The
 // programs are interpreted from their packed bundles (batch.h) with every cell in shared memory
 // (one 32-bit word per thread and slot, bank-conflict free), RR in a register.  The bundle words
@@ -160,9 +161,8 @@ __global__ void __launch_bounds__(B) tc_batch_kernel(TcBatchDev d)
             return;
         const TcBatchJob J = d.jobs[d.unit_job[unit]];
         const uint16_t *L = d.lists + J.lists;
-        const uint64_t w0 = (uint64_t)(unit - J.first_unit) * TC_BATCH_UNIT_WORDS;
-        const uint64_t w1 = w0 + TC_BATCH_UNIT_WORDS < J.words ? w0 + TC_BATCH_UNIT_WORDS
-                                                               : J.words;
+        const uint64_t w0 = (uint64_t)(unit - J.first_unit) * J.unit_words;
+        const uint64_t w1 = w0 + J.unit_words < J.words ? w0 + J.unit_words : J.words;
         uint32_t recorded = 0;  // meaningful in thread 0
         unsigned long long hits = 0;
         for (uint64_t base = w0; base < w1; base += B) {
