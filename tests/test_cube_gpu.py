@@ -214,3 +214,29 @@ def test_life_512_boards_20_generations(w, h):
             O.life_scalar(want, w, h)
         got = [(int(mem[c][k // 32]) >> (k % 32)) & 1 for c in p.board]
         assert got == list(want), k
+
+
+def every_mask_program(dims: int) -> str:
+    """y<m> = x of machine k ^ m for every mask m < 2^dims: a trie of links (the link for m reads
+    the link for m without its top bit across that bit's dimension), then a copy of each."""
+    lines = [".in x"] + [".out " + " ".join("y%d" % m for m in range(i, min(i + 32, 1 << dims)))
+                         for i in range(0, 1 << dims, 32)]
+    name = {0: "x"}
+    for m in range(1, 1 << dims):
+        top = m.bit_length() - 1
+        name[m] = "l%d" % m
+        lines.append(".link l%d = %s @ %d" % (m, name[m ^ (1 << top)], top))
+    for m in range(1 << dims):
+        lines += ["NAND ZERO", "NAND " + name[m], "NAND ONE", "STO y%d" % m]
+    return "\n".join(lines) + "\n"
+
+
+@pytest.mark.parametrize("dims", [9, 11])
+def test_every_link_mask(dims):
+    """Every lane permutation a link chain can make (tests/test_cube.c:157-172 checks the 512 of
+    one group): lanes inside a word, across a warp's words (shuffles) and, at 2,048 machines,
+    across warps through memory, each machine's y<m> against the reference machine."""
+    p = T.Program.from_asm(every_mask_program(dims))
+    assert p.dims() == dims
+    r = T.check(p, seed=dims, ticks=2)
+    assert r["ok"], r
