@@ -37,3 +37,17 @@ def test_150_random_link_programs():
         if not r["ok"]:
             bad.append((seed, dims, r))
     assert not bad, bad[:3]
+
+
+def test_60_big_random_programs_with_read_only_stores():
+    """The shape of tests/test_cube.c:934-1000: 1,024 to 4,096 machines, half of the links across
+    groups, chains of links, stores to constants, ids and links mixed in (ignored)."""
+    from cube_cases import big_random_program
+    bad = []
+    for k in range(60):
+        p, dims = big_random_program(0xB16 + k)
+        assert p.dims() == dims
+        r = T.check(p, seed=900 + k, ticks=3)
+        if not r["ok"]:
+            bad.append((k, dims, r))
+    assert not bad, bad[:3]
