@@ -52,3 +52,44 @@ def gather_merge(local: dict, group=None) -> dict:
 def run_share(mode, a, b=None, spec=None, ticks=1, rank=0, world=1) -> dict:
     """This rank's share on its GPU (cuda_enum_run with --part rank/world)."""
     return T.enum_run(mode, a, b, spec, ticks, **share(rank, world))
+
+
+class ShardError(RuntimeError):
+    """A share failed on some rank, or a rank's record never came."""
+
+
+def check_records(records) -> list:
+    """The shares' records, or ShardError naming the ranks whose share failed or whose record is
+    not a share result (a corrupted or missing record)."""
+    bad = []
+    for r, rec in enumerate(records):
+        if not isinstance(rec, dict) or "error" in rec:
+            bad.append("rank %d: %s" % (r, rec.get("error") if isinstance(rec, dict) else
+                                        "no share result"))
+        elif not all(k in rec for k in ("space", "tried", "hits", "hit", "ops")):
+            bad.append("rank %d: a record without %s" % (
+                r, ", ".join(k for k in ("space", "tried", "hits", "hit", "ops") if k not in rec)))
+    if bad:
+        raise ShardError("; ".join(bad))
+    return records
+
+
+def gather_merge_checked(local, group=None) -> dict:
+    """gather_merge with failures reported: a rank whose share raised contributes its error
+    instead of a result, and every rank raises ShardError rather than merging a partial total.
+    A rank that never reaches the gather (it died, or hangs) ends the collective with the process
+    group's timeout, which raises on the others."""
+    import torch.distributed as dist
+    parts = [None] * dist.get_world_size(group)
+    dist.all_gather_object(parts, local, group=group)
+    return merge(check_records(parts))
+
+
+def run_share_checked(mode, a, b=None, spec=None, ticks=1, rank=0, world=1, group=None) -> dict:
+    """This rank's share, gathered and merged with every rank's; a failure on any rank raises
+    ShardError on all of them."""
+    try:
+        local = run_share(mode, a, b, spec, ticks, rank, world)
+    except Exception as e:  # the share's failure goes to every rank
+        local = {"error": "%s: %s" % (type(e).__name__, e)}
+    return gather_merge_checked(local, group)

@@ -95,3 +95,62 @@ def test_gpu_shares_over_gloo_merge_to_the_whole(world):
         for r in range(world):
             for k in KEYS:
                 assert results[r][i][k] == whole[k], (i, r, k)
+
+
+def failing_rank_main(rank, world, port, out, how):
+    """Rank 1 fails its share (how = "raises": its enumeration raises; "corrupt": it sends a
+    record without its counts; "absent": it leaves before the gather).  The others must learn
+    of it on the host and raise, not hang or merge a partial total."""
+    import datetime
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world,
+                            timeout=datetime.timedelta(seconds=10))
+    mode, a, b, spec = jobs()[0]
+    try:
+        if rank == 1 and how == "absent":
+            out[rank] = "left"
+            return
+        if rank == 1 and how == "raises":
+            local = {"error": "RuntimeError: the share's device is gone"}
+        elif rank == 1 and how == "corrupt":
+            local = {"space": 1, "hit": []}
+        else:
+            local = O.enum_run(mode, a, b, spec, **shard.share(rank, world))
+        try:
+            shard.gather_merge_checked(local)
+            out[rank] = "merged"
+        except shard.ShardError as e:
+            out[rank] = "ShardError: " + str(e)
+        except RuntimeError as e:  # the collective's timeout or a closed peer
+            out[rank] = "collective failed: " + type(e).__name__
+    finally:
+        try:
+            dist.destroy_process_group()
+        except Exception:
+            pass
+
+
+@pytest.mark.parametrize("how", ["raises", "corrupt", "absent"])
+def test_a_failed_share_is_reported_on_every_rank(how):
+    world, port = 3, free_port()
+    with mp.get_context("spawn").Manager() as mgr:
+        out = mgr.dict()
+        mp.spawn(failing_rank_main, args=(world, port, out, how), nprocs=world, join=True)
+        results = dict(out)
+    others = [results[r] for r in (0, 2)]
+    if how == "absent":
+        assert results[1] == "left"
+        assert all(x.startswith("collective failed") or x.startswith("ShardError") for x in others), others
+    else:
+        assert all(x.startswith("ShardError: rank 1") for x in others + [results[1]]), results
+
+
+def test_check_records_names_the_bad_ranks():
+    good = {"space": 8, "tried": 8, "hits": 0, "hit": [], "ops": 1}
+    assert shard.check_records([good, good]) == [good, good]
+    with pytest.raises(shard.ShardError, match="rank 1: boom"):
+        shard.check_records([good, {"error": "boom"}])
+    with pytest.raises(shard.ShardError, match="rank 0: a record without tried"):
+        shard.check_records([{"space": 8, "hits": 0, "hit": [], "ops": 1}, good])
+    with pytest.raises(shard.ShardError, match="rank 1: no share result"):
+        shard.check_records([good, None])
