@@ -202,3 +202,16 @@ def test_recomputing_kernels_compile(which):
                                 "-Xptxas", "-O2", "-c", path, "-o", path + ".o"],
                                capture_output=True, text=True, timeout=600)
             assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_recomputing_never_adds_kernels():
+    """On random link programs over 1,024 to 8,192 machines, recomputing far reads only ever
+    removes cuts: never more kernels than the plain rule."""
+    fewer = 0
+    for seed in range(40):
+        text = random_link_program(500 + seed, 10 + seed % 4, 20, 16, 300)
+        p = T.Program.from_asm(text)
+        with_rc, plain = cube_source(p, recompute=True)[0], cube_source(p, recompute=False)[0]
+        assert with_rc <= plain, seed
+        fewer += with_rc < plain
+    assert fewer > 0  # the programs do exercise it
