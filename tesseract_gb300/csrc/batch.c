@@ -913,8 +913,8 @@ void tc_wave_free(TcWave *w)
    route: both engines enumerate the whole job. */
 
 int    tc_serve_batch(const Enum *const *jobs, int njobs, const CudaServeOpts *opts,
-                      const signed char *route, double *finish, EnumResult *results,
-                      int *engine_used, char *err, size_t errlen);
+                      const signed char *route, int first_wave, double *finish,
+                      EnumResult *results, int *engine_used, char *err, size_t errlen);
 double tc_route_compile_s(const Enum *e, double instrs);
 extern double tc_serve_last_wave_at, tc_serve_last_compile_busy, tc_serve_last_compile_load,
     tc_serve_last_loop_end;
@@ -1016,7 +1016,9 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
     o.compile_threads = any ? threads : -1;
     o.compiled_slots = 8;
     o.route = any ? CUDA_SERVE_AUTO : CUDA_SERVE_INTERPRETER;
-    int ok = tc_serve_batch(order, njobs, &o, route, finish, res, engine, err, errlen);
+    /* a first wave of a sixteenth: the GPU, and the held compiles, start once it is packed */
+    int first = njobs >= 1024 ? njobs / 16 : 0;
+    int ok = tc_serve_batch(order, njobs, &o, route, first, finish, res, engine, err, errlen);
     double wall = tc_now() - t0;
     if (ok) {
         for (int k = 0; k < njobs; k++) {

@@ -201,8 +201,8 @@ static void nap(void)
    wave (tc_serve_batch) has the GPU nearly to itself. */
 static int serve(const Enum *const *jobs, const double *arrival, int njobs,
                  const CudaServeOpts *opts, double rate_interp, const signed char *route,
-                 double *start, double *finish, EnumResult *results, int *engine_used, char *err,
-                 size_t errlen);
+                 int first_wave, double *start, double *finish, EnumResult *results,
+                 int *engine_used, char *err, size_t errlen);
 
 /* when the last call's first interpreter wave went out, in seconds from its start (-1: none) */
 double tc_serve_last_wave_at = -1;
@@ -215,19 +215,19 @@ int cuda_serve_run(const Enum *const *jobs, const double *arrival, int njobs,
                    const CudaServeOpts *opts, double *start, double *finish, EnumResult *results,
                    int *engine_used, char *err, size_t errlen)
 {
-    return serve(jobs, arrival, njobs, opts, RATE_INTERP, NULL, start, finish, results,
+    return serve(jobs, arrival, njobs, opts, RATE_INTERP, NULL, 0, start, finish, results,
                  engine_used, err, errlen);
 }
 
 /* Every job arriving at once with its engine chosen by the caller (route[i]: 1 generated code,
    0 the interpreter). */
 int tc_serve_batch(const Enum *const *jobs, int njobs, const CudaServeOpts *opts,
-                   const signed char *route, double *finish, EnumResult *results,
+                   const signed char *route, int first_wave, double *finish, EnumResult *results,
                    int *engine_used, char *err, size_t errlen)
 {
     double *zero = tc_xcalloc((size_t)njobs, sizeof *zero);
     double *start = tc_xcalloc((size_t)njobs, sizeof *start);
-    int ok = serve(jobs, zero, njobs, opts, RATE_INTERP, route, start, finish, results,
+    int ok = serve(jobs, zero, njobs, opts, RATE_INTERP, route, first_wave, start, finish, results,
                    engine_used, err, errlen);
     free(zero);
     free(start);
@@ -236,8 +236,8 @@ int tc_serve_batch(const Enum *const *jobs, int njobs, const CudaServeOpts *opts
 
 static int serve(const Enum *const *jobs, const double *arrival, int njobs,
                  const CudaServeOpts *opts, double rate_interp, const signed char *route,
-                 double *start, double *finish, EnumResult *results, int *engine_used, char *err,
-                 size_t errlen)
+                 int first_wave, double *start, double *finish, EnumResult *results,
+                 int *engine_used, char *err, size_t errlen)
 {
     if (njobs <= 0)
         return 1;
@@ -428,7 +428,9 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
         }
         if (s >= 0 && !pending && rhead < nready && inflight < o.max_inflight_jobs) {
             int n = 0;
-            while (rhead + n < nready && n < o.max_wave_jobs && inflight + n < o.max_inflight_jobs)
+            /* a batch's first wave is smaller: the GPU (and the held compiles) start sooner */
+            int cap = wave_launched_at < 0 && first_wave > 0 ? first_wave : o.max_wave_jobs;
+            while (rhead + n < nready && n < cap && inflight + n < o.max_inflight_jobs)
                 n++;
             for (int i = 0; i < n; i++)
                 wj[i] = jobs[ready[rhead + i]];
