@@ -162,7 +162,8 @@ int  cuda_device_info(char *buf, size_t len);
    as the code generator laid it out: LUTs run every step, LUTs run once per stretch of
    stretch_steps steps, and the bit-sliced output compare (compare_ops, -1 when the spec is
    evaluated per lane); logic_ops_per_word = luts_per_step + luts_per_stretch / stretch_steps +
-   compare_ops, or 0 when not counted.
+   compare_ops, or 0 when not counted.  ptx = 1 when the kernel was built from PTX that the engine
+   writes directly (the quick-start build of an equivalence or search job), 0 for CUDA C.
    Neither has a counterpart in the reference, whose engines run on the CPU. */
 typedef struct {
     double   kernel_ms;
@@ -172,6 +173,7 @@ typedef struct {
     int      cached;
     int      luts_per_step, luts_per_stretch, stretch_steps, compare_ops;
     double   logic_ops_per_word;
+    int      ptx;
 } CudaLaunchStats;
 int  cuda_last_launch(CudaLaunchStats *s);
 int  cuda_lop3_peak(double *ops_per_second, double *seconds, char *err, size_t errlen);

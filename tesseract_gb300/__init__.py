@@ -104,7 +104,7 @@ class LaunchStats(C.Structure):
                 ("grid", C.c_uint), ("block", C.c_uint), ("compile_seconds", C.c_double),
                 ("cached", C.c_int), ("luts_per_step", C.c_int), ("luts_per_stretch", C.c_int),
                 ("stretch_steps", C.c_int), ("compare_ops", C.c_int),
-                ("logic_ops_per_word", C.c_double)]
+                ("logic_ops_per_word", C.c_double), ("ptx", C.c_int)]
 
 
 _lib = None
@@ -678,6 +678,51 @@ def codegen_enum_source(mode, a: Program, b: Program | None = None, spec: Spec |
                         ticks=1) -> str:
     """The CUDA C the engine generates for an enumeration (for inspection and host tests)."""
     return _codegen(mode, a, b, spec, ticks)
+
+
+def codegen_ptx_source(mode, a: Program, b: Program | None = None, spec: Spec | None = None,
+                       target: str = "sm_103a") -> str:
+    """The PTX the engine writes directly for a quick-start build of an equivalence or search job
+    (ptxgen.c), for the .target given (for inspection and ptxas tests)."""
+    return codegen_ptx_module([(mode, a, b, spec)], target)
+
+
+def codegen_ptx_module(jobs, target: str = "sm_103a") -> str:
+    """The PTX module of several (mode, a, b, spec) jobs built together: kernels tc_enum_0 .. ."""
+    L = lib()
+    fn = L.tc_codegen_ptx_for
+    fn.restype = C.c_void_p
+    fn.argtypes = [C.POINTER(C.POINTER(EnumStruct)), C.c_int, C.c_char_p,
+                   C.POINTER(C.c_size_t), C.c_char_p, C.c_size_t]
+    es = [make_enum(*j) for j in jobs]
+    arr = (C.POINTER(EnumStruct) * len(es))(*[C.pointer(e) for e in es])
+    n, err = C.c_size_t(), _err()
+    p = fn(arr, len(es), target.encode(), C.byref(n), err, len(err))
+    if not p:
+        raise EngineError(err.value.decode())
+    s = C.string_at(p, n.value).decode()
+    L.tc_free.argtypes = [C.c_void_p]
+    L.tc_free(p)
+    return s
+
+
+def set_enum_ptx(on: bool) -> bool:
+    """Switches the quick-start builds of equivalence and search jobs between PTX written directly
+    (on, the default) and CUDA C through NVRTC; returns the previous setting."""
+    v = C.c_int.in_dll(lib(), "tc_enum_ptx")
+    old = bool(v.value)
+    v.value = 1 if on else 0
+    return old
+
+
+def set_enum_quick(on: bool) -> bool:
+    """Makes enum_run build and run quick-start kernels, as a batch's compiled jobs are built (PTX
+    written directly for equivalence and search jobs), even where the optimised kernel of the same
+    job is cached; returns the previous setting."""
+    v = C.c_int.in_dll(lib(), "tc_enum_run_fast")
+    old = bool(v.value)
+    v.value = 2 if on else 0
+    return old
 
 
 def _codegen(mode, a, b, spec, ticks):

@@ -33,7 +33,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # overrides it, and the step is skipped where the tree is absent (the GPU machine).
 REFERENCE = os.environ.get("TESSERACT_REFERENCE", "/root/reference")
 
-HOST_C = ["program", "asm", "spec", "gen", "lutmap", "codegen", "engine", "cube", "ref_host", "batch", "tester",
+HOST_C = ["program", "asm", "spec", "gen", "lutmap", "codegen", "ptxgen", "engine", "cube", "ref_host", "batch", "tester",
           "serve", "super_host", "cli_support"]
 CUDA_SRC = ["peak_kernels", "batch_kernels", "super_kernels", "enum_static", "tester_kernels"]
 CFLAGS = ["-std=c11", "-O2", "-g", "-Wall", "-Wextra", "-fPIC", "-D_GNU_SOURCE",
@@ -100,7 +100,7 @@ def build(verbose: bool = False, reference: bool = True) -> dict:
     cuda_lib = os.path.join(CUDA, "lib64")
     if _stale(LIB, objs):
         _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs +
-             ["-L" + cuda_lib, "-lnvrtc", "-Xlinker", "-rpath," + cuda_lib, "-lpthread"], verbose)
+             ["-L" + cuda_lib, "-lnvrtc", "-lnvJitLink", "-Xlinker", "-rpath," + cuda_lib, "-lpthread"], verbose)
     cli_src = os.path.join(CSRC, "cli.c")
     if os.path.exists(cli_src) and _stale(CLI, [cli_src, LIB] + headers):
         _run(["gcc"] + CFLAGS + [cli_src, "-o", CLI, "-L" + PKG, "-ltesseract_gb300",

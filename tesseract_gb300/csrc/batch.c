@@ -919,7 +919,7 @@ double tc_route_compile_s(const Enum *e, double instrs);
 extern double tc_serve_last_wave_at, tc_serve_last_compile_busy, tc_serve_last_compile_load,
     tc_serve_last_loop_end;
 extern int    tc_serve_last_routed, tc_serve_last_taken_back;
-double tc_route_compiled_s(double work);
+double tc_route_compiled_s(const Enum *e, double work);
 
 /* The interpreter's rate on a batch with most of the GPU (1.39e14 NAND/STO lane-ops/s measured
    on the 4,096-job batch alone; host packing and a 90 % share of the blocks beside compiled
@@ -935,7 +935,7 @@ int tc_batch_threads = 0;
 double tc_batch_plan_share = 0.5;
 
 typedef struct {
-    double work, instrs, compile_s, gain;
+    double work, instrs, compile_s, compiled_s, gain;
     int    i;
 } Planned;
 
@@ -955,7 +955,7 @@ static void plan(Planned *p, int n, int threads, signed char *route)
     for (int k = 0; k < n; k++)
         interp += p[k].work / BATCH_RATE_INTERP;
     for (int k = 0; k < n; k++) {
-        double saved = p[k].work / BATCH_RATE_INTERP - tc_route_compiled_s(p[k].work);
+        double saved = p[k].work / BATCH_RATE_INTERP - p[k].compiled_s;
         double c = p[k].compile_s / threads;
         /* half the interpreter's time: compiles start once its first wave is packed and run
            slower than modelled when every core compiles; jobs still queued when the
@@ -990,7 +990,8 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
                     p[i].instrs;
         /* a job whose GPU time saved would not pay for a launch stays on the interpreter
            whatever the cache holds: no need to look (the look hashes both programs) */
-        int worth = p[i].work / BATCH_RATE_INTERP - tc_route_compiled_s(p[i].work) > 0;
+        p[i].compiled_s = tc_route_compiled_s(e, p[i].work);
+        int worth = p[i].work / BATCH_RATE_INTERP - p[i].compiled_s > 0;
         p[i].compile_s = e->parts == 1 && worth ? tc_route_compile_s(e, p[i].instrs) : 1e30;
         p[i].gain = p[i].work / (p[i].compile_s > 0 ? p[i].compile_s : 1e-9);
     }

@@ -56,6 +56,15 @@ typedef struct {
    enumeration index y stands for). */
 char *tc_codegen_enum(const TcGenEnum *g, size_t *len);
 
+/* Can the PTX writer (ptxgen.c) make this job's kernel?  Equivalence and search jobs of one tick,
+   LUT-mapped. */
+int   tc_ptx_enum_ok(const TcGenEnum *g);
+/* PTX for the enumeration kernels of n such jobs (malloc'd; *len gets its length): one entry
+   `tc_enum` for n = 1, else tc_enum_0 .. tc_enum_<n-1>, for `.target` target ("sm_103a"), each
+   taking TcEnumArgs as the CUDA C kernel does.  work[k], when work is not NULL, gets kernel k's
+   work per word. */
+char *tc_ptx_enum(TcGenEnum *const *g, int n, const char *target, TcGenWork *work, size_t *len);
+
 /* CUDA C for the truth-table kernel `tc_table` of a program without id or link cells. */
 char *tc_codegen_table(const Program *p, unsigned ticks, int block, size_t *len);
 

@@ -5,6 +5,7 @@
    modules are compiled for the device's own architecture (sm_103a on GB300) and kept for the
    life of the process, keyed by the full text of the generated source. */
 #include <cuda_runtime_api.h>
+#include <nvJitLink.h>
 #include <nvrtc.h>
 #include <pthread.h>
 #include <stdarg.h>
@@ -115,6 +116,7 @@ int cuda_last_launch(CudaLaunchStats *s)
                                 ? m->luts_per_step + (double)m->luts_per_stretch /
                                   m->stretch_steps + m->compare_ops
                                 : 0;
+    s->ptx = m->ptx;
     return tc_engine.ready;
 }
 
@@ -231,6 +233,52 @@ int tc_module_build(const char *src, size_t len, const char *extra_opt, TcBuilt 
     b->info.cubin_bytes = b->cubin_len;
     snprintf(b->info.log, sizeof b->info.log, "%s", log);
     free(log);
+    return 1;
+}
+
+int tc_module_build_ptx(const char *ptx, size_t len, TcBuilt *b, char *err, size_t errlen)
+{
+    memset(b, 0, sizeof *b);
+    b->info.hash = text_hash(ptx, len);
+    TcModule m;
+    if (cache_find(ptx, len, b->info.hash, &m)) {
+        b->cached = 1;
+        return 1;
+    }
+    double t0 = tc_now();
+    char arch[32];
+    snprintf(arch, sizeof arch, "-arch=sm_%d%da", tc_engine.cc_major, tc_engine.cc_minor);
+    const char *opts[] = {arch, tc_enum_ptx_opt ? "-O3" : "-O0"};
+    nvJitLinkHandle h;
+    nvJitLinkResult r = nvJitLinkCreate(&h, 2, opts);
+    if (r != NVJITLINK_SUCCESS)
+        return tc_fail(err, errlen, "nvJitLinkCreate: error %d", (int)r);
+    r = nvJitLinkAddData(h, NVJITLINK_INPUT_PTX, ptx, len, "tesseract_gen.ptx");
+    if (r == NVJITLINK_SUCCESS)
+        r = nvJitLinkComplete(h);
+    if (r == NVJITLINK_SUCCESS)
+        r = nvJitLinkGetLinkedCubinSize(h, &b->cubin_len);
+    if (r == NVJITLINK_SUCCESS) {
+        b->cubin = tc_xmalloc(b->cubin_len + 1);
+        r = nvJitLinkGetLinkedCubin(h, b->cubin);
+    }
+    if (r != NVJITLINK_SUCCESS) {
+        size_t n = 0;
+        char log[512] = "";
+        if (nvJitLinkGetErrorLogSize(h, &n) == NVJITLINK_SUCCESS && n > 0) {
+            char *full = tc_xmalloc(n + 1);
+            if (nvJitLinkGetErrorLog(h, full) == NVJITLINK_SUCCESS)
+                snprintf(log, sizeof log, "%s", full);
+            free(full);
+        }
+        nvJitLinkDestroy(&h);
+        tc_built_free(b);
+        return tc_fail(err, errlen, "nvJitLink on generated PTX: error %d: %s", (int)r, log);
+    }
+    nvJitLinkDestroy(&h);
+    b->info.ptx = 1;
+    b->info.compile_seconds = tc_now() - t0;
+    b->info.cubin_bytes = b->cubin_len;
     return 1;
 }
 
@@ -565,6 +613,31 @@ char *tc_codegen_enum_for(const Enum *e, size_t *len, char *err, size_t errlen)
     return src;
 }
 
+/* The PTX module of n jobs as a quick-start build writes it (for inspection and ptxas tests) */
+char *tc_codegen_ptx_for(const Enum *const *e, int n, const char *target, size_t *len, char *err,
+                         size_t errlen)
+{
+    if (n < 1 || n > TC_MAX_KERNELS) {
+        tc_fail(err, errlen, "a module of %d jobs: 1 to %d", n, TC_MAX_KERNELS);
+        return NULL;
+    }
+    EnumPlan pl[TC_MAX_KERNELS];
+    TcGenEnum *g[TC_MAX_KERNELS];
+    int np = 0, ok = 1;
+    for (int i = 0; ok && i < n; i++) {
+        ok = plan_enum(e[i], &pl[i], err, errlen);
+        if (ok) {
+            g[np++] = &pl[i].g;
+            if (!tc_ptx_enum_ok(g[i]))
+                ok = tc_fail(err, errlen,
+                             "the PTX writer takes equivalence and search jobs of one tick");
+        }
+    }
+    char *src = ok ? tc_ptx_enum(g, n, target, NULL, len) : NULL;
+    for (int i = 0; i < np; i++)
+        plan_free(&pl[i]);
+    return src;
+}
 
 /* ---- the autotuner's choices ---------------------------------------------------------------
 
@@ -617,10 +690,24 @@ static void remember_tuning(uint64_t k1, uint64_t k2, int block, int step_bits)
    the option, so the two builds are cached apart. */
 #define FAST_NVRTC_OPT "--ptxas-options=-O0"
 
-/* The quick-start build's key from the optimised build's */
-static void fast_key(uint64_t *k2)
+int tc_enum_ptx = 1;
+
+/* The quick-start build's key from the optimised build's: NVRTC's and the PTX writer's builds are
+   cached apart (the same job's two kernels give the same results, but a test or a measurement may
+   want the one it asked for) */
+int tc_enum_ptx_opt = 0;
+
+int tc_enum_quick_ptx(const Enum *e)
 {
-    *k2 ^= 0x9E3779B97F4A7C15ull;
+    return tc_enum_ptx && (e->mode == EN_EQUIV || e->mode == EN_SEARCH) && e->ticks == 1 &&
+           e->a && e->a->ninputs >= 1 && e->a->ninputs <= 64;
+}
+
+static void fast_key(const TcGenEnum *g, uint64_t *k2)
+{
+    *k2 ^= tc_enum_ptx && tc_ptx_enum_ok(g)
+               ? 0xC2B2AE3D27D4EB4Full + (uint64_t)tc_enum_ptx_opt
+               : 0x9E3779B97F4A7C15ull;
 }
 
 /* The loaded kernel of an enumeration, only when an earlier run of the same job compiled and
@@ -649,7 +736,7 @@ int tc_enum_cached(const Enum *e, int fast, TcModule *m, char *err, size_t errle
     enum_key(&pl.g, &k1, &k2);
     if (lookup_enum(k1, k2, m))
         return 1;
-    fast_key(&k2);
+    fast_key(&pl.g, &k2);
     if (fast && lookup_enum(k1, k2, m))
         return 1;
     return tc_fail(err, errlen, "cuda_enum_run_static: this job's kernel is not loaded; run the "
@@ -741,61 +828,90 @@ static char *group_source(char **srcs, const size_t *lens, int n, size_t *len)
 
 /* The kernels for the plans in g[0..n): from the cache (m[i] filled, pend[i] NULL), else
    generated and compiled together (pend[i]: the group's build, for enum_module_load); `fast`
-   compiles them for a quick start (FAST_NVRTC_OPT), unless the optimised build is cached. */
+   compiles them for a quick start (FAST_NVRTC_OPT, or PTX written directly for the jobs the PTX
+   writer takes), unless the optimised build is cached (fast = 1) or always (fast = 2).  The jobs of a call that need building
+   form at most two groups: one NVRTC program and one PTX module. */
 static int enum_modules_build(TcGenEnum *const *g, int n, int fast, TcModule *m,
                               TcEnumPending **pend, int *kidx, char *err, size_t errlen)
 {
-    TcEnumPending *p = NULL;
-    char *srcs[TC_MAX_KERNELS];
-    size_t lens[TC_MAX_KERNELS];
-    int who[TC_MAX_KERNELS], nb = 0;
+    TcEnumPending *p[2] = {NULL, NULL};  /* [0] NVRTC, [1] PTX */
+    TcGenEnum *gk[2][TC_MAX_KERNELS];
+    int who[2][TC_MAX_KERNELS], nb[2] = {0, 0};
     for (int i = 0; i < n; i++) {
         pend[i] = NULL;
         kidx[i] = 0;
         uint64_t k1, k2;
         enum_key(g[i], &k1, &k2);
-        if (lookup_enum(k1, k2, &m[i]))
+        if (fast < 2 && lookup_enum(k1, k2, &m[i]))
             continue;
         if (fast)
-            fast_key(&k2);
+            fast_key(g[i], &k2);
         if (fast && lookup_enum(k1, k2, &m[i]))
             continue;
-        if (!p)
-            p = tc_xcalloc(1, sizeof *p);
-        int k = nb++;
-        g[i]->work = &p->k[k].work;
-        srcs[k] = tc_codegen_enum(g[i], &lens[k]);
-        g[i]->work = NULL;
-        if (fast) {
-            static const char mark[] = "// built with " FAST_NVRTC_OPT "\n";
-            char *s2 = tc_xmalloc(lens[k] + sizeof mark);
-            memcpy(s2, mark, sizeof mark - 1);
-            memcpy(s2 + sizeof mark - 1, srcs[k], lens[k] + 1);
-            free(srcs[k]);
-            srcs[k] = s2;
-            lens[k] += sizeof mark - 1;
-        }
-        p->k[k].k1 = k1;
-        p->k[k].k2 = k2;
-        p->k[k].block = g[i]->block;
-        who[k] = i;
+        const int kind = fast && tc_enum_ptx && tc_ptx_enum_ok(g[i]);
+        if (!p[kind])
+            p[kind] = tc_xcalloc(1, sizeof *p[kind]);
+        int k = nb[kind]++;
+        p[kind]->k[k].k1 = k1;
+        p[kind]->k[k].k2 = k2;
+        p[kind]->k[k].block = g[i]->block;
+        gk[kind][k] = g[i];
+        who[kind][k] = i;
         kidx[i] = k;
     }
-    if (!p)
-        return 1;
-    p->n = nb;
-    p->src = group_source(srcs, lens, nb, &p->len);
-    for (int k = 0; k < nb; k++)
-        free(srcs[k]);
-    if (!tc_module_build(p->src, p->len, fast ? FAST_NVRTC_OPT : NULL, &p->b, err, errlen)) {
-        free(p->src);
-        free(p);
-        return 0;
+    int ok = 1;
+    if (p[0]) {
+        char *srcs[TC_MAX_KERNELS];
+        size_t lens[TC_MAX_KERNELS];
+        for (int k = 0; k < nb[0]; k++) {
+            gk[0][k]->work = &p[0]->k[k].work;
+            srcs[k] = tc_codegen_enum(gk[0][k], &lens[k]);
+            gk[0][k]->work = NULL;
+            if (fast) {
+                static const char mark[] = "// built with " FAST_NVRTC_OPT "\n";
+                char *s2 = tc_xmalloc(lens[k] + sizeof mark);
+                memcpy(s2, mark, sizeof mark - 1);
+                memcpy(s2 + sizeof mark - 1, srcs[k], lens[k] + 1);
+                free(srcs[k]);
+                srcs[k] = s2;
+                lens[k] += sizeof mark - 1;
+            }
+        }
+        p[0]->n = nb[0];
+        p[0]->src = group_source(srcs, lens, nb[0], &p[0]->len);
+        for (int k = 0; k < nb[0]; k++)
+            free(srcs[k]);
+        ok = tc_module_build(p[0]->src, p[0]->len, fast ? FAST_NVRTC_OPT : NULL, &p[0]->b, err,
+                             errlen);
     }
-    p->refs = nb;
-    for (int k = 0; k < nb; k++)
-        pend[who[k]] = p;
-    return 1;
+    if (ok && p[1]) {
+        char target[16];
+        TcGenWork work[TC_MAX_KERNELS];
+        snprintf(target, sizeof target, "sm_%d%da", tc_engine.cc_major, tc_engine.cc_minor);
+        p[1]->n = nb[1];
+        char *ptx = tc_ptx_enum(gk[1], nb[1], target, work, &p[1]->len);
+        /* the text is the module cache's key: it records the optimisation level */
+        p[1]->src = tc_xmalloc(p[1]->len + 32);
+        p[1]->len = (size_t)sprintf(p[1]->src, "// ptxas -O%d\n%s", tc_enum_ptx_opt ? 3 : 0, ptx);
+        free(ptx);
+        for (int k = 0; k < nb[1]; k++)
+            p[1]->k[k].work = work[k];
+        ok = tc_module_build_ptx(p[1]->src, p[1]->len, &p[1]->b, err, errlen);
+    }
+    for (int kind = 0; kind < 2; kind++) {
+        if (!p[kind])
+            continue;
+        if (!ok) {
+            tc_built_free(&p[kind]->b);
+            free(p[kind]->src);
+            free(p[kind]);
+            continue;
+        }
+        p[kind]->refs = nb[kind];
+        for (int k = 0; k < nb[kind]; k++)
+            pend[who[kind][k]] = p[kind];
+    }
+    return ok;
 }
 
 /* Job i's kernel of a built group, loading the group's module first if no job of it has (the
@@ -1075,11 +1191,16 @@ static int run_prepared(const TcEnumJob *jp, EnumResult *r, char *err, size_t er
     return 1;
 }
 
+/* 1: cuda_enum_run builds quick-start kernels, as a batch does, unless the optimised kernel is
+   cached; 2: always (tests of those builds) */
+int tc_enum_run_fast = 0;
+
 int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)
 {
     memset(r, 0, sizeof *r);
     TcEnumJob j;
-    return tc_enum_job_prepare(e, &j, 0, err, errlen) && run_prepared(&j, r, err, errlen);
+    return tc_enum_job_prepare(e, &j, tc_enum_run_fast, err, errlen) &&
+           run_prepared(&j, r, err, errlen);
 }
 
 /* ---- the autotuner --------------------------------------------------------------------------- */

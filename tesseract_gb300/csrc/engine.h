@@ -29,6 +29,7 @@ typedef struct {
        (TcGenWork); stretch_steps = 0 for other kernels */
     int      luts_per_step, luts_per_stretch, stretch_steps, compare_ops;
     int      block;  /* generated enumeration kernels: the threads per block they were made for */
+    int      ptx;    /* built from PTX written directly (tc_module_build_ptx) */
     char     log[2048];
 } TcModInfo;
 
@@ -82,6 +83,19 @@ int    tc_module_build(const char *src, size_t len, const char *extra_opt, TcBui
                        size_t errlen);
 int    tc_module_load(const char *src, size_t len, TcBuilt *b, const char *const *kernels,
                       int nkernels, TcModule *out, char *err, size_t errlen);
+/* tc_module_build for PTX text (ptxas through nvJitLink, without optimisation); the module cache
+   is keyed by the text as for CUDA C */
+int    tc_module_build_ptx(const char *ptx, size_t len, TcBuilt *b, char *err, size_t errlen);
+/* 1 (default): quick-start builds of equivalence and search jobs write PTX directly (ptxgen.c)
+   instead of CUDA C for NVRTC */
+extern int tc_enum_ptx;
+/* ptxas optimisation of those builds: 0 (default) or 3 */
+extern int tc_enum_ptx_opt;
+/* Is job e's quick-start build PTX written directly? */
+int tc_enum_quick_ptx(const Enum *e);
+/* 1: cuda_enum_run builds quick-start kernels unless the optimised one is cached, 2: always
+   (default 0: the optimised build) */
+extern int tc_enum_run_fast;
 void   tc_built_free(TcBuilt *b);
 int    tc_enum_prepare(const Enum *e, int *in_map, int *out_map, char *err, size_t errlen);
 /* The loaded kernel of a job that an earlier enumeration compiled (with `fast`, its quick-start

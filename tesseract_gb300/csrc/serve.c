@@ -57,6 +57,13 @@ void   tc_wave_pool_trim(void);
 #define RATE_COMPILED_FAST 1.7e15
 #define COMPILE_S0_FAST 0.053
 #define COMPILE_S_PER_INSTR_FAST 8.3e-6
+/* A batch's equivalence and search jobs are built from PTX written directly (ptxgen.c): measured
+   on the GB300 over 78 jobs of the 4,096-job batch, 0.0153 s + 2.63 us per NAND/STO instruction
+   (ptxas without optimisation through nvJitLink, against 0.051 s + 9.2 us through NVRTC), the
+   kernels at about 1.1e15 lane-ops/s on the heavier jobs. */
+#define RATE_COMPILED_PTX 1.1e15
+#define COMPILE_S0_PTX 0.0153
+#define COMPILE_S_PER_INSTR_PTX 2.63e-6
 /* A job whose kernel is already compiled (the cache is keyed by what the code generator reads)
    costs only its launch and the polling of its event: about this many seconds. */
 #define LAUNCH_S 3.0e-5
@@ -180,14 +187,15 @@ double tc_route_compile_s(const Enum *e, double instrs)
 {
     TcModule m;
     char why[8];
-    return tc_enum_cached(e, 1, &m, why, sizeof why)
-               ? 0.0
-               : COMPILE_S0_FAST + COMPILE_S_PER_INSTR_FAST * instrs;
+    if (tc_enum_cached(e, 1, &m, why, sizeof why))
+        return 0.0;
+    return tc_enum_quick_ptx(e) ? COMPILE_S0_PTX + COMPILE_S_PER_INSTR_PTX * instrs
+                                : COMPILE_S0_FAST + COMPILE_S_PER_INSTR_FAST * instrs;
 }
 
-double tc_route_compiled_s(double work)
+double tc_route_compiled_s(const Enum *e, double work)
 {
-    return work / RATE_COMPILED_FAST + LAUNCH_S;
+    return work / (tc_enum_quick_ptx(e) ? RATE_COMPILED_PTX : RATE_COMPILED_FAST) + LAUNCH_S;
 }
 
 static void nap(void)
