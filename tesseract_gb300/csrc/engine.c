@@ -236,7 +236,8 @@ int tc_module_build(const char *src, size_t len, const char *extra_opt, TcBuilt 
     return 1;
 }
 
-int tc_module_build_ptx(const char *ptx, size_t len, TcBuilt *b, char *err, size_t errlen)
+int tc_module_build_ptx(const char *ptx, size_t len, int opt, TcBuilt *b, char *err,
+                        size_t errlen)
 {
     memset(b, 0, sizeof *b);
     b->info.hash = text_hash(ptx, len);
@@ -248,7 +249,7 @@ int tc_module_build_ptx(const char *ptx, size_t len, TcBuilt *b, char *err, size
     double t0 = tc_now();
     char arch[32];
     snprintf(arch, sizeof arch, "-arch=sm_%d%da", tc_engine.cc_major, tc_engine.cc_minor);
-    const char *opts[] = {arch, tc_enum_ptx_opt ? "-O3" : "-O0"};
+    const char *opts[] = {arch, opt ? "-O3" : "-O0"};
     nvJitLinkHandle h;
     nvJitLinkResult r = nvJitLinkCreate(&h, 2, opts);
     if (r != NVJITLINK_SUCCESS)
@@ -691,10 +692,6 @@ static void remember_tuning(uint64_t k1, uint64_t k2, int block, int step_bits)
 #define FAST_NVRTC_OPT "--ptxas-options=-O0"
 
 int tc_enum_ptx = 1;
-
-/* The quick-start build's key from the optimised build's: NVRTC's and the PTX writer's builds are
-   cached apart (the same job's two kernels give the same results, but a test or a measurement may
-   want the one it asked for) */
 int tc_enum_ptx_opt = 0;
 
 int tc_enum_quick_ptx(const Enum *e)
@@ -703,15 +700,38 @@ int tc_enum_quick_ptx(const Enum *e)
            e->a && e->a->ninputs >= 1 && e->a->ninputs <= 64;
 }
 
-static void fast_key(const TcGenEnum *g, uint64_t *k2)
+/* Build modes (the `fast` argument of the build and lookup functions):
+     TC_BUILD_OPT      NVRTC with ptxas -O2, the kernel cuda_enum_run keeps;
+     TC_BUILD_QUICK    a quick start: PTX written directly (ptxas at tc_enum_ptx_opt) for the jobs
+                       the PTX writer takes, NVRTC with FAST_NVRTC_OPT for the rest; an optimised
+                       build in the cache is taken instead (a batch's compiled jobs);
+     TC_BUILD_QUICK_ONLY  the same, but never the optimised build (tests of quick builds);
+     TC_BUILD_SERVE    PTX written directly with ptxas -O3 for the jobs the PTX writer takes (the
+                       optimised build's speed at a third of NVRTC's compile time), the optimised
+                       NVRTC build for the rest (a served stream's compiled jobs). */
+static int is_quick(const TcGenEnum *g, int fast)
+{
+    return fast == TC_BUILD_QUICK || fast == TC_BUILD_QUICK_ONLY ||
+           (fast == TC_BUILD_SERVE && tc_enum_ptx && tc_ptx_enum_ok(g));
+}
+
+static int ptx_opt(int fast)
+{
+    return fast == TC_BUILD_SERVE ? 3 : tc_enum_ptx_opt ? 3 : 0;
+}
+
+/* A quick build's key from the optimised build's: NVRTC's and the PTX writer's builds, and the
+   latter at each ptxas level, are cached apart (they give the same results, but a test or a
+   measurement may want the one it asked for) */
+static void fast_key(const TcGenEnum *g, int fast, uint64_t *k2)
 {
     *k2 ^= tc_enum_ptx && tc_ptx_enum_ok(g)
-               ? 0xC2B2AE3D27D4EB4Full + (uint64_t)tc_enum_ptx_opt
+               ? 0xC2B2AE3D27D4EB4Full + (uint64_t)ptx_opt(fast)
                : 0x9E3779B97F4A7C15ull;
 }
 
 /* The loaded kernel of an enumeration, only when an earlier run of the same job compiled and
-   loaded it (the optimised build; with `fast`, the quick-start build too): no code generation, no
+   loaded it (the optimised build, or the quick build of mode `fast`): no code generation, no
    compilation, no module load.  For cuda_enum_run_static, whose callers cannot allocate, and the
    serving loop's routing. */
 int tc_enum_cached(const Enum *e, int fast, TcModule *m, char *err, size_t errlen)
@@ -736,9 +756,11 @@ int tc_enum_cached(const Enum *e, int fast, TcModule *m, char *err, size_t errle
     enum_key(&pl.g, &k1, &k2);
     if (lookup_enum(k1, k2, m))
         return 1;
-    fast_key(&pl.g, &k2);
-    if (fast && lookup_enum(k1, k2, m))
-        return 1;
+    if (is_quick(&pl.g, fast)) {
+        fast_key(&pl.g, fast, &k2);
+        if (lookup_enum(k1, k2, m))
+            return 1;
+    }
     return tc_fail(err, errlen, "cuda_enum_run_static: this job's kernel is not loaded; run the "
                    "same job once through cuda_enum_run first");
 }
@@ -827,10 +849,9 @@ static char *group_source(char **srcs, const size_t *lens, int n, size_t *len)
 }
 
 /* The kernels for the plans in g[0..n): from the cache (m[i] filled, pend[i] NULL), else
-   generated and compiled together (pend[i]: the group's build, for enum_module_load); `fast`
-   compiles them for a quick start (FAST_NVRTC_OPT, or PTX written directly for the jobs the PTX
-   writer takes), unless the optimised build is cached (fast = 1) or always (fast = 2).  The jobs of a call that need building
-   form at most two groups: one NVRTC program and one PTX module. */
+   generated and compiled together (pend[i]: the group's build, for enum_module_load) in the build
+   mode `fast` (TC_BUILD_*).  The jobs of a call that need building form at most two groups: one
+   NVRTC program and one PTX module. */
 static int enum_modules_build(TcGenEnum *const *g, int n, int fast, TcModule *m,
                               TcEnumPending **pend, int *kidx, char *err, size_t errlen)
 {
@@ -842,13 +863,14 @@ static int enum_modules_build(TcGenEnum *const *g, int n, int fast, TcModule *m,
         kidx[i] = 0;
         uint64_t k1, k2;
         enum_key(g[i], &k1, &k2);
-        if (fast < 2 && lookup_enum(k1, k2, &m[i]))
+        if (fast != TC_BUILD_QUICK_ONLY && lookup_enum(k1, k2, &m[i]))
             continue;
-        if (fast)
-            fast_key(g[i], &k2);
-        if (fast && lookup_enum(k1, k2, &m[i]))
+        const int quick = is_quick(g[i], fast);
+        if (quick)
+            fast_key(g[i], fast, &k2);
+        if (quick && lookup_enum(k1, k2, &m[i]))
             continue;
-        const int kind = fast && tc_enum_ptx && tc_ptx_enum_ok(g[i]);
+        const int kind = quick && tc_enum_ptx && tc_ptx_enum_ok(g[i]);
         if (!p[kind])
             p[kind] = tc_xcalloc(1, sizeof *p[kind]);
         int k = nb[kind]++;
@@ -867,7 +889,7 @@ static int enum_modules_build(TcGenEnum *const *g, int n, int fast, TcModule *m,
             gk[0][k]->work = &p[0]->k[k].work;
             srcs[k] = tc_codegen_enum(gk[0][k], &lens[k]);
             gk[0][k]->work = NULL;
-            if (fast) {
+            if (is_quick(gk[0][k], fast)) {
                 static const char mark[] = "// built with " FAST_NVRTC_OPT "\n";
                 char *s2 = tc_xmalloc(lens[k] + sizeof mark);
                 memcpy(s2, mark, sizeof mark - 1);
@@ -881,8 +903,10 @@ static int enum_modules_build(TcGenEnum *const *g, int n, int fast, TcModule *m,
         p[0]->src = group_source(srcs, lens, nb[0], &p[0]->len);
         for (int k = 0; k < nb[0]; k++)
             free(srcs[k]);
-        ok = tc_module_build(p[0]->src, p[0]->len, fast ? FAST_NVRTC_OPT : NULL, &p[0]->b, err,
-                             errlen);
+        /* NVRTC's jobs of a call are all quick or all optimised (TC_BUILD_SERVE sends the quick
+           ones to PTX) */
+        ok = tc_module_build(p[0]->src, p[0]->len, is_quick(gk[0][0], fast) ? FAST_NVRTC_OPT : NULL,
+                             &p[0]->b, err, errlen);
     }
     if (ok && p[1]) {
         char target[16];
@@ -892,11 +916,11 @@ static int enum_modules_build(TcGenEnum *const *g, int n, int fast, TcModule *m,
         char *ptx = tc_ptx_enum(gk[1], nb[1], target, work, &p[1]->len);
         /* the text is the module cache's key: it records the optimisation level */
         p[1]->src = tc_xmalloc(p[1]->len + 32);
-        p[1]->len = (size_t)sprintf(p[1]->src, "// ptxas -O%d\n%s", tc_enum_ptx_opt ? 3 : 0, ptx);
+        p[1]->len = (size_t)sprintf(p[1]->src, "// ptxas -O%d\n%s", ptx_opt(fast), ptx);
         free(ptx);
         for (int k = 0; k < nb[1]; k++)
             p[1]->k[k].work = work[k];
-        ok = tc_module_build_ptx(p[1]->src, p[1]->len, &p[1]->b, err, errlen);
+        ok = tc_module_build_ptx(p[1]->src, p[1]->len, ptx_opt(fast), &p[1]->b, err, errlen);
     }
     for (int kind = 0; kind < 2; kind++) {
         if (!p[kind])
@@ -1191,8 +1215,7 @@ static int run_prepared(const TcEnumJob *jp, EnumResult *r, char *err, size_t er
     return 1;
 }
 
-/* 1: cuda_enum_run builds quick-start kernels, as a batch does, unless the optimised kernel is
-   cached; 2: always (tests of those builds) */
+/* cuda_enum_run's build mode (TC_BUILD_*; tests and measurements of the other builds) */
 int tc_enum_run_fast = 0;
 
 int cuda_enum_run(const Enum *e, EnumResult *r, char *err, size_t errlen)

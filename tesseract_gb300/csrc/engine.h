@@ -83,24 +83,26 @@ int    tc_module_build(const char *src, size_t len, const char *extra_opt, TcBui
                        size_t errlen);
 int    tc_module_load(const char *src, size_t len, TcBuilt *b, const char *const *kernels,
                       int nkernels, TcModule *out, char *err, size_t errlen);
-/* tc_module_build for PTX text (ptxas through nvJitLink, without optimisation); the module cache
-   is keyed by the text as for CUDA C */
-int    tc_module_build_ptx(const char *ptx, size_t len, TcBuilt *b, char *err, size_t errlen);
+/* tc_module_build for PTX text (ptxas through nvJitLink at -O0, or -O3 when opt is set); the
+   module cache is keyed by the text as for CUDA C */
+int    tc_module_build_ptx(const char *ptx, size_t len, int opt, TcBuilt *b, char *err,
+                           size_t errlen);
+/* Build modes of the generated enumeration kernels (engine.c says what each builds) */
+enum { TC_BUILD_OPT, TC_BUILD_QUICK, TC_BUILD_QUICK_ONLY, TC_BUILD_SERVE };
 /* 1 (default): quick-start builds of equivalence and search jobs write PTX directly (ptxgen.c)
    instead of CUDA C for NVRTC */
 extern int tc_enum_ptx;
-/* ptxas optimisation of those builds: 0 (default) or 3 */
+/* ptxas optimisation of a batch's PTX builds: 0 (default) or 3 */
 extern int tc_enum_ptx_opt;
 /* Is job e's quick-start build PTX written directly? */
 int tc_enum_quick_ptx(const Enum *e);
-/* 1: cuda_enum_run builds quick-start kernels unless the optimised one is cached, 2: always
-   (default 0: the optimised build) */
+/* cuda_enum_run's build mode (default TC_BUILD_OPT) */
 extern int tc_enum_run_fast;
 void   tc_built_free(TcBuilt *b);
 int    tc_enum_prepare(const Enum *e, int *in_map, int *out_map, char *err, size_t errlen);
-/* The loaded kernel of a job that an earlier enumeration compiled (with `fast`, its quick-start
-   build counts too), else an error; allocates nothing (its maps are fixed buffers, so programs of
-   more than TC_CACHED_MAX_OUTPUTS outputs are refused). */
+/* The loaded kernel of a job that an earlier enumeration compiled (the optimised build, or the
+   quick one of build mode `fast`), else an error; allocates nothing (its maps are fixed buffers,
+   so programs of more than TC_CACHED_MAX_OUTPUTS outputs are refused). */
 #define TC_CACHED_MAX_OUTPUTS 4096
 int    tc_enum_cached(const Enum *e, int fast, TcModule *m, char *err, size_t errlen);
 
@@ -119,10 +121,9 @@ typedef struct {
     TcEnumPending *pending;  /* built by tc_enum_job_build, not yet loaded */
     int            pidx;     /* its kernel in the pending group */
 } TcEnumJob;
-/* fast: compiled for a quick start (ptxas without optimisation) unless the optimised kernel is
-   cached already.  prepare = build (code generation and NVRTC: no CUDA call) + load (the module
-   load, which waits for the device's running work, and the launch shape); drop frees a build
-   that will not be loaded. */
+/* fast: the build mode (TC_BUILD_*).  prepare = build (code generation and NVRTC or ptxas: no
+   CUDA call) + load (the module load, which waits for the device's running work, and the launch
+   shape); drop frees a build that will not be loaded. */
 int    tc_enum_job_prepare(const Enum *e, TcEnumJob *j, int fast, char *err, size_t errlen);
 int    tc_enum_job_build(const Enum *e, TcEnumJob *j, int fast, char *err, size_t errlen);
 /* n (1..TC_MAX_KERNELS) jobs built together: their uncached kernels in one NVRTC program and,

@@ -69,7 +69,7 @@ extern "C" int cuda_enum_run_static(const Enum *e, EnumResult *r, char *err, siz
         return tc_fail(err, errlen, "cuda_enum_run_static: the engine is not started; run the "
                        "same job once through cuda_enum_run first");
     TcModule m;
-    if (!tc_enum_cached(e, 0, &m, err, errlen))
+    if (!tc_enum_cached(e, TC_BUILD_OPT, &m, err, errlen))
         return 0;
     if (!cuda_engine_init(0, err, errlen))  // started already: makes its device current
         return 0;

@@ -62,6 +62,14 @@ void   tc_wave_pool_trim(void);
    (ptxas without optimisation through nvJitLink, against 0.051 s + 9.2 us through NVRTC), the
    kernels at about 1.1e15 lane-ops/s on the heavier jobs. */
 #define RATE_COMPILED_PTX 1.1e15
+/* A served stream's equivalence and search jobs are built from PTX with ptxas -O3: 0.020 s +
+   6.6 us per instruction against NVRTC's 0.058 s + 13.3 us (same 78 jobs), the kernels as fast
+   (3.4e15 lane-ops/s on the heavier jobs, both).  In the serving model's terms, which include a
+   compile thread's wait for its module load: */
+#define COMPILE_S0_SERVE_PTX 0.063
+#define COMPILE_S_PER_INSTR_SERVE_PTX 3.3e-5
+/* 1 (default): a served stream's equivalence and search jobs are built so; 0: by NVRTC */
+int tc_serve_quick = 1;
 #define COMPILE_S0_PTX 0.0153
 #define COMPILE_S_PER_INSTR_PTX 2.63e-6
 /* A job whose kernel is already compiled (the cache is keyed by what the code generator reads)
@@ -123,7 +131,9 @@ static void *compile_worker(void *arg)
             js[i] = &c->prep[ids[i]];
         }
         double t0 = tc_now();
-        int ok = tc_enum_jobs_build(es, js, n, c->defer, e2, sizeof e2);
+        int ok = tc_enum_jobs_build(es, js, n,
+                                    c->defer ? TC_BUILD_QUICK
+                                    : tc_serve_quick ? TC_BUILD_SERVE : TC_BUILD_OPT, e2, sizeof e2);
         for (int i = 0; ok && !c->defer && i < n; i++)
             if (!tc_enum_job_load(es[i], js[i], e2, sizeof e2)) {
                 for (int k = i; k < n; k++)
@@ -172,10 +182,15 @@ static int route_compiled(const Enum *e, const CudaServeOpts *o, int threads, do
         return 1;
     double instrs = (double)e->a->len + (e->mode == EN_EQUIV ? (double)e->b->len : 0.0);
     double work = (double)(1ull << e->a->ninputs) * (double)e->ticks * instrs;
-    double saved = work / rate_interp - work / RATE_COMPILED;
     TcModule m;
     char why[8];
-    if (tc_enum_cached(e, 0, &m, why, sizeof why))
+    double saved = work / rate_interp - work / RATE_COMPILED;
+    if (tc_serve_quick && tc_enum_quick_ptx(e)) {
+        if (tc_enum_cached(e, TC_BUILD_SERVE, &m, why, sizeof why))
+            return saved > LAUNCH_S;
+        return saved > (COMPILE_S0_SERVE_PTX + COMPILE_S_PER_INSTR_SERVE_PTX * instrs) / threads;
+    }
+    if (tc_enum_cached(e, TC_BUILD_OPT, &m, why, sizeof why))
         return saved > LAUNCH_S;
     return saved > (COMPILE_S0 + COMPILE_S_PER_INSTR * instrs) / threads;
 }
@@ -187,7 +202,7 @@ double tc_route_compile_s(const Enum *e, double instrs)
 {
     TcModule m;
     char why[8];
-    if (tc_enum_cached(e, 1, &m, why, sizeof why))
+    if (tc_enum_cached(e, TC_BUILD_QUICK, &m, why, sizeof why))
         return 0.0;
     return tc_enum_quick_ptx(e) ? COMPILE_S0_PTX + COMPILE_S_PER_INSTR_PTX * instrs
                                 : COMPILE_S0_FAST + COMPILE_S_PER_INSTR_FAST * instrs;
