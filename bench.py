@@ -296,9 +296,10 @@ def config_life(gens=1000):
 def config_batch(njobs=4096):
     """Config 3: the 4,096 random equivalence pairs (workloads.batch_equiv_jobs) in one call,
     every verdict against the reference's own (tests/golden/batch_equiv.json.gz).  The batch
-    runs twice: cold (nothing of it compiled: the interpreter runs the light jobs in one
-    persistent launch while the host compiles the heavy ones) and again with the kernels the
-    first run compiled in the cache.  The plain engine (one NVRTC-compiled kernel per job, in
+    runs three times: cold (nothing of it compiled: the interpreter runs the light jobs in one
+    persistent launch while the host compiles the heavy ones), again with the kernels the
+    first run compiled in the cache, and once more after cuda_batch_prepare has compiled the
+    kernel of every job worth a launch (its seconds reported apart).  The plain engine (one NVRTC-compiled kernel per job, in
     order) runs 32 jobs of the same distribution that the batch does not contain (seeds 4096 +
     128 k), compiling and then cached."""
     import tesseract_gb300 as T
@@ -306,8 +307,15 @@ def config_batch(njobs=4096):
     jobs = batch_equiv_jobs(njobs)
     T.batch_run(batch_equiv_jobs(seeds=range(100000, 100064)))  # warm-up on other programs
     runs = {}
+    prep_s = nprep = None
     with Clocks() as clk:
-        for label in ("cold", "cached"):
+        for label in ("cold", "cached", "all_kernels_cached"):
+            if label == "all_kernels_cached":
+                # every job worth a launch compiled and loaded beforehand: the batch against
+                # the plain engine with its kernels cached, like for like
+                t0 = time.perf_counter()
+                nprep = T.batch_prepare(jobs)
+                prep_s = time.perf_counter() - t0
             t0 = time.perf_counter()
             res = T.batch_run(jobs)
             wall = time.perf_counter() - t0
@@ -337,8 +345,8 @@ def config_batch(njobs=4096):
             ref = ref and got == want
     res = runs["cold"]["results"]
     keys = ("space", "tried", "hits", "hit", "ops")
-    same_runs = all(a[k] == b[k] for a, b in zip(runs["cold"]["results"],
-                                                 runs["cached"]["results"]) for k in keys)
+    same_runs = all(a[k] == b[k] for other in ("cached", "all_kernels_cached")
+                    for a, b in zip(runs["cold"]["results"], runs[other]["results"]) for k in keys)
     controls = [r["hits"] for j, r in zip(jobs, res) if j["mutated"]]
     sample = batch_equiv_jobs(seeds=range(4096, 4096 + 32 * 128, 128))
     t0 = time.perf_counter()
@@ -363,6 +371,9 @@ def config_batch(njobs=4096):
            "plain_jobs_per_s_with_compile": pc, "plain_jobs_per_s_cached": pw,
            "speedup_vs_plain_with_compile": rate / pc,
            "speedup_cached_vs_plain_cached": runs["cached"]["jobs_per_s"] / pw,
+           "prepared_kernels": nprep, "prepare_s": prep_s,
+           "speedup_all_kernels_cached_vs_plain_cached":
+               runs["all_kernels_cached"]["jobs_per_s"] / pw,
            "sample_batched_identical_to_plain": same, "clocks": clk.summary()}
     return rec, bool(same and same_runs and ref is not False)
 

@@ -255,6 +255,13 @@ typedef struct {
         loop_end;
 } CudaBatchStats;
 int  cuda_batch_stats(CudaBatchStats *s);
+/* Compiles and loads, on the host's cores less two, the kernel of every job of an array that a
+   batch could run as generated code (whole spaces whose work pays for a launch; optimised, as a
+   served job's: PTX through ptxas -O3 for equivalence and search, NVRTC -O2 for the rest), so
+   that a later cuda_batch_run of the same jobs finds every such kernel cached; *prepared (when
+   not NULL) gets how many.  For job sets that run repeatedly. */
+int  cuda_batch_prepare(const Enum *const *jobs, int njobs, int *prepared, char *err,
+                        size_t errlen);
 
 /* The superoptimizer.  cuda_super_parse replaces super_parse (src/super.c:225-371): same
    language, same SuperSpec.  cuda_super_search replaces super_search (src/super.c:821-896):

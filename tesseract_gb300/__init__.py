@@ -447,6 +447,24 @@ def batch_run(jobs) -> list:
     return [res[i].as_dict() for i in range(n)]
 
 
+def batch_prepare(jobs) -> int:
+    """Compiles and loads the quick-start kernel of every job a batch_run of these jobs could run
+    as generated code (cuda_batch_prepare); returns how many."""
+    jobs = list(jobs)
+    n = len(jobs)
+    structs = [make_enum(j["mode"], j["a"], j.get("b"), j.get("spec"), j.get("ticks", 1))
+               for j in jobs]
+    arr = (C.POINTER(EnumStruct) * max(n, 1))(*[C.pointer(s) for s in structs])
+    got, err = C.c_int(), _err()
+    L = lib()
+    L.cuda_batch_prepare.restype = C.c_int
+    L.cuda_batch_prepare.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_char_p,
+                                     C.c_size_t]
+    if not L.cuda_batch_prepare(C.cast(arr, C.c_void_p), n, C.byref(got), err, len(err)):
+        raise EngineError(err.value.decode())
+    return got.value
+
+
 class BatchStats(C.Structure):
     _fields_ = [("jobs", C.c_int), ("compiled", C.c_int), ("interpreted", C.c_int),
                 ("compile_threads", C.c_int), ("planned", C.c_int), ("taken_back", C.c_int),

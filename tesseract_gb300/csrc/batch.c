@@ -1056,6 +1056,106 @@ int cuda_batch_run(const Enum *const *jobs, int njobs, EnumResult *results, char
     return ok;
 }
 
+/* cuda_batch_prepare: compile threads take groups of up to four jobs in turn */
+typedef struct {
+    const Enum *const *jobs;
+    const int         *ids;
+    TcEnumJob         *prep;
+    int                n, next, failed;
+    double             busy;
+    char               err[512];
+    pthread_mutex_t    mu;
+} Prepare;
+
+static void *prepare_worker(void *arg)
+{
+    Prepare *w = arg;
+    for (;;) {
+        pthread_mutex_lock(&w->mu);
+        int k0 = w->next, n = w->n - k0 < 4 ? w->n - k0 : 4;
+        w->next += n > 0 ? n : 0;
+        int stop = n <= 0 || w->failed;
+        pthread_mutex_unlock(&w->mu);
+        if (stop)
+            return NULL;
+        const Enum *es[4];
+        TcEnumJob *js[4];
+        for (int i = 0; i < n; i++) {
+            es[i] = w->jobs[w->ids[k0 + i]];
+            js[i] = &w->prep[k0 + i];
+        }
+        char e2[512];
+        double t0 = tc_now();
+        int ok = tc_enum_jobs_build(es, js, n, TC_BUILD_SERVE, e2, sizeof e2);
+        pthread_mutex_lock(&w->mu);
+        w->busy += tc_now() - t0;
+        if (!ok && !w->failed) {
+            w->failed = 1;
+            snprintf(w->err, sizeof w->err, "%s", e2);
+        }
+        pthread_mutex_unlock(&w->mu);
+    }
+}
+
+double tc_batch_last_prepare_busy;
+
+int cuda_batch_prepare(const Enum *const *jobs, int njobs, int *prepared, char *err,
+                       size_t errlen)
+{
+    if (prepared)
+        *prepared = 0;
+    if (njobs <= 0)
+        return 1;
+    if (!cuda_engine_init(0, err, errlen))
+        return 0;
+    long cores = sysconf(_SC_NPROCESSORS_ONLN);
+    int threads = tc_batch_threads > 0 ? tc_batch_threads : cores > 3 ? (int)cores - 2 : 1;
+    if (threads > 64)
+        threads = 64;
+    Prepare w;
+    memset(&w, 0, sizeof w);
+    pthread_mutex_init(&w.mu, NULL);
+    int *ids = tc_xmalloc((size_t)njobs * sizeof *ids);
+    /* the jobs a batch could send to generated code: whole spaces whose work pays for a launch */
+    for (int i = 0; i < njobs; i++) {
+        const Enum *e = jobs[i];
+        double instrs = (double)e->a->len + (e->mode == EN_EQUIV && e->b ? (double)e->b->len : 0);
+        double work = (e->a->ninputs < 64 ? (double)(1ull << e->a->ninputs) : 0) * e->ticks *
+                      instrs;
+        if (e->parts == 1 && work / BATCH_RATE_INTERP - tc_route_compiled_s(e, work) > 0)
+            ids[w.n++] = i;
+    }
+    w.jobs = jobs;
+    w.ids = ids;
+    w.prep = tc_xcalloc((size_t)w.n + 1, sizeof *w.prep);
+    pthread_t tid[64];
+    int nt = 0;
+    for (; nt < threads && nt * 4 < w.n; nt++)
+        if (pthread_create(&tid[nt], NULL, prepare_worker, &w) != 0)
+            break;
+    if (nt == 0)
+        prepare_worker(&w);
+    for (int i = 0; i < nt; i++)
+        pthread_join(tid[i], NULL);
+    int ok = !w.failed;
+    if (!ok)
+        tc_fail(err, errlen, "%s", w.err);
+    /* every build loaded: the first load of a module waits for the device's running work */
+    for (int k = 0; k < w.n; k++) {
+        if (ok && w.prep[k].pending)
+            ok = tc_enum_job_load(jobs[ids[k]], &w.prep[k], err, errlen);
+        else
+            tc_enum_job_drop(&w.prep[k]);
+    }
+    if (ok && prepared)
+        *prepared = w.n;
+    tc_batch_last_prepare_busy = w.busy;
+    pthread_mutex_destroy(&w.mu);
+    free(w.prep);
+    free(ids);
+    return ok;
+}
+
 int cuda_batch_stats(CudaBatchStats *s)
 {
     *s = last_batch;

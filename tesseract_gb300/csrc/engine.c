@@ -730,6 +730,26 @@ static void fast_key(const TcGenEnum *g, int fast, uint64_t *k2)
                : 0x9E3779B97F4A7C15ull;
 }
 
+/* The cached kernel of plan g (keys k1, k2 of its optimised build) for build mode `fast`: the
+   optimised NVRTC build, else for a quick mode the PTX writer's -O3 build, else the mode's own
+   quick build (TC_BUILD_QUICK_ONLY: only its own) */
+static int lookup_built(const TcGenEnum *g, int fast, uint64_t k1, uint64_t k2, TcModule *m)
+{
+    if (fast != TC_BUILD_QUICK_ONLY && lookup_enum(k1, k2, m))
+        return 1;
+    if (!is_quick(g, fast))
+        return 0;
+    uint64_t q = k2;
+    if (fast == TC_BUILD_QUICK && tc_enum_ptx && tc_ptx_enum_ok(g)) {
+        fast_key(g, TC_BUILD_SERVE, &q);
+        if (lookup_enum(k1, q, m))
+            return 1;
+        q = k2;
+    }
+    fast_key(g, fast, &q);
+    return lookup_enum(k1, q, m);
+}
+
 /* The loaded kernel of an enumeration, only when an earlier run of the same job compiled and
    loaded it (the optimised build, or the quick build of mode `fast`): no code generation, no
    compilation, no module load.  For cuda_enum_run_static, whose callers cannot allocate, and the
@@ -754,13 +774,8 @@ int tc_enum_cached(const Enum *e, int fast, TcModule *m, char *err, size_t errle
     apply_tuning(&pl.g);
     uint64_t k1, k2;
     enum_key(&pl.g, &k1, &k2);
-    if (lookup_enum(k1, k2, m))
+    if (lookup_built(&pl.g, fast, k1, k2, m))
         return 1;
-    if (is_quick(&pl.g, fast)) {
-        fast_key(&pl.g, fast, &k2);
-        if (lookup_enum(k1, k2, m))
-            return 1;
-    }
     return tc_fail(err, errlen, "cuda_enum_run_static: this job's kernel is not loaded; run the "
                    "same job once through cuda_enum_run first");
 }
@@ -863,14 +878,16 @@ static int enum_modules_build(TcGenEnum *const *g, int n, int fast, TcModule *m,
         kidx[i] = 0;
         uint64_t k1, k2;
         enum_key(g[i], &k1, &k2);
-        if (fast != TC_BUILD_QUICK_ONLY && lookup_enum(k1, k2, &m[i]))
+        if (lookup_built(g[i], fast, k1, k2, &m[i]))
             continue;
         const int quick = is_quick(g[i], fast);
         if (quick)
             fast_key(g[i], fast, &k2);
-        if (quick && lookup_enum(k1, k2, &m[i]))
-            continue;
         const int kind = quick && tc_enum_ptx && tc_ptx_enum_ok(g[i]);
+        /* PTX kernels run in blocks of 128: ptxas without optimisation takes more registers,
+           and smaller blocks fill an SM's register file in finer steps */
+        if (kind)
+            g[i]->block = TC_PTX_BLOCK;
         if (!p[kind])
             p[kind] = tc_xcalloc(1, sizeof *p[kind]);
         int k = nb[kind]++;

@@ -12,6 +12,7 @@ extern "C" {
 #endif
 
 #define TC_ENUM_BLOCK 256
+#define TC_PTX_BLOCK 128  /* threads per block of the kernels built from PTX written directly */
 #define TC_MAX_KERNELS 8
 
 typedef struct {

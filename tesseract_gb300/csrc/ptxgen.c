@@ -13,10 +13,10 @@
    Loops: a chunk's 1,024 words are 32 steps of 32 (one word per lane).  Within a chunk only the
    five inputs on word bits 5..9 change from step to step; the inputs on the lane's word bits
    0..4 and on the chunk's bits stay, and so does every LUT that depends on no step input.
-   Those LUTs run once per chunk, before its steps, when they are at least a fifth of the
-   network and the values the steps read from them fit in registers (the same rule as codegen.c's
-   stretches).  Every branch that surrounds a warp-wide vote or shuffle is uniform across the
-   warp; the per-lane valid mask is computed with selects. */
+   Those inputs and LUTs are computed once per chunk, before its steps, when the values the steps
+   read from them fit in registers.  Every branch before the warp's final store is uniform across
+   the warp and says so (bra.uni), so ptxas needs no reconvergence around the votes and shuffles;
+   the per-lane valid mask is computed with selects. */
 #include <stdarg.h>
 #include <stdlib.h>
 #include <string.h>
@@ -151,16 +151,24 @@ static void put_kernel(Ptx *o, const TcGenEnum *g, const char *name, TcGenWork *
     for (int w = 0; w < nwant; w++)
         HOLD(want[w]);
 #undef HOLD
-    const int split = hoisted > 0 && 5 * hoisted >= norder && nheld <= PTX_MAX_FIELDS;
+    /* moving a chunk's invariant work out of its steps costs only the registers that hold it */
+    const int split = nheld <= PTX_MAX_FIELDS;
+    /* inputs that no LUT and no compare reads are not computed */
+    char *used = tc_xcalloc((size_t)size + 1, 1);
+    for (int i = 0; i < norder; i++)
+        for (int q = 0; q < 3; q++)
+            used[lv[i][q]] = 1;
+    for (int w = 0; w < nwant; w++)
+        used[want[w]] = 1;
 
     put(o, "\n.visible .entry %s(\n\t.param .align 8 .b8 tc_args[64]\n)\n.maxntid %d, 1, 1\n{\n",
         name, g->block);
     put(o, "\t.reg .pred %%p_ch, %%p_run, %%p_in, %%p_sp, %%p_full, %%p_any, %%p_rec, %%p_l0;\n"
            "\t.reg .b32 %%lane, %%tidx, %%cta, %%nthr, %%rec, %%nsel, %%parts, %%part, %%clo, "
-           "%%chi, %%wlo, %%whi, %%valid, %%vpart, %%dl, %%one, %%m, %%pc, %%any, %%src, %%mm, "
-           "%%xlo, %%xhi, %%ylo, %%yhi, %%tz, %%t;\n"
+           "%%chi, %%wlo, %%valid, %%vpart, %%dl, %%one, %%m, %%pc, %%any, %%src, %%mm, "
+           "%%xlo, %%xhi, %%ylo, %%yhi, %%tz, %%t, %%st, %%stend, %%chits, %%x32, %%space32;\n"
            "\t.reg .b64 %%words, %%space, %%per_warp, %%hits_p, %%list_p, %%count_p, %%warp, "
-           "%%s0, %%s1, %%s, %%send, %%j, %%chunk, %%cbase, %%word, %%x0, %%d, %%t64, %%u64, "
+           "%%s0, %%s1, %%s, %%send, %%j, %%chunk, %%cbase, %%word, %%x0, %%t64, %%u64, "
            "%%hits, %%xb, %%lane64, %%addr, %%q, %%rr, %%nsel64, %%parts64, %%part64;\n"
            "\t.reg .b32 %%v<%d>;\n", nreg);
     /* the argument block: TcEnumArgs (codegen.h) */
@@ -187,41 +195,46 @@ static void put_kernel(Ptx *o, const TcGenEnum *g, const char *name, TcGenWork *
            "\tmov.b32 %%v%d, 0;\n\tmov.b32 %%v%d, -1;\n"
            "\tcvt.u64.u32 %%nsel64, %%nsel;\n\tcvt.u64.u32 %%parts64, %%parts;\n"
            "\tcvt.u64.u32 %%part64, %%part;\n"
-           "\tsetp.eq.u32 %%p_ch, %%nsel, %%parts;\n"
-           "\tsetp.ge.u64 %%p_run, %%s, %%s1;\n\t@%%p_run bra $DONE;\n", reg[0], reg[1]);
+           "\tsetp.eq.u32 %%p_ch, %%nsel, %%parts;\n\tmov.u32 %%space32, %u;\n"
+           "\tsetp.ge.u64 %%p_run, %%s, %%s1;\n\t@%%p_run bra.uni $DONE;\n", reg[0], reg[1],
+        n < 15 ? 1u << n : 0u);
     /* a chunk: the selected chunk's number, its base word (with the lane), the end of its steps */
-    put(o, "$CHUNK:\n\tshr.u64 %%j, %%s, 10;\n\tmov.u64 %%chunk, %%j;\n\t@%%p_ch bra $BASE;\n"
+    put(o, "$CHUNK:\n\tshr.u64 %%j, %%s, 10;\n\tmov.u64 %%chunk, %%j;\n\t@%%p_ch bra.uni $BASE;\n"
            "\tdiv.u64 %%q, %%j, %%nsel64;\n\trem.u64 %%rr, %%j, %%nsel64;\n"
            "\tmad.lo.u64 %%chunk, %%q, %%parts64, %%part64;\n\tadd.u64 %%chunk, %%chunk, %%rr;\n"
            "$BASE:\n\tshl.b64 %%cbase, %%chunk, 10;\n\tor.b64 %%cbase, %%cbase, %%lane64;\n"
            "\tor.b64 %%send, %%s, 1023;\n\tadd.u64 %%send, %%send, 1;\n"
            "\tmin.u64 %%send, %%send, %%s1;\n"
            "\tcvt.u32.u64 %%clo, %%cbase;\n\tshr.u64 %%t64, %%cbase, 32;\n"
-           "\tcvt.u32.u64 %%chi, %%t64;\n");
+           "\tcvt.u32.u64 %%chi, %%t64;\n"
+           /* the steps as 32-bit word offsets within the chunk: st .. stend by 32 */
+           "\tcvt.u32.u64 %%st, %%s;\n\tand.b32 %%st, %%st, 1023;\n"
+           "\tsub.u64 %%t64, %%send, %%s;\n\tcvt.u32.u64 %%stend, %%t64;\n"
+           "\tadd.u32 %%stend, %%stend, %%st;\n\tmov.u32 %%chits, 0;\n");
     if (split) {
         for (int k = 0; k < n; k++)
-            if (!(step >> k & 1))
+            if (!(step >> k & 1) && used[leaf[k]])
                 put_input(o, reg[leaf[k]], n - 1 - k, "%clo", "%chi");
         for (int i = 0; i < norder; i++)
             if (!(sup[order[i]] & step))
                 put(o, "\tlop3.b32 %%v%d, %%v%d, %%v%d, %%v%d, 0x%02x;\n", reg[order[i]],
                     reg[lv[i][0]], reg[lv[i][1]], reg[lv[i][2]], (unsigned)tt[i]);
     }
-    /* a step: the word, the step's inputs, the lanes of it that count */
-    put(o, "$STEP:\n\tand.b64 %%t64, %%s, 992;\n\tor.b64 %%word, %%cbase, %%t64;\n"
-           "\tcvt.u32.u64 %%wlo, %%word;\n\tshr.u64 %%t64, %%word, 32;\n"
-           "\tcvt.u32.u64 %%whi, %%t64;\n");
+    /* a step: the word's low half (its high half is the chunk's), the step's inputs */
+    put(o, "$STEP:\n\tor.b32 %%wlo, %%clo, %%st;\n");
     for (int k = 0; k < n; k++)
-        if (!split || (step >> k & 1))
-            put_input(o, reg[leaf[k]], n - 1 - k, "%wlo", "%whi");
-    put(o, "\tshl.b64 %%x0, %%word, 5;\n"
-           "\tadd.u64 %%t64, %%s, %%lane64;\n\tsetp.lt.u64 %%p_in, %%t64, %%s1;\n"
-           "\tsetp.lt.u64 %%p_sp, %%x0, %%space;\n\tand.pred %%p_in, %%p_in, %%p_sp;\n"
-           "\tsub.u64 %%d, %%space, %%x0;\n\tsetp.ge.u64 %%p_full, %%d, 32;\n"
-           "\tcvt.u32.u64 %%dl, %%d;\n\tand.b32 %%dl, %%dl, 31;\n"
-           "\tshl.b32 %%vpart, %%one, %%dl;\n\tsub.u32 %%vpart, %%vpart, 1;\n"
-           "\tselp.b32 %%valid, -1, %%vpart, %%p_full;\n"
-           "\tselp.b32 %%valid, %%valid, 0, %%p_in;\n");
+        if ((!split || (step >> k & 1)) && used[leaf[k]])
+            put_input(o, reg[leaf[k]], n - 1 - k, "%wlo", "%chi");
+    /* the lanes that count: a warp's words are whole multiples of 32 (per_warp and the selected
+       words are), and with 15 inputs or more every selected chunk lies inside the space; only a
+       space smaller than one chunk has words, and lanes, past its end */
+    if (n < 15)
+        put(o, "\tshl.b32 %%x32, %%wlo, 5;\n\tsub.u32 %%dl, %%space32, %%x32;\n"
+               "\tsetp.lt.u32 %%p_in, %%x32, %%space32;\n\tsetp.ge.u32 %%p_full, %%dl, 32;\n"
+               "\tand.b32 %%dl, %%dl, 31;\n\tshl.b32 %%vpart, %%one, %%dl;\n"
+               "\tsub.u32 %%vpart, %%vpart, 1;\n"
+               "\tselp.b32 %%valid, -1, %%vpart, %%p_full;\n"
+               "\tselp.b32 %%valid, %%valid, 0, %%p_in;\n");
     for (int i = 0; i < norder; i++)
         if (!split || (sup[order[i]] & step))
             put(o, "\tlop3.b32 %%v%d, %%v%d, %%v%d, %%v%d, 0x%02x;\n", reg[order[i]],
@@ -237,12 +250,16 @@ static void put_kernel(Ptx *o, const TcGenEnum *g, const char *name, TcGenWork *
             put(o, "\tlop3.b32 %%m, %%m, %%v%d, %%v%d, 0x%s;\n", reg[want[bit]], reg[want[bit]],
                 (g->target >> bit) & 1 ? "c0" : "30");
     }
-    put(o, "\tand.b32 %%m, %%m, %%valid;\n\tpopc.b32 %%pc, %%m;\n\tcvt.u64.u32 %%t64, %%pc;\n"
-           "\tadd.u64 %%hits, %%hits, %%t64;\n\tsetp.ne.u32 %%p_any, %%m, 0;\n"
-           "\tvote.sync.ballot.b32 %%any, %%p_any, -1;\n");
+    if (n < 15)
+        put(o, "\tand.b32 %%m, %%m, %%valid;\n");
+    put(o, "\tpopc.b32 %%pc, %%m;\n\tadd.u32 %%chits, %%chits, %%pc;\n"
+           "\tsetp.ne.u32 %%p_any, %%m, 0;\n\tvote.sync.ballot.b32 %%any, %%p_any, -1;\n"
+           "\tsetp.eq.u32 %%p_rec, %%any, 0;\n\t@%%p_rec bra.uni $NEXT;\n"
+           "\tsetp.ge.u32 %%p_rec, %%rec, 16;\n\t@%%p_rec bra.uni $NEXT;\n"
+           "\tmov.b64 %%word, {%%wlo, %%chi};\n\tshl.b64 %%x0, %%word, 5;\n");
     /* the warp's first 16 hits, lane by lane in order, each lane's bits in order: lane 0 stores */
-    put(o, "$LANE:\n\tsetp.eq.u32 %%p_rec, %%any, 0;\n\t@%%p_rec bra $NEXT;\n"
-           "\tsetp.ge.u32 %%p_rec, %%rec, 16;\n\t@%%p_rec bra $NEXT;\n"
+    put(o, "$LANE:\n\tsetp.eq.u32 %%p_rec, %%any, 0;\n\t@%%p_rec bra.uni $NEXT;\n"
+           "\tsetp.ge.u32 %%p_rec, %%rec, 16;\n\t@%%p_rec bra.uni $NEXT;\n"
            "\tbrev.b32 %%t, %%any;\n\tbfind.shiftamt.u32 %%src, %%t;\n"
            "\tshfl.sync.idx.b32 %%mm, %%m, %%src, 31, -1;\n"
            "\tmov.b64 {%%xlo, %%xhi}, %%x0;\n"
@@ -250,8 +267,8 @@ static void put_kernel(Ptx *o, const TcGenEnum *g, const char *name, TcGenWork *
            "\tshfl.sync.idx.b32 %%xhi, %%xhi, %%src, 31, -1;\n"
            "\tmov.b64 %%xb, {%%xlo, %%xhi};\n"
            "\tsetp.eq.u32 %%p_l0, %%lane, 0;\n"
-           "$BIT:\n\tsetp.eq.u32 %%p_rec, %%mm, 0;\n\t@%%p_rec bra $LANE_END;\n"
-           "\tsetp.ge.u32 %%p_rec, %%rec, 16;\n\t@%%p_rec bra $LANE_END;\n"
+           "$BIT:\n\tsetp.eq.u32 %%p_rec, %%mm, 0;\n\t@%%p_rec bra.uni $LANE_END;\n"
+           "\tsetp.ge.u32 %%p_rec, %%rec, 16;\n\t@%%p_rec bra.uni $LANE_END;\n"
            "\tbrev.b32 %%t, %%mm;\n\tbfind.shiftamt.u32 %%tz, %%t;\n"
            "\tcvt.u64.u32 %%t64, %%tz;\n\tadd.u64 %%u64, %%xb, %%t64;\n"
            "\tshl.b64 %%addr, %%warp, 4;\n\tcvt.u64.u32 %%t64, %%rec;\n"
@@ -262,8 +279,10 @@ static void put_kernel(Ptx *o, const TcGenEnum *g, const char *name, TcGenWork *
            "\tbra.uni $BIT;\n"
            "$LANE_END:\n\tsub.u32 %%t, %%any, 1;\n\tand.b32 %%any, %%any, %%t;\n"
            "\tbra.uni $LANE;\n");
-    put(o, "$NEXT:\n\tadd.u64 %%s, %%s, 32;\n\tsetp.lt.u64 %%p_run, %%s, %%send;\n"
-           "\t@%%p_run bra $STEP;\n\tsetp.lt.u64 %%p_run, %%s, %%s1;\n\t@%%p_run bra $CHUNK;\n");
+    put(o, "$NEXT:\n\tadd.u32 %%st, %%st, 32;\n\tsetp.lt.u32 %%p_run, %%st, %%stend;\n"
+           "\t@%%p_run bra.uni $STEP;\n"
+           "\tcvt.u64.u32 %%t64, %%chits;\n\tadd.u64 %%hits, %%hits, %%t64;\n"
+           "\tmov.u64 %%s, %%send;\n\tsetp.lt.u64 %%p_run, %%s, %%s1;\n\t@%%p_run bra.uni $CHUNK;\n");
     /* the warp's count and hit total */
     put(o, "$DONE:\n");
     for (int d = 16; d > 0; d >>= 1)
@@ -284,6 +303,7 @@ static void put_kernel(Ptx *o, const TcGenEnum *g, const char *name, TcGenWork *
         work->stretch_steps = split ? 32 : 1;
         work->compare_ops = g->mode == EN_EQUIV ? (int)a->noutputs : nwant;
     }
+    free(used);
     free(held);
     free(sup);
     free(tt);

@@ -347,6 +347,7 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
        needs the host's cores first */
     int held = route != NULL, nheld = 0;
     int *held_ids = tc_xmalloc((size_t)njobs * sizeof *held_ids);
+    int *loaded = tc_xmalloc((size_t)njobs * sizeof *loaded), nloaded = 0, lhead = 0;
     TcWave *pending = NULL;  /* a wave prepared but not yet admitted */
     int pending_n = 0;
     size_t pending_need = 0;
@@ -388,14 +389,37 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
             }
             if (!loads_open && !held && next == njobs && rhead == nready && !pending)
                 loads_open = 1;  /* a batch's interpreter has every job it will get */
-            for (int s = 0; loads_open && s < nsl && cc.rhead < cc.rtail; s++) {
-                if (slot[s].id >= 0)
-                    continue;
+            /* a batch loads every build that is ready before it launches any of them: the first
+               load waits for the device's running work and the others find it idle, where a
+               load before each launch would wait for the compiled jobs just launched */
+            while (ok && cc.defer && loads_open && cc.rhead < cc.rtail) {
                 int id = cc.ready[cc.rhead++];
                 pthread_mutex_unlock(&cc.mu);  /* the compile threads go on while this loads */
                 double tl = tc_now();
                 ok = tc_enum_job_load(jobs[id], &cc.prep[id], err, errlen);
                 load_s += tc_now() - tl;
+                pthread_mutex_lock(&cc.mu);
+                if (ok)
+                    loaded[nloaded++] = id;
+                progress = 1;
+            }
+            for (int s = 0; ok && loads_open && s < nsl; s++) {
+                if (slot[s].id >= 0)
+                    continue;
+                int id;
+                if (cc.defer) {
+                    if (lhead == nloaded)
+                        break;
+                    id = loaded[lhead++];
+                    pthread_mutex_unlock(&cc.mu);
+                } else {
+                    if (cc.rhead == cc.rtail)
+                        break;
+                    id = cc.ready[cc.rhead++];
+                    pthread_mutex_unlock(&cc.mu);
+                    /* loaded by its compile thread: the launch shape */
+                    ok = tc_enum_job_load(jobs[id], &cc.prep[id], err, errlen);
+                }
                 if (ok)
                     ok = tc_enum_job_launch(&cc.prep[id], slot[s].dev, slot[s].host, slot[s].st,
                                             err, errlen) &&
@@ -569,6 +593,7 @@ static int serve(const Enum *const *jobs, const double *arrival, int njobs,
     free(ready);
     free(wj);
     free(held_ids);
+    free(loaded);
     tc_serve_last_wave_at = wave_launched_at;
     tc_serve_last_routed = routed;
     tc_serve_last_taken_back = taken_back;

@@ -98,3 +98,20 @@ def test_batch_with_ptx_builds_equals_nvrtc_builds():
         if not j["mutated"]:
             assert r["hits"] == 0
     assert st["jobs"] == len(jobs) and st["compiled"] > 0
+
+
+def test_batch_with_every_kernel_prepared():
+    """cuda_batch_prepare compiles the quick kernels of every job worth a launch; the next batch
+    of the same jobs runs each of those on its cached kernel (none compiled, none taken back) and
+    gives the results of the cold batch."""
+    from tesseract_gb300.workloads import batch_equiv_jobs
+    T.set_enum_quick(False)
+    jobs = batch_equiv_jobs(seeds=range(940000, 940256))
+    cold = T.batch_run(jobs)
+    n = T.batch_prepare(jobs)
+    warm = T.batch_run(jobs)
+    st = T.batch_stats()
+    keys = ("space", "tried", "hits", "hit", "ops")
+    assert all(x[k] == y[k] for x, y in zip(cold, warm) for k in keys)
+    assert n > 0 and st["compiled"] == n and st["taken_back"] == 0
+    assert st["compile_busy"] < 0.05 * n

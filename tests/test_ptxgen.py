@@ -99,3 +99,20 @@ def test_refusals():
     a = T.Program.random_in(12, 10, 100, 3)
     with pytest.raises(T.EngineError, match="equivalence and search"):
         T.codegen_ptx_module([(T.EN_EQUIV, a, a, None, 2)])
+
+
+@pytest.mark.parametrize("job", [c[1] for c in CASES], ids=[c[0] for c in CASES])
+def test_every_value_is_written_before_it_is_read(job):
+    """In the text, every %v register a lop3 reads has been written above it (in the prologue,
+    the chunk's part or earlier in the step): the split into a chunk's and a step's LUTs keeps
+    the mapped order's dependences."""
+    ptx = T.codegen_ptx_source(*job)
+    written = set()
+    for line in ptx.splitlines():
+        m = re.match(r"\s*(mov\.b32|shr\.s32|lop3\.b32) %v(\d+), (.*);", line)
+        if not m:
+            continue
+        if m.group(1) == "lop3.b32":
+            for r in re.findall(r"%v(\d+)", m.group(3)):
+                assert r in written, line
+        written.add(m.group(2))
