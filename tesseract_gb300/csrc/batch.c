@@ -925,7 +925,9 @@ double tc_route_compiled_s(const Enum *e, double work);
    on the 4,096-job batch alone; host packing and a 90 % share of the blocks beside compiled
    jobs bring it to about this). */
 #define BATCH_RATE_INTERP 1.1e14
-#define BATCH_SHARE 0.9
+/* the interpreter's share of the GPU's resident blocks when jobs also run compiled */
+double tc_batch_share = 0.9;
+#define BATCH_SHARE tc_batch_share
 
 static CudaBatchStats last_batch;
 

@@ -102,7 +102,8 @@ typedef struct {
 /* Jobs a compile thread builds together (one NVRTC program, one module load): NVRTC's fixed
    cost (0.053 s of a heavy job's 0.14 s) is paid once, and a load waits for the device's running
    work once for the group. */
-#define COMPILE_GROUP 4
+#define COMPILE_GROUP TC_MAX_KERNELS
+int tc_compile_group = 4;  /* jobs a compile thread takes at most (1..COMPILE_GROUP) */
 
 static void *compile_worker(void *arg)
 {
@@ -117,7 +118,7 @@ static void *compile_worker(void *arg)
         }
         /* a fair share of the queue, up to COMPILE_GROUP jobs: the other threads get theirs */
         int waiting = c->qtail - c->qhead, n = 1;
-        while (n < COMPILE_GROUP && n * c->threads < waiting)
+        while (n < tc_compile_group && n < COMPILE_GROUP && n * c->threads < waiting)
             n++;
         int ids[COMPILE_GROUP];
         for (int i = 0; i < n; i++)
