@@ -57,6 +57,11 @@ int tc_cube_gm_warps = 4;
 int tc_cube_copy_swap = 1;
 /* 1: far reads of computed cells are recomputed where they can be, instead of cutting */
 int tc_cube_recompute = 1;
+/* (node, mask) visits the recomputations of one segment may take in all: a bound on the code
+   recomputing adds to one kernel, which cannot be split (Life on 65,536 machines takes under 6,000;
+   the NTT product on 2,048 machines wanted over 300,000 and made one kernel of 400,000 LOP3 that
+   compiled for minutes, against 8 kernels of at most 170,000 with cuts) */
+int tc_cube_recompute_budget = 65536;
 /* the most instructions in one kernel: longer segments are split.  Fewer, longer kernels win
    once they are split over warps (Life on 65,536 machines: 3 kernels of up to 125,722
    instructions run 36-38k generations/s, 13 kernels of 12,000 run 29k), at the price of a longer
@@ -137,8 +142,8 @@ static unsigned find_cuts(const Program *p, size_t *first, unsigned far_dim)
    NANDs, and reads of a value in another machine (a link: that node at machine ^ mask).  A far
    read of a computed cell is recomputable when its node, evaluated at machine ^ mask, reaches
    only start values of cells not written so far in the segment, ids and constants (not RR's
-   start value), in at most RECOMPUTE_LIMIT
-   (node, mask) visits.  flags[s] is set for segments that recompute; their code must be
+   start value), in at most RECOMPUTE_LIMIT (node, mask) visits, and the segment's
+   recomputations stay within tc_cube_recompute_budget visits in all.  flags[s] is set for segments that recompute; their code must be
    generated as one kernel (the recomputation starts from the segment's start values). */
 enum { V_CONST, V_START, V_ID, V_RR0, V_NAND, V_LINK };
 #define RECOMPUTE_LIMIT 4096
@@ -238,6 +243,7 @@ static unsigned find_cuts_recompute(const Program *p, size_t *first, unsigned ch
     int32_t zero = dag_add(&g, V_CONST, 0, 0), one = dag_add(&g, V_CONST, 1, 0);
     uint32_t seg = 1;
     unsigned n = 0;
+    size_t spent = 0;  /* visits of this segment's recomputations */
     int32_t rr = dag_add(&g, V_RR0, 0, 0);
     first[n] = 0;
     flags[n++] = 0;
@@ -259,13 +265,16 @@ static unsigned find_cuts_recompute(const Program *p, size_t *first, unsigned ch
                 g.seg = seg;
                 if (g.seen)
                     memset(g.seen, 0, g.capseen * sizeof *g.seen);
-                if (dag_recomputable(&g, cur[a], mask)) {
+                if (dag_recomputable(&g, cur[a], mask) &&
+                    spent + g.nseen <= (size_t)tc_cube_recompute_budget) {
+                    spent += g.nseen;
                     for (size_t k = 0; k < g.nreads; k++)
                         read[g.reads[k]] = seg;
                     flags[n - 1] = 1;
                     v = dag_add(&g, V_LINK, cur[a], (int32_t)mask);
                 } else {  /* a new segment: the value is read from memory there */
                     seg++;
+                    spent = 0;
                     rr = dag_add(&g, V_RR0, 0, 0);
                     first[n] = i;
                     flags[n++] = 0;
@@ -285,6 +294,7 @@ static unsigned find_cuts_recompute(const Program *p, size_t *first, unsigned ch
         } else if (!tc_program_readonly(p, in.addr)) {
             if (read[in.addr] == seg) {
                 seg++;
+                spent = 0;
                 rr = dag_add(&g, V_RR0, 0, 0);
                 first[n] = i;
                 flags[n++] = 0;

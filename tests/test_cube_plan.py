@@ -215,3 +215,28 @@ def test_recomputing_never_adds_kernels():
         assert with_rc <= plain, seed
         fewer += with_rc < plain
     assert fewer > 0  # the programs do exercise it
+
+
+def kernel_lop3(src):
+    """LOP3 count of each kernel in a pass's source."""
+    return [k.count("TC_LOP3(") for k in src.split('extern "C" __global__')[1:]]
+
+
+def test_recomputing_stays_within_its_budget():
+    """The NTT product on 2,048 machines: recomputing every far read it could would put most of
+    the pass into one kernel that cannot be split (400,000 LOP3, minutes of compiling); the
+    per-segment budget cuts instead, so no kernel is much larger than the plain rule's largest
+    (the small recomputations the budget allows add a few LOP3).  Life's
+    recomputations fit the budget (one kernel per generation, the test above)."""
+    p = T.Program.gen_cube_demo("polymul", 11)
+    _, with_rc = cube_source(p, recompute=True)
+    _, plain = cube_source(p, recompute=False)
+    assert max(kernel_lop3(with_rc)) <= 1.05 * max(kernel_lop3(plain))
+    L = T.lib()
+    budget = C.c_int.in_dll(L, "tc_cube_recompute_budget")
+    old, budget.value = budget.value, 1 << 30
+    try:
+        _, unbounded = cube_source(p, recompute=True)
+    finally:
+        budget.value = old
+    assert max(kernel_lop3(unbounded)) > 2 * max(kernel_lop3(plain))  # what the budget prevents
