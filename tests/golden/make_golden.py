@@ -342,6 +342,19 @@ CLI_CPU_CASES = [
      [["search", "{hash16}", "--want", "h = 1", "--part", "0/1", "--raw"]]),
     (["verify", "{mul10}", "--spec", "p = a * b", "--merge", "{raw0}", "missing.raw"],
      [["verify", "{mul10}", "--spec", "p = a * b", "--part", "0/2", "--raw"]]),
+    # tester1 --merge (src/tester.c:279-429): shares of several sizes, a passes limit that
+    # leaves runs without a cycle, a time limit that cuts programs off, a missing file
+    (["tester1", "--merge", "{raw0}", "{raw1}"],
+     [["tester1", "--cells", "8,16,32", "--programs", "8", "--raw", "--threads", "1"],
+      ["tester1", "--cells", "16,64", "--programs", "6", "--seed", "9", "--raw", "--threads",
+       "2"]]),
+    (["tester1", "--merge", "{raw0}", "{raw1}"],
+     [["tester1", "--cells", "100,400", "--programs", "6", "--max-passes", "256", "--raw",
+       "--threads", "1"],
+      ["tester1", "--cells", "3000", "--ratio", "8", "--seconds", "0.3", "--raw", "--threads",
+       "2"]]),
+    (["tester1", "--programs", "2", "--merge", "{raw0}", "missing.raw"],
+     [["tester1", "--cells", "8", "--programs", "2", "--raw", "--threads", "1"]]),
     (["verify"], []),
     (["verify", "{mul4}"], []),
     (["search", "{mul4}"], []),

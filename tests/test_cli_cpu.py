@@ -1,8 +1,9 @@
 """The command line (bin/alpha-cuda) on paths that need no GPU, against the reference's own
 stdout, stderr and exit code (tests/golden/cli_cpu.json, made by tests/golden/make_golden.py
 --cli-cpu): --merge of shares whose --raw lines the reference wrote (complete, partial, a missing
-file), option errors, spec errors and the enumeration's refusals.  The usage text (exit code 2)
-is the tool's own and only its exit code is compared."""
+file), tester1's --merge of the reference's histogram lines (several sizes, runs without a cycle,
+programs cut off by a time limit), option errors, spec errors and the enumeration's refusals.
+The usage text (exit code 2) is the tool's own and only its exit code is compared."""
 import os
 import subprocess
 
