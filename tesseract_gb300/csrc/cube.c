@@ -67,6 +67,10 @@ int tc_cube_recompute_budget = 65536;
    instructions run 36-38k generations/s, 13 kernels of 12,000 run 29k), at the price of a longer
    compile (7 s against 0.5 s) */
 int tc_cube_chunk = 140000;
+/* a segment too long for one kernel is split into equal kernels of at most this many
+   instructions: they compile in parallel, and NVRTC's time grows faster than a kernel's length
+   (the NTT product on 512 machines, 272,001 instructions: 2 kernels took 85 s to compile) */
+int tc_cube_piece = 50000;
 
 struct CudaCube {
     Program     p;
@@ -1467,18 +1471,27 @@ static void plan_cube(CudaCube *c, const Program *p)
             c->slot1 = NULL;
         }
     }
-    /* split long segments into kernels of at most tc_cube_chunk instructions (not those that
-       recompute: the recomputation starts from the segment's start values) */
+    /* split segments longer than tc_cube_chunk instructions into equal kernels of at most
+       tc_cube_piece (not those that recompute: the recomputation starts from the segment's start
+       values) */
     size_t chunk = tc_cube_chunk > 0 ? (size_t)tc_cube_chunk : 12000;
-    c->first = tc_xmalloc((p->len / chunk + c->nseg + 2) * sizeof *c->first);
+    size_t piece = tc_cube_piece > 0 && (size_t)tc_cube_piece < chunk ? (size_t)tc_cube_piece
+                                                                         : chunk;
+    c->first = tc_xmalloc((p->len / piece + c->nseg + 2) * sizeof *c->first);
     c->nk = 0;
-    for (unsigned s = 0; s < c->nseg; s++)
+    for (unsigned s = 0; s < c->nseg; s++) {
+        size_t len = cuts[s + 1] - cuts[s], step = len;
+        if (!recomputes[s] && len > chunk) {
+            size_t kernels = (len + piece - 1) / piece;
+            step = (len + kernels - 1) / kernels;
+        }
         for (size_t i = cuts[s]; i < cuts[s + 1] || (i == cuts[s] && cuts[s] == cuts[s + 1]);
-             i += recomputes[s] ? cuts[s + 1] - cuts[s] : chunk) {
+             i += step) {
             c->first[c->nk++] = i;
             if (cuts[s] == cuts[s + 1])
                 break;
         }
+    }
     free(recomputes);
     c->first[c->nk] = p->len;
     c->loop = c->nk == 1 && c->dims <= FAR_DIM;
