@@ -20,9 +20,9 @@
    more, unless the value read can be computed again by the reading warp from cells the segment
    does not write (then it is: a Life board's halo corners).  Each segment is its own kernel
    launch; inside a segment every far load sees the value the cell had when the segment started,
-   which is what lockstep shows it.  Long segments are split
-   into kernels of at most tc_cube_chunk instructions that hand their cells over through memory,
-   so no single kernel is too large for the compiler.  When the whole pass is one kernel and no
+   which is what lockstep shows it.  A segment longer than tc_cube_chunk
+   instructions is split into equal kernels of at most tc_cube_piece that hand their cells over
+   through memory, so no single kernel is too large for the compiler.  When the whole pass is one kernel and no
    read crosses warps (at most 1024 machines), the passes loop inside the kernel.
 
    A pass that ends in a segment of plain copies A <- B (a Life board taking its next generation
@@ -69,7 +69,8 @@ int tc_cube_recompute_budget = 65536;
 int tc_cube_chunk = 140000;
 /* a segment too long for one kernel is split into equal kernels of at most this many
    instructions: they compile in parallel, and NVRTC's time grows faster than a kernel's length
-   (the NTT product on 512 machines, 272,001 instructions: 2 kernels took 85 s to compile) */
+   (the NTT product on 512 machines, 272,001 instructions: 2 kernels took 85 s to compile, 6 take
+   13.5 s) */
 int tc_cube_piece = 50000;
 
 struct CudaCube {
