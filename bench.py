@@ -592,7 +592,9 @@ def headline(args):
     line = {
         "metric": METRIC, "value": value, "unit": "lane-ops/s", "n_gpus": world,
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * launch_s,
-        "higher_is_better": True, "scaling": "strong" if sharded else "weak",
+        # the space is fixed and split into one share per rank (one share of the whole space at
+        # N = 1); --replicas runs the whole space on every rank
+        "higher_is_better": True, "scaling": "weak" if args.replicas else "strong",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "assignments_per_s": tried / kernel_s,
         "config": {"workload": WORKLOAD + ("" if args.share == 1 else
@@ -602,8 +604,8 @@ def headline(args):
                    "l2": "no DRAM inputs: cell state lives in registers and every input word is "
                          "derived from the lane index, so there is nothing to flush",
                    "device": info,
-                   "parallelism": (f"--part shares x{world}" if sharded else
-                                   f"replicas x{world}")},
+                   "parallelism": (f"replicas x{world}" if args.replicas else
+                                   f"--part shares x{world}")},
         "result": {"mismatches": 0, "tried_per_step": tried // steps,
                    "negative_control": control,
                    "merged_shares": ({k: merged[k] for k in ("space", "tried", "hits", "ops")}
