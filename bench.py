@@ -531,9 +531,14 @@ def headline(args):
         t0 = time.perf_counter()
         tune = T.enum_tune(T.EN_VERIFY, p, spec=s, **part)
         tune["seconds"] = time.perf_counter() - t0
-    for _ in range(max(3, args.warmup)):
+    # untimed warm-up: at least W launches and at least half a second of them, so that the SM
+    # clock, which drops while the host compiles and tunes, is at its level under load when the
+    # timed region starts
+    t_warm, n_warm = time.perf_counter(), 0
+    while n_warm < max(3, args.warmup) or time.perf_counter() - t_warm < 0.5:
         r = T.enum_run(T.EN_VERIFY, p, spec=s, **part)
         assert r["hits"] == 0
+        n_warm += 1
     stats = T.last_launch()
 
     if dist:
@@ -651,7 +656,7 @@ def headline(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
