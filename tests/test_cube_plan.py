@@ -240,3 +240,15 @@ def test_recomputing_stays_within_its_budget():
     finally:
         budget.value = old
     assert max(kernel_lop3(unbounded)) > 2 * max(kernel_lop3(plain))  # what the budget prevents
+
+
+def test_long_segments_split_into_equal_kernels():
+    """A segment longer than one kernel may hold (140,000 instructions) is split into equal
+    kernels of at most 50,000, which compile in parallel: the NTT product on 512 machines (one
+    segment of 272,001) becomes 6 kernels.  Life on 512 machines (130,575) stays one kernel, so
+    its passes still loop inside it."""
+    p = T.Program.gen_cube_demo("polymul", 9)
+    assert p.s.len == 272001
+    assert cube_source(p)[0] == 6
+    life = T.Program.gen_life_cube(32, 32, 4, 5)
+    assert cube_source(life)[0] == 1
