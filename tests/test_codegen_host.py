@@ -191,3 +191,15 @@ def test_unperm_is_a_bijection_that_keeps_chunks():
     assert len(seen) == 1 << 15
     for y in (1 << 15, 5 << 15 | 12345, (1 << 20) - 1):
         assert L.tc_host_unperm(y) >> 15 == y >> 15
+
+
+def test_no_inputs_on_host():
+    """A program without inputs has one assignment, 0: the generated code, run on the host, gives
+    the reference's results (its --raw lines: verify "y = 0" one hit, "y = 1" none, search
+    "y = 1" one hit, equivalence with a program whose z differs one hit)."""
+    p = T.Program.from_asm(".out y z\nNAND ZERO\nSTO y\nNAND ONE\nSTO z\n")
+    q = T.Program.from_asm(".out y z\nNAND ZERO\nSTO y\nSTO z\n")
+    assert emulate(T.EN_VERIFY, p, None, T.Spec(p, "y = 0"), {"ticks": 1}) == (1, [0])
+    assert emulate(T.EN_VERIFY, p, None, T.Spec(p, "y = 1"), {"ticks": 1}) == (0, [])
+    assert emulate(T.EN_SEARCH, p, None, T.Spec(p, "y = 1", False), {"ticks": 1}) == (1, [0])
+    assert emulate(T.EN_EQUIV, p, q, None, {"ticks": 1}) == (1, [0])
