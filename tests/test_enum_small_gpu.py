@@ -1,6 +1,8 @@
-"""Enumeration at the smallest spaces, on the GPU: programs with no inputs (one assignment, the
-empty input) and with one to three inputs (fewer assignments than the 32 lanes of a word), in
-every mode and with ticks 1 and 2, through cuda_enum_run and through cuda_batch_run.
+"""Enumeration at the smallest and the largest spaces, on the GPU: programs with no inputs (one
+assignment, the empty input) and with one to three inputs (fewer assignments than the 32 lanes of
+a word), in every mode and with ticks 1 and 2, through cuda_enum_run and through cuda_batch_run;
+and 46 inputs, the most the reference enumerates (src/enum.h EN_MAX_IN), on shares of its 2^46
+assignments, checked by properties that need no CPU run of the space, with 48 refused.
 
 The no-input results are the reference's own `--raw` lines for these programs
 (src/work.c:435-443; `alpha verify|search|equiv ... --raw` run on them):
@@ -75,3 +77,31 @@ def test_smallest_spaces_in_a_batch():
     wants = [oracle(j) for j in jobs]
     for got, want in zip(T.batch_run(jobs), wants):
         assert same_result(got, want), (got, want)
+
+
+def test_46_inputs_on_shares():
+    """A 23 x 23 multiplier: 2^46 assignments in 2^31 chunks of 32,768, split into 2^26 shares of
+    32 chunks (share s holds chunks s + k 2^26, src/enum.c:232-234).  Input a0, a's lowest bit, is
+    the assignment's top bit (45).  Against the true product a share has no mismatch; against
+    the product + 1 every assignment is one, the smallest 16 being its first chunk's first;
+    against the product ^ (a & 1) exactly the chunks from 2^30 on (bit 45 set)."""
+    p = T.Program.gen_mul(23)
+    assert len(p.inputs) == 46
+    parts, chunk = 1 << 26, 32768
+    per = 32 * chunk
+    ops = 32 * 64 * 512 * len(p)  # 64 passes of 512 lanes per chunk
+    true, off, top = (T.Spec(p, t) for t in ("p = a * b", "p = a * b + 1", "p = a * b ^ (a & 1)"))
+    for part in (0, 12345, parts - 1):
+        r = T.enum_run(T.EN_VERIFY, p, spec=true, part=part, parts=parts)
+        assert (r["space"], r["tried"], r["hits"], r["hit"], r["ops"]) == (1 << 46, per, 0, [], ops)
+        r = T.enum_run(T.EN_VERIFY, p, spec=off, part=part, parts=parts)
+        assert r["hits"] == per and r["hit"] == [part * chunk + i for i in range(16)], r
+        r = T.enum_run(T.EN_VERIFY, p, spec=top, part=part, parts=parts)
+        first = part + 16 * parts  # the share's first chunk at or past 2^30
+        assert r["hits"] == 16 * chunk and r["hit"] == [first * chunk + i for i in range(16)], r
+
+
+def test_48_inputs_are_refused():
+    p = T.Program.gen_mul(24)
+    with pytest.raises(T.EngineError, match="48 inputs is too many to try them all"):
+        T.enum_run(T.EN_VERIFY, p, spec=T.Spec(p, "p = a * b"), part=0, parts=1 << 30)
