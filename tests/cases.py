@@ -113,3 +113,32 @@ def program_digest(s, rename=None) -> str:
                                                         names[s.special[c].src])
                                          for c in range(s.ncells)))).encode())
     return h.hexdigest()
+
+
+def reordered(text: str, seed: int) -> str:
+    """The same program with the names of its .in and .out lines in another order.  Cells are
+    numbered in declaration order, so its inputs and outputs come in another order; equivalence
+    matches them by name (src/enum.c:48-78)."""
+    import random
+    r = random.Random(seed)
+    out = []
+    for line in text.splitlines():
+        words = line.split()
+        if words and words[0] in (".in", ".out"):
+            names = words[1:]
+            r.shuffle(names)
+            line = " ".join([words[0]] + names)
+        out.append(line)
+    return "\n".join(out) + "\n"
+
+
+def reordered_pairs():
+    """(a, b) equivalence pairs whose second program declares its inputs and outputs in another
+    order: identity-rewritten copies (equivalent) and mutated ones, 4 to 12 inputs."""
+    pairs = []
+    for seed in range(6):
+        a = T.Program.random_in(8 + 5 * seed, 4 + seed + seed // 2, 30 + 90 * seed, 5150 + seed)
+        for mutate in (False, True):
+            b = T.Program.from_asm(reordered(a.rewrite(seed + 40, mutate).text(), seed))
+            pairs.append((a, b, mutate))
+    return pairs
