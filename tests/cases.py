@@ -142,3 +142,35 @@ def reordered_pairs():
             b = T.Program.from_asm(reordered(a.rewrite(seed + 40, mutate).text(), seed))
             pairs.append((a, b, mutate))
     return pairs
+
+
+def with_written_inputs(text: str, k: int) -> str:
+    """A random program (every cell an output, src/main.c:1028-1069) with its first k cells made
+    inputs, which its stores then overwrite: each pass starts from the assignment, and later
+    reads see what the program stored (src/enum.c:115-133)."""
+    out, first = [], True
+    for line in text.splitlines():
+        words = line.split()
+        if first and words and words[0] == ".out":  # the first line lists c0 .. c15
+            assert len(words) > k + 1
+            out.append(" ".join([".in"] + words[1:k + 1]))
+            line = " ".join([".out"] + words[k + 1:])
+            first = False
+        out.append(line)
+    return "\n".join(out) + "\n"
+
+
+def written_input_jobs():
+    """(mode, a, b, spec text, ticks) jobs over random programs that store into their inputs:
+    equivalence with rewritten and mutated copies and searches for one output, 3 to 12 inputs,
+    ticks 1 and 2."""
+    jobs = []
+    for seed in range(6):
+        cells, k = 8 + 6 * seed, 3 + (seed * 7) % 10
+        a = T.Program.from_asm(with_written_inputs(
+            T.Program.random(cells, 200 + 250 * seed, 9100 + seed).text(), k))
+        for ticks in (1, 2):
+            for mutate in (False, True):
+                jobs.append((T.EN_EQUIV, a, a.rewrite(seed + 7, mutate), None, ticks))
+            jobs.append((T.EN_SEARCH, a, None, "c%d = %d" % (k, seed % 2), ticks))
+    return jobs
