@@ -173,15 +173,22 @@ def cpu_sample(seconds_target=12.0):
 
 def run_reference(args):
     """The reference arm: the reference's own enumerator where it was built from its sources on
-    this host (oracle/_ref/alpha, x86 only: `alpha verify ... --part i/64 --raw`, a 1/64 share of
-    the space per step), otherwise the oracle's C port of it on every host core."""
+    this host (oracle/_ref/alpha, x86 only: `alpha verify ... --part i/K --raw`, a 1/K share of
+    the space per step, K = 64 for up to 100 steps and more beyond), otherwise the oracle's C port
+    of it on every host core on a sample of chunks sized per step; either way the whole run takes
+    about two minutes."""
     world, rank, _ = dist_env()
     if rank != 0:
         return 0
     import oracle as O
     threads = os.cpu_count() or 1
+    # each step is a bounded sample, sized so that all warm-up and timed steps take about two
+    # minutes whatever --steps is (at most 4 s a step)
+    nsteps = args.steps + args.warmup
+    per_step_s = min(4.0, 120.0 / max(1, nsteps))
     if O.have_reference():
         import tempfile
+        parts = 64 * max(1, -(-nsteps // 100))  # a share of 2^32 / parts assignments per step
         with tempfile.TemporaryDirectory() as d:
             prog = os.path.join(d, "mul16.asm")
             with open(prog, "w") as f:
@@ -190,7 +197,7 @@ def run_reference(args):
 
             def step(i):
                 out = subprocess.run([O.REF_BIN, "verify", prog, "--spec", "p = a * b", "--part",
-                                      "%d/64" % (i % 64), "--raw"], check=True,
+                                      "%d/%d" % (i % parts, parts), "--raw"], check=True,
                                      capture_output=True, text=True).stdout
                 f = out.split("\n")[0].split()
                 assert f[0] == "EN" and int(f[4]) == 0
@@ -202,12 +209,13 @@ def run_reference(args):
             for i in range(args.steps):
                 ops += step(args.warmup + i)
             dt = time.perf_counter() - t0
-        kind, sample = "reference", "alpha verify --part i/64 (2^26 assignments) per step"
+        kind, sample = "reference", ("alpha verify --part i/%d (2^32 / %d assignments) per step"
+                                     % (parts, parts))
     else:
         prog, spec = reference_inputs()
         e = O.verify_struct(prog, spec)
         base, _, _ = cpu_sample(seconds_target=4.0)
-        chunks = int(base["sample"].split()[0])
+        chunks = max(threads, int(int(base["sample"].split()[0]) * per_step_s / 4.0))
         for _ in range(args.warmup):
             O.enum_run_struct(e, threads=threads, limit_chunks=max(1, chunks // 8))
         ops = 0
@@ -222,7 +230,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "lane-ops/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "scaling": "strong", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "sample_per_step": sample},
             "cpu_baseline": {"value": v, "unit": "lane-ops/s", "cores": threads, "kind": kind,
                              "sample": sample},
